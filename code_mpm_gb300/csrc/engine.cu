@@ -1,0 +1,958 @@
+// GB300 explicit-MPM engine: context, step orchestration and the C ABI
+// declared in include/mpm_gb300.h.
+//
+// One context owns a regular grid, its particles and every device buffer.
+// All work is issued on one CUDA stream; the host only computes the
+// per-step scalars (time, timeline velocity) and launches kernels.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "kernels.cuh"
+#include "mpm_gb300.h"
+#include "radix_sort.cuh"
+
+using namespace mpm;
+
+namespace {
+
+constexpr int NTHREADS = 256;
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+struct ProfRec {
+    int name;
+    cudaEvent_t a, b;
+};
+
+}  // namespace
+
+struct mpm_ctx {
+    int form = MPM_FORM_FP64;
+    int device = 0;
+    size_t tsize = 8;  // bytes of the transfer/grid real type
+    Geom g{};
+    double length[3]{};
+    int cells[3]{};
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::string err;
+    // options
+    int floor_friction = 0;
+    int profile = 0;
+    // simulation scalars
+    mpm_sim sim{0.0, 1.0e-3, 0.0, 0.0, 10.0, 0};
+    // counts
+    long long n = 0;
+    long long nn = 0;
+    int nmat = 0;
+    int ndc = 0;
+    std::vector<double> tl_t, tl_v;
+    bool have_particles = false, have_nodes = false;
+    // device buffers
+    std::vector<DevBuf*> all;
+    DevBuf xtab, err_word;
+    // particles
+    DevBuf pos, vel, fext, mass, vol, vol0, F, stress, strain, eps_p, e_strain, e_strain_max, e_strain_ti, e_plastic,
+        backstress, mp_mg, strain_rate, material, pflags, dc_mult;
+    // nodes
+    DevBuf g_mass, g_mom, g_vel, g_force, g_ftemp, g_mg, g_state, g_fixed, g_friction, g_ratio, g_q, g_owner,
+        g_nowner, g_need;
+    DevBuf cstart, cend;
+    // sort
+    DevBuf keys0, vals0, keys1, vals1, keys_copy, counts;
+    DevBuf dclist, mats, staging;
+    // host pinned staging for the error word
+    unsigned* h_err = nullptr;
+    // profiling
+    std::vector<std::string> prof_names;
+    std::vector<ProfRec> prof_pending;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<double> prof_ms;
+    std::vector<long long> prof_cnt;
+    long long launches = 0;
+    const unsigned* last_perm = nullptr;
+
+    mpm_ctx() {
+        DevBuf* list[] = {&xtab, &err_word, &pos, &vel, &fext, &mass, &vol, &vol0, &F, &stress, &strain, &eps_p,
+                          &e_strain, &e_strain_max, &e_strain_ti, &e_plastic, &backstress, &mp_mg, &strain_rate,
+                          &material, &pflags, &dc_mult, &g_mass, &g_mom, &g_vel, &g_force, &g_ftemp, &g_mg,
+                          &g_state, &g_fixed, &g_friction, &g_ratio, &g_q, &g_owner, &g_nowner, &g_need, &cstart,
+                          &cend, &keys0, &vals0, &keys1, &vals1, &keys_copy, &counts, &dclist, &mats, &staging};
+        all.assign(std::begin(list), std::end(list));
+    }
+};
+
+namespace {
+
+int fail(mpm_ctx* c, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    return code;
+}
+
+#define CK(call)                                                                                     \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess) return fail(c, MPM_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+int ensure(mpm_ctx* c, DevBuf& b, size_t bytes) {
+    if (b.bytes >= bytes && b.p) return MPM_OK;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(&b.p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(c, MPM_ERR_NOMEM, "cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+    }
+    b.bytes = bytes;
+    return MPM_OK;
+}
+
+template <typename T>
+PView<T> pview(mpm_ctx* c) {
+    PView<T> v;
+    v.pos = (double*)c->pos.p;
+    v.vel = (T*)c->vel.p;
+    v.fext = (T*)c->fext.p;
+    v.mass = (T*)c->mass.p;
+    v.vol = (T*)c->vol.p;
+    v.vol0 = (T*)c->vol0.p;
+    v.F = (T*)c->F.p;
+    v.stress = (T*)c->stress.p;
+    v.strain = (T*)c->strain.p;
+    v.eps_p = (T*)c->eps_p.p;
+    v.e_strain = (double*)c->e_strain.p;
+    v.e_strain_max = (double*)c->e_strain_max.p;
+    v.e_strain_ti = (double*)c->e_strain_ti.p;
+    v.e_plastic = (double*)c->e_plastic.p;
+    v.backstress = (T*)c->backstress.p;
+    v.mp_mg = (double*)c->mp_mg.p;
+    v.strain_rate = (T*)c->strain_rate.p;
+    v.material = (int32_t*)c->material.p;
+    v.pflags = (uint8_t*)c->pflags.p;
+    v.dc_mult = (float*)c->dc_mult.p;
+    v.n = c->n;
+    return v;
+}
+
+template <typename T>
+NView<T> nview(mpm_ctx* c) {
+    NView<T> v;
+    v.mass = (T*)c->g_mass.p;
+    v.mom = (T*)c->g_mom.p;
+    v.vel = (T*)c->g_vel.p;
+    v.force = (T*)c->g_force.p;
+    v.ftemp = (T*)c->g_ftemp.p;
+    v.mg = (double*)c->g_mg.p;
+    v.state = (unsigned*)c->g_state.p;
+    v.fixed = (uint8_t*)c->g_fixed.p;
+    v.friction = (double*)c->g_friction.p;
+    v.ratio = (T*)c->g_ratio.p;
+    v.q = (T*)c->g_q.p;
+    v.owner = (unsigned*)c->g_owner.p;
+    v.nowner = (unsigned*)c->g_nowner.p;
+    v.nn = c->nn;
+    return v;
+}
+
+unsigned blocks_for(long long n, int threads = NTHREADS) {
+    long long b = (n + threads - 1) / threads;
+    return (unsigned)std::max<long long>(1, b);
+}
+
+// ---- profiling --------------------------------------------------------------
+int prof_id(mpm_ctx* c, const char* name) {
+    for (size_t i = 0; i < c->prof_names.size(); ++i)
+        if (c->prof_names[i] == name) return (int)i;
+    c->prof_names.push_back(name);
+    c->prof_ms.push_back(0.0);
+    c->prof_cnt.push_back(0);
+    return (int)c->prof_names.size() - 1;
+}
+
+cudaEvent_t take_event(mpm_ctx* c) {
+    if (!c->ev_pool.empty()) {
+        cudaEvent_t e = c->ev_pool.back();
+        c->ev_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+
+struct Launch {
+    mpm_ctx* c;
+    int id = -1;
+    cudaEvent_t a = nullptr;
+    Launch(mpm_ctx* c_, const char* name) : c(c_) {
+        c->launches++;
+        if (c->profile) {
+            id = prof_id(c, name);
+            a = take_event(c);
+            cudaEventRecord(a, c->stream);
+        }
+    }
+    ~Launch() {
+        if (c->profile) {
+            cudaEvent_t b = take_event(c);
+            cudaEventRecord(b, c->stream);
+            c->prof_pending.push_back({id, a, b});
+        }
+    }
+};
+
+int prof_resolve(mpm_ctx* c) {
+    if (c->prof_pending.empty()) return MPM_OK;
+    CK(cudaStreamSynchronize(c->stream));
+    for (auto& r : c->prof_pending) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, r.a, r.b);
+        c->prof_ms[r.name] += ms;
+        c->prof_cnt[r.name] += 1;
+        c->ev_pool.push_back(r.a);
+        c->ev_pool.push_back(r.b);
+    }
+    c->prof_pending.clear();
+    return MPM_OK;
+}
+
+#define LAUNCH(name, kernel, grid, block, ...)                             \
+    do {                                                                   \
+        Launch l_(c, name);                                                \
+        kernel<<<(grid), (block), 0, c->stream>>>(__VA_ARGS__);            \
+    } while (0)
+
+// ---- host-side timeline (TimeLine::getVelocity, TimeLine.h:33-46) ----------
+void timeline_velocity(const mpm_ctx* c, double t, double out[3]) {
+    out[0] = out[1] = out[2] = 0.0;
+    int nt = (int)c->tl_t.size();
+    for (int k = 0; k + 1 < nt; ++k) {
+        if (c->tl_t[k] <= t && t < c->tl_t[k + 1]) {
+            double s = (t - c->tl_t[k]) / (c->tl_t[k + 1] - c->tl_t[k]);
+            for (int a = 0; a < 3; ++a) {
+                volatile double l = (1.0 - s) * c->tl_v[3 * k + a];
+                volatile double r = s * c->tl_v[3 * (k + 1) + a];
+                out[a] = l + r;
+            }
+        }
+    }
+}
+
+// ---- unpack / pack between host n x k row-major doubles and device SoA -----
+template <typename T>
+__global__ void k_unpack(const double* __restrict__ src, T* __restrict__ dst, long long n, int k) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n * k) return;
+    long long p = i / k;
+    int c = (int)(i - p * k);
+    dst[(long long)c * n + p] = (T)src[i];
+}
+template <typename T>
+__global__ void k_pack(const T* __restrict__ src, double* __restrict__ dst, long long n, int k) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n * k) return;
+    long long p = i / k;
+    int c = (int)(i - p * k);
+    dst[i] = (double)src[(long long)c * n + p];
+}
+template <typename T>
+__global__ void k_fill(T* __restrict__ dst, long long n, T v) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = v;
+}
+__global__ void k_identity9(void* dst, long long n, int fp64) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= 9 * n) return;
+    long long c = i / n;
+    double v = (c == 0 || c == 4 || c == 8) ? 1.0 : 0.0;
+    if (fp64)
+        ((double*)dst)[i] = v;
+    else
+        ((float*)dst)[i] = (float)v;
+}
+__global__ void k_state_u8_to_u32(const uint8_t* __restrict__ src, unsigned* __restrict__ dst, long long n) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = src[i];
+}
+__global__ void k_state_u32_to_u8(const unsigned* __restrict__ src, uint8_t* __restrict__ dst, long long n) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = (uint8_t)src[i];
+}
+__global__ void k_mark_dc(const unsigned* __restrict__ list, int ndc, uint8_t* __restrict__ pflags) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < ndc) pflags[list[k]] |= (uint8_t)PF_IN_DC;
+}
+__global__ void k_clear_flag(uint8_t* __restrict__ pflags, long long n, uint8_t bits) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) pflags[i] &= (uint8_t)~bits;
+}
+
+// Upload one field: host n x k doubles (or NULL -> default) into a device SoA array of the field's real type.
+int upload_field(mpm_ctx* c, DevBuf& dst, const double* host, long long n, int k, bool fp64, double def) {
+    size_t esz = fp64 ? 8 : 4;
+    int rc = ensure(c, dst, (size_t)n * k * esz);
+    if (rc) return rc;
+    if (n == 0) return MPM_OK;
+    if (host) {
+        rc = ensure(c, c->staging, (size_t)n * k * 8);
+        if (rc) return rc;
+        CK(cudaMemcpyAsync(c->staging.p, host, (size_t)n * k * 8, cudaMemcpyHostToDevice, c->stream));
+        if (fp64)
+            LAUNCH("unpack", k_unpack<double>, blocks_for(n * k), NTHREADS, (const double*)c->staging.p,
+                   (double*)dst.p, n, k);
+        else
+            LAUNCH("unpack", k_unpack<float>, blocks_for(n * k), NTHREADS, (const double*)c->staging.p,
+                   (float*)dst.p, n, k);
+    } else if (def == 0.0) {
+        CK(cudaMemsetAsync(dst.p, 0, (size_t)n * k * esz, c->stream));
+    } else if (fp64) {
+        LAUNCH("fill", k_fill<double>, blocks_for(n * k), NTHREADS, (double*)dst.p, n * k, def);
+    } else {
+        LAUNCH("fill", k_fill<float>, blocks_for(n * k), NTHREADS, (float*)dst.p, n * k, (float)def);
+    }
+    return MPM_OK;
+}
+
+int download_field(mpm_ctx* c, const DevBuf& src, double* host, long long n, int k, bool fp64) {
+    if (!host || n == 0) return MPM_OK;
+    int rc = ensure(c, c->staging, (size_t)n * k * 8);
+    if (rc) return rc;
+    if (fp64)
+        LAUNCH("pack", k_pack<double>, blocks_for(n * k), NTHREADS, (const double*)src.p, (double*)c->staging.p, n,
+               k);
+    else
+        LAUNCH("pack", k_pack<float>, blocks_for(n * k), NTHREADS, (const float*)src.p, (double*)c->staging.p, n, k);
+    CK(cudaMemcpyAsync(host, c->staging.p, (size_t)n * k * 8, cudaMemcpyDeviceToHost, c->stream));
+    return MPM_OK;
+}
+
+int check_device_error(mpm_ctx* c) {
+    CK(cudaMemcpyAsync(c->h_err, c->err_word.p, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    unsigned e = *c->h_err;
+    if (e) {
+        CK(cudaMemsetAsync(c->err_word.p, 0, sizeof(unsigned), c->stream));
+        std::string what;
+        if (e & ERR_NONFINITE_POSITION) what += " non-finite particle position;";
+        if (e & ERR_BAD_MATERIAL) what += " particle without a valid material;";
+        return fail(c, MPM_ERR_DEVICE, "device reported:%s", what.c_str());
+    }
+    return MPM_OK;
+}
+
+// ---- one time step -----------------------------------------------------------
+template <typename T>
+int step_impl(mpm_ctx* c, double dt, int contact) {
+    const long long n = c->n, nn = c->nn;
+    PView<T> P = pview<T>(c);
+    NView<T> N = nview<T>(c);
+    const Geom& g = c->g;
+    unsigned* err = (unsigned*)c->err_word.p;
+
+    LAUNCH("reset_grid", k_reset_grid<T>, blocks_for(nn), NTHREADS, N, contact);
+    if (n > 0) {
+        // cell keys + stable radix sort by key
+        LAUNCH("cell_keys", k_cell_keys, blocks_for(n), NTHREADS, (const double*)c->pos.p, n, g,
+               (unsigned*)c->keys0.p, (unsigned*)c->vals0.p, (unsigned*)c->keys_copy.p, err);
+        int bits = 1;
+        while (bits < 32 && ((unsigned long long)1 << bits) <= (unsigned long long)g.key_max) ++bits;
+        const int nblocks = (int)((n + RS_TILE - 1) / RS_TILE);
+        unsigned *kin = (unsigned*)c->keys0.p, *vin = (unsigned*)c->vals0.p;
+        unsigned *kout = (unsigned*)c->keys1.p, *vout = (unsigned*)c->vals1.p;
+        for (int shift = 0; shift < bits; shift += 8) {
+            LAUNCH("rs_hist", k_rs_hist, nblocks, RS_THREADS, kin, n, shift, (unsigned*)c->counts.p, nblocks);
+            LAUNCH("rs_scan", k_rs_scan, 1, 1024, (unsigned*)c->counts.p, 256 * nblocks);
+            LAUNCH("rs_scatter", k_rs_scatter, nblocks, RS_THREADS, kin, vin, kout, vout, n, shift,
+                   (const unsigned*)c->counts.p, nblocks);
+            std::swap(kin, kout);
+            std::swap(vin, vout);
+        }
+        const unsigned* skeys = kin;
+        const unsigned* perm = vin;
+        c->last_perm = perm;
+        const unsigned* keys = (const unsigned*)c->keys_copy.p;
+        if (contact) {
+            CK(cudaMemsetAsync(c->cstart.p, 0, (size_t)g.key_max * 4, c->stream));
+            CK(cudaMemsetAsync(c->cend.p, 0, (size_t)g.key_max * 4, c->stream));
+        }
+        LAUNCH("cell_ranges", k_cell_ranges, blocks_for(n), NTHREADS, skeys, n, g, N.state,
+               contact ? (unsigned*)c->cstart.p : nullptr, contact ? (unsigned*)c->cend.p : nullptr);
+        LAUNCH("p2g", k_p2g<T>, blocks_for(n), NTHREADS, P, N, g, skeys, perm, n);
+        if (c->ndc > 0) {
+            CK(cudaMemsetAsync(c->g_owner.p, 0, (size_t)3 * nn * 4, c->stream));
+            LAUNCH("dc_claim", k_dc_claim, blocks_for(c->ndc), NTHREADS, (const unsigned*)c->dclist.p, c->ndc, keys,
+                   (const uint8_t*)c->pflags.p, g, (unsigned*)c->g_owner.p, nn, contact);
+        }
+        if (contact) {
+            CK(cudaMemsetAsync(c->g_need.p, 0, (size_t)nn * 4, c->stream));
+            LAUNCH("contact_need", k_contact_need<T>, blocks_for(n), NTHREADS, P, keys, g, (unsigned*)c->g_need.p);
+            LAUNCH("contact_mass_gradient", k_contact_mass_gradient<T>, blocks_for(nn, 128), 128, P, N, g,
+                   (const unsigned*)c->g_need.p, perm, (const unsigned*)c->cstart.p, (const unsigned*)c->cend.p);
+            LAUNCH("contact_mp_gradient", k_contact_mp_gradient<T>, blocks_for(n), NTHREADS, P, N, g, keys);
+            LAUNCH("contact_reset", k_contact_reset<T>, blocks_for(nn), NTHREADS, N);
+            LAUNCH("contact_normal", k_contact_normal<T>, blocks_for(n), NTHREADS, P, N, g, keys, 0);
+            LAUNCH("contact_normal", k_contact_normal<T>, blocks_for(n), NTHREADS, P, N, g, keys, 1);
+            LAUNCH("contact_flags", k_contact_flags<T>, blocks_for(n), NTHREADS, P, N, g, keys);
+        }
+        if (!contact && c->ndc > 0)
+            LAUNCH("dc_apply", k_dc_apply<T>, blocks_for(c->ndc), NTHREADS, (const unsigned*)c->dclist.p, c->ndc,
+                   keys, P, N, g, contact);
+        LAUNCH("grid_update", k_grid_update<T>, blocks_for(nn), NTHREADS, N, (T)dt, c->sim.damping, contact,
+               c->floor_friction);
+        if (contact && c->ndc > 0)
+            LAUNCH("dc_apply", k_dc_apply<T>, blocks_for(c->ndc), NTHREADS, (const unsigned*)c->dclist.p, c->ndc,
+                   keys, P, N, g, contact);
+        LAUNCH("node_ratio", k_node_ratio<T>, blocks_for(nn), NTHREADS, N, (const T*)c->g_force.p, c->sim.mass_min,
+               1);
+        LAUNCH("pass1_remap", k_pass1_remap<T>, blocks_for(n), NTHREADS, P, N, g, skeys, perm, n, (T)dt,
+               c->sim.mass_min, contact);
+        LAUNCH("node_remap", k_node_remap<T>, blocks_for(nn), NTHREADS, N, c->sim.mass_min);
+        if (!contact) {
+            if (c->ndc > 0)
+                LAUNCH("dc_apply", k_dc_apply<T>, blocks_for(c->ndc), NTHREADS, (const unsigned*)c->dclist.p,
+                       c->ndc, keys, P, N, g, contact);
+            LAUNCH("node_bc", k_node_bc<T>, blocks_for(nn), NTHREADS, N);
+        } else {
+            LAUNCH("node_bc", k_node_bc<T>, blocks_for(nn), NTHREADS, N);
+            if (c->ndc > 0)
+                LAUNCH("dc_apply", k_dc_apply<T>, blocks_for(c->ndc), NTHREADS, (const unsigned*)c->dclist.p,
+                       c->ndc, keys, P, N, g, contact);
+        }
+        LAUNCH("node_ratio", k_node_ratio<T>, blocks_for(nn), NTHREADS, N, (const T*)c->g_mom.p, c->sim.mass_min, 0);
+        StepArgs a;
+        a.dt = dt;
+        a.mass_min = c->sim.mass_min;
+        timeline_velocity(c, c->sim.time, a.tv);
+        a.has_timeline = c->tl_t.empty() ? 0 : 1;
+        a.contact = contact;
+        LAUNCH("pass2", k_pass2<T>, blocks_for(n), NTHREADS, P, N, g, keys, (const MatConst*)c->mats.p, c->nmat, a,
+               err);
+    }
+    CK(cudaGetLastError());
+    // d_Time += dTimeIncrement; i_TimeCycle++ (…MPLocks.cpp:802-803)
+    c->sim.time += dt;
+    c->sim.step += 1;
+    return MPM_OK;
+}
+
+int step(mpm_ctx* c, double dt, int contact) {
+    return c->form == MPM_FORM_FP64 ? step_impl<double>(c, dt, contact) : step_impl<float>(c, dt, contact);
+}
+
+int alloc_particles(mpm_ctx* c, long long n) {
+    const size_t t = c->tsize;
+    struct {
+        DevBuf* b;
+        size_t bytes;
+    } plan[] = {{&c->pos, 3 * 8},     {&c->vel, 3 * t},        {&c->fext, 3 * t},        {&c->mass, t},
+                {&c->vol, t},         {&c->vol0, t},           {&c->F, 9 * t},           {&c->stress, 6 * t},
+                {&c->strain, 6 * t},  {&c->eps_p, 6 * t},      {&c->e_strain, 8},        {&c->e_strain_max, 8},
+                {&c->e_strain_ti, 8}, {&c->e_plastic, 8},      {&c->backstress, t},      {&c->mp_mg, 3 * 8},
+                {&c->strain_rate, 6 * t}, {&c->material, 4},   {&c->pflags, 1},          {&c->dc_mult, 4},
+                {&c->keys0, 4},       {&c->vals0, 4},          {&c->keys1, 4},           {&c->vals1, 4},
+                {&c->keys_copy, 4}};
+    for (auto& e : plan) {
+        int rc = ensure(c, *e.b, (size_t)n * e.bytes);
+        if (rc) return rc;
+    }
+    const long long nblocks = std::max<long long>(1, (n + RS_TILE - 1) / RS_TILE);
+    return ensure(c, c->counts, (size_t)256 * nblocks * 4);
+}
+
+}  // namespace
+
+// =============================================================================
+// C ABI
+// =============================================================================
+extern "C" {
+
+int mpm_device_info(char* name, int name_len, int* sm_count, int* cc_major, int* cc_minor) {
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return MPM_ERR_CUDA;
+    }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) return MPM_ERR_CUDA;
+    if (name && name_len > 0) {
+        strncpy(name, prop.name, (size_t)name_len - 1);
+        name[name_len - 1] = 0;
+    }
+    if (sm_count) *sm_count = prop.multiProcessorCount;
+    if (cc_major) *cc_major = prop.major;
+    if (cc_minor) *cc_minor = prop.minor;
+    return MPM_OK;
+}
+
+int mpm_create(const mpm_grid_desc* grid, int form, mpm_ctx** out) {
+    if (!out) return MPM_ERR_ARG;
+    *out = nullptr;
+    if (!grid || (form != MPM_FORM_FP64 && form != MPM_FORM_FP32)) return MPM_ERR_ARG;
+    long long keyspace = 1;
+    for (int a = 0; a < 3; ++a) {
+        if (!(grid->length[a] > 0.0) || !std::isfinite(grid->length[a]) || grid->cells[a] < 1) return MPM_ERR_ARG;
+        keyspace *= (long long)grid->cells[a] + 2;
+    }
+    if (keyspace >= 0xffffffffLL) return MPM_ERR_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return MPM_ERR_CUDA;
+    }
+    mpm_ctx* c = new mpm_ctx();
+    c->form = form;
+    c->tsize = form == MPM_FORM_FP64 ? 8 : 4;
+    cudaGetDevice(&c->device);
+    Geom& g = c->g;
+    for (int a = 0; a < 3; ++a) {
+        c->length[a] = grid->length[a];
+        c->cells[a] = grid->cells[a];
+        // d3_Length_Cell = d3Length_Grid / dvec3(i3Cells)
+        g.h[a] = grid->length[a] / (double)grid->cells[a];
+        g.inv_h[a] = 1.0 / g.h[a];
+        g.nn[a] = grid->cells[a] + 1;
+        g.kd[a] = grid->cells[a] + 2;
+    }
+    g.key_max = (unsigned)keyspace;
+    g.n_nodes = (long long)g.nn[0] * g.nn[1] * g.nn[2];
+    c->nn = g.n_nodes;
+    // padded node coordinate tables: entry n+1 for node n in [-1, nn]
+    std::vector<double> tab;
+    for (int a = 0; a < 3; ++a) {
+        g.xoff[a] = (int)tab.size();
+        for (int i = -1; i <= g.nn[a]; ++i) tab.push_back(i * grid->length[a] / grid->cells[a]);
+    }
+    int rc = MPM_OK;
+    auto bail = [&](int code) {
+        mpm_destroy(c);
+        return code;
+    };
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(MPM_ERR_CUDA);
+    c->own_stream = true;
+    if ((rc = ensure(c, c->xtab, tab.size() * 8))) return bail(rc);
+    if (cudaMemcpy(c->xtab.p, tab.data(), tab.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess)
+        return bail(MPM_ERR_CUDA);
+    g.xtab = (const double*)c->xtab.p;
+    if ((rc = ensure(c, c->err_word, 4))) return bail(rc);
+    cudaMemset(c->err_word.p, 0, 4);
+    if (cudaMallocHost((void**)&c->h_err, sizeof(unsigned)) != cudaSuccess) return bail(MPM_ERR_CUDA);
+    const size_t t = c->tsize, nn = (size_t)c->nn;
+    struct {
+        DevBuf* b;
+        size_t bytes;
+    } plan[] = {{&c->g_mass, nn * t},      {&c->g_mom, 3 * nn * t},  {&c->g_vel, 3 * nn * t},
+                {&c->g_force, 3 * nn * t}, {&c->g_ftemp, 3 * nn * t}, {&c->g_mg, 3 * nn * 8},
+                {&c->g_state, nn * 4},     {&c->g_fixed, nn},        {&c->g_friction, nn * 8},
+                {&c->g_ratio, 3 * nn * t}, {&c->g_q, 3 * nn * t},    {&c->g_owner, 3 * nn * 4},
+                {&c->g_nowner, nn * 4},    {&c->g_need, nn * 4},     {&c->cstart, (size_t)g.key_max * 4},
+                {&c->cend, (size_t)g.key_max * 4}};
+    for (auto& e : plan) {
+        if ((rc = ensure(c, *e.b, e.bytes))) return bail(rc);
+        if (cudaMemset(e.b->p, 0, e.bytes) != cudaSuccess) return bail(MPM_ERR_CUDA);
+    }
+    *out = c;
+    return MPM_OK;
+}
+
+void mpm_destroy(mpm_ctx* c) {
+    if (!c) return;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto& r : c->prof_pending) {
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    for (auto e : c->ev_pool) cudaEventDestroy(e);
+    for (DevBuf* b : c->all)
+        if (b->p) cudaFree(b->p);
+    if (c->h_err) cudaFreeHost(c->h_err);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+const char* mpm_last_error(const mpm_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int mpm_set_stream(mpm_ctx* c, void* stream) {
+    if (!c) return MPM_ERR_ARG;
+    CK(cudaStreamSynchronize(c->stream));
+    if (c->own_stream) cudaStreamDestroy(c->stream);
+    c->own_stream = false;
+    c->stream = (cudaStream_t)stream;
+    return MPM_OK;
+}
+
+int mpm_set_option(mpm_ctx* c, int key, double value) {
+    if (!c) return MPM_ERR_ARG;
+    switch (key) {
+        case MPM_OPT_FLOOR_FRICTION: c->floor_friction = value != 0.0; return MPM_OK;
+        case MPM_OPT_PROFILE: c->profile = value != 0.0; return MPM_OK;
+        default: return fail(c, MPM_ERR_ARG, "unknown option %d", key);
+    }
+}
+
+int mpm_upload_materials(mpm_ctx* c, const mpm_material* m, int32_t n) {
+    if (!c || n < 0 || (n > 0 && !m)) return c ? fail(c, MPM_ERR_ARG, "bad material table") : MPM_ERR_ARG;
+    std::vector<MatConst> mc((size_t)std::max(1, n));
+    for (int i = 0; i < n; ++i) {
+        MatConst& k = mc[i];
+        memset(&k, 0, sizeof(k));
+        const double E = m[i].E, nu = m[i].nu;
+        k.type = m[i].type == MPM_MAT_ELASTIC ? 0 : (m[i].type == MPM_MAT_VONMISESHARDENING ? 4 : 3);
+        k.E = E;
+        k.nu = nu;
+        k.Y = m[i].yield;
+        k.C0 = m[i].C0;
+        k.C1 = m[i].C1;
+        // the reference's own expressions (…_Elastic.cpp:9, …_PerfectlyPlastic.cpp:13,43,64, …_VonMisesHardening.cpp:87)
+        k.C = E / (1.0 + nu) / (1.0 - 2.0 * nu);
+        k.one_m_nu = 1.0 - nu;
+        k.half_m_nu = 0.5 - nu;
+        k.G = 0.5 * E / (1.0 + nu);
+        k.k0 = m[i].yield / std::sqrt(3.0);
+        k.s23C1 = std::sqrt(2.0 / 3.0) * m[i].C1;
+        k.inv_E = 1.0 / E;
+        k.nu_over_E = nu / E;
+        k.inv_G = 1.0 / k.G;
+    }
+    int rc = ensure(c, c->mats, mc.size() * sizeof(MatConst));
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(c->mats.p, mc.data(), mc.size() * sizeof(MatConst), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->nmat = n;
+    return MPM_OK;
+}
+
+int mpm_upload_particles(mpm_ctx* c, const mpm_particles* p, int64_t n) {
+    if (!c) return MPM_ERR_ARG;
+    if (!p || n < 0 || n >= 0x7fffffffLL) return fail(c, MPM_ERR_ARG, "bad particle upload (n=%lld)", (long long)n);
+    const bool f64 = c->form == MPM_FORM_FP64;
+    int rc = alloc_particles(c, n);
+    if (rc) return rc;
+    c->n = n;
+    struct {
+        DevBuf* b;
+        const double* h;
+        int k;
+        bool fp64;
+        double def;
+    } fields[] = {{&c->pos, p->pos, 3, true, 0.0},
+                  {&c->vel, p->vel, 3, f64, 0.0},
+                  {&c->fext, p->fext, 3, f64, 0.0},
+                  {&c->mass, p->mass, 1, f64, 0.0},
+                  {&c->vol, p->vol, 1, f64, 0.0},
+                  {&c->vol0, p->vol0, 1, f64, 0.0},
+                  {&c->stress, p->stress, 6, f64, 0.0},
+                  {&c->strain, p->strain, 6, f64, 0.0},
+                  {&c->eps_p, p->eps_p, 6, f64, 0.0},
+                  {&c->e_strain, p->e_strain, 1, true, 0.0},
+                  {&c->e_strain_max, p->e_strain_max, 1, true, 0.0},
+                  {&c->e_strain_ti, p->e_strain_ti, 1, true, 0.0},
+                  {&c->e_plastic, p->e_plastic, 1, true, 0.0},
+                  {&c->backstress, p->backstress, 1, f64, 0.0},
+                  {&c->mp_mg, p->mp_mass_gradient, 3, true, 0.0},
+                  {&c->strain_rate, p->strain_rate, 6, f64, 0.0}};
+    for (auto& f : fields)
+        if ((rc = upload_field(c, *f.b, f.h, n, f.k, f.fp64, f.def))) return rc;
+    if (p->F) {
+        if ((rc = upload_field(c, c->F, p->F, n, 9, f64, 0.0))) return rc;
+    } else if (n > 0) {
+        LAUNCH("fill", k_identity9, blocks_for(9 * n), NTHREADS, c->F.p, (long long)n, f64 ? 1 : 0);
+    }
+    if (n > 0) {
+        if (p->material)
+            CK(cudaMemcpyAsync(c->material.p, p->material, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
+        else
+            CK(cudaMemsetAsync(c->material.p, 0, (size_t)n * 4, c->stream));
+        if (p->pflags) {
+            CK(cudaMemcpyAsync(c->pflags.p, p->pflags, (size_t)n, cudaMemcpyHostToDevice, c->stream));
+            LAUNCH("fill", k_clear_flag, blocks_for(n), NTHREADS, (uint8_t*)c->pflags.p, (long long)n,
+                   (uint8_t)PF_IN_DC);
+        } else {
+            CK(cudaMemsetAsync(c->pflags.p, 0, (size_t)n, c->stream));
+        }
+        if (p->dc_mult)
+            CK(cudaMemcpyAsync(c->dc_mult.p, p->dc_mult, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
+        else
+            LAUNCH("fill", k_fill<float>, blocks_for(n), NTHREADS, (float*)c->dc_mult.p, (long long)n, 1.0f);
+        if (c->ndc > 0)
+            LAUNCH("fill", k_mark_dc, blocks_for(c->ndc), NTHREADS, (const unsigned*)c->dclist.p, c->ndc,
+                   (uint8_t*)c->pflags.p);
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->stream));
+    c->have_particles = true;
+    return MPM_OK;
+}
+
+int mpm_upload_dc_list(mpm_ctx* c, const uint32_t* idx, int64_t n) {
+    if (!c) return MPM_ERR_ARG;
+    if (n < 0 || (n > 0 && !idx)) return fail(c, MPM_ERR_ARG, "bad displacement-control list");
+    if (!c->have_particles && n > 0) return fail(c, MPM_ERR_STATE, "upload particles before the dc list");
+    std::vector<uint32_t> sorted(idx, idx + n);
+    std::sort(sorted.begin(), sorted.end());
+    for (int64_t i = 0; i < n; ++i) {
+        if (sorted[i] >= (uint64_t)c->n) return fail(c, MPM_ERR_ARG, "dc index %u out of range", sorted[i]);
+        if (i > 0 && sorted[i] == sorted[i - 1]) return fail(c, MPM_ERR_ARG, "duplicate dc index %u", sorted[i]);
+    }
+    int rc = ensure(c, c->dclist, (size_t)std::max<int64_t>(1, n) * 4);
+    if (rc) return rc;
+    if (c->n > 0)
+        LAUNCH("fill", k_clear_flag, blocks_for(c->n), NTHREADS, (uint8_t*)c->pflags.p, c->n, (uint8_t)PF_IN_DC);
+    if (n > 0) {
+        CK(cudaMemcpyAsync(c->dclist.p, idx, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
+        LAUNCH("fill", k_mark_dc, blocks_for(n), NTHREADS, (const unsigned*)c->dclist.p, (int)n,
+               (uint8_t*)c->pflags.p);
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    c->ndc = (int)n;
+    return MPM_OK;
+}
+
+int mpm_upload_nodes(mpm_ctx* c, const mpm_nodes* nd) {
+    if (!c) return MPM_ERR_ARG;
+    if (!nd) return fail(c, MPM_ERR_ARG, "null node view");
+    const long long nn = c->nn;
+    const bool f64 = c->form == MPM_FORM_FP64;
+    int rc;
+    if (nd->fixed)
+        CK(cudaMemcpyAsync(c->g_fixed.p, nd->fixed, (size_t)nn, cudaMemcpyHostToDevice, c->stream));
+    if (nd->friction)
+        CK(cudaMemcpyAsync(c->g_friction.p, nd->friction, (size_t)nn * 8, cudaMemcpyHostToDevice, c->stream));
+    struct {
+        DevBuf* b;
+        const double* h;
+        int k;
+        bool fp64;
+    } fields[] = {{&c->g_mass, nd->mass, 1, f64},  {&c->g_mom, nd->mom, 3, f64},
+                  {&c->g_vel, nd->vel, 3, f64},    {&c->g_force, nd->force, 3, f64},
+                  {&c->g_ftemp, nd->force_temp, 3, f64}, {&c->g_mg, nd->mass_gradient, 3, true}};
+    for (auto& f : fields)
+        if (f.h && (rc = upload_field(c, *f.b, f.h, nn, f.k, f.fp64, 0.0))) return rc;
+    if (nd->state) {
+        int rc2 = ensure(c, c->staging, (size_t)nn);
+        if (rc2) return rc2;
+        CK(cudaMemcpyAsync(c->staging.p, nd->state, (size_t)nn, cudaMemcpyHostToDevice, c->stream));
+        LAUNCH("unpack", k_state_u8_to_u32, blocks_for(nn), NTHREADS, (const uint8_t*)c->staging.p,
+               (unsigned*)c->g_state.p, nn);
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->stream));
+    c->have_nodes = true;
+    return MPM_OK;
+}
+
+int mpm_set_timeline(mpm_ctx* c, const double* t, const double* v3, int32_t n) {
+    if (!c) return MPM_ERR_ARG;
+    if (n < 0 || (n > 0 && (!t || !v3))) return fail(c, MPM_ERR_ARG, "bad timeline");
+    c->tl_t.assign(t, t + n);
+    c->tl_v.assign(v3, v3 + 3 * (size_t)n);
+    return MPM_OK;
+}
+
+int mpm_set_sim(mpm_ctx* c, const mpm_sim* s) {
+    if (!c || !s) return MPM_ERR_ARG;
+    c->sim = *s;
+    return MPM_OK;
+}
+
+int mpm_get_sim(const mpm_ctx* c, mpm_sim* s) {
+    if (!c || !s) return MPM_ERR_ARG;
+    *s = c->sim;
+    return MPM_OK;
+}
+
+int mpm_download_particles(mpm_ctx* c, mpm_particles* p) {
+    if (!c || !p) return MPM_ERR_ARG;
+    const long long n = c->n;
+    const bool f64 = c->form == MPM_FORM_FP64;
+    int rc;
+    struct {
+        DevBuf* b;
+        double* h;
+        int k;
+        bool fp64;
+    } fields[] = {{&c->pos, p->pos, 3, true},
+                  {&c->vel, p->vel, 3, f64},
+                  {&c->fext, p->fext, 3, f64},
+                  {&c->mass, p->mass, 1, f64},
+                  {&c->vol, p->vol, 1, f64},
+                  {&c->vol0, p->vol0, 1, f64},
+                  {&c->F, p->F, 9, f64},
+                  {&c->stress, p->stress, 6, f64},
+                  {&c->strain, p->strain, 6, f64},
+                  {&c->eps_p, p->eps_p, 6, f64},
+                  {&c->e_strain, p->e_strain, 1, true},
+                  {&c->e_strain_max, p->e_strain_max, 1, true},
+                  {&c->e_strain_ti, p->e_strain_ti, 1, true},
+                  {&c->e_plastic, p->e_plastic, 1, true},
+                  {&c->backstress, p->backstress, 1, f64},
+                  {&c->mp_mg, p->mp_mass_gradient, 3, true},
+                  {&c->strain_rate, p->strain_rate, 6, f64}};
+    for (auto& f : fields) {
+        if (!f.h) continue;
+        if ((rc = download_field(c, *f.b, f.h, n, f.k, f.fp64))) return rc;
+        CK(cudaStreamSynchronize(c->stream));  // staging is reused by the next field
+    }
+    if (n > 0) {
+        if (p->material)
+            CK(cudaMemcpyAsync(p->material, c->material.p, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
+        if (p->pflags) {
+            CK(cudaMemcpyAsync(p->pflags, c->pflags.p, (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+        }
+        if (p->dc_mult)
+            CK(cudaMemcpyAsync(p->dc_mult, c->dc_mult.p, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    if (p->pflags)
+        for (long long i = 0; i < n; ++i) p->pflags[i] &= (uint8_t)~PF_IN_DC;
+    return check_device_error(c);
+}
+
+int mpm_download_nodes(mpm_ctx* c, mpm_nodes* nd) {
+    if (!c || !nd) return MPM_ERR_ARG;
+    const long long nn = c->nn;
+    const bool f64 = c->form == MPM_FORM_FP64;
+    int rc;
+    struct {
+        DevBuf* b;
+        double* h;
+        int k;
+        bool fp64;
+    } fields[] = {{&c->g_mass, nd->mass, 1, f64},  {&c->g_mom, nd->mom, 3, f64},
+                  {&c->g_vel, nd->vel, 3, f64},    {&c->g_force, nd->force, 3, f64},
+                  {&c->g_ftemp, nd->force_temp, 3, f64}, {&c->g_mg, nd->mass_gradient, 3, true}};
+    for (auto& f : fields) {
+        if (!f.h) continue;
+        if ((rc = download_field(c, *f.b, f.h, nn, f.k, f.fp64))) return rc;
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    if (nd->fixed) CK(cudaMemcpyAsync(nd->fixed, c->g_fixed.p, (size_t)nn, cudaMemcpyDeviceToHost, c->stream));
+    if (nd->friction)
+        CK(cudaMemcpyAsync(nd->friction, c->g_friction.p, (size_t)nn * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (nd->state) {
+        if ((rc = ensure(c, c->staging, (size_t)nn))) return rc;
+        LAUNCH("pack", k_state_u32_to_u8, blocks_for(nn), NTHREADS, (const unsigned*)c->g_state.p,
+               (uint8_t*)c->staging.p, nn);
+        CK(cudaMemcpyAsync(nd->state, c->staging.p, (size_t)nn, cudaMemcpyDeviceToHost, c->stream));
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    return check_device_error(c);
+}
+
+int mpm_advance(mpm_ctx* c, int32_t nsteps, double dt, int contact) {
+    if (!c) return MPM_ERR_ARG;
+    if (nsteps < 0 || !(dt > 0.0) || !std::isfinite(dt)) return fail(c, MPM_ERR_ARG, "bad step request");
+    if (!c->have_particles) return fail(c, MPM_ERR_STATE, "no particles uploaded");
+    if (c->nmat <= 0 && c->n > 0) return fail(c, MPM_ERR_STATE, "no materials uploaded");
+    for (int s = 0; s < nsteps; ++s) {
+        int rc = step(c, dt, contact ? 1 : 0);
+        if (rc) return rc;
+    }
+    return MPM_OK;
+}
+
+int mpm_run(mpm_ctx* c, double dt_total, int contact, int* done) {
+    if (!c) return MPM_ERR_ARG;
+    if (!(dt_total >= 0.0)) return fail(c, MPM_ERR_ARG, "bad dt_total");
+    // …MPLocks.cpp:449-458
+    double acc = 0.0;
+    while (acc < dt_total) {
+        double dt = c->sim.dt_max;
+        if (c->sim.dt_max > (dt_total - acc)) dt = dt_total - acc;
+        acc += dt;
+        int rc = mpm_advance(c, 1, dt, contact);
+        if (rc) return rc;
+    }
+    int rc = mpm_synchronize(c);
+    if (rc) return rc;
+    if (done) *done = c->sim.time < c->sim.time_end ? 0 : 1;
+    return MPM_OK;
+}
+
+int mpm_synchronize(mpm_ctx* c) {
+    if (!c) return MPM_ERR_ARG;
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaGetLastError());
+    return check_device_error(c);
+}
+
+int mpm_advance_timed(mpm_ctx* c, int32_t nsteps, double dt, int contact, float* ms) {
+    if (!c) return MPM_ERR_ARG;
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    CK(cudaEventRecord(a, c->stream));
+    int rc = mpm_advance(c, nsteps, dt, contact);
+    cudaEventRecord(b, c->stream);
+    cudaEventSynchronize(b);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (ms) *ms = t;
+    if (rc) return rc;
+    return check_device_error(c);
+}
+
+int mpm_cell_order(mpm_ctx* c, uint32_t* keys, uint32_t* sorted_order, int64_t n) {
+    if (!c) return MPM_ERR_ARG;
+    if (n != c->n) return fail(c, MPM_ERR_ARG, "n = %lld, engine holds %lld particles", (long long)n, c->n);
+    if (!c->last_perm && n > 0) return fail(c, MPM_ERR_STATE, "no step has run yet");
+    if (n > 0 && keys) CK(cudaMemcpyAsync(keys, c->keys_copy.p, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
+    if (n > 0 && sorted_order)
+        CK(cudaMemcpyAsync(sorted_order, c->last_perm, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return MPM_OK;
+}
+
+int mpm_profile_read(mpm_ctx* c, mpm_kernel_stat* out, int32_t max, int32_t* count) {
+    if (!c) return MPM_ERR_ARG;
+    int rc = prof_resolve(c);
+    if (rc) return rc;
+    int n = (int)c->prof_names.size();
+    if (count) *count = n;
+    for (int i = 0; i < n && i < max && out; ++i) {
+        memset(out[i].name, 0, sizeof(out[i].name));
+        strncpy(out[i].name, c->prof_names[i].c_str(), sizeof(out[i].name) - 1);
+        out[i].launches = c->prof_cnt[i];
+        out[i].total_ms = c->prof_ms[i];
+    }
+    return MPM_OK;
+}
+
+int mpm_profile_reset(mpm_ctx* c) {
+    if (!c) return MPM_ERR_ARG;
+    int rc = prof_resolve(c);
+    if (rc) return rc;
+    std::fill(c->prof_ms.begin(), c->prof_ms.end(), 0.0);
+    std::fill(c->prof_cnt.begin(), c->prof_cnt.end(), 0LL);
+    return MPM_OK;
+}
+
+int mpm_launch_count(const mpm_ctx* c, int64_t* count) {
+    if (!c || !count) return MPM_ERR_ARG;
+    *count = c->launches;
+    return MPM_OK;
+}
+
+}  // extern "C"

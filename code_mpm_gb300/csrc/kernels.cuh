@@ -1,0 +1,784 @@
+// Step kernels of the GB300 MPM engine.  One step of the reference's
+// double-pass loop (PhysicsEngine_runSimulation_Classic_DoublePass_MPLocks.cpp:462-792,
+// contact variant PhysicsEngine_runSimulation_Classic_DoublePass_MPLocks_Contact.cpp:27-543)
+// maps onto:
+//   k_reset_grid        ResetGrid (:4-22)
+//   k_cell_keys         FindAGPs cell lookup, floor(x/h) (GridPoint_Mediator.cpp:8)
+//   radix sort          particles ordered by cell key
+//   k_cell_ranges       active-node marking (b_Active, :36) + per-cell particle ranges
+//   k_p2g               M2G (:48-89): warp-segmented reduction, then one atomic per run
+//   k_dc_claim/apply    DisplacementControl (:143-174), last writer in list order
+//   k_grid_update       IntegrateGrid (:90-142; contact :242-277)
+//   k_node_ratio        f/m per node (the divisor of G2P pass 1)
+//   k_pass1_remap       G2P pass 1 (:489-510) fused with the velocity remap (:539-564)
+//   k_node_remap        v_i += (sum N m_p v_p) / m_i
+//   k_node_bc           BC reapply (:573-599)
+//   k_pass2             G2P_P2_SmallStrain (:175-280; contact :438-525) fused with the
+//                       constitutive increment and the platen timeline (:766-789)
+//   k_contact_*         contact detection (…_Contact.cpp:152-237), bit-exact
+#pragma once
+
+#include "common.cuh"
+#include "physics.cuh"
+
+namespace mpm {
+
+// ---------------------------------------------------------------------------
+// grid reset: zero every node that was active (the reference only clears
+// active nodes; inactive ones are already zero).
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_reset_grid(NView<T> nd, int contact) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= nd.nn) return;
+    unsigned st = nd.state[i];
+    if (!(st & 1u)) return;
+    const long long nn = nd.nn;
+    nd.state[i] = contact ? 0u : (st & ~1u);
+    nd.mass[i] = (T)0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        if (contact) nd.mg[c * nn + i] = 0.0;
+        nd.vel[c * nn + i] = (T)0;
+        nd.mom[c * nn + i] = (T)0;
+        nd.force[c * nn + i] = (T)0;
+        nd.ftemp[c * nn + i] = (T)0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// cell keys: base cell b = floor(x/h) per axis with the IEEE quotient, as
+// glm::floor(d3Position / d3_Length_Cell) (GridPoint_Mediator.cpp:8), so the
+// cell index is bit-identical to the reference.  Particles whose base cell
+// lies outside [-1, cells] have no node in range and get key_max.
+// ---------------------------------------------------------------------------
+__global__ void k_cell_keys(const double* __restrict__ pos, long long n, Geom g, unsigned* __restrict__ keys,
+                            unsigned* __restrict__ vals, unsigned* __restrict__ keys_copy, unsigned* err) {
+    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    bool ok = true;
+    int b[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        double q = __ddiv_rn(pos[a * n + p], g.h[a]);
+        if (!isfinite(q)) {
+            atomicOr(err, ERR_NONFINITE_POSITION);
+            ok = false;
+            b[a] = 0;
+            continue;
+        }
+        double f = floor(q);
+        if (f < -1.0 || f > (double)(g.nn[a] - 1)) ok = false;
+        b[a] = ok ? (int)f : 0;
+    }
+    unsigned key = ok ? (unsigned)((b[0] + 1) + g.kd[0] * ((b[1] + 1) + g.kd[1] * (b[2] + 1))) : g.key_max;
+    keys[p] = key;
+    keys_copy[p] = key;
+    vals[p] = (unsigned)p;
+}
+
+// ---------------------------------------------------------------------------
+// Active nodes (the union of the in-range corners of every occupied cell) and
+// per-cell [start, end) ranges in sorted order.
+// ---------------------------------------------------------------------------
+__global__ void k_cell_ranges(const unsigned* __restrict__ skeys, long long n, Geom g, unsigned* __restrict__ state,
+                              unsigned* __restrict__ cstart, unsigned* __restrict__ cend) {
+    long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    unsigned key = skeys[s];
+    if (key >= g.key_max) return;
+    if (s == 0 || skeys[s - 1] != key) {
+        if (cstart) cstart[key] = (unsigned)s;
+        int b[3];
+        key_to_base(key, g, b);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            long long nid = corner_node(g, b, k);
+            if (nid >= 0) atomicOr(&state[nid], 1u);
+        }
+    }
+    if (cend && (s == n - 1 || skeys[s + 1] != key)) cend[key] = (unsigned)(s + 1);
+}
+
+// ---------------------------------------------------------------------------
+// Warp-segmented inclusive sum over runs of equal keys (sorted order puts a
+// cell's particles in adjacent lanes); the run's last lane ends with the total.
+// ---------------------------------------------------------------------------
+struct Runs {
+    int lane, head_lane, maxrun;
+    bool tail;
+    __device__ __forceinline__ void init(unsigned key) {
+        lane = threadIdx.x & 31;
+        unsigned kp = __shfl_up_sync(FULL_MASK, key, 1);
+        unsigned kn = __shfl_down_sync(FULL_MASK, key, 1);
+        bool head = (lane == 0) || (kp != key);
+        tail = (lane == 31) || (kn != key);
+        unsigned hm = __ballot_sync(FULL_MASK, head);
+        head_lane = 31 - __clz(hm & (0xffffffffu >> (31 - lane)));
+        maxrun = __reduce_max_sync(FULL_MASK, (unsigned)(lane - head_lane + 1));
+    }
+    template <typename T>
+    __device__ __forceinline__ T sum(T v) const {
+        for (int off = 1; off < maxrun; off <<= 1) {
+            T o = __shfl_up_sync(FULL_MASK, v, off);
+            if (lane - off >= head_lane) v += o;
+        }
+        return v;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// P2G (M2G, …MPLocks.cpp:48-89): per particle and corner, mass N m, momentum
+// N (m v), force -V (grad N . sigma) + N f_ext (Voigt order xx yy zz xy yz zx,
+// :79-84).  One thread per sorted slot; contributions of a cell's particles
+// are summed across lanes before one atomic per (node, field).
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) k_p2g(PView<T> P, NView<T> nd, Geom g, const unsigned* __restrict__ skeys,
+                                             const unsigned* __restrict__ perm, long long n) {
+    long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    unsigned key = (s < n) ? skeys[s] : 0xffffffffu;
+    const bool valid = key < g.key_max;
+    Runs run;
+    run.init(key);
+    const long long np = P.n, nn = nd.nn;
+    int b[3] = {0, 0, 0};
+    Bases<T> B;
+    T m = 0, V = 0, v[3] = {0, 0, 0}, sg[6] = {0, 0, 0, 0, 0, 0}, fe[3] = {0, 0, 0};
+    if (valid) {
+        long long p = perm[s];
+        key_to_base(key, g, b);
+        double x[3] = {P.pos[p], P.pos[np + p], P.pos[2 * np + p]};
+        B.init(g, x, b);
+        m = P.mass[p];
+        V = P.vol[p];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            v[c] = P.vel[c * np + p];
+            fe[c] = P.fext[c * np + p];
+        }
+#pragma unroll
+        for (int c = 0; c < 6; ++c) sg[c] = P.stress[c * np + p];
+    }
+    T mv[3] = {m * v[0], m * v[1], m * v[2]};
+#pragma unroll 1
+    for (int k = 0; k < 8; ++k) {
+        T N = 0, G[3] = {0, 0, 0};
+        if (valid) B.corner(k, N, G);
+        T c0 = N * m;
+        T c1 = N * mv[0], c2 = N * mv[1], c3 = N * mv[2];
+        T c4 = -V * (G[0] * sg[0] + G[1] * sg[3] + G[2] * sg[5]) + N * fe[0];
+        T c5 = -V * (G[1] * sg[1] + G[0] * sg[3] + G[2] * sg[4]) + N * fe[1];
+        T c6 = -V * (G[2] * sg[2] + G[0] * sg[5] + G[1] * sg[4]) + N * fe[2];
+        c0 = run.sum(c0);
+        c1 = run.sum(c1);
+        c2 = run.sum(c2);
+        c3 = run.sum(c3);
+        c4 = run.sum(c4);
+        c5 = run.sum(c5);
+        c6 = run.sum(c6);
+        if (valid && run.tail) {
+            long long nid = corner_node(g, b, k);
+            if (nid >= 0) {
+                atomicAdd(&nd.mass[nid], c0);
+                atomicAdd(&nd.mom[nid], c1);
+                atomicAdd(&nd.mom[nn + nid], c2);
+                atomicAdd(&nd.mom[2 * nn + nid], c3);
+                atomicAdd(&nd.force[nid], c4);
+                atomicAdd(&nd.force[nn + nid], c5);
+                atomicAdd(&nd.force[2 * nn + nid], c6);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Displacement control (…MPLocks.cpp:143-174; contact :283-297, :416-432).
+// The reference overwrites node velocity/momentum/force from each controlled
+// particle in list order, so a node shared by several keeps the last one's.
+// k_dc_claim records, per node and axis, the largest list position writing
+// it; k_dc_apply lets only that particle write.  contact: all three axes.
+// ---------------------------------------------------------------------------
+__global__ void k_dc_claim(const unsigned* __restrict__ dclist, int ndc, const unsigned* __restrict__ keys,
+                           const uint8_t* __restrict__ pflags, Geom g, unsigned* __restrict__ owner, long long nn,
+                           int contact) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= ndc) return;
+    unsigned p = dclist[k];
+    unsigned key = keys[p];
+    if (key >= g.key_max) return;
+    unsigned axes = contact ? 7u : (pflags[p] & 7u);
+    int b[3];
+    key_to_base(key, g, b);
+    for (int c8 = 0; c8 < 8; ++c8) {
+        long long nid = corner_node(g, b, c8);
+        if (nid < 0) continue;
+        for (int a = 0; a < 3; ++a)
+            if (axes & (1u << a)) atomicMax(&owner[a * nn + nid], (unsigned)k + 1u);
+    }
+}
+
+template <typename T>
+__global__ void k_dc_apply(const unsigned* __restrict__ dclist, int ndc, const unsigned* __restrict__ keys,
+                           PView<T> P, NView<T> nd, Geom g, int contact) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= ndc) return;
+    unsigned p = dclist[k];
+    unsigned key = keys[p];
+    if (key >= g.key_max) return;
+    const long long nn = nd.nn, np = P.n;
+    unsigned axes = contact ? 7u : (P.pflags[p] & 7u);
+    int b[3];
+    key_to_base(key, g, b);
+    for (int c8 = 0; c8 < 8; ++c8) {
+        long long nid = corner_node(g, b, c8);
+        if (nid < 0) continue;
+        for (int a = 0; a < 3; ++a) {
+            if (!(axes & (1u << a)) || nd.owner[a * nn + nid] != (unsigned)k + 1u) continue;
+            T vp = P.vel[a * np + p];
+            nd.vel[a * nn + nid] = vp;
+            nd.mom[a * nn + nid] = nd.mass[nid] * vp;
+            nd.force[a * nn + nid] = (T)0;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Grid momentum update with boundary conditions (IntegrateGrid,
+// …MPLocks.cpp:90-142).  Non-contact order: damping, x-wall Coulomb friction
+// on y (:106-124), zero fixed axes (y-fixed nodes accumulate the reaction
+// force, :129), then p += f dt.  Contact order (…_Contact.cpp:250-276):
+// damping, p += f dt, then zero fixed axes; optionally Coulomb friction on
+// the x/y tangents of z-fixed nodes (floor_friction, an extension).
+// Damping is skipped when its coefficient is zero (f - 0*x == f).
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ void coulomb(T p_t, T& f_t, T fn, T mu, T dt) {
+    T trial = p_t + f_t * dt;
+    T ff = mu * (T)((T(0) < -trial) - (-trial < T(0))) * fabs(fn);
+    if (fabs(ff * dt) > fabs(trial)) ff *= fabs(trial / dt) / fabs(ff);
+    f_t += ff;
+}
+
+template <typename T>
+__global__ void k_grid_update(NView<T> nd, T dt, double damping, int contact, int floor_friction) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= nd.nn || !(nd.state[i] & 1u)) return;
+    const long long nn = nd.nn;
+    T p[3], f[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        p[c] = nd.mom[c * nn + i];
+        f[c] = nd.force[c * nn + i];
+    }
+    const unsigned fx = nd.fixed[i];
+    if (damping != 0.0) {
+        T pp = p[0] * p[0] + p[1] * p[1] + p[2] * p[2];
+        if (sqrt(pp) > (T)1.0e-24) {
+            T inv = (T)1 / sqrt(pp);
+            T nrm[3] = {p[0] * inv, p[1] * inv, p[2] * inv};
+            T sc = (T)damping * fabs(f[0] * nrm[0] + f[1] * nrm[1] + f[2] * nrm[2]);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) f[c] = f[c] - sc * nrm[c];
+        }
+    }
+    bool zero[3] = {false, false, false};
+    T ft_y = 0;
+    if (!contact) {
+        if (fx & 1u) {
+            T trial_y = p[1] + f[1] * dt;
+            if (fabs(trial_y * dt) > (T)1.0e-24 && f[0] > (T)0) coulomb<T>(p[1], f[1], f[0], (T)nd.friction[i], dt);
+            zero[0] = true;
+            p[0] = 0;
+            f[0] = 0;
+        }
+        if (fx & 2u) {
+            ft_y = f[1];
+            zero[1] = true;
+            p[1] = 0;
+            f[1] = 0;
+        }
+        if (fx & 4u) {
+            zero[2] = true;
+            p[2] = 0;
+            f[2] = 0;
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) p[c] = p[c] + f[c] * dt;
+    } else {
+        if (floor_friction && (fx & 4u) && nd.friction[i] > 0.0 && f[2] < (T)0) {
+            T fz = f[2], mu = (T)nd.friction[i];
+#pragma unroll
+            for (int t = 0; t < 2; ++t) {
+                T trial = p[t] + f[t] * dt;
+                if (fabs(trial * dt) > (T)1.0e-24) coulomb<T>(p[t], f[t], fz, mu, dt);
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) p[c] = p[c] + f[c] * dt;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            if (fx & (1u << c)) {
+                if (c == 1) ft_y = f[1];
+                zero[c] = true;
+                p[c] = 0;
+                f[c] = 0;
+            }
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        nd.mom[c * nn + i] = p[c];
+        nd.force[c * nn + i] = f[c];
+        if (zero[c]) nd.vel[c * nn + i] = (T)0;
+    }
+    if (fx & 2u) nd.ftemp[nn + i] += ft_y;
+}
+
+// ratio = src / m for nodes with m > mass_min (else 0).  src = force before
+// pass 1 (the f_i/m_i of …MPLocks.cpp:508), momentum before pass 2 (:198).
+// Also clears the remap accumulator when asked.
+template <typename T>
+__global__ void k_node_ratio(NView<T> nd, const T* __restrict__ src, double mass_min, int clear_q) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= nd.nn) return;
+    const long long nn = nd.nn;
+    if (!(nd.state[i] & 1u)) return;
+    T m = nd.mass[i];
+    bool has = (double)m > mass_min;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        nd.ratio[c * nn + i] = has ? src[c * nn + i] / m : (T)0;
+        if (clear_q) nd.q[c * nn + i] = (T)0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// G2P pass 1 (…MPLocks.cpp:489-510): v_p += N (f_i/m_i) dt over the corners
+// in findAdjacentGridPoints order, fused with the velocity remap (:539-564):
+// each particle then scatters N m_p v_p, summed per run before the atomic.
+// Contact path: particles flagged b_DisplacementControl are skipped.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) k_pass1_remap(PView<T> P, NView<T> nd, Geom g,
+                                                     const unsigned* __restrict__ skeys,
+                                                     const unsigned* __restrict__ perm, long long n, T dt,
+                                                     double mass_min, int contact) {
+    long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    unsigned key = (s < n) ? skeys[s] : 0xffffffffu;
+    Runs run;
+    run.init(key);
+    bool valid = key < g.key_max;
+    const long long np = P.n, nn = nd.nn;
+    long long p = 0;
+    if (valid) {
+        p = perm[s];
+        if (contact && (P.pflags[p] & 8u)) valid = false;
+    }
+    int b[3] = {0, 0, 0};
+    Bases<T> B;
+    T m = 0, v[3] = {0, 0, 0};
+    if (valid) {
+        key_to_base(key, g, b);
+        double x[3] = {P.pos[p], P.pos[np + p], P.pos[2 * np + p]};
+        B.init(g, x, b);
+        m = P.mass[p];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) v[c] = P.vel[c * np + p];
+#pragma unroll 1
+        for (int k = 0; k < 8; ++k) {
+            long long nid = corner_node(g, b, k);
+            if (nid < 0) continue;
+            if (!((double)nd.mass[nid] > mass_min)) continue;
+            T N, G[3];
+            B.corner(k, N, G);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) v[c] = v[c] + N * nd.ratio[c * nn + nid] * dt;
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) P.vel[c * np + p] = v[c];
+    }
+    T mv[3] = {m * v[0], m * v[1], m * v[2]};
+#pragma unroll 1
+    for (int k = 0; k < 8; ++k) {
+        T N = 0, G[3];
+        if (valid) B.corner(k, N, G);
+        T q0 = run.sum(N * mv[0]);
+        T q1 = run.sum(N * mv[1]);
+        T q2 = run.sum(N * mv[2]);
+        if (valid && run.tail) {
+            long long nid = corner_node(g, b, k);
+            if (nid >= 0) {
+                atomicAdd(&nd.q[nid], q0);
+                atomicAdd(&nd.q[nn + nid], q1);
+                atomicAdd(&nd.q[2 * nn + nid], q2);
+            }
+        }
+    }
+}
+
+// Remap finish: v_i += q_i / m_i on nodes with m_i > mass_min (:559-560).
+template <typename T>
+__global__ void k_node_remap(NView<T> nd, double mass_min) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= nd.nn || !(nd.state[i] & 1u)) return;
+    const long long nn = nd.nn;
+    T m = nd.mass[i];
+    if (!((double)m > mass_min)) return;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) nd.vel[c * nn + i] += nd.q[c * nn + i] / m;
+}
+
+// BC reapply (:573-599): zero the fixed components of v, p and f.
+template <typename T>
+__global__ void k_node_bc(NView<T> nd) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= nd.nn || !(nd.state[i] & 1u)) return;
+    const long long nn = nd.nn;
+    unsigned fx = nd.fixed[i];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        if (fx & (1u << c)) {
+            nd.vel[c * nn + i] = (T)0;
+            nd.mom[c * nn + i] = (T)0;
+            nd.force[c * nn + i] = (T)0;
+        }
+    }
+}
+
+// TimeLine::getVelocity (TimeLine.h:33-46) is evaluated on the host each step
+// and passed in as tv.
+struct StepArgs {
+    double dt;
+    double mass_min;
+    double tv[3];
+    int has_timeline;
+    int contact;
+};
+
+// ---------------------------------------------------------------------------
+// G2P pass 2 + constitutive update + platen (G2P_P2_SmallStrain,
+// …MPLocks.cpp:175-280; contact …_Contact.cpp:438-525 and :531-540).
+// One thread per particle in index order (coalesced particle streams).
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) k_pass2(PView<T> P, NView<T> nd, Geom g, const unsigned* __restrict__ keys,
+                                               const MatConst* __restrict__ mats, int nmat, StepArgs a,
+                                               unsigned* err) {
+    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long np = P.n, nn = nd.nn;
+    if (p >= np) return;
+    const unsigned fl = P.pflags[p];
+    const T dt = (T)a.dt;
+    const bool skip = a.contact && (fl & 8u);
+    if (!skip) {
+        unsigned key = keys[p];
+        double x[3] = {P.pos[p], P.pos[np + p], P.pos[2 * np + p]};
+        T L[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) L[k] = 0;
+        if (key < g.key_max) {
+            int b[3];
+            key_to_base(key, g, b);
+            Bases<T> B;
+            B.init(g, x, b);
+            const double ddt = a.dt;
+#pragma unroll 1
+            for (int k = 0; k < 8; ++k) {
+                long long nid = corner_node(g, b, k);
+                if (nid < 0) continue;
+                T N, G[3];
+                B.corner(k, N, G);
+                if ((double)nd.mass[nid] > a.mass_min) {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) x[c] = x[c] + (double)(N * nd.ratio[c * nn + nid]) * ddt;
+                }
+                T vi[3] = {nd.vel[nid], nd.vel[nn + nid], nd.vel[2 * nn + nid]};
+                // outerProduct(v_i, grad N): column c, row r = v_i[r] * G[c]
+#pragma unroll
+                for (int c = 0; c < 3; ++c)
+#pragma unroll
+                    for (int r = 0; r < 3; ++r) L[3 * c + r] += vi[r] * G[c];
+            }
+#pragma unroll
+            for (int c = 0; c < 3; ++c) P.pos[c * np + p] = x[c];
+        }
+        // strain increment: (1 + L_ii dt) - 1 on the diagonal, (L_ij + L_ji) dt off it
+        T Ldt[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Ldt[k] = L[k] * dt;
+        T e[6];
+        e[0] = ((T)1 + Ldt[0]) - (T)1;
+        e[1] = ((T)1 + Ldt[4]) - (T)1;
+        e[2] = ((T)1 + Ldt[8]) - (T)1;
+        e[3] = Ldt[1] + Ldt[3];
+        e[4] = Ldt[5] + Ldt[7];
+        e[5] = Ldt[6] + Ldt[2];
+        int mi = P.material[p];
+        T F[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) F[k] = P.F[k * np + p];
+        T Fn[9];
+        if (!a.contact) {
+            // F <- F * dF, dF = I + L dt (glm column-major product)
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    T d0 = (c == 0 ? (T)1 : (T)0) + Ldt[3 * c + 0];
+                    T d1 = (c == 1 ? (T)1 : (T)0) + Ldt[3 * c + 1];
+                    T d2 = (c == 2 ? (T)1 : (T)0) + Ldt[3 * c + 2];
+                    Fn[3 * c + r] = F[r] * d0 + F[3 + r] * d1 + F[6 + r] * d2;
+                }
+        } else {
+            // F <- F + (L F) dt
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+#pragma unroll
+                for (int r = 0; r < 3; ++r)
+                    Fn[3 * c + r] = F[3 * c + r] + (L[r] * F[3 * c] + L[3 + r] * F[3 * c + 1] + L[6 + r] * F[3 * c + 2]) * dt;
+            // contact: strain is accumulated before the material check (…_Contact.cpp:483-484)
+#pragma unroll
+            for (int k = 0; k < 6; ++k) P.strain[k * np + p] += e[k];
+#pragma unroll
+            for (int k = 0; k < 9; ++k) P.F[k * np + p] = Fn[k];
+            T det = Fn[0] * (Fn[4] * Fn[8] - Fn[7] * Fn[5]) - Fn[3] * (Fn[1] * Fn[8] - Fn[7] * Fn[2]) +
+                    Fn[6] * (Fn[1] * Fn[5] - Fn[4] * Fn[2]);
+            P.vol[p] = det * P.vol0[p];
+        }
+        if (mi >= 0 && mi < nmat) {
+            const MatConst& M = mats[mi];
+            T sig[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) sig[k] = P.stress[k * np + p];
+            T R = P.backstress[p];
+            CrOut<T> o;
+            cr_increment<T>(M, R, sig, e, o);
+            T V;
+            if (!a.contact) {
+#pragma unroll
+                for (int k = 0; k < 9; ++k) P.F[k * np + p] = Fn[k];
+                T det = Fn[0] * (Fn[4] * Fn[8] - Fn[7] * Fn[5]) - Fn[3] * (Fn[1] * Fn[8] - Fn[7] * Fn[2]) +
+                        Fn[6] * (Fn[1] * Fn[5] - Fn[4] * Fn[2]);
+                V = det * P.vol0[p];
+                P.vol[p] = V;
+#pragma unroll
+                for (int k = 0; k < 6; ++k) P.strain[k * np + p] += e[k];
+            } else {
+                V = P.vol[p];
+#pragma unroll
+                for (int k = 0; k < 6; ++k) P.strain_rate[k * np + p] = e[k] / dt;
+            }
+            double dEs = 0.0, dEp = 0.0;
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                T sn = sig[k] + o.dsig[k];
+                P.stress[k * np + p] = sn;
+                P.eps_p[k * np + p] += o.deps_p[k];
+                if (!a.contact) {
+                    T mid = sn - (T)0.5 * o.dsig[k];
+                    dEs += (double)(mid * e[k] * V);
+                    dEp += (double)(mid * o.deps_p[k] * V);
+                } else {
+                    dEs += (double)(sn * e[k] * V);
+                    dEp += (double)(sn * o.deps_p[k] * V);
+                }
+            }
+            double es = P.e_strain[p] + dEs;
+            P.e_strain[p] = es;
+            if (!a.contact) {
+                P.e_strain_ti[p] += es * a.dt;
+                if (es > P.e_strain_max[p]) P.e_strain_max[p] = es;
+            }
+            P.e_plastic[p] += dEp;
+            P.backstress[p] = R + o.dR;
+        } else if (!a.contact) {
+            atomicOr(err, ERR_BAD_MATERIAL);
+        }
+    }
+    // platen timeline (…MPLocks.cpp:766-789; contact :531-540)
+    if (fl & PF_IN_DC) {
+        if (!a.contact) {
+            if (a.has_timeline) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c)
+                    if (fl & (1u << c)) P.vel[c * np + p] = (T)((double)P.dc_mult[p] * a.tv[c]);
+            }
+        } else {
+            double vv[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                vv[c] = a.has_timeline ? (double)P.dc_mult[p] * a.tv[c] : (double)P.vel[c * np + p];
+                P.vel[c * np + p] = (T)vv[c];
+                P.pos[c * np + p] += vv[c] * a.dt;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Contact detection (…_Contact.cpp:152-237), bit-exact.
+// Node mass gradients sum grad N m_p over all particles; the reference adds
+// them in particle index order (one thread), and the max-norm selection that
+// follows is sensitive to the last bit.  Only nodes adjacent to surface
+// particles are ever read, so those nodes are summed here by one thread each,
+// merging the (index-ordered) particle ranges of the eight surrounding cells
+// in index order, with the reference's exact per-pair gradient.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_contact_need(PView<T> P, const unsigned* __restrict__ keys, Geom g, unsigned* __restrict__ need) {
+    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (p >= P.n || !(P.pflags[p] & 16u)) return;
+    unsigned key = keys[p];
+    if (key >= g.key_max) return;
+    int b[3];
+    key_to_base(key, g, b);
+    for (int k = 0; k < 8; ++k) {
+        long long nid = corner_node(g, b, k);
+        if (nid >= 0) need[nid] = 1u;
+    }
+}
+
+template <typename T>
+__global__ void k_contact_mass_gradient(PView<T> P, NView<T> nd, Geom g, const unsigned* __restrict__ need,
+                                        const unsigned* __restrict__ perm, const unsigned* __restrict__ cstart,
+                                        const unsigned* __restrict__ cend) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= nd.nn || !need[i]) return;
+    const long long np = P.n, nn = nd.nn;
+    int node[3];
+    node[0] = (int)(i % g.nn[0]);
+    node[1] = (int)((i / g.nn[0]) % g.nn[1]);
+    node[2] = (int)(i / ((long long)g.nn[0] * g.nn[1]));
+    unsigned cur[8], end[8];
+    int nc = 0;
+    for (int k = 0; k < 8; ++k) {
+        int cb[3] = {node[0] - ((k >> 2) & 1), node[1] - ((k >> 1) & 1), node[2] - (k & 1)};
+        unsigned key = (unsigned)((cb[0] + 1) + g.kd[0] * ((cb[1] + 1) + g.kd[1] * (cb[2] + 1)));
+        unsigned s0 = cstart[key], s1 = cend[key];
+        if (s1 > s0) {
+            cur[nc] = s0;
+            end[nc] = s1;
+            ++nc;
+        }
+    }
+    double gsum[3] = {0.0, 0.0, 0.0};
+    while (true) {
+        int best = -1;
+        unsigned bp = 0xffffffffu;
+        for (int c = 0; c < nc; ++c) {
+            if (cur[c] < end[c]) {
+                unsigned pp = perm[cur[c]];
+                if (pp < bp) {
+                    bp = pp;
+                    best = c;
+                }
+            }
+        }
+        if (best < 0) break;
+        cur[best]++;
+        double x[3] = {P.pos[bp], P.pos[np + bp], P.pos[2 * np + bp]};
+        double G[3];
+        exact_gradient(g, x, node, G);
+        double m = (double)P.mass[bp];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) gsum[c] = __dadd_rn(gsum[c], __dmul_rn(G[c], m));
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) nd.mg[c * nn + i] = gsum[c];
+}
+
+// Surface particle normal: the corner gradient of largest norm, first wins on ties (:156-172).
+template <typename T>
+__global__ void k_contact_mp_gradient(PView<T> P, NView<T> nd, Geom g, const unsigned* __restrict__ keys) {
+    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (p >= P.n || !(P.pflags[p] & 16u)) return;
+    const long long np = P.n, nn = nd.nn;
+    double gp[3] = {0.0, 0.0, 0.0};
+    unsigned key = keys[p];
+    if (key < g.key_max) {
+        int b[3];
+        key_to_base(key, g, b);
+        for (int k = 0; k < 8; ++k) {
+            long long nid = corner_node(g, b, k);
+            if (nid < 0) continue;
+            double gi[3] = {nd.mg[nid], nd.mg[nn + nid], nd.mg[2 * nn + nid]};
+            if (len3_rn(gi) > len3_rn(gp)) {
+                gp[0] = gi[0];
+                gp[1] = gi[1];
+                gp[2] = gi[2];
+            }
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) P.mp_mg[c * np + p] = gp[c];
+}
+
+// Reset the node mass gradient of active nodes (:177-186) and the normal claims.
+template <typename T>
+__global__ void k_contact_reset(NView<T> nd) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= nd.nn) return;
+    nd.nowner[i] = 0u;
+    if (!(nd.state[i] & 1u)) return;
+    const long long nn = nd.nn;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) nd.mg[c * nn + i] = 0.0;
+}
+
+// Node normal from surface particles with (x_i - x_p) . g_p > 0 (:191-210);
+// the reference overwrites in index order, so the largest index wins.
+template <typename T>
+__global__ void k_contact_normal(PView<T> P, NView<T> nd, Geom g, const unsigned* __restrict__ keys, int apply) {
+    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (p >= P.n || !(P.pflags[p] & 16u)) return;
+    const long long np = P.n, nn = nd.nn;
+    unsigned key = keys[p];
+    if (key >= g.key_max) return;
+    int b[3];
+    key_to_base(key, g, b);
+    double x[3] = {P.pos[p], P.pos[np + p], P.pos[2 * np + p]};
+    double gp[3] = {P.mp_mg[p], P.mp_mg[np + p], P.mp_mg[2 * np + p]};
+    for (int k = 0; k < 8; ++k) {
+        long long nid = corner_node(g, b, k);
+        if (nid < 0) continue;
+        int n3[3] = {b[0] + ((k >> 2) & 1), b[1] + ((k >> 1) & 1), b[2] + (k & 1)};
+        double d[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) d[c] = __dadd_rn(node_coord(g, c, n3[c]), -x[c]);
+        if (!(dot3_rn(d, gp) > 0.0)) continue;
+        if (!apply) {
+            atomicMax(&nd.nowner[nid], (unsigned)p + 1u);
+        } else if (nd.nowner[nid] == (unsigned)p + 1u) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) nd.mg[c * nn + nid] = gp[c];
+        }
+    }
+}
+
+// Contact flags (:215-237): g_i . g_p >= 0.001 |g_i| |g_p| -> positive, <= -tol -> negative.
+template <typename T>
+__global__ void k_contact_flags(PView<T> P, NView<T> nd, Geom g, const unsigned* __restrict__ keys) {
+    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (p >= P.n || !(P.pflags[p] & 16u)) return;
+    const long long np = P.n, nn = nd.nn;
+    unsigned key = keys[p];
+    if (key >= g.key_max) return;
+    int b[3];
+    key_to_base(key, g, b);
+    double gp[3] = {P.mp_mg[p], P.mp_mg[np + p], P.mp_mg[2 * np + p]};
+    const double lp = len3_rn(gp);
+    for (int k = 0; k < 8; ++k) {
+        long long nid = corner_node(g, b, k);
+        if (nid < 0) continue;
+        double gi[3] = {nd.mg[nid], nd.mg[nn + nid], nd.mg[2 * nn + nid]};
+        double tol = __dmul_rn(__dmul_rn(0.001, len3_rn(gi)), lp);
+        double dd = dot3_rn(gi, gp);
+        if (dd >= tol)
+            atomicOr(&nd.state[nid], 4u);
+        else if (dd <= -tol)
+            atomicOr(&nd.state[nid], 8u);
+    }
+}
+
+}  // namespace mpm

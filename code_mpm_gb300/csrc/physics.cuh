@@ -1,0 +1,172 @@
+// Per-particle physics shared by the step kernels: trilinear bases and the
+// constitutive increments.
+#pragma once
+
+#include "common.cuh"
+
+namespace mpm {
+
+// ---------------------------------------------------------------------------
+// Trilinear (tent) bases of calculateBases_Classic (GridPoint_Mediator.cpp:95-144)
+// for the two nodes b and b+1 along one axis.  N = 1 - |d/h| clamped to
+// [0,1]; the gradient factor is sign(d)/h when 1e-12 < |d/h| < 1 - 1e-12,
+// else 0.  Here d/h is formed as d * (1/h): within a few ulp of the
+// reference, which the parity tolerance covers.
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ void axis_bases(const Geom& g, int a, double x, int b, T N[2], T gf[2]) {
+#pragma unroll
+    for (int o = 0; o < 2; ++o) {
+        double d = x - node_coord(g, a, b + o);
+        T r = (T)(d * g.inv_h[a]);
+        T ar = r >= (T)0 ? r : -r;
+        T nv = (T)1 - ar;
+        if (nv < (T)0 || nv > (T)1) nv = (T)0;
+        N[o] = nv;
+        T s = (T)((d > 0.0) - (d < 0.0));
+        gf[o] = (ar > (T)1.0e-12 && ar < (T)(1.0 - 1.0e-12)) ? s * (T)g.inv_h[a] : (T)0;
+    }
+}
+
+template <typename T>
+struct Bases {
+    T Nx[2], Ny[2], Nz[2];
+    T gx[2], gy[2], gz[2];
+    __device__ __forceinline__ void init(const Geom& g, const double x[3], const int b[3]) {
+        axis_bases<T>(g, 0, x[0], b[0], Nx, gx);
+        axis_bases<T>(g, 1, x[1], b[1], Ny, gy);
+        axis_bases<T>(g, 2, x[2], b[2], Nz, gz);
+    }
+    // corner k = 4*ix + 2*iy + iz
+    __device__ __forceinline__ void corner(int k, T& N, T G[3]) const {
+        int ix = (k >> 2) & 1, iy = (k >> 1) & 1, iz = k & 1;
+        T nx = Nx[ix], ny = Ny[iy], nz = Nz[iz];
+        N = nx * ny * nz;
+        G[0] = -(ny * nz) * gx[ix];
+        G[1] = -(nx * nz) * gy[iy];
+        G[2] = -(nx * ny) * gz[iz];
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Bit-exact restatement of calculateBases_Classic's gradient for one
+// (particle, node) pair, used where results must match the reference to the
+// bit (contact mass gradients): IEEE division d/h and the reference's
+// association order, with the _rn intrinsics so nothing is contracted.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void exact_gradient(const Geom& g, const double x[3], const int node[3], double G[3]) {
+    double Nv[3], d[3], r[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        d[a] = __dadd_rn(x[a], -node_coord(g, a, node[a]));
+        r[a] = __ddiv_rn(d[a], g.h[a]);
+        double ar = r[a] >= 0.0 ? r[a] : -r[a];
+        Nv[a] = __dadd_rn(1.0, -ar);
+        if (Nv[a] < 0.0 || Nv[a] > 1.0) Nv[a] = 0.0;
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        double ar = r[a] >= 0.0 ? r[a] : -r[a];
+        G[a] = 0.0;
+        if (ar > 1.0e-12 && ar < 1.0 - 1.0e-12) {
+            double o1 = Nv[a == 0 ? 1 : 0], o2 = Nv[a == 2 ? 1 : 2];
+            double sg = (double)((d[a] > 0.0) - (d[a] < 0.0));
+            G[a] = __ddiv_rn(__dmul_rn(__dmul_rn(-o1, o2), sg), g.h[a]);
+        }
+    }
+}
+
+// glm::dot / glm::length without contraction (glmshim order: (x*x + y*y) + z*z).
+__device__ __forceinline__ double dot3_rn(const double a[3], const double b[3]) {
+    return __dadd_rn(__dadd_rn(__dmul_rn(a[0], b[0]), __dmul_rn(a[1], b[1])), __dmul_rn(a[2], b[2]));
+}
+__device__ __forceinline__ double len3_rn(const double a[3]) { return __dsqrt_rn(dot3_rn(a, a)); }
+
+// ---------------------------------------------------------------------------
+// Constitutive increments (ConstitutiveRelation_calculateIncrement_*.cpp)
+// ---------------------------------------------------------------------------
+template <typename T>
+struct CrOut {
+    T dsig[6];
+    T deps_p[6];
+    T dR;
+};
+
+template <typename T>
+__device__ __forceinline__ void trial_increment(const MatConst& m, const T e[6], T d[6]) {
+    const T C = (T)m.C, a = (T)m.one_m_nu, nu = (T)m.nu, hb = (T)m.half_m_nu;
+    d[0] = C * (a * e[0] + nu * e[1] + nu * e[2]);
+    d[1] = C * (a * e[1] + nu * e[0] + nu * e[2]);
+    d[2] = C * (a * e[2] + nu * e[0] + nu * e[1]);
+    d[3] = C * (hb * e[3]);
+    d[4] = C * (hb * e[4]);
+    d[5] = C * (hb * e[5]);
+}
+
+// Elastic (…_Elastic.cpp:4-18); PerfectlyPlastic radial return
+// (…_PerfectlyPlastic.cpp:4-76, radius k0); von Mises with explicit
+// isotropic hardening (…_VonMisesHardening.cpp:4-92, radius k0 + R/sqrt 2,
+// dR = C0 (sqrt(2/3) C1 - R) sqrt(2/3 sum deps_p^2) when positive).
+template <typename T>
+__device__ __forceinline__ void cr_increment(const MatConst& m, T R, const T sig[6], const T e[6], CrOut<T>& o) {
+    T dtr[6];
+    trial_increment<T>(m, e, dtr);
+    o.dR = (T)0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) o.deps_p[i] = (T)0;
+    if (m.type == 0) {
+#pragma unroll
+        for (int i = 0; i < 6; ++i) o.dsig[i] = dtr[i];
+        return;
+    }
+    const bool hard = (m.type == 4);
+    T tr[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) tr[i] = sig[i] + dtr[i];
+    const T hyd = (T)(1.0 / 3.0) * (tr[0] + tr[1] + tr[2]);
+    const T a01 = tr[0] - tr[1], a12 = tr[1] - tr[2], a20 = tr[2] - tr[0];
+    T J2 = (T)(1.0 / 6.0) * a01 * a01;
+    J2 += (T)(1.0 / 6.0) * a12 * a12;
+    J2 += (T)(1.0 / 6.0) * a20 * a20;
+    J2 += tr[3] * tr[3];
+    J2 += tr[4] * tr[4];
+    J2 += tr[5] * tr[5];
+    T rad = (T)m.k0;
+    if (hard) rad = rad + R * (T)0.70710678118654752440;  // R / sqrt(2)
+    if (J2 <= rad * rad) {
+#pragma unroll
+        for (int i = 0; i < 6; ++i) o.dsig[i] = dtr[i];
+        return;
+    }
+    const T sc = rad / sqrt(J2);
+    T dev[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) dev[i] = tr[i];
+    dev[0] -= hyd;
+    dev[1] -= hyd;
+    dev[2] -= hyd;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) o.dsig[i] = dev[i] * sc - sig[i];
+    o.dsig[0] += hyd;
+    o.dsig[1] += hyd;
+    o.dsig[2] += hyd;
+    const T iE = (T)m.inv_E, nE = (T)m.nu_over_E, iG = (T)m.inv_G;
+    T ee[6];
+    ee[0] = o.dsig[0] * iE - o.dsig[1] * nE - o.dsig[2] * nE;
+    ee[1] = o.dsig[1] * iE - o.dsig[0] * nE - o.dsig[2] * nE;
+    ee[2] = o.dsig[2] * iE - o.dsig[0] * nE - o.dsig[1] * nE;
+    ee[3] = o.dsig[3] * iG;
+    ee[4] = o.dsig[4] * iG;
+    ee[5] = o.dsig[5] * iG;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) o.deps_p[i] = e[i] - ee[i];
+    if (!hard) return;
+    T ep = (T)0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) ep += o.deps_p[i] * o.deps_p[i];
+    ep = sqrt(ep * (T)(2.0 / 3.0));
+    const T sat = (T)m.s23C1 - R;
+    o.dR = (sat > (T)0) ? (T)m.C0 * sat * ep : (T)0;
+}
+
+}  // namespace mpm

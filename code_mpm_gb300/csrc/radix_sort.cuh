@@ -1,0 +1,116 @@
+// Stable LSD radix sort of (32-bit key, 32-bit value) pairs, 8-bit digits.
+//
+// Used to order particles by cell key each step.  Stability within a digit
+// pass comes from ranking every key against the keys before it in its tile
+// (warp match + per-warp digit counters, then a prefix over the warps), so
+// equal keys keep their input order; with values 0..n-1 as input the output
+// is the particle order of a stable CPU sort by key (std::stable_sort).
+//
+// Per pass: k_rs_hist (per-tile digit histogram, digit-major layout),
+// k_rs_scan (one-block exclusive scan of the histogram), k_rs_scatter.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace mpm {
+
+constexpr int RS_THREADS = 256;
+constexpr int RS_WARPS = RS_THREADS / 32;
+constexpr int RS_ITEMS = 16;  // keys per thread
+constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
+constexpr int RS_WARP_TILE = 32 * RS_ITEMS;
+
+__global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const unsigned* __restrict__ keys, long long n, int shift,
+                                                         unsigned* __restrict__ counts, int nblocks) {
+    __shared__ unsigned h[256];
+    for (int i = threadIdx.x; i < 256; i += RS_THREADS) h[i] = 0;
+    __syncthreads();
+    long long base = (long long)blockIdx.x * RS_TILE;
+#pragma unroll 4
+    for (int j = 0; j < RS_ITEMS; ++j) {
+        long long idx = base + (long long)j * RS_THREADS + threadIdx.x;
+        if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 256; i += RS_THREADS) counts[(size_t)i * nblocks + blockIdx.x] = h[i];
+}
+
+// Exclusive scan of counts[0..total) in place, one block of 1024 threads.
+__global__ void __launch_bounds__(1024) k_rs_scan(unsigned* __restrict__ counts, int total) {
+    __shared__ unsigned part[1024];
+    const int t = threadIdx.x;
+    const int per = (total + 1023) / 1024;
+    const int lo = t * per, hi = min(total, lo + per);
+    unsigned s = 0;
+    for (int i = lo; i < hi; ++i) s += counts[i];
+    part[t] = s;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        unsigned v = (t >= off) ? part[t - off] : 0u;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    unsigned run = part[t] - s;  // exclusive prefix of this thread's chunk
+    for (int i = lo; i < hi; ++i) {
+        unsigned c = counts[i];
+        counts[i] = run;
+        run += c;
+    }
+}
+
+__global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const unsigned* __restrict__ kin,
+                                                            const unsigned* __restrict__ vin,
+                                                            unsigned* __restrict__ kout, unsigned* __restrict__ vout,
+                                                            long long n, int shift,
+                                                            const unsigned* __restrict__ offs, int nblocks) {
+    __shared__ unsigned wcnt[RS_WARPS][256];
+    __shared__ unsigned gofs[256];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int i = threadIdx.x; i < RS_WARPS * 256; i += RS_THREADS) (&wcnt[0][0])[i] = 0;
+    for (int i = threadIdx.x; i < 256; i += RS_THREADS) gofs[i] = offs[(size_t)i * nblocks + blockIdx.x];
+    __syncthreads();
+    const long long base = (long long)blockIdx.x * RS_TILE + (long long)w * RS_WARP_TILE;
+    const unsigned lt = (1u << lane) - 1u;
+    unsigned k[RS_ITEMS], v[RS_ITEMS], r[RS_ITEMS];
+#pragma unroll
+    for (int c = 0; c < RS_ITEMS; ++c) {
+        long long idx = base + c * 32 + lane;
+        bool ok = idx < n;
+        unsigned key = ok ? kin[idx] : 0u;
+        unsigned val = ok ? vin[idx] : 0u;
+        unsigned d = ok ? ((key >> shift) & 255u) : (256u + lane);  // invalid lanes never match a digit
+        unsigned peers = __match_any_sync(0xffffffffu, d);
+        unsigned rank = 0;
+        if (ok) rank = wcnt[w][d] + __popc(peers & lt);
+        __syncwarp();
+        if (ok && lane == __ffs(peers) - 1) wcnt[w][d] += __popc(peers);
+        __syncwarp();
+        k[c] = key;
+        v[c] = val;
+        r[c] = rank;
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < 256; d += RS_THREADS) {
+        unsigned run = 0;
+        for (int ww = 0; ww < RS_WARPS; ++ww) {
+            unsigned t = wcnt[ww][d];
+            wcnt[ww][d] = run;
+            run += t;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < RS_ITEMS; ++c) {
+        long long idx = base + c * 32 + lane;
+        if (idx < n) {
+            unsigned d = (k[c] >> shift) & 255u;
+            unsigned dst = gofs[d] + wcnt[w][d] + r[c];
+            kout[dst] = k[c];
+            vout[dst] = v[c];
+        }
+    }
+}
+
+}  // namespace mpm

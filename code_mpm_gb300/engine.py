@@ -1,0 +1,323 @@
+"""Host-side mirror of the reference's PhysicsEngine solver interface over the C ABI.
+
+``Engine`` owns one ``mpm_ctx`` (include/mpm_gb300.h) and exposes the
+reference's entry points with their meaning and return values:
+
+    runSimulation_Classic_DoublePass_MPLocks(dTimeIncrement_Total)          PhysicsEngine.h:54
+    runSimulation_Classic_DoublePass_MPLocks_Contact(dTimeIncrement_Total)  PhysicsEngine.h:55
+        advance by dTimeIncrement_Total in steps of d_TimeIncrement_Maximum,
+        the last one shortened (…MPLocks.cpp:449-458); return 1 once
+        d_Time >= d_TimeEnd, else 0 (:806-814)
+    getTime_Current / getTime_End / getTime_Increment                       PhysicsEngine.h:66-71
+    getCount_MaterialPoint / getCount_GridPoint                             PhysicsEngine.h:73-75
+
+plus state transfer as ``code_mpm_gb300.snapshot.State``.  Every call goes
+through libmpm_gb300.so; there is no CPU path, and a missing library or
+device raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Dict, Optional
+
+import numpy as np
+
+from . import snapshot
+from .snapshot import State
+
+_LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libmpm_gb300.so")
+_lib = None
+
+FORM_FP64 = 0
+FORM_FP32 = 1
+OPT_FLOOR_FRICTION = 1
+OPT_PROFILE = 2
+
+
+class MPMError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"mpm error {code}: {msg}")
+        self.code = code
+
+
+class GridDesc(C.Structure):
+    _fields_ = [("length", C.c_double * 3), ("cells", C.c_int32 * 3), ("pad", C.c_int32)]
+
+
+class Material(C.Structure):
+    _fields_ = [("type", C.c_int32), ("pad", C.c_int32), ("density", C.c_double), ("E", C.c_double),
+                ("nu", C.c_double), ("yield_", C.c_double), ("C0", C.c_double), ("C1", C.c_double)]
+
+
+class Sim(C.Structure):
+    _fields_ = [("time", C.c_double), ("dt_max", C.c_double), ("mass_min", C.c_double), ("damping", C.c_double),
+                ("time_end", C.c_double), ("step", C.c_int64)]
+
+
+_PFIELDS = ("pos", "vel", "fext", "mass", "vol", "vol0", "F", "stress", "strain", "eps_p", "e_strain", "e_strain_max",
+            "e_strain_ti", "e_plastic", "backstress", "mp_mass_gradient", "strain_rate")
+
+
+class Particles(C.Structure):
+    _fields_ = [(k, C.c_void_p) for k in _PFIELDS] + [("material", C.c_void_p), ("pflags", C.c_void_p),
+                                                      ("dc_mult", C.c_void_p)]
+
+
+_NMAP = (("fixed", "fixed"), ("friction", "friction"), ("mass", "g_mass"), ("mom", "g_mom"), ("vel", "g_vel"),
+         ("force", "g_force"), ("force_temp", "g_force_temp"), ("mass_gradient", "g_mass_gradient"),
+         ("state", "g_state"))
+
+
+class Nodes(C.Structure):
+    _fields_ = [(k, C.c_void_p) for k, _ in _NMAP]
+
+
+class KernelStat(C.Structure):
+    _fields_ = [("name", C.c_char * 32), ("launches", C.c_int64), ("total_ms", C.c_double)]
+
+
+def library_path() -> str:
+    return _LIB_PATH
+
+
+def lib():
+    """Load libmpm_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            raise RuntimeError(f"{_LIB_PATH} is missing: build it with `python -m code_mpm_gb300.build`")
+        L = C.CDLL(_LIB_PATH)
+        vp, i32, i64, dbl = C.c_void_p, C.c_int32, C.c_int64, C.c_double
+        sig = {
+            "mpm_create": ([C.POINTER(GridDesc), C.c_int, C.POINTER(vp)], C.c_int),
+            "mpm_destroy": ([vp], None),
+            "mpm_last_error": ([vp], C.c_char_p),
+            "mpm_device_info": ([C.c_char_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)],
+                                C.c_int),
+            "mpm_set_stream": ([vp, vp], C.c_int),
+            "mpm_set_option": ([vp, C.c_int, dbl], C.c_int),
+            "mpm_upload_materials": ([vp, C.POINTER(Material), i32], C.c_int),
+            "mpm_upload_particles": ([vp, C.POINTER(Particles), i64], C.c_int),
+            "mpm_upload_dc_list": ([vp, vp, i64], C.c_int),
+            "mpm_upload_nodes": ([vp, C.POINTER(Nodes)], C.c_int),
+            "mpm_set_timeline": ([vp, vp, vp, i32], C.c_int),
+            "mpm_set_sim": ([vp, C.POINTER(Sim)], C.c_int),
+            "mpm_get_sim": ([vp, C.POINTER(Sim)], C.c_int),
+            "mpm_download_particles": ([vp, C.POINTER(Particles)], C.c_int),
+            "mpm_download_nodes": ([vp, C.POINTER(Nodes)], C.c_int),
+            "mpm_advance": ([vp, i32, dbl, C.c_int], C.c_int),
+            "mpm_run": ([vp, dbl, C.c_int, C.POINTER(C.c_int)], C.c_int),
+            "mpm_synchronize": ([vp], C.c_int),
+            "mpm_advance_timed": ([vp, i32, dbl, C.c_int, C.POINTER(C.c_float)], C.c_int),
+            "mpm_profile_read": ([vp, C.POINTER(KernelStat), i32, C.POINTER(i32)], C.c_int),
+            "mpm_profile_reset": ([vp], C.c_int),
+            "mpm_launch_count": ([vp, C.POINTER(i64)], C.c_int),
+            "mpm_cell_order": ([vp, vp, vp, i64], C.c_int),
+        }
+        for name, (args, res) in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = L
+    return _lib
+
+
+def device_info() -> Dict[str, object]:
+    name = C.create_string_buffer(256)
+    sm, ma, mi = C.c_int(), C.c_int(), C.c_int()
+    rc = lib().mpm_device_info(name, 256, C.byref(sm), C.byref(ma), C.byref(mi))
+    if rc != 0:
+        raise MPMError(rc, "no CUDA device")
+    return {"name": name.value.decode(), "sm_count": sm.value, "cc": (ma.value, mi.value)}
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data
+
+
+class Engine:
+    """One GPU engine instance (an ``mpm_ctx``)."""
+
+    def __init__(self, length, cells, form: int = FORM_FP64):
+        self._L = lib()
+        g = GridDesc()
+        for a in range(3):
+            g.length[a] = float(length[a])
+            g.cells[a] = int(cells[a])
+        h = C.c_void_p()
+        rc = self._L.mpm_create(C.byref(g), int(form), C.byref(h))
+        if rc != 0 or not h.value:
+            raise MPMError(rc, "mpm_create failed (no usable CUDA device or bad grid)")
+        self._h = h
+        self.form = int(form)
+        self.length = np.asarray(length, dtype=np.float64)
+        self.cells = np.asarray(cells, dtype=np.int32)
+        self.n_particles = 0
+        self.n_nodes = int(np.prod(self.cells.astype(np.int64) + 1))
+        self._keep = []
+
+    # -- plumbing -------------------------------------------------------------------
+    def _check(self, rc: int) -> None:
+        if rc != 0:
+            msg = self._L.mpm_last_error(self._h)
+            raise MPMError(rc, msg.decode() if msg else "")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._L.mpm_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self) -> int:
+        return self._h.value
+
+    def set_option(self, key: int, value: float) -> None:
+        self._check(self._L.mpm_set_option(self._h, int(key), float(value)))
+
+    def set_stream(self, stream_ptr: int) -> None:
+        self._check(self._L.mpm_set_stream(self._h, C.c_void_p(stream_ptr)))
+
+    # -- state ------------------------------------------------------------------------
+    @classmethod
+    def from_state(cls, st: State, form: int = FORM_FP64, time_end: float = 1.0e300) -> "Engine":
+        e = cls(st.length, st.cells, form)
+        e.upload_state(st, time_end=time_end)
+        return e
+
+    def upload_state(self, st: State, time_end: float = 1.0e300) -> None:
+        mats = st["materials"]
+        tab = (Material * max(1, len(mats)))()
+        for i, m in enumerate(mats):
+            tab[i].type = int(m["type"])
+            tab[i].density, tab[i].E, tab[i].nu = float(m["density"]), float(m["E"]), float(m["nu"])
+            tab[i].yield_, tab[i].C0, tab[i].C1 = float(m["yield_"]), float(m["C0"]), float(m["C1"])
+        self._check(self._L.mpm_upload_materials(self._h, tab, len(mats)))
+        arrs = {k: np.ascontiguousarray(st[k]) for k in _PFIELDS}
+        arrs["material"] = np.ascontiguousarray(st["material"], dtype=np.int32)
+        arrs["pflags"] = np.ascontiguousarray(st["pflags"], dtype=np.uint8)
+        arrs["dc_mult"] = np.ascontiguousarray(st["dc_mult"], dtype=np.float32)
+        p = Particles(**{k: _ptr(v) for k, v in arrs.items()})
+        self._check(self._L.mpm_upload_particles(self._h, C.byref(p), st.n_particles))
+        self.n_particles = st.n_particles
+        dcl = np.ascontiguousarray(st["dc_list"], dtype=np.uint32)
+        self._check(self._L.mpm_upload_dc_list(self._h, _ptr(dcl), len(dcl)))
+        narr = {k: np.ascontiguousarray(st[src]) for k, src in _NMAP}
+        nd = Nodes(**{k: _ptr(v) for k, v in narr.items()})
+        self._check(self._L.mpm_upload_nodes(self._h, C.byref(nd)))
+        t = np.ascontiguousarray(st["tl_time"], dtype=np.float64)
+        v = np.ascontiguousarray(st["tl_vel"], dtype=np.float64)
+        self._check(self._L.mpm_set_timeline(self._h, _ptr(t), _ptr(v), len(t)))
+        self.set_sim(time=st.time, dt_max=st.dt_max, mass_min=st.mass_min, damping=st.damping, step=st.step,
+                     time_end=time_end)
+
+    def download_state(self, template: State) -> State:
+        """A copy of ``template`` with every particle and node field replaced by the engine's."""
+        st = template.copy()
+        arrs = {k: st[k] for k in _PFIELDS}
+        arrs["material"] = st["material"]
+        arrs["pflags"] = st["pflags"]
+        arrs["dc_mult"] = st["dc_mult"]
+        p = Particles(**{k: _ptr(v) for k, v in arrs.items()})
+        self._check(self._L.mpm_download_particles(self._h, C.byref(p)))
+        nd = Nodes(**{k: _ptr(st[src]) for k, src in _NMAP})
+        self._check(self._L.mpm_download_nodes(self._h, C.byref(nd)))
+        s = self.get_sim()
+        st.time, st.step = s["time"], s["step"]
+        return st
+
+    def download_particles(self, fields: Dict[str, np.ndarray]) -> None:
+        """Fill the given preallocated host arrays (names as in State) from the device."""
+        p = Particles(**{k: _ptr(v) for k, v in fields.items()})
+        self._check(self._L.mpm_download_particles(self._h, C.byref(p)))
+
+    def upload_particles(self, fields: Dict[str, np.ndarray], n: int) -> None:
+        p = Particles(**{k: _ptr(v) for k, v in fields.items()})
+        self._check(self._L.mpm_upload_particles(self._h, C.byref(p), int(n)))
+
+    def set_sim(self, time: float, dt_max: float, mass_min: float = 0.0, damping: float = 0.0, step: int = 0,
+                time_end: float = 1.0e300) -> None:
+        s = Sim(float(time), float(dt_max), float(mass_min), float(damping), float(time_end), int(step))
+        self._check(self._L.mpm_set_sim(self._h, C.byref(s)))
+
+    def get_sim(self) -> Dict[str, float]:
+        s = Sim()
+        self._check(self._L.mpm_get_sim(self._h, C.byref(s)))
+        return {"time": s.time, "dt_max": s.dt_max, "mass_min": s.mass_min, "damping": s.damping,
+                "time_end": s.time_end, "step": s.step}
+
+    # -- stepping ----------------------------------------------------------------------
+    def advance(self, nsteps: int, dt: Optional[float] = None, contact: bool = False) -> None:
+        if dt is None:
+            dt = self.get_sim()["dt_max"]
+        self._check(self._L.mpm_advance(self._h, int(nsteps), float(dt), 1 if contact else 0))
+
+    def advance_timed(self, nsteps: int, dt: Optional[float] = None, contact: bool = False) -> float:
+        if dt is None:
+            dt = self.get_sim()["dt_max"]
+        ms = C.c_float(0.0)
+        self._check(self._L.mpm_advance_timed(self._h, int(nsteps), float(dt), 1 if contact else 0, C.byref(ms)))
+        return float(ms.value)
+
+    def synchronize(self) -> None:
+        self._check(self._L.mpm_synchronize(self._h))
+
+    def runSimulation_Classic_DoublePass_MPLocks(self, dTimeIncrement_Total: float) -> int:
+        done = C.c_int(0)
+        self._check(self._L.mpm_run(self._h, float(dTimeIncrement_Total), 0, C.byref(done)))
+        return int(done.value)
+
+    def runSimulation_Classic_DoublePass_MPLocks_Contact(self, dTimeIncrement_Total: float) -> int:
+        done = C.c_int(0)
+        self._check(self._L.mpm_run(self._h, float(dTimeIncrement_Total), 1, C.byref(done)))
+        return int(done.value)
+
+    def getTime_Current(self) -> float:
+        return self.get_sim()["time"]
+
+    def getTime_End(self) -> float:
+        return self.get_sim()["time_end"]
+
+    def getTime_Increment(self) -> float:
+        return self.get_sim()["dt_max"]
+
+    def getCount_MaterialPoint(self) -> int:
+        return self.n_particles
+
+    def getCount_GridPoint(self) -> int:
+        return self.n_nodes
+
+    def cell_order(self):
+        """(cell key per particle, particle order sorted by key) of the last step."""
+        keys = np.zeros(self.n_particles, dtype=np.uint32)
+        perm = np.zeros(self.n_particles, dtype=np.uint32)
+        self._check(self._L.mpm_cell_order(self._h, _ptr(keys), _ptr(perm), self.n_particles))
+        return keys, perm
+
+    # -- profiling ----------------------------------------------------------------------
+    def profile(self) -> Dict[str, Dict[str, float]]:
+        arr = (KernelStat * 128)()
+        cnt = C.c_int32(0)
+        self._check(self._L.mpm_profile_read(self._h, arr, 128, C.byref(cnt)))
+        return {arr[i].name.decode(): {"launches": int(arr[i].launches), "ms": float(arr[i].total_ms)}
+                for i in range(min(cnt.value, 128))}
+
+    def profile_reset(self) -> None:
+        self._check(self._L.mpm_profile_reset(self._h))
+
+    def launch_count(self) -> int:
+        c = C.c_int64(0)
+        self._check(self._L.mpm_launch_count(self._h, C.byref(c)))
+        return int(c.value)

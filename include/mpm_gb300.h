@@ -1,0 +1,198 @@
+/*
+ * mpm_gb300.h -- C ABI of the GB300 explicit-MPM engine.
+ *
+ * The engine replaces one hot path of the reference solver: the classic
+ * double-pass (USL) step of
+ *   PhysicsEngine::runSimulation_Classic_DoublePass_MPLocks(double)          PhysicsEngine.h:54
+ *   PhysicsEngine::runSimulation_Classic_DoublePass_MPLocks_Contact(double)  PhysicsEngine.h:55
+ * i.e. reset grid -> find adjacent grid points -> P2G (mass, momentum, force
+ * [, mass gradient]) -> displacement control -> grid update with boundary
+ * conditions and friction -> G2P pass 1 -> velocity remap -> boundary
+ * conditions / displacement control -> G2P pass 2 with the constitutive
+ * increment -> platen timeline, on one NVIDIA GB300 (sm_103a).
+ *
+ * Conventions
+ *   - Every call returns an int status: MPM_OK (0) or a negative MPM_ERR_*;
+ *     mpm_last_error() gives the message of the last failure on a context.
+ *   - The caller owns every host buffer; the context owns all device memory.
+ *   - Per-particle vectors are n x k row-major host arrays (the k components
+ *     of particle 0 first); the 3x3 deformation gradient is stored in glm's
+ *     column-major element order, F[c][r] at offset 3*c + r
+ *     (MaterialPoint_BC.h:52).  Node arrays use the reference's node index
+ *     ix + iy*nx + iz*nx*ny (GridPoint_Factory.h:18-22), nx = cells_x + 1.
+ *   - A context is not thread-safe; all work is ordered on one CUDA stream.
+ *   - No CPU fallback: every compute entry point runs CUDA kernels, and
+ *     mpm_create fails when no usable device is present.
+ */
+#ifndef MPM_GB300_H
+#define MPM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MPM_OK 0
+#define MPM_ERR_ARG (-1)     /* invalid argument or size */
+#define MPM_ERR_CUDA (-2)    /* a CUDA runtime call failed */
+#define MPM_ERR_STATE (-3)   /* call out of order (e.g. advance before upload) */
+#define MPM_ERR_DEVICE (-4)  /* a kernel reported a data error (non-finite position, ...) */
+#define MPM_ERR_NOMEM (-5)   /* device allocation failed */
+
+/* Numerical forms. */
+#define MPM_FORM_FP64 0 /* plain form: the reference method in FP64 */
+#define MPM_FORM_FP32 1 /* chosen form: FP32 transfers and grid, FP64 positions and energies */
+
+/* Material type ids, as Material_BC.h:6-11. Unknown ids use the PerfectlyPlastic law (…MPLocks.cpp:238). */
+#define MPM_MAT_ELASTIC 0
+#define MPM_MAT_PLASTIC 3
+#define MPM_MAT_VONMISESHARDENING 4
+
+/* Particle flag bits (MaterialPoint_BC.h:32-43). */
+#define MPM_PF_DC_X 1u     /* b3_DisplacementControl.x */
+#define MPM_PF_DC_Y 2u     /* b3_DisplacementControl.y */
+#define MPM_PF_DC_Z 4u     /* b3_DisplacementControl.z */
+#define MPM_PF_DC_SKIP 8u  /* b_DisplacementControl: skipped by G2P on the contact path */
+#define MPM_PF_SURFACE 16u /* b_Surface: takes part in contact detection */
+
+/* Node fixed bits (GridPoint.h:20, b3_Fixed) and node state bits. */
+#define MPM_NF_FIX_X 1u
+#define MPM_NF_FIX_Y 2u
+#define MPM_NF_FIX_Z 4u
+#define MPM_NS_ACTIVE 1u   /* b_Active */
+#define MPM_NS_CONTACT 2u  /* b_Contact */
+#define MPM_NS_POSITIVE 4u /* b_Contact_Positive */
+#define MPM_NS_NEGATIVE 8u /* b_Contact_Negative */
+
+/* Options for mpm_set_option. */
+#define MPM_OPT_FLOOR_FRICTION 1 /* contact path: Coulomb friction on x/y of z-fixed nodes (extension; default 0) */
+#define MPM_OPT_PROFILE 2        /* 1: time every kernel with CUDA events (default 0) */
+
+typedef struct mpm_ctx mpm_ctx;
+
+/* Regular grid: cells[a] cells of size length[a]/cells[a] along axis a
+ * (GridPoint_Factory.h:33-68; GridPoint_Mediator.h:25-28). */
+typedef struct mpm_grid_desc {
+    double length[3];
+    int32_t cells[3];
+    int32_t pad;
+} mpm_grid_desc;
+
+/* Material_BC.h:13-35. */
+typedef struct mpm_material {
+    int32_t type;
+    int32_t pad;
+    double density, E, nu, yield, C0, C1;
+} mpm_material;
+
+/* Scalars of the time loop (PhysicsEngine.h:83-116). */
+typedef struct mpm_sim {
+    double time;     /* d_Time */
+    double dt_max;   /* d_TimeIncrement_Maximum */
+    double mass_min; /* d_Mass_Minimum */
+    double damping;  /* d_DampingCoefficient */
+    double time_end; /* d_TimeEnd */
+    int64_t step;    /* i_TimeCycle */
+} mpm_sim;
+
+/* Host views of the particle state (MaterialPoint_BC.h:25-85).  On upload a
+ * NULL field takes its default (zero; F = identity; dc_mult = 1); on
+ * download a NULL field is skipped. */
+typedef struct mpm_particles {
+    double *pos, *vel, *fext;        /* n x 3 */
+    double *mass, *vol, *vol0;       /* n */
+    double* F;                       /* n x 9, column-major */
+    double *stress, *strain, *eps_p; /* n x 6, Voigt xx yy zz xy yz zx, engineering shear strain */
+    double *e_strain, *e_strain_max, *e_strain_ti, *e_plastic, *backstress; /* n */
+    double* mp_mass_gradient;        /* n x 3 (contact path output) */
+    double* strain_rate;             /* n x 6 (contact path output) */
+    int32_t* material;               /* n, index into the uploaded material table (<0: none) */
+    uint8_t* pflags;                 /* n, MPM_PF_* */
+    float* dc_mult;                  /* n, f_DisplacementControl_Multiplier */
+} mpm_particles;
+
+/* Host views of the node state (GridPoint.h:6-45), n_nodes entries each. */
+typedef struct mpm_nodes {
+    uint8_t* fixed;        /* MPM_NF_* */
+    double* friction;      /* d_FrictionCoefficient */
+    double* mass;          /* d_Mass */
+    double *mom, *vel, *force, *force_temp, *mass_gradient; /* n_nodes x 3 */
+    uint8_t* state;        /* MPM_NS_* */
+} mpm_nodes;
+
+/* Per-kernel timing record (MPM_OPT_PROFILE). */
+typedef struct mpm_kernel_stat {
+    char name[32];
+    int64_t launches;
+    double total_ms;
+} mpm_kernel_stat;
+
+/* --- lifetime --------------------------------------------------------------
+ * Replaces the engine set-up the reference scene builders do
+ * (GridPoint_Factory::createGrid, GridPoint_Factory.h:33-68, and the mediator
+ * geometry, e.g. PhysicsEngine_initializeWorld_Classic_Bar.cpp:15-27). */
+int mpm_create(const mpm_grid_desc* grid, int form, mpm_ctx** out);
+void mpm_destroy(mpm_ctx* ctx); /* PhysicsEngine::~PhysicsEngine, PhysicsEngine.cpp:4-38 */
+const char* mpm_last_error(const mpm_ctx* ctx);
+int mpm_device_info(char* name, int name_len, int* sm_count, int* cc_major, int* cc_minor);
+
+/* Use the caller's CUDA stream (cudaStream_t passed as void*) instead of the context's own. */
+int mpm_set_stream(mpm_ctx* ctx, void* stream);
+int mpm_set_option(mpm_ctx* ctx, int key, double value);
+
+/* --- state transfer ---------------------------------------------------------
+ * The reference keeps this state in PhysicsEngine's vectors v_allMaterial,
+ * allMaterialPoint, v_MarkedMaterialPoints_Displacement_Control and
+ * allGridPoint (PhysicsEngine.h:89-93) and m_TimeLine (:82). */
+int mpm_upload_materials(mpm_ctx* ctx, const mpm_material* mats, int32_t n);
+int mpm_upload_particles(mpm_ctx* ctx, const mpm_particles* p, int64_t n);
+/* Indices of displacement-controlled particles, in the order of
+ * v_MarkedMaterialPoints_Displacement_Control (that order decides which
+ * particle's velocity a shared node keeps).  Duplicates are rejected. */
+int mpm_upload_dc_list(mpm_ctx* ctx, const uint32_t* idx, int64_t n);
+int mpm_upload_nodes(mpm_ctx* ctx, const mpm_nodes* nodes);
+int mpm_set_timeline(mpm_ctx* ctx, const double* t, const double* v3, int32_t n); /* TimeLine::addTimePoint */
+int mpm_set_sim(mpm_ctx* ctx, const mpm_sim* sim);
+int mpm_get_sim(const mpm_ctx* ctx, mpm_sim* sim);
+int mpm_download_particles(mpm_ctx* ctx, mpm_particles* p);
+int mpm_download_nodes(mpm_ctx* ctx, mpm_nodes* nodes);
+
+/* --- time stepping -----------------------------------------------------------
+ * mpm_advance: `nsteps` steps of increment dt each, on the context's stream
+ * (asynchronous).  contact = 0 is the step of
+ * runSimulation_Classic_DoublePass_MPLocks (…MPLocks.cpp:462-792), contact = 1
+ * the step of runSimulation_Classic_DoublePass_MPLocks_Contact
+ * (…_Contact.cpp:27-543).  Time and step count advance as d_Time += dt,
+ * i_TimeCycle++ (…MPLocks.cpp:802-803). */
+int mpm_advance(mpm_ctx* ctx, int32_t nsteps, double dt, int contact);
+/* mpm_run: the whole while-loop of runSimulation_…(dTimeIncrement_Total)
+ * (…MPLocks.cpp:449-458, 806-814) without the console report: steps of
+ * dt_max, the last one shortened to end exactly at dt_total; *done = 1 when
+ * time >= time_end.  Returns after the work is complete. */
+int mpm_run(mpm_ctx* ctx, double dt_total, int contact, int* done);
+/* Wait for the stream and surface any device-side error. */
+int mpm_synchronize(mpm_ctx* ctx);
+/* mpm_advance bracketed by CUDA events on the context's stream; *ms = device time. */
+int mpm_advance_timed(mpm_ctx* ctx, int32_t nsteps, double dt, int contact, float* ms);
+
+/* Diagnostics: the cell key of every particle (base cell (bx,by,bz) =
+ * floor(x/h) as in GridPoint_Mediator.cpp:8, key = (bx+1) + (cx+2)*((by+1) +
+ * (cy+2)*(bz+1)), or (cx+2)(cy+2)(cz+2) when no node is in range) and the
+ * particle order sorted by key (stable) used by the last step.  Either
+ * pointer may be NULL; n must equal the particle count. */
+int mpm_cell_order(mpm_ctx* ctx, uint32_t* keys, uint32_t* sorted_order, int64_t n);
+
+/* --- profiling ---------------------------------------------------------------
+ * Per-kernel CUDA-event timers (the reference's a_Runtime, PhysicsEngine.h:87). */
+int mpm_profile_read(mpm_ctx* ctx, mpm_kernel_stat* out, int32_t max, int32_t* count);
+int mpm_profile_reset(mpm_ctx* ctx);
+/* Number of kernels the engine launched since creation (all kinds). */
+int mpm_launch_count(const mpm_ctx* ctx, int64_t* count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MPM_GB300_H */
