@@ -52,7 +52,7 @@ __global__ void k_reset_grid(NView<T> nd, int contact) {
 // cell index is bit-identical to the reference.  Particles whose base cell
 // lies outside [-1, cells] have no node in range and get key_max.
 // ---------------------------------------------------------------------------
-__global__ void k_cell_keys(const double* __restrict__ pos, long long n, Geom g, unsigned* __restrict__ keys,
+static __global__ void k_cell_keys(const double* __restrict__ pos, long long n, Geom g, unsigned* __restrict__ keys,
                             unsigned* __restrict__ vals, unsigned* __restrict__ keys_copy, unsigned* err) {
     long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (p >= n) return;
@@ -81,7 +81,7 @@ __global__ void k_cell_keys(const double* __restrict__ pos, long long n, Geom g,
 // Active nodes (the union of the in-range corners of every occupied cell) and
 // per-cell [start, end) ranges in sorted order.
 // ---------------------------------------------------------------------------
-__global__ void k_cell_ranges(const unsigned* __restrict__ skeys, long long n, Geom g, unsigned* __restrict__ state,
+static __global__ void k_cell_ranges(const unsigned* __restrict__ skeys, long long n, Geom g, unsigned* __restrict__ state,
                               unsigned* __restrict__ cstart, unsigned* __restrict__ cend) {
     long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (s >= n) return;
@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(256) k_p2g(PView<T> P, NView<T> nd, Geom g, co
 // k_dc_claim records, per node and axis, the largest list position writing
 // it; k_dc_apply lets only that particle write.  contact: all three axes.
 // ---------------------------------------------------------------------------
-__global__ void k_dc_claim(const unsigned* __restrict__ dclist, int ndc, const unsigned* __restrict__ keys,
+static __global__ void k_dc_claim(const unsigned* __restrict__ dclist, int ndc, const unsigned* __restrict__ keys,
                            const uint8_t* __restrict__ pflags, Geom g, unsigned* __restrict__ owner, long long nn,
                            int contact) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;

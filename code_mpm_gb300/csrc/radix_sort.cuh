@@ -21,7 +21,7 @@ constexpr int RS_ITEMS = 16;  // keys per thread
 constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
 constexpr int RS_WARP_TILE = 32 * RS_ITEMS;
 
-__global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const unsigned* __restrict__ keys, long long n, int shift,
+static __global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const unsigned* __restrict__ keys, long long n, int shift,
                                                          unsigned* __restrict__ counts, int nblocks) {
     __shared__ unsigned h[256];
     for (int i = threadIdx.x; i < 256; i += RS_THREADS) h[i] = 0;
@@ -37,7 +37,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const unsigned* __restri
 }
 
 // Exclusive scan of counts[0..total) in place, one block of 1024 threads.
-__global__ void __launch_bounds__(1024) k_rs_scan(unsigned* __restrict__ counts, int total) {
+static __global__ void __launch_bounds__(1024) k_rs_scan(unsigned* __restrict__ counts, int total) {
     __shared__ unsigned part[1024];
     const int t = threadIdx.x;
     const int per = (total + 1023) / 1024;
@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(1024) k_rs_scan(unsigned* __restrict__ counts,
     }
 }
 
-__global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const unsigned* __restrict__ kin,
+static __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const unsigned* __restrict__ kin,
                                                             const unsigned* __restrict__ vin,
                                                             unsigned* __restrict__ kout, unsigned* __restrict__ vout,
                                                             long long n, int shift,

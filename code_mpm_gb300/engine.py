@@ -114,6 +114,7 @@ def lib():
             "mpm_profile_reset": ([vp], C.c_int),
             "mpm_launch_count": ([vp, C.POINTER(i64)], C.c_int),
             "mpm_cell_order": ([vp, vp, vp, i64], C.c_int),
+            "mpm_cell_order_noalloc": ([C.POINTER(GridDesc), vp, i64, vp, vp, vp], C.c_int),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -134,6 +135,25 @@ def device_info() -> Dict[str, object]:
 
 def _ptr(a: Optional[np.ndarray]):
     return None if a is None else a.ctypes.data
+
+
+NOALLOC_MAX_PARTICLES = 1 << 20
+
+
+def cell_order_noalloc(length, cells, d_pos: int, n: int, d_keys: int, d_order: int, stream: int = 0) -> int:
+    """mpm_cell_order_noalloc on caller-owned device buffers (addresses as ints); returns the status code.
+
+    For callers that cannot allocate device memory: the library works in a
+    fixed static scratch array and allocates nothing.  Calls share that
+    scratch, so calls that overlap on the GPU race; at most
+    NOALLOC_MAX_PARTICLES particles (larger n returns -6).
+    """
+    g = GridDesc()
+    for a in range(3):
+        g.length[a] = float(length[a])
+        g.cells[a] = int(cells[a])
+    return int(lib().mpm_cell_order_noalloc(C.byref(g), C.c_void_p(d_pos), int(n), C.c_void_p(d_keys),
+                                            C.c_void_p(d_order), C.c_void_p(stream or None)))
 
 
 class Engine:

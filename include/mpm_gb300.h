@@ -40,6 +40,7 @@ extern "C" {
 #define MPM_ERR_STATE (-3)   /* call out of order (e.g. advance before upload) */
 #define MPM_ERR_DEVICE (-4)  /* a kernel reported a data error (non-finite position, ...) */
 #define MPM_ERR_NOMEM (-5)   /* device allocation failed */
+#define MPM_ERR_TOO_LARGE (-6) /* size exceeds the fixed capacity of an entry point that does not allocate */
 
 /* Numerical forms. */
 #define MPM_FORM_FP64 0 /* plain form: the reference method in FP64 */
@@ -183,6 +184,37 @@ int mpm_advance_timed(mpm_ctx* ctx, int32_t nsteps, double dt, int contact, floa
  * particle order sorted by key (stable) used by the last step.  Either
  * pointer may be NULL; n must equal the particle count. */
 int mpm_cell_order(mpm_ctx* ctx, uint32_t* keys, uint32_t* sorted_order, int64_t n);
+
+/* --- cell order without allocation --------------------------------------------
+ * No counterpart in the reference (which has no device and no allocator to
+ * avoid).  For callers that cannot allocate device memory when they need the
+ * cell order: code running inside a memory pool or arena that owns the whole
+ * device heap, plug-ins whose host framework forbids cudaMalloc/cudaFree on
+ * the calling thread, and loops where an allocation (or the device-wide
+ * synchronisation of cudaFree) is not acceptable.
+ *
+ * Computes, for n particles at device positions d_pos (structure of arrays:
+ * x[0..n), y[0..n), z[0..n), doubles), the cell key of every particle into
+ * d_keys and the particle order sorted stably by key into d_order (both
+ * device arrays of n uint32), exactly as mpm_cell_order() reports them.
+ * No memory is allocated, by this call or by any routine it calls: the
+ * working memory is one fixed array of static device storage inside the
+ * library (about 16.3 MiB, sized for MPM_NOALLOC_MAX_PARTICLES), which every
+ * GPU that loads the library holds until the process exits.
+ *   - n > MPM_NOALLOC_MAX_PARTICLES returns MPM_ERR_TOO_LARGE and does nothing.
+ *   - Work is queued on `stream` (a cudaStream_t, NULL for the default
+ *     stream); the outputs are ready once that stream has been synchronised.
+ *   - All calls share the one scratch array (each call starts by clearing
+ *     what it needs), so calls whose work overlaps on the GPU -- on different
+ *     streams, or from different threads -- race and corrupt each other's
+ *     results: serialise them.
+ *   - The first call on each device looks up the scratch array's device
+ *     address (a one-time set-up, done with that device current); make that
+ *     first call before any stream capture on the device.
+ *   - A non-finite position gets the out-of-grid key (the largest key). */
+#define MPM_NOALLOC_MAX_PARTICLES (1 << 20)
+int mpm_cell_order_noalloc(const mpm_grid_desc* grid, const double* d_pos, int64_t n, uint32_t* d_keys,
+                           uint32_t* d_order, void* stream);
 
 /* --- profiling ---------------------------------------------------------------
  * Per-kernel CUDA-event timers (the reference's a_Runtime, PhysicsEngine.h:87). */
