@@ -49,6 +49,7 @@ struct mpm_ctx {
     // options
     int floor_friction = 0;
     int profile = 0;
+    int p2g_reduce = 1, p2g_block = 256, pass_block = 256;
     // simulation scalars
     mpm_sim sim{0.0, 1.0e-3, 0.0, 0.0, 10.0, 0};
     // counts
@@ -66,11 +67,12 @@ struct mpm_ctx {
         backstress, mp_mg, strain_rate, material, pflags, dc_mult;
     // nodes
     DevBuf g_mass, g_mom, g_vel, g_force, g_ftemp, g_mg, g_state, g_fixed, g_friction, g_ratio, g_q, g_owner,
-        g_nowner, g_need;
+        g_nowner, g_need, g_list, g_count, rs_chunk;
+    int sm_count = 152;
     DevBuf cstart, cend;
     // sort
     DevBuf keys0, vals0, keys1, vals1, keys_copy, counts;
-    DevBuf dclist, mats, staging;
+    DevBuf dclist, mats, staging, tune_backup;
     // host pinned staging for the error word
     unsigned* h_err = nullptr;
     // profiling
@@ -86,8 +88,8 @@ struct mpm_ctx {
         DevBuf* list[] = {&xtab, &err_word, &pos, &vel, &fext, &mass, &vol, &vol0, &F, &stress, &strain, &eps_p,
                           &e_strain, &e_strain_max, &e_strain_ti, &e_plastic, &backstress, &mp_mg, &strain_rate,
                           &material, &pflags, &dc_mult, &g_mass, &g_mom, &g_vel, &g_force, &g_ftemp, &g_mg,
-                          &g_state, &g_fixed, &g_friction, &g_ratio, &g_q, &g_owner, &g_nowner, &g_need, &cstart,
-                          &cend, &keys0, &vals0, &keys1, &vals1, &keys_copy, &counts, &dclist, &mats, &staging};
+                          &g_state, &g_fixed, &g_friction, &g_ratio, &g_q, &g_owner, &g_nowner, &g_need, &g_list, &g_count, &rs_chunk, &cstart,
+                          &cend, &keys0, &vals0, &keys1, &vals1, &keys_copy, &counts, &dclist, &mats, &staging, &tune_backup};
         all.assign(std::begin(list), std::end(list));
     }
 };
@@ -257,21 +259,27 @@ void timeline_velocity(const mpm_ctx* c, double t, double out[3]) {
 }
 
 // ---- unpack / pack between host n x k row-major doubles and device SoA -----
+// shift_identity: the FP32 form stores a 3x3 F as H = F - I (diagonal
+// components 0, 4, 8 shifted by one, in FP64 before the conversion).
 template <typename T>
-__global__ void k_unpack(const double* __restrict__ src, T* __restrict__ dst, long long n, int k) {
+__global__ void k_unpack(const double* __restrict__ src, T* __restrict__ dst, long long n, int k, int shift_identity) {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= n * k) return;
     long long p = i / k;
     int c = (int)(i - p * k);
-    dst[(long long)c * n + p] = (T)src[i];
+    double v = src[i];
+    if (shift_identity && (c == 0 || c == 4 || c == 8)) v -= 1.0;
+    dst[(long long)c * n + p] = (T)v;
 }
 template <typename T>
-__global__ void k_pack(const T* __restrict__ src, double* __restrict__ dst, long long n, int k) {
+__global__ void k_pack(const T* __restrict__ src, double* __restrict__ dst, long long n, int k, int shift_identity) {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= n * k) return;
     long long p = i / k;
     int c = (int)(i - p * k);
-    dst[i] = (double)src[(long long)c * n + p];
+    double v = (double)src[(long long)c * n + p];
+    if (shift_identity && (c == 0 || c == 4 || c == 8)) v += 1.0;
+    dst[i] = v;
 }
 template <typename T>
 __global__ void k_fill(T* __restrict__ dst, long long n, T v) {
@@ -306,7 +314,8 @@ __global__ void k_clear_flag(uint8_t* __restrict__ pflags, long long n, uint8_t 
 }
 
 // Upload one field: host n x k doubles (or NULL -> default) into a device SoA array of the field's real type.
-int upload_field(mpm_ctx* c, DevBuf& dst, const double* host, long long n, int k, bool fp64, double def) {
+int upload_field(mpm_ctx* c, DevBuf& dst, const double* host, long long n, int k, bool fp64, double def,
+                 int shift_identity = 0) {
     size_t esz = fp64 ? 8 : 4;
     int rc = ensure(c, dst, (size_t)n * k * esz);
     if (rc) return rc;
@@ -317,10 +326,10 @@ int upload_field(mpm_ctx* c, DevBuf& dst, const double* host, long long n, int k
         CK(cudaMemcpyAsync(c->staging.p, host, (size_t)n * k * 8, cudaMemcpyHostToDevice, c->stream));
         if (fp64)
             LAUNCH("unpack", k_unpack<double>, blocks_for(n * k), NTHREADS, (const double*)c->staging.p,
-                   (double*)dst.p, n, k);
+                   (double*)dst.p, n, k, shift_identity);
         else
             LAUNCH("unpack", k_unpack<float>, blocks_for(n * k), NTHREADS, (const double*)c->staging.p,
-                   (float*)dst.p, n, k);
+                   (float*)dst.p, n, k, shift_identity);
     } else if (def == 0.0) {
         CK(cudaMemsetAsync(dst.p, 0, (size_t)n * k * esz, c->stream));
     } else if (fp64) {
@@ -331,15 +340,17 @@ int upload_field(mpm_ctx* c, DevBuf& dst, const double* host, long long n, int k
     return MPM_OK;
 }
 
-int download_field(mpm_ctx* c, const DevBuf& src, double* host, long long n, int k, bool fp64) {
+int download_field(mpm_ctx* c, const DevBuf& src, double* host, long long n, int k, bool fp64,
+                   int shift_identity = 0) {
     if (!host || n == 0) return MPM_OK;
     int rc = ensure(c, c->staging, (size_t)n * k * 8);
     if (rc) return rc;
     if (fp64)
         LAUNCH("pack", k_pack<double>, blocks_for(n * k), NTHREADS, (const double*)src.p, (double*)c->staging.p, n,
-               k);
+               k, shift_identity);
     else
-        LAUNCH("pack", k_pack<float>, blocks_for(n * k), NTHREADS, (const float*)src.p, (double*)c->staging.p, n, k);
+        LAUNCH("pack", k_pack<float>, blocks_for(n * k), NTHREADS, (const float*)src.p, (double*)c->staging.p, n, k,
+               shift_identity);
     CK(cudaMemcpyAsync(host, c->staging.p, (size_t)n * k * 8, cudaMemcpyDeviceToHost, c->stream));
     return MPM_OK;
 }
@@ -377,11 +388,21 @@ int step_impl(mpm_ctx* c, double dt, int contact) {
         const int nblocks = (int)((n + RS_TILE - 1) / RS_TILE);
         unsigned *kin = (unsigned*)c->keys0.p, *vin = (unsigned*)c->vals0.p;
         unsigned *kout = (unsigned*)c->keys1.p, *vout = (unsigned*)c->vals1.p;
+        const int hist_total = 256 * nblocks;
+        const int nchunks = (hist_total + RS_SCAN_CHUNK - 1) / RS_SCAN_CHUNK;
         for (int shift = 0; shift < bits; shift += 8) {
             LAUNCH("rs_hist", k_rs_hist, nblocks, RS_THREADS, kin, n, shift, (unsigned*)c->counts.p, nblocks);
-            LAUNCH("rs_scan", k_rs_scan, 1, 1024, (unsigned*)c->counts.p, 256 * nblocks);
+            const unsigned* chunk_prefix = nullptr;
+            if (nchunks > 1) {
+                LAUNCH("rs_scan", k_rs_scan_chunks, nchunks, RS_SCAN_THREADS, (unsigned*)c->counts.p, hist_total,
+                       (unsigned*)c->rs_chunk.p);
+                LAUNCH("rs_scan", k_rs_scan, 1, 1024, (unsigned*)c->rs_chunk.p, nchunks);
+                chunk_prefix = (const unsigned*)c->rs_chunk.p;
+            } else {
+                LAUNCH("rs_scan", k_rs_scan, 1, 1024, (unsigned*)c->counts.p, hist_total);
+            }
             LAUNCH("rs_scatter", k_rs_scatter, nblocks, RS_THREADS, kin, vin, kout, vout, n, shift,
-                   (const unsigned*)c->counts.p, nblocks);
+                   (const unsigned*)c->counts.p, nblocks, chunk_prefix);
             std::swap(kin, kout);
             std::swap(vin, vout);
         }
@@ -395,17 +416,32 @@ int step_impl(mpm_ctx* c, double dt, int contact) {
         }
         LAUNCH("cell_ranges", k_cell_ranges, blocks_for(n), NTHREADS, skeys, n, g, N.state,
                contact ? (unsigned*)c->cstart.p : nullptr, contact ? (unsigned*)c->cend.p : nullptr);
-        LAUNCH("p2g", k_p2g<T>, blocks_for(n), NTHREADS, P, N, g, skeys, perm, n);
+        // FP32 form: the contact mass gradient is accumulated by P2G itself
+        // (the bit-exact ordered gather below serves the FP64 form).
+        const int mg_in_p2g = (contact && c->form == MPM_FORM_FP32) ? 1 : 0;
+        if (c->p2g_reduce)
+            LAUNCH("p2g", (k_p2g<T, 1>), blocks_for(n, c->p2g_block), c->p2g_block, P, N, g, skeys, perm, n,
+                   mg_in_p2g);
+        else
+            LAUNCH("p2g", (k_p2g<T, 0>), blocks_for(n, c->p2g_block), c->p2g_block, P, N, g, skeys, perm, n,
+                   mg_in_p2g);
         if (c->ndc > 0) {
             CK(cudaMemsetAsync(c->g_owner.p, 0, (size_t)3 * nn * 4, c->stream));
             LAUNCH("dc_claim", k_dc_claim, blocks_for(c->ndc), NTHREADS, (const unsigned*)c->dclist.p, c->ndc, keys,
                    (const uint8_t*)c->pflags.p, g, (unsigned*)c->g_owner.p, nn, contact);
         }
         if (contact) {
-            CK(cudaMemsetAsync(c->g_need.p, 0, (size_t)nn * 4, c->stream));
-            LAUNCH("contact_need", k_contact_need<T>, blocks_for(n), NTHREADS, P, keys, g, (unsigned*)c->g_need.p);
-            LAUNCH("contact_mass_gradient", k_contact_mass_gradient<T>, blocks_for(nn, 128), 128, P, N, g,
-                   (const unsigned*)c->g_need.p, perm, (const unsigned*)c->cstart.p, (const unsigned*)c->cend.p);
+            if (!mg_in_p2g) {
+                CK(cudaMemsetAsync(c->g_need.p, 0, (size_t)nn * 4, c->stream));
+                CK(cudaMemsetAsync(c->g_count.p, 0, 4, c->stream));
+                LAUNCH("contact_need", k_contact_need<T>, blocks_for(n), NTHREADS, P, keys, g,
+                       (unsigned*)c->g_need.p);
+                LAUNCH("contact_compact", k_contact_compact, blocks_for(nn), NTHREADS, (const unsigned*)c->g_need.p,
+                       nn, (unsigned*)c->g_list.p, (unsigned*)c->g_count.p);
+                LAUNCH("contact_mass_gradient", k_contact_mass_gradient<T>, (unsigned)c->sm_count * 8, CG_WARPS * 32,
+                       P, N, g, (const unsigned*)c->g_list.p, (const unsigned*)c->g_count.p, perm,
+                       (const unsigned*)c->cstart.p, (const unsigned*)c->cend.p);
+            }
             LAUNCH("contact_mp_gradient", k_contact_mp_gradient<T>, blocks_for(n), NTHREADS, P, N, g, keys);
             LAUNCH("contact_reset", k_contact_reset<T>, blocks_for(nn), NTHREADS, N);
             LAUNCH("contact_normal", k_contact_normal<T>, blocks_for(n), NTHREADS, P, N, g, keys, 0);
@@ -443,7 +479,8 @@ int step_impl(mpm_ctx* c, double dt, int contact) {
         timeline_velocity(c, c->sim.time, a.tv);
         a.has_timeline = c->tl_t.empty() ? 0 : 1;
         a.contact = contact;
-        LAUNCH("pass2", k_pass2<T>, blocks_for(n), NTHREADS, P, N, g, keys, (const MatConst*)c->mats.p, c->nmat, a,
+        LAUNCH("pass2", k_pass2<T>, blocks_for(n, c->pass_block), c->pass_block, P, N, g, keys,
+               (const MatConst*)c->mats.p, c->nmat, a,
                err);
     }
     CK(cudaGetLastError());
@@ -474,7 +511,10 @@ int alloc_particles(mpm_ctx* c, long long n) {
         if (rc) return rc;
     }
     const long long nblocks = std::max<long long>(1, (n + RS_TILE - 1) / RS_TILE);
-    return ensure(c, c->counts, (size_t)256 * nblocks * 4);
+    int rc = ensure(c, c->counts, (size_t)256 * nblocks * 4);
+    if (rc) return rc;
+    const long long nchunks = (256 * nblocks + RS_SCAN_CHUNK - 1) / RS_SCAN_CHUNK;
+    return ensure(c, c->rs_chunk, (size_t)std::max<long long>(1, nchunks) * 4);
 }
 
 }  // namespace
@@ -524,6 +564,8 @@ int mpm_create(const mpm_grid_desc* grid, int form, mpm_ctx** out) {
     c->form = form;
     c->tsize = form == MPM_FORM_FP64 ? 8 : 4;
     cudaGetDevice(&c->device);
+    cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
+    if (c->sm_count <= 0) c->sm_count = 152;
     Geom& g = c->g;
     for (int a = 0; a < 3; ++a) {
         c->length[a] = grid->length[a];
@@ -565,7 +607,8 @@ int mpm_create(const mpm_grid_desc* grid, int form, mpm_ctx** out) {
                 {&c->g_force, 3 * nn * t}, {&c->g_ftemp, 3 * nn * t}, {&c->g_mg, 3 * nn * 8},
                 {&c->g_state, nn * 4},     {&c->g_fixed, nn},        {&c->g_friction, nn * 8},
                 {&c->g_ratio, 3 * nn * t}, {&c->g_q, 3 * nn * t},    {&c->g_owner, 3 * nn * 4},
-                {&c->g_nowner, nn * 4},    {&c->g_need, nn * 4},     {&c->cstart, (size_t)g.key_max * 4},
+                {&c->g_nowner, nn * 4},    {&c->g_need, nn * 4},     {&c->g_list, nn * 4},
+                {&c->g_count, 4},          {&c->cstart, (size_t)g.key_max * 4},
                 {&c->cend, (size_t)g.key_max * 4}};
     for (auto& e : plan) {
         if ((rc = ensure(c, *e.b, e.bytes))) return bail(rc);
@@ -606,6 +649,14 @@ int mpm_set_option(mpm_ctx* c, int key, double value) {
     switch (key) {
         case MPM_OPT_FLOOR_FRICTION: c->floor_friction = value != 0.0; return MPM_OK;
         case MPM_OPT_PROFILE: c->profile = value != 0.0; return MPM_OK;
+        case MPM_OPT_P2G_REDUCE: c->p2g_reduce = value != 0.0; return MPM_OK;
+        case MPM_OPT_P2G_BLOCK:
+        case MPM_OPT_PASS_BLOCK: {
+            int b = (int)value;
+            if (b != 128 && b != 256 && b != 512) return fail(c, MPM_ERR_ARG, "block size must be 128, 256 or 512");
+            (key == MPM_OPT_P2G_BLOCK ? c->p2g_block : c->pass_block) = b;
+            return MPM_OK;
+        }
         default: return fail(c, MPM_ERR_ARG, "unknown option %d", key);
     }
 }
@@ -674,9 +725,12 @@ int mpm_upload_particles(mpm_ctx* c, const mpm_particles* p, int64_t n) {
     for (auto& f : fields)
         if ((rc = upload_field(c, *f.b, f.h, n, f.k, f.fp64, f.def))) return rc;
     if (p->F) {
-        if ((rc = upload_field(c, c->F, p->F, n, 9, f64, 0.0))) return rc;
+        if ((rc = upload_field(c, c->F, p->F, n, 9, f64, 0.0, f64 ? 0 : 1))) return rc;
     } else if (n > 0) {
-        LAUNCH("fill", k_identity9, blocks_for(9 * n), NTHREADS, c->F.p, (long long)n, f64 ? 1 : 0);
+        if (f64)
+            LAUNCH("fill", k_identity9, blocks_for(9 * n), NTHREADS, c->F.p, (long long)n, 1);
+        else
+            CK(cudaMemsetAsync(c->F.p, 0, (size_t)n * 9 * sizeof(float), c->stream));  // H = F - I = 0
     }
     if (n > 0) {
         if (p->material)
@@ -810,7 +864,8 @@ int mpm_download_particles(mpm_ctx* c, mpm_particles* p) {
                   {&c->strain_rate, p->strain_rate, 6, f64}};
     for (auto& f : fields) {
         if (!f.h) continue;
-        if ((rc = download_field(c, *f.b, f.h, n, f.k, f.fp64))) return rc;
+        const int shift = (f.b == &c->F && !f64) ? 1 : 0;
+        if ((rc = download_field(c, *f.b, f.h, n, f.k, f.fp64, shift))) return rc;
         CK(cudaStreamSynchronize(c->stream));  // staging is reused by the next field
     }
     if (n > 0) {
@@ -923,6 +978,92 @@ int mpm_cell_order(mpm_ctx* c, uint32_t* keys, uint32_t* sorted_order, int64_t n
         CK(cudaMemcpyAsync(sorted_order, c->last_perm, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     return MPM_OK;
+}
+
+int mpm_autotune(mpm_ctx* c, int32_t steps, double dt, int contact, mpm_tune_result* out) {
+    if (!c) return MPM_ERR_ARG;
+    if (steps < 1 || !(dt > 0.0)) return fail(c, MPM_ERR_ARG, "bad autotune request");
+    if (!c->have_particles) return fail(c, MPM_ERR_STATE, "no particles uploaded");
+    // everything a step writes that outlives the step
+    DevBuf* state[] = {&c->pos,        &c->vel,      &c->F,          &c->stress,  &c->strain,  &c->eps_p,
+                       &c->vol,        &c->e_strain, &c->e_strain_max, &c->e_strain_ti, &c->e_plastic,
+                       &c->backstress, &c->mp_mg,    &c->strain_rate, &c->g_mass, &c->g_mom,   &c->g_vel,
+                       &c->g_force,    &c->g_ftemp,  &c->g_mg,       &c->g_state};
+    size_t total = 0;
+    for (DevBuf* b : state) total += b->bytes;
+    int rc = ensure(c, c->tune_backup, total);
+    if (rc) return rc;
+    auto copy_all = [&](bool save) -> int {
+        size_t off = 0;
+        for (DevBuf* b : state) {
+            char* bk = (char*)c->tune_backup.p + off;
+            if (b->bytes)
+                CK(cudaMemcpyAsync(save ? bk : b->p, save ? b->p : bk, b->bytes, cudaMemcpyDeviceToDevice,
+                                   c->stream));
+            off += b->bytes;
+        }
+        return MPM_OK;
+    };
+    if ((rc = copy_all(true))) return rc;
+    const mpm_sim sim0 = c->sim;
+    const int prof0 = c->profile;
+    c->profile = 0;
+    const int old[3] = {c->p2g_reduce, c->p2g_block, c->pass_block};
+    int best[3] = {old[0], old[1], old[2]};
+    double best_ms = 1e300, worst_ms = 0.0;
+    int ncand = 0;
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    const int blocks[3] = {128, 256, 512};
+    for (int red = 0; red < 2 && rc == MPM_OK; ++red)
+        for (int pb = 0; pb < 3 && rc == MPM_OK; ++pb)
+            for (int qb = 0; qb < 3 && rc == MPM_OK; ++qb) {
+                c->p2g_reduce = red;
+                c->p2g_block = blocks[pb];
+                c->pass_block = blocks[qb];
+                if ((rc = step(c, dt, contact))) break;  // warm-up for this configuration
+                cudaEventRecord(a, c->stream);
+                for (int s = 0; s < steps && rc == MPM_OK; ++s) rc = step(c, dt, contact);
+                cudaEventRecord(b, c->stream);
+                cudaEventSynchronize(b);
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, a, b);
+                const double per = ms / steps;
+                ++ncand;
+                if (per < best_ms) {
+                    best_ms = per;
+                    best[0] = red;
+                    best[1] = blocks[pb];
+                    best[2] = blocks[qb];
+                }
+                worst_ms = std::max(worst_ms, per);
+                if (copy_all(false) != MPM_OK) rc = MPM_ERR_CUDA;
+                c->sim = sim0;
+            }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    c->profile = prof0;
+    c->sim = sim0;
+    if (rc) {
+        c->p2g_reduce = old[0];
+        c->p2g_block = old[1];
+        c->pass_block = old[2];
+        return rc;
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    c->p2g_reduce = best[0];
+    c->p2g_block = best[1];
+    c->pass_block = best[2];
+    if (out) {
+        out->p2g_reduce = best[0];
+        out->p2g_block = best[1];
+        out->pass_block = best[2];
+        out->candidates = ncand;
+        out->best_ms_per_step = best_ms;
+        out->worst_ms_per_step = worst_ms;
+    }
+    return check_device_error(c);
 }
 
 int mpm_profile_read(mpm_ctx* c, mpm_kernel_stat* out, int32_t max, int32_t* count) {

@@ -47,10 +47,11 @@ __global__ void k_reset_grid(NView<T> nd, int contact) {
 }
 
 // ---------------------------------------------------------------------------
-// cell keys: base cell b = floor(x/h) per axis with the IEEE quotient, as
-// glm::floor(d3Position / d3_Length_Cell) (GridPoint_Mediator.cpp:8), so the
-// cell index is bit-identical to the reference.  Particles whose base cell
-// lies outside [-1, cells] have no node in range and get key_max.
+// cell keys: base cell b = floor(x/h) per axis with the correctly rounded
+// quotient, as glm::floor(d3Position / d3_Length_Cell)
+// (GridPoint_Mediator.cpp:8), so the cell index is bit-identical to the
+// reference.  Particles whose base cell lies outside [-1, cells] have no node
+// in range and get key_max.
 // ---------------------------------------------------------------------------
 static __global__ void k_cell_keys(const double* __restrict__ pos, long long n, Geom g, unsigned* __restrict__ keys,
                             unsigned* __restrict__ vals, unsigned* __restrict__ keys_copy, unsigned* err) {
@@ -60,7 +61,7 @@ static __global__ void k_cell_keys(const double* __restrict__ pos, long long n, 
     int b[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        double q = __ddiv_rn(pos[a * n + p], g.h[a]);
+        double q = div_rn_by(pos[a * n + p], g.h[a], g.inv_h[a]);
         if (!isfinite(q)) {
             atomicOr(err, ERR_NONFINITE_POSITION);
             ok = false;
@@ -130,63 +131,81 @@ struct Runs {
 // ---------------------------------------------------------------------------
 // P2G (M2G, …MPLocks.cpp:48-89): per particle and corner, mass N m, momentum
 // N (m v), force -V (grad N . sigma) + N f_ext (Voigt order xx yy zz xy yz zx,
-// :79-84).  One thread per sorted slot; contributions of a cell's particles
-// are summed across lanes before one atomic per (node, field).
+// :79-84), and (with_mg) the mass gradient grad N m of the contact path
+// (…_Contact.cpp:131).  One thread per sorted slot.
+//   REDUCE = 1: a cell's particles sit in adjacent lanes; their contributions
+//               are summed across the lanes of the run first, then one atomic
+//               per (node, field) per run.
+//   REDUCE = 0: one atomic per (particle, node, field); the adds happen in L2.
+// The choice (and the block size) is made per form by the autotuner.
 // ---------------------------------------------------------------------------
-template <typename T>
-__global__ void __launch_bounds__(256) k_p2g(PView<T> P, NView<T> nd, Geom g, const unsigned* __restrict__ skeys,
-                                             const unsigned* __restrict__ perm, long long n) {
+template <typename T, int REDUCE>
+__global__ void __launch_bounds__(512) k_p2g(PView<T> P, NView<T> nd, Geom g, const unsigned* __restrict__ skeys,
+                                             const unsigned* __restrict__ perm, long long n, int with_mg) {
     long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     unsigned key = (s < n) ? skeys[s] : 0xffffffffu;
     const bool valid = key < g.key_max;
     Runs run;
-    run.init(key);
+    if (REDUCE) run.init(key);
+    else if (!valid) return;
     const long long np = P.n, nn = nd.nn;
     int b[3] = {0, 0, 0};
     Bases<T> B;
-    T m = 0, V = 0, v[3] = {0, 0, 0}, sg[6] = {0, 0, 0, 0, 0, 0}, fe[3] = {0, 0, 0};
+    T m = 0, vs[6] = {0, 0, 0, 0, 0, 0}, mv[3] = {0, 0, 0}, fe[3] = {0, 0, 0};
     if (valid) {
         long long p = perm[s];
         key_to_base(key, g, b);
         double x[3] = {P.pos[p], P.pos[np + p], P.pos[2 * np + p]};
         B.init(g, x, b);
         m = P.mass[p];
-        V = P.vol[p];
+        const T V = P.vol[p];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            v[c] = P.vel[c * np + p];
+            mv[c] = m * P.vel[c * np + p];
             fe[c] = P.fext[c * np + p];
         }
 #pragma unroll
-        for (int c = 0; c < 6; ++c) sg[c] = P.stress[c * np + p];
+        for (int c = 0; c < 6; ++c) vs[c] = -V * P.stress[c * np + p];  // -V sigma
     }
-    T mv[3] = {m * v[0], m * v[1], m * v[2]};
 #pragma unroll 1
     for (int k = 0; k < 8; ++k) {
         T N = 0, G[3] = {0, 0, 0};
         if (valid) B.corner(k, N, G);
-        T c0 = N * m;
-        T c1 = N * mv[0], c2 = N * mv[1], c3 = N * mv[2];
-        T c4 = -V * (G[0] * sg[0] + G[1] * sg[3] + G[2] * sg[5]) + N * fe[0];
-        T c5 = -V * (G[1] * sg[1] + G[0] * sg[3] + G[2] * sg[4]) + N * fe[1];
-        T c6 = -V * (G[2] * sg[2] + G[0] * sg[5] + G[1] * sg[4]) + N * fe[2];
-        c0 = run.sum(c0);
-        c1 = run.sum(c1);
-        c2 = run.sum(c2);
-        c3 = run.sum(c3);
-        c4 = run.sum(c4);
-        c5 = run.sum(c5);
-        c6 = run.sum(c6);
-        if (valid && run.tail) {
+        T c[10];
+        c[0] = N * m;
+        c[1] = N * mv[0];
+        c[2] = N * mv[1];
+        c[3] = N * mv[2];
+        c[4] = G[0] * vs[0] + G[1] * vs[3] + G[2] * vs[5] + N * fe[0];
+        c[5] = G[1] * vs[1] + G[0] * vs[3] + G[2] * vs[4] + N * fe[1];
+        c[6] = G[2] * vs[2] + G[0] * vs[5] + G[1] * vs[4] + N * fe[2];
+        c[7] = G[0] * m;
+        c[8] = G[1] * m;
+        c[9] = G[2] * m;
+        const int nf = with_mg ? 10 : 7;
+        if (REDUCE) {
+#pragma unroll
+            for (int f = 0; f < 7; ++f) c[f] = run.sum(c[f]);
+            if (with_mg) {
+#pragma unroll
+                for (int f = 7; f < 10; ++f) c[f] = run.sum(c[f]);
+            }
+        }
+        if (valid && (!REDUCE || run.tail)) {
             long long nid = corner_node(g, b, k);
             if (nid >= 0) {
-                atomicAdd(&nd.mass[nid], c0);
-                atomicAdd(&nd.mom[nid], c1);
-                atomicAdd(&nd.mom[nn + nid], c2);
-                atomicAdd(&nd.mom[2 * nn + nid], c3);
-                atomicAdd(&nd.force[nid], c4);
-                atomicAdd(&nd.force[nn + nid], c5);
-                atomicAdd(&nd.force[2 * nn + nid], c6);
+                atomicAdd(&nd.mass[nid], c[0]);
+                atomicAdd(&nd.mom[nid], c[1]);
+                atomicAdd(&nd.mom[nn + nid], c[2]);
+                atomicAdd(&nd.mom[2 * nn + nid], c[3]);
+                atomicAdd(&nd.force[nid], c[4]);
+                atomicAdd(&nd.force[nn + nid], c[5]);
+                atomicAdd(&nd.force[2 * nn + nid], c[6]);
+                if (nf == 10) {
+                    atomicAdd(&nd.mg[nid], (double)c[7]);
+                    atomicAdd(&nd.mg[nn + nid], (double)c[8]);
+                    atomicAdd(&nd.mg[2 * nn + nid], (double)c[9]);
+                }
             }
         }
     }
@@ -462,7 +481,7 @@ struct StepArgs {
 // One thread per particle in index order (coalesced particle streams).
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(256) k_pass2(PView<T> P, NView<T> nd, Geom g, const unsigned* __restrict__ keys,
+__global__ void __launch_bounds__(512) k_pass2(PView<T> P, NView<T> nd, Geom g, const unsigned* __restrict__ keys,
                                                const MatConst* __restrict__ mats, int nmat, StepArgs a,
                                                unsigned* err) {
     long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -503,14 +522,15 @@ __global__ void __launch_bounds__(256) k_pass2(PView<T> P, NView<T> nd, Geom g, 
 #pragma unroll
             for (int c = 0; c < 3; ++c) P.pos[c * np + p] = x[c];
         }
-        // strain increment: (1 + L_ii dt) - 1 on the diagonal, (L_ij + L_ji) dt off it
+        // strain increment: diagonal from dF = I + L dt (form-specific, see
+        // Kinematics), off-diagonal (L_ij + L_ji) dt in Voigt engineering shear
         T Ldt[9];
 #pragma unroll
         for (int k = 0; k < 9; ++k) Ldt[k] = L[k] * dt;
         T e[6];
-        e[0] = ((T)1 + Ldt[0]) - (T)1;
-        e[1] = ((T)1 + Ldt[4]) - (T)1;
-        e[2] = ((T)1 + Ldt[8]) - (T)1;
+        e[0] = Kinematics<T>::strain_diag(Ldt[0]);
+        e[1] = Kinematics<T>::strain_diag(Ldt[4]);
+        e[2] = Kinematics<T>::strain_diag(Ldt[8]);
         e[3] = Ldt[1] + Ldt[3];
         e[4] = Ldt[5] + Ldt[7];
         e[5] = Ldt[6] + Ldt[2];
@@ -519,32 +539,14 @@ __global__ void __launch_bounds__(256) k_pass2(PView<T> P, NView<T> nd, Geom g, 
 #pragma unroll
         for (int k = 0; k < 9; ++k) F[k] = P.F[k * np + p];
         T Fn[9];
-        if (!a.contact) {
-            // F <- F * dF, dF = I + L dt (glm column-major product)
-#pragma unroll
-            for (int c = 0; c < 3; ++c)
-#pragma unroll
-                for (int r = 0; r < 3; ++r) {
-                    T d0 = (c == 0 ? (T)1 : (T)0) + Ldt[3 * c + 0];
-                    T d1 = (c == 1 ? (T)1 : (T)0) + Ldt[3 * c + 1];
-                    T d2 = (c == 2 ? (T)1 : (T)0) + Ldt[3 * c + 2];
-                    Fn[3 * c + r] = F[r] * d0 + F[3 + r] * d1 + F[6 + r] * d2;
-                }
-        } else {
-            // F <- F + (L F) dt
-#pragma unroll
-            for (int c = 0; c < 3; ++c)
-#pragma unroll
-                for (int r = 0; r < 3; ++r)
-                    Fn[3 * c + r] = F[3 * c + r] + (L[r] * F[3 * c] + L[3 + r] * F[3 * c + 1] + L[6 + r] * F[3 * c + 2]) * dt;
-            // contact: strain is accumulated before the material check (…_Contact.cpp:483-484)
+        Kinematics<T>::update(a.contact != 0, F, L, Ldt, dt, Fn);
+        if (a.contact) {
+            // contact: strain, F and V are updated before the material check (…_Contact.cpp:464-484)
 #pragma unroll
             for (int k = 0; k < 6; ++k) P.strain[k * np + p] += e[k];
 #pragma unroll
             for (int k = 0; k < 9; ++k) P.F[k * np + p] = Fn[k];
-            T det = Fn[0] * (Fn[4] * Fn[8] - Fn[7] * Fn[5]) - Fn[3] * (Fn[1] * Fn[8] - Fn[7] * Fn[2]) +
-                    Fn[6] * (Fn[1] * Fn[5] - Fn[4] * Fn[2]);
-            P.vol[p] = det * P.vol0[p];
+            P.vol[p] = Kinematics<T>::det(Fn) * P.vol0[p];
         }
         if (mi >= 0 && mi < nmat) {
             const MatConst& M = mats[mi];
@@ -558,9 +560,7 @@ __global__ void __launch_bounds__(256) k_pass2(PView<T> P, NView<T> nd, Geom g, 
             if (!a.contact) {
 #pragma unroll
                 for (int k = 0; k < 9; ++k) P.F[k * np + p] = Fn[k];
-                T det = Fn[0] * (Fn[4] * Fn[8] - Fn[7] * Fn[5]) - Fn[3] * (Fn[1] * Fn[8] - Fn[7] * Fn[2]) +
-                        Fn[6] * (Fn[1] * Fn[5] - Fn[4] * Fn[2]);
-                V = det * P.vol0[p];
+                V = Kinematics<T>::det(Fn) * P.vol0[p];
                 P.vol[p] = V;
 #pragma unroll
                 for (int k = 0; k < 6; ++k) P.strain[k * np + p] += e[k];
@@ -639,34 +639,42 @@ __global__ void k_contact_need(PView<T> P, const unsigned* __restrict__ keys, Ge
     }
 }
 
-template <typename T>
-__global__ void k_contact_mass_gradient(PView<T> P, NView<T> nd, Geom g, const unsigned* __restrict__ need,
-                                        const unsigned* __restrict__ perm, const unsigned* __restrict__ cstart,
-                                        const unsigned* __restrict__ cend) {
+// Compact the needed nodes into a list (order irrelevant: nodes are independent).
+static __global__ void k_contact_compact(const unsigned* __restrict__ need, long long nn, unsigned* __restrict__ list,
+                                         unsigned* __restrict__ count) {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= nd.nn || !need[i]) return;
-    const long long np = P.n, nn = nd.nn;
-    int node[3];
-    node[0] = (int)(i % g.nn[0]);
-    node[1] = (int)((i / g.nn[0]) % g.nn[1]);
-    node[2] = (int)(i / ((long long)g.nn[0] * g.nn[1]));
+    bool take = i < nn && need[i];
+    unsigned m = __ballot_sync(FULL_MASK, take);
+    if (!m) return;
+    int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(count, (unsigned)__popc(m));
+    base = __shfl_sync(m, base, leader);
+    if (take) list[base + __popc(m & ((1u << lane) - 1u))] = (unsigned)i;
+}
+
+// One warp per needed node: gather the particle ids of the eight surrounding
+// cells into shared memory, rank them by id, compute each pair's exact
+// grad N * m in parallel, then add them in id order on one lane.  Nodes with
+// more than CG_CAP contributors take the one-lane merge below.
+constexpr int CG_WARPS = 4;
+constexpr int CG_CAP = 256;
+
+template <typename T>
+__device__ __noinline__ void mass_gradient_merge(const PView<T>& P, const Geom& g, const int node[3],
+                                                 const unsigned* __restrict__ perm, const unsigned cs[8],
+                                                 const unsigned ce[8], double gsum[3]) {
+    const long long np = P.n;
     unsigned cur[8], end[8];
-    int nc = 0;
     for (int k = 0; k < 8; ++k) {
-        int cb[3] = {node[0] - ((k >> 2) & 1), node[1] - ((k >> 1) & 1), node[2] - (k & 1)};
-        unsigned key = (unsigned)((cb[0] + 1) + g.kd[0] * ((cb[1] + 1) + g.kd[1] * (cb[2] + 1)));
-        unsigned s0 = cstart[key], s1 = cend[key];
-        if (s1 > s0) {
-            cur[nc] = s0;
-            end[nc] = s1;
-            ++nc;
-        }
+        cur[k] = cs[k];
+        end[k] = ce[k];
     }
-    double gsum[3] = {0.0, 0.0, 0.0};
+    gsum[0] = gsum[1] = gsum[2] = 0.0;
     while (true) {
         int best = -1;
         unsigned bp = 0xffffffffu;
-        for (int c = 0; c < nc; ++c) {
+        for (int c = 0; c < 8; ++c) {
             if (cur[c] < end[c]) {
                 unsigned pp = perm[cur[c]];
                 if (pp < bp) {
@@ -681,11 +689,100 @@ __global__ void k_contact_mass_gradient(PView<T> P, NView<T> nd, Geom g, const u
         double G[3];
         exact_gradient(g, x, node, G);
         double m = (double)P.mass[bp];
-#pragma unroll
         for (int c = 0; c < 3; ++c) gsum[c] = __dadd_rn(gsum[c], __dmul_rn(G[c], m));
     }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(CG_WARPS * 32) k_contact_mass_gradient(PView<T> P, NView<T> nd, Geom g,
+                                                                         const unsigned* __restrict__ list,
+                                                                         const unsigned* __restrict__ count,
+                                                                         const unsigned* __restrict__ perm,
+                                                                         const unsigned* __restrict__ cstart,
+                                                                         const unsigned* __restrict__ cend) {
+    __shared__ unsigned s_id[CG_WARPS][CG_CAP];
+    __shared__ double s_c[CG_WARPS][CG_CAP][3];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long np = P.n, nn = nd.nn;
+    const unsigned total_nodes = *count;
+    for (unsigned item = blockIdx.x * CG_WARPS + w; item < total_nodes; item += gridDim.x * CG_WARPS) {
+        const long long i = list[item];
+        int node[3];
+        node[0] = (int)(i % g.nn[0]);
+        node[1] = (int)((i / g.nn[0]) % g.nn[1]);
+        node[2] = (int)(i / ((long long)g.nn[0] * g.nn[1]));
+        // lanes 0..7: the eight surrounding cells (cell = node - {0,1}^3)
+        unsigned s0 = 0, len = 0;
+        if (lane < 8) {
+            int cb[3] = {node[0] - ((lane >> 2) & 1), node[1] - ((lane >> 1) & 1), node[2] - (lane & 1)};
+            unsigned key = (unsigned)((cb[0] + 1) + g.kd[0] * ((cb[1] + 1) + g.kd[1] * (cb[2] + 1)));
+            s0 = cstart[key];
+            unsigned s1 = cend[key];
+            len = s1 > s0 ? s1 - s0 : 0u;
+        }
+        // exclusive offsets of the segments
+        unsigned off = len;
 #pragma unroll
-    for (int c = 0; c < 3; ++c) nd.mg[c * nn + i] = gsum[c];
+        for (int d = 1; d < 8; d <<= 1) {
+            unsigned o = __shfl_up_sync(FULL_MASK, off, d);
+            if (lane >= d) off += o;
+        }
+        const unsigned total = __shfl_sync(FULL_MASK, off, 7);
+        off -= len;
+        unsigned segs[8], offs[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            segs[k] = __shfl_sync(FULL_MASK, s0, k);
+            offs[k] = __shfl_sync(FULL_MASK, off, k);
+        }
+        double gsum[3] = {0.0, 0.0, 0.0};
+        if (total > (unsigned)CG_CAP) {
+            if (lane == 0) {
+                unsigned cs[8], ce[8];
+                for (int k = 0; k < 8; ++k) {
+                    cs[k] = segs[k];
+                    ce[k] = segs[k] + ((k < 7 ? offs[k + 1] : total) - offs[k]);
+                }
+                mass_gradient_merge<T>(P, g, node, perm, cs, ce, gsum);
+            }
+        } else {
+            for (unsigned e = lane; e < total; e += 32) {
+                int k = 0;
+#pragma unroll
+                for (int kk = 1; kk < 8; ++kk)
+                    if (e >= offs[kk]) k = kk;
+                s_id[w][e] = perm[segs[k] + (e - offs[k])];
+            }
+            __syncwarp();
+            for (unsigned e = lane; e < total; e += 32) {
+                const unsigned id = s_id[w][e];
+                unsigned rank = 0;
+                for (unsigned j = 0; j < total; ++j) rank += s_id[w][j] < id ? 1u : 0u;
+                double x[3] = {P.pos[id], P.pos[np + id], P.pos[2 * np + id]};
+                double G[3];
+                exact_gradient(g, x, node, G);
+                const double m = (double)P.mass[id];
+                s_c[w][rank][0] = __dmul_rn(G[0], m);
+                s_c[w][rank][1] = __dmul_rn(G[1], m);
+                s_c[w][rank][2] = __dmul_rn(G[2], m);
+            }
+            __syncwarp();
+            if (lane < 3) {
+                double acc = 0.0;
+                for (unsigned e = 0; e < total; ++e) acc = __dadd_rn(acc, s_c[w][e][lane]);
+                gsum[lane] = acc;
+            }
+        }
+        if (total > (unsigned)CG_CAP) {
+            if (lane == 0) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) nd.mg[c * nn + i] = gsum[c];
+            }
+        } else if (lane < 3) {
+            nd.mg[lane * nn + i] = gsum[lane];
+        }
+        __syncwarp();
+    }
 }
 
 // Surface particle normal: the corner gradient of largest norm, first wins on ties (:156-172).

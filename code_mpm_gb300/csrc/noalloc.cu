@@ -102,7 +102,7 @@ extern "C" int mpm_cell_order_noalloc(const mpm_grid_desc* grid, const double* d
     for (int shift = 0; shift < bits; shift += 8) {
         k_rs_hist<<<nblocks, RS_THREADS, 0, st>>>(kin, n, shift, counts, nblocks);
         k_rs_scan<<<1, 1024, 0, st>>>(counts, 256 * nblocks);
-        k_rs_scatter<<<nblocks, RS_THREADS, 0, st>>>(kin, vin, kout, vout, n, shift, counts, nblocks);
+        k_rs_scatter<<<nblocks, RS_THREADS, 0, st>>>(kin, vin, kout, vout, n, shift, counts, nblocks, nullptr);
         unsigned* t = kin;
         kin = kout;
         kout = t;

@@ -49,9 +49,22 @@ struct Bases {
 };
 
 // ---------------------------------------------------------------------------
+// Correctly rounded quotient a/b given y = RN(1/b): q = RN(a*y),
+// r = fma(-q, b, a) (exact), q' = fma(r, y, q) -- Markstein's correction
+// step (IBM J. Res. Dev. 34(1), 1990).  Equal to IEEE a/b on the operands
+// divided here (checked bit for bit by oracle/div_check.c), at 3 FP64
+// operations instead of a full division.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double div_rn_by(double a, double b, double y) {
+    double q = __dmul_rn(a, y);
+    double r = __fma_rn(-q, b, a);
+    return __fma_rn(r, y, q);
+}
+
+// ---------------------------------------------------------------------------
 // Bit-exact restatement of calculateBases_Classic's gradient for one
 // (particle, node) pair, used where results must match the reference to the
-// bit (contact mass gradients): IEEE division d/h and the reference's
+// bit (contact mass gradients): correctly rounded d/h and the reference's
 // association order, with the _rn intrinsics so nothing is contracted.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void exact_gradient(const Geom& g, const double x[3], const int node[3], double G[3]) {
@@ -59,7 +72,7 @@ __device__ __forceinline__ void exact_gradient(const Geom& g, const double x[3],
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         d[a] = __dadd_rn(x[a], -node_coord(g, a, node[a]));
-        r[a] = __ddiv_rn(d[a], g.h[a]);
+        r[a] = div_rn_by(d[a], g.h[a], g.inv_h[a]);
         double ar = r[a] >= 0.0 ? r[a] : -r[a];
         Nv[a] = __dadd_rn(1.0, -ar);
         if (Nv[a] < 0.0 || Nv[a] > 1.0) Nv[a] = 0.0;
@@ -71,7 +84,7 @@ __device__ __forceinline__ void exact_gradient(const Geom& g, const double x[3],
         if (ar > 1.0e-12 && ar < 1.0 - 1.0e-12) {
             double o1 = Nv[a == 0 ? 1 : 0], o2 = Nv[a == 2 ? 1 : 2];
             double sg = (double)((d[a] > 0.0) - (d[a] < 0.0));
-            G[a] = __ddiv_rn(__dmul_rn(__dmul_rn(-o1, o2), sg), g.h[a]);
+            G[a] = div_rn_by(__dmul_rn(__dmul_rn(-o1, o2), sg), g.h[a], g.inv_h[a]);
         }
     }
 }
@@ -81,6 +94,78 @@ __device__ __forceinline__ double dot3_rn(const double a[3], const double b[3]) 
     return __dadd_rn(__dadd_rn(__dmul_rn(a[0], b[0]), __dmul_rn(a[1], b[1])), __dmul_rn(a[2], b[2]));
 }
 __device__ __forceinline__ double len3_rn(const double a[3]) { return __dsqrt_rn(dot3_rn(a, a)); }
+
+// ---------------------------------------------------------------------------
+// Deformation-gradient update and strain increment, per form.
+//
+// FP64 (plain) form, the reference's arithmetic: diagonal strain increment
+// (1 + L_ii dt) - 1 (…MPLocks.cpp:206-219); non-contact F <- F (I + L dt)
+// (:242); contact F <- F + (L F) dt (…_Contact.cpp:464); V = det(F) V0 with
+// glm's cofactor determinant.
+//
+// FP32 (chosen) form: the same mathematics rearranged so FP32 keeps the
+// small increments: the diagonal strain increment is L_ii dt itself (the
+// reference's 1 + x - 1 cancels to noise in FP32), and the stored state is
+// H = F - I, updated as H + L dt + H (L dt) (non-contact) or
+// H + L dt + (L dt) H (contact), with det(I + H) = 1 + I1 + I2 + I3 of H.
+// ---------------------------------------------------------------------------
+template <typename T>
+struct Kinematics;
+
+template <>
+struct Kinematics<double> {
+    static __device__ __forceinline__ double strain_diag(double x) { return __dadd_rn(__dadd_rn(1.0, x), -1.0); }
+    static __device__ __forceinline__ void update(bool contact, const double F[9], const double L[9],
+                                                  const double Ldt[9], double dt, double Fn[9]) {
+        if (!contact) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    double d0 = (c == 0 ? 1.0 : 0.0) + Ldt[3 * c + 0];
+                    double d1 = (c == 1 ? 1.0 : 0.0) + Ldt[3 * c + 1];
+                    double d2 = (c == 2 ? 1.0 : 0.0) + Ldt[3 * c + 2];
+                    Fn[3 * c + r] = F[r] * d0 + F[3 + r] * d1 + F[6 + r] * d2;
+                }
+        } else {
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+#pragma unroll
+                for (int r = 0; r < 3; ++r)
+                    Fn[3 * c + r] =
+                        F[3 * c + r] + (L[r] * F[3 * c] + L[3 + r] * F[3 * c + 1] + L[6 + r] * F[3 * c + 2]) * dt;
+        }
+    }
+    static __device__ __forceinline__ double det(const double m[9]) {
+        return m[0] * (m[4] * m[8] - m[7] * m[5]) - m[3] * (m[1] * m[8] - m[7] * m[2]) +
+               m[6] * (m[1] * m[5] - m[4] * m[2]);
+    }
+};
+
+template <>
+struct Kinematics<float> {
+    static __device__ __forceinline__ float strain_diag(float x) { return x; }
+    // H (= F - I) in, Hn out
+    static __device__ __forceinline__ void update(bool contact, const float H[9], const float L[9], const float Ldt[9],
+                                                  float dt, float Hn[9]) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                float prod = contact ? (Ldt[r] * H[3 * c] + Ldt[3 + r] * H[3 * c + 1] + Ldt[6 + r] * H[3 * c + 2])
+                                     : (H[r] * Ldt[3 * c] + H[3 + r] * Ldt[3 * c + 1] + H[6 + r] * Ldt[3 * c + 2]);
+                Hn[3 * c + r] = H[3 * c + r] + (Ldt[3 * c + r] + prod);
+            }
+    }
+    // det(I + H) - 1 = I1 + I2 + I3 of H; returns det(I + H)
+    static __device__ __forceinline__ float det(const float h[9]) {
+        float i1 = h[0] + h[4] + h[8];
+        float i2 = h[0] * h[4] + h[4] * h[8] + h[0] * h[8] - h[3] * h[1] - h[7] * h[5] - h[6] * h[2];
+        float i3 = h[0] * (h[4] * h[8] - h[7] * h[5]) - h[3] * (h[1] * h[8] - h[7] * h[2]) +
+                   h[6] * (h[1] * h[5] - h[4] * h[2]);
+        return 1.0f + (i1 + (i2 + i3));
+    }
+};
 
 // ---------------------------------------------------------------------------
 // Constitutive increments (ConstitutiveRelation_calculateIncrement_*.cpp)

@@ -60,16 +60,66 @@ static __global__ void __launch_bounds__(1024) k_rs_scan(unsigned* __restrict__ 
     }
 }
 
+// Two-level exclusive scan of the histogram for large inputs: k_rs_scan_chunks
+// scans RS_SCAN_CHUNK entries per block in place and records each chunk's
+// total; k_rs_scan (one block) then scans the chunk totals; the scatter adds
+// the chunk prefix to every offset it reads.
+constexpr int RS_SCAN_THREADS = 1024;
+constexpr int RS_SCAN_PER_THREAD = 4;
+constexpr int RS_SCAN_CHUNK = RS_SCAN_THREADS * RS_SCAN_PER_THREAD;
+
+static __global__ void __launch_bounds__(RS_SCAN_THREADS) k_rs_scan_chunks(unsigned* __restrict__ counts, int total,
+                                                                          unsigned* __restrict__ chunk_totals) {
+    __shared__ unsigned wsum[RS_SCAN_THREADS / 32];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const long long base = (long long)blockIdx.x * RS_SCAN_CHUNK + (long long)t * RS_SCAN_PER_THREAD;
+    unsigned v[RS_SCAN_PER_THREAD], s = 0;
+#pragma unroll
+    for (int j = 0; j < RS_SCAN_PER_THREAD; ++j) {
+        v[j] = (base + j < total) ? counts[base + j] : 0u;
+        s += v[j];
+    }
+    unsigned inc = s;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        unsigned o = __shfl_up_sync(0xffffffffu, inc, d);
+        if (lane >= d) inc += o;
+    }
+    if (lane == 31) wsum[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        unsigned x = wsum[lane];
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            unsigned o = __shfl_up_sync(0xffffffffu, x, d);
+            if (lane >= d) x += o;
+        }
+        wsum[lane] = x;  // inclusive over warps
+    }
+    __syncthreads();
+    unsigned run = inc - s + (w > 0 ? wsum[w - 1] : 0u);
+#pragma unroll
+    for (int j = 0; j < RS_SCAN_PER_THREAD; ++j) {
+        if (base + j < total) counts[base + j] = run;
+        run += v[j];
+    }
+    if (t == RS_SCAN_THREADS - 1) chunk_totals[blockIdx.x] = wsum[31];
+}
+
 static __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const unsigned* __restrict__ kin,
                                                             const unsigned* __restrict__ vin,
                                                             unsigned* __restrict__ kout, unsigned* __restrict__ vout,
                                                             long long n, int shift,
-                                                            const unsigned* __restrict__ offs, int nblocks) {
+                                                            const unsigned* __restrict__ offs, int nblocks,
+                                                            const unsigned* __restrict__ chunk_prefix) {
     __shared__ unsigned wcnt[RS_WARPS][256];
     __shared__ unsigned gofs[256];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int i = threadIdx.x; i < RS_WARPS * 256; i += RS_THREADS) (&wcnt[0][0])[i] = 0;
-    for (int i = threadIdx.x; i < 256; i += RS_THREADS) gofs[i] = offs[(size_t)i * nblocks + blockIdx.x];
+    for (int i = threadIdx.x; i < 256; i += RS_THREADS) {
+        size_t j = (size_t)i * nblocks + blockIdx.x;
+        gofs[i] = offs[j] + (chunk_prefix ? chunk_prefix[j / RS_SCAN_CHUNK] : 0u);
+    }
     __syncthreads();
     const long long base = (long long)blockIdx.x * RS_TILE + (long long)w * RS_WARP_TILE;
     const unsigned lt = (1u << lane) - 1u;

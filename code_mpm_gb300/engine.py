@@ -77,6 +77,16 @@ class KernelStat(C.Structure):
     _fields_ = [("name", C.c_char * 32), ("launches", C.c_int64), ("total_ms", C.c_double)]
 
 
+class TuneResult(C.Structure):
+    _fields_ = [("p2g_reduce", C.c_int32), ("p2g_block", C.c_int32), ("pass_block", C.c_int32),
+                ("candidates", C.c_int32), ("best_ms_per_step", C.c_double), ("worst_ms_per_step", C.c_double)]
+
+
+OPT_P2G_REDUCE = 3
+OPT_P2G_BLOCK = 4
+OPT_PASS_BLOCK = 5
+
+
 def library_path() -> str:
     return _LIB_PATH
 
@@ -115,6 +125,7 @@ def lib():
             "mpm_launch_count": ([vp, C.POINTER(i64)], C.c_int),
             "mpm_cell_order": ([vp, vp, vp, i64], C.c_int),
             "mpm_cell_order_noalloc": ([C.POINTER(GridDesc), vp, i64, vp, vp, vp], C.c_int),
+            "mpm_autotune": ([vp, i32, dbl, C.c_int, C.POINTER(TuneResult)], C.c_int),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -293,6 +304,16 @@ class Engine:
 
     def synchronize(self) -> None:
         self._check(self._L.mpm_synchronize(self._h))
+
+    def autotune(self, steps: int = 3, dt: Optional[float] = None, contact: bool = False) -> Dict[str, float]:
+        """Pick the fastest launch configuration on the current state (which is restored afterwards)."""
+        if dt is None:
+            dt = self.get_sim()["dt_max"]
+        r = TuneResult()
+        self._check(self._L.mpm_autotune(self._h, int(steps), float(dt), 1 if contact else 0, C.byref(r)))
+        return {"p2g_reduce": r.p2g_reduce, "p2g_block": r.p2g_block, "pass_block": r.pass_block,
+                "candidates": r.candidates, "best_ms_per_step": r.best_ms_per_step,
+                "worst_ms_per_step": r.worst_ms_per_step}
 
     def runSimulation_Classic_DoublePass_MPLocks(self, dTimeIncrement_Total: float) -> int:
         done = C.c_int(0)

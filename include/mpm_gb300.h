@@ -70,6 +70,9 @@ extern "C" {
 /* Options for mpm_set_option. */
 #define MPM_OPT_FLOOR_FRICTION 1 /* contact path: Coulomb friction on x/y of z-fixed nodes (extension; default 0) */
 #define MPM_OPT_PROFILE 2        /* 1: time every kernel with CUDA events (default 0) */
+#define MPM_OPT_P2G_REDUCE 3     /* P2G: 1 = sum each cell's run of particles across lanes before the atomics, 0 = one atomic per particle */
+#define MPM_OPT_P2G_BLOCK 4      /* P2G threads per block (128, 256 or 512) */
+#define MPM_OPT_PASS_BLOCK 5     /* G2P pass-2 threads per block (128, 256 or 512) */
 
 typedef struct mpm_ctx mpm_ctx;
 
@@ -177,6 +180,18 @@ int mpm_run(mpm_ctx* ctx, double dt_total, int contact, int* done);
 int mpm_synchronize(mpm_ctx* ctx);
 /* mpm_advance bracketed by CUDA events on the context's stream; *ms = device time. */
 int mpm_advance_timed(mpm_ctx* ctx, int32_t nsteps, double dt, int contact, float* ms);
+
+/* Autotuner (no counterpart in the reference, which has one fixed OpenMP
+ * loop): times `steps` steps of dt for every candidate launch configuration
+ * (P2G reduction mode x P2G block size x pass-2 block size) on the current
+ * state, keeps the fastest, and restores the particle and node state and the
+ * time exactly as they were.  Results are the chosen options and the best
+ * and worst candidate times per step. */
+typedef struct mpm_tune_result {
+    int32_t p2g_reduce, p2g_block, pass_block, candidates;
+    double best_ms_per_step, worst_ms_per_step;
+} mpm_tune_result;
+int mpm_autotune(mpm_ctx* ctx, int32_t steps, double dt, int contact, mpm_tune_result* out);
 
 /* Diagnostics: the cell key of every particle (base cell (bx,by,bz) =
  * floor(x/h) as in GridPoint_Mediator.cpp:8, key = (bx+1) + (cx+2)*((by+1) +

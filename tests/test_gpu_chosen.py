@@ -1,0 +1,80 @@
+"""The chosen (FP32-transfer) form against the FP64 oracle, and the autotuner.
+
+Accuracy bars of the chosen form (stated per result, from the path's target):
+  * von Mises stress: max |vm_fp32 - vm_fp64| / max vm_fp64 <= 1e-2;
+  * strain energy (sum over particles): relative error <= 5e-3;
+  * positions: max |x_fp32 - x_fp64| <= 1e-4 h (positions are accumulated in FP64).
+"""
+import numpy as np
+import pytest
+
+import pyoracle
+from code_mpm_gb300 import engine, metrics, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    from code_mpm_gb300 import build
+
+    build.build()
+    engine.lib()
+
+
+def run(st, steps, contact, form, floor=0):
+    with engine.Engine.from_state(st, form) as e:
+        if floor:
+            e.set_option(engine.OPT_FLOOR_FRICTION, 1)
+        e.advance(steps, st.dt_max, contact)
+        return e.download_state(st)
+
+
+CASES = [("mixed", lambda: scenes.mixed_small(seed=1), 0, 25, 0),
+         ("contact", lambda: scenes.contact_small(seed=2), 1, 25, 0),
+         ("bar", lambda: scenes.bar(), 0, 400, 0),
+         ("block", lambda: scenes.platen_block(size=(0.012, 0.012, 0.008), speed=20.0, yield_=120.0e6), 1, 150, 1)]
+
+
+@pytest.mark.parametrize("name,make,contact,steps,floor", CASES)
+def test_chosen_form_within_stated_error(name, make, contact, steps, floor):
+    st = make()
+    ref = st.copy()
+    pyoracle.advance(ref, steps, contact, floor_friction=floor)
+    out = run(st, steps, contact, engine.FORM_FP32, floor)
+    err = metrics.form_errors(out, ref)
+    h = float((st.length / st.cells).min())
+    assert err["vm_stress_rel"] <= 1e-2, err
+    assert err["strain_energy_rel"] <= 5e-3, err
+    assert err["pos_abs_max"] <= 1e-4 * h, err
+
+
+@pytest.mark.parametrize("form", [engine.FORM_FP64, engine.FORM_FP32])
+def test_autotune_restores_state_and_picks_valid_options(golden, form):
+    st = golden("contact_in")
+    with engine.Engine.from_state(st, form) as e:
+        before = e.download_state(st)
+        res = e.autotune(steps=2, contact=True)
+        after = e.download_state(st)
+        assert res["candidates"] == 18 and res["p2g_block"] in (128, 256, 512) and res["pass_block"] in (128, 256, 512)
+        assert res["best_ms_per_step"] <= res["worst_ms_per_step"]
+        for k in ("pos", "vel", "stress", "F", "g_mass", "g_state"):
+            assert np.array_equal(before[k], after[k]), k
+        assert after.time == before.time and after.step == before.step
+
+
+def test_plain_form_parity_holds_for_every_launch_configuration(golden):
+    st = golden("contact_in")
+    ref = golden("contact_ref25")
+    for red in (0, 1):
+        for blk in (128, 512):
+            with engine.Engine.from_state(st) as e:
+                e.set_option(engine.OPT_P2G_REDUCE, red)
+                e.set_option(engine.OPT_P2G_BLOCK, blk)
+                e.set_option(engine.OPT_PASS_BLOCK, blk)
+                e.advance(25, st.dt_max, True)
+                out = e.download_state(st)
+            for k in ("pos", "vel", "stress"):
+                scale = np.abs(ref[k]).max()
+                assert np.abs(out[k] - ref[k]).max() / scale <= 1e-9, (red, blk, k)
+            assert np.array_equal(out["g_state"], ref["g_state"])
