@@ -72,7 +72,8 @@ struct mpm_ctx {
     DevBuf cstart, cend;
     // sort
     DevBuf keys0, vals0, keys1, vals1, keys_copy, counts;
-    DevBuf dclist, mats, staging, tune_backup;
+    DevBuf dclist, mats, staging, tune_backup, surf;
+    int nsurf = 0;
     // host pinned staging for the error word
     unsigned* h_err = nullptr;
     // profiling
@@ -89,7 +90,7 @@ struct mpm_ctx {
                           &e_strain, &e_strain_max, &e_strain_ti, &e_plastic, &backstress, &mp_mg, &strain_rate,
                           &material, &pflags, &dc_mult, &g_mass, &g_mom, &g_vel, &g_force, &g_ftemp, &g_mg,
                           &g_state, &g_fixed, &g_friction, &g_ratio, &g_q, &g_owner, &g_nowner, &g_need, &g_list, &g_count, &rs_chunk, &cstart,
-                          &cend, &keys0, &vals0, &keys1, &vals1, &keys_copy, &counts, &dclist, &mats, &staging, &tune_backup};
+                          &cend, &keys0, &vals0, &keys1, &vals1, &keys_copy, &counts, &dclist, &mats, &staging, &tune_backup, &surf};
         all.assign(std::begin(list), std::end(list));
     }
 };
@@ -308,6 +309,18 @@ __global__ void k_mark_dc(const unsigned* __restrict__ list, int ndc, uint8_t* _
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < ndc) pflags[list[k]] |= (uint8_t)PF_IN_DC;
 }
+__global__ void k_compact_flag(const uint8_t* __restrict__ pflags, long long n, uint8_t bit,
+                               unsigned* __restrict__ list, unsigned* __restrict__ count) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    bool take = i < n && (pflags[i] & bit);
+    unsigned m = __ballot_sync(0xffffffffu, take);
+    if (!m) return;
+    int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(count, (unsigned)__popc(m));
+    base = __shfl_sync(m, base, leader);
+    if (take) list[base + __popc(m & ((1u << lane) - 1u))] = (unsigned)i;
+}
 __global__ void k_clear_flag(uint8_t* __restrict__ pflags, long long n, uint8_t bits) {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i < n) pflags[i] &= (uint8_t)~bits;
@@ -431,22 +444,29 @@ int step_impl(mpm_ctx* c, double dt, int contact) {
                    (const uint8_t*)c->pflags.p, g, (unsigned*)c->g_owner.p, nn, contact);
         }
         if (contact) {
+            const unsigned* surf = (const unsigned*)c->surf.p;
+            const int ns = c->nsurf;
+            const unsigned sb = blocks_for(ns);
             if (!mg_in_p2g) {
                 CK(cudaMemsetAsync(c->g_need.p, 0, (size_t)nn * 4, c->stream));
                 CK(cudaMemsetAsync(c->g_count.p, 0, 4, c->stream));
-                LAUNCH("contact_need", k_contact_need<T>, blocks_for(n), NTHREADS, P, keys, g,
-                       (unsigned*)c->g_need.p);
+                if (ns > 0)
+                    LAUNCH("contact_need", k_contact_need<T>, sb, NTHREADS, P, keys, g, (unsigned*)c->g_need.p, surf,
+                           ns);
                 LAUNCH("contact_compact", k_contact_compact, blocks_for(nn), NTHREADS, (const unsigned*)c->g_need.p,
                        nn, (unsigned*)c->g_list.p, (unsigned*)c->g_count.p);
                 LAUNCH("contact_mass_gradient", k_contact_mass_gradient<T>, (unsigned)c->sm_count * 8, CG_WARPS * 32,
                        P, N, g, (const unsigned*)c->g_list.p, (const unsigned*)c->g_count.p, perm,
                        (const unsigned*)c->cstart.p, (const unsigned*)c->cend.p);
             }
-            LAUNCH("contact_mp_gradient", k_contact_mp_gradient<T>, blocks_for(n), NTHREADS, P, N, g, keys);
+            if (ns > 0)
+                LAUNCH("contact_mp_gradient", k_contact_mp_gradient<T>, sb, NTHREADS, P, N, g, keys, surf, ns);
             LAUNCH("contact_reset", k_contact_reset<T>, blocks_for(nn), NTHREADS, N);
-            LAUNCH("contact_normal", k_contact_normal<T>, blocks_for(n), NTHREADS, P, N, g, keys, 0);
-            LAUNCH("contact_normal", k_contact_normal<T>, blocks_for(n), NTHREADS, P, N, g, keys, 1);
-            LAUNCH("contact_flags", k_contact_flags<T>, blocks_for(n), NTHREADS, P, N, g, keys);
+            if (ns > 0) {
+                LAUNCH("contact_normal", k_contact_normal<T>, sb, NTHREADS, P, N, g, keys, surf, ns, 0);
+                LAUNCH("contact_normal", k_contact_normal<T>, sb, NTHREADS, P, N, g, keys, surf, ns, 1);
+                LAUNCH("contact_flags", k_contact_flags<T>, sb, NTHREADS, P, N, g, keys, surf, ns);
+            }
         }
         if (!contact && c->ndc > 0)
             LAUNCH("dc_apply", k_dc_apply<T>, blocks_for(c->ndc), NTHREADS, (const unsigned*)c->dclist.p, c->ndc,
@@ -752,8 +772,16 @@ int mpm_upload_particles(mpm_ctx* c, const mpm_particles* p, int64_t n) {
             LAUNCH("fill", k_mark_dc, blocks_for(c->ndc), NTHREADS, (const unsigned*)c->dclist.p, c->ndc,
                    (uint8_t*)c->pflags.p);
     }
+    // the surface particles (b_Surface) as a list, for the contact kernels
+    if ((rc = ensure(c, c->surf, (size_t)std::max<long long>(1, n) * 4))) return rc;
+    CK(cudaMemsetAsync(c->g_count.p, 0, 4, c->stream));
+    if (n > 0)
+        LAUNCH("fill", k_compact_flag, blocks_for(n), NTHREADS, (const uint8_t*)c->pflags.p, (long long)n,
+               (uint8_t)MPM_PF_SURFACE, (unsigned*)c->surf.p, (unsigned*)c->g_count.p);
+    CK(cudaMemcpyAsync(c->h_err, c->g_count.p, 4, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(c->stream));
+    c->nsurf = (int)*c->h_err;
     c->have_particles = true;
     return MPM_OK;
 }

@@ -502,6 +502,10 @@ __global__ void __launch_bounds__(512) k_pass2(PView<T> P, NView<T> nd, Geom g, 
             Bases<T> B;
             B.init(g, x, b);
             const double ddt = a.dt;
+            // FP32 form: the displacement sum N (p/m) is formed in FP32 and
+            // added to the FP64 position once; FP64 form: added per corner
+            // as the reference does (…MPLocks.cpp:197-198).
+            T disp[3] = {0, 0, 0};
 #pragma unroll 1
             for (int k = 0; k < 8; ++k) {
                 long long nid = corner_node(g, b, k);
@@ -509,8 +513,13 @@ __global__ void __launch_bounds__(512) k_pass2(PView<T> P, NView<T> nd, Geom g, 
                 T N, G[3];
                 B.corner(k, N, G);
                 if ((double)nd.mass[nid] > a.mass_min) {
+                    if constexpr (sizeof(T) == 4) {
 #pragma unroll
-                    for (int c = 0; c < 3; ++c) x[c] = x[c] + (double)(N * nd.ratio[c * nn + nid]) * ddt;
+                        for (int c = 0; c < 3; ++c) disp[c] += N * nd.ratio[c * nn + nid];
+                    } else {
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) x[c] = x[c] + (double)(N * nd.ratio[c * nn + nid]) * ddt;
+                    }
                 }
                 T vi[3] = {nd.vel[nid], nd.vel[nn + nid], nd.vel[2 * nn + nid]};
                 // outerProduct(v_i, grad N): column c, row r = v_i[r] * G[c]
@@ -518,6 +527,10 @@ __global__ void __launch_bounds__(512) k_pass2(PView<T> P, NView<T> nd, Geom g, 
                 for (int c = 0; c < 3; ++c)
 #pragma unroll
                     for (int r = 0; r < 3; ++r) L[3 * c + r] += vi[r] * G[c];
+            }
+            if constexpr (sizeof(T) == 4) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) x[c] += (double)(disp[c] * dt);
             }
 #pragma unroll
             for (int c = 0; c < 3; ++c) P.pos[c * np + p] = x[c];
@@ -569,7 +582,9 @@ __global__ void __launch_bounds__(512) k_pass2(PView<T> P, NView<T> nd, Geom g, 
 #pragma unroll
                 for (int k = 0; k < 6; ++k) P.strain_rate[k * np + p] = e[k] / dt;
             }
-            double dEs = 0.0, dEp = 0.0;
+            // the step's energy increments are summed in the form's type and
+            // added once to the FP64 energy accumulators
+            T dEs = 0, dEp = 0;
 #pragma unroll
             for (int k = 0; k < 6; ++k) {
                 T sn = sig[k] + o.dsig[k];
@@ -577,20 +592,20 @@ __global__ void __launch_bounds__(512) k_pass2(PView<T> P, NView<T> nd, Geom g, 
                 P.eps_p[k * np + p] += o.deps_p[k];
                 if (!a.contact) {
                     T mid = sn - (T)0.5 * o.dsig[k];
-                    dEs += (double)(mid * e[k] * V);
-                    dEp += (double)(mid * o.deps_p[k] * V);
+                    dEs += mid * e[k] * V;
+                    dEp += mid * o.deps_p[k] * V;
                 } else {
-                    dEs += (double)(sn * e[k] * V);
-                    dEp += (double)(sn * o.deps_p[k] * V);
+                    dEs += sn * e[k] * V;
+                    dEp += sn * o.deps_p[k] * V;
                 }
             }
-            double es = P.e_strain[p] + dEs;
+            double es = P.e_strain[p] + (double)dEs;
             P.e_strain[p] = es;
             if (!a.contact) {
                 P.e_strain_ti[p] += es * a.dt;
                 if (es > P.e_strain_max[p]) P.e_strain_max[p] = es;
             }
-            P.e_plastic[p] += dEp;
+            P.e_plastic[p] += (double)dEp;
             P.backstress[p] = R + o.dR;
         } else if (!a.contact) {
             atomicOr(err, ERR_BAD_MATERIAL);
@@ -626,9 +641,11 @@ __global__ void __launch_bounds__(512) k_pass2(PView<T> P, NView<T> nd, Geom g, 
 // in index order, with the reference's exact per-pair gradient.
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void k_contact_need(PView<T> P, const unsigned* __restrict__ keys, Geom g, unsigned* __restrict__ need) {
-    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (p >= P.n || !(P.pflags[p] & 16u)) return;
+__global__ void k_contact_need(PView<T> P, const unsigned* __restrict__ keys, Geom g, unsigned* __restrict__ need,
+                               const unsigned* __restrict__ surf, int nsurf) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nsurf) return;
+    const long long p = surf[t];
     unsigned key = keys[p];
     if (key >= g.key_max) return;
     int b[3];
@@ -785,22 +802,42 @@ __global__ void __launch_bounds__(CG_WARPS * 32) k_contact_mass_gradient(PView<T
     }
 }
 
+// The contact kernels below run one thread per surface particle (a list
+// compacted at upload).  FP64 form: the reference's uncontracted FP64
+// arithmetic, bit-exact.  FP32 form: the same tests in FP32 (the flags only
+// feed output, as in the reference, where nothing reads them back).
+__device__ __forceinline__ float dot3f(const float a[3], const float b[3]) {
+    return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+
 // Surface particle normal: the corner gradient of largest norm, first wins on ties (:156-172).
 template <typename T>
-__global__ void k_contact_mp_gradient(PView<T> P, NView<T> nd, Geom g, const unsigned* __restrict__ keys) {
-    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (p >= P.n || !(P.pflags[p] & 16u)) return;
+__global__ void k_contact_mp_gradient(PView<T> P, NView<T> nd, Geom g, const unsigned* __restrict__ keys,
+                                      const unsigned* __restrict__ surf, int nsurf) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nsurf) return;
+    const long long p = surf[t];
     const long long np = P.n, nn = nd.nn;
     double gp[3] = {0.0, 0.0, 0.0};
     unsigned key = keys[p];
     if (key < g.key_max) {
         int b[3];
         key_to_base(key, g, b);
+        float best2 = 0.0f;
         for (int k = 0; k < 8; ++k) {
             long long nid = corner_node(g, b, k);
             if (nid < 0) continue;
             double gi[3] = {nd.mg[nid], nd.mg[nn + nid], nd.mg[2 * nn + nid]};
-            if (len3_rn(gi) > len3_rn(gp)) {
+            bool take;
+            if constexpr (sizeof(T) == 8) {
+                take = len3_rn(gi) > len3_rn(gp);
+            } else {
+                float f[3] = {(float)gi[0], (float)gi[1], (float)gi[2]};
+                float l2 = dot3f(f, f);
+                take = l2 > best2;
+                if (take) best2 = l2;
+            }
+            if (take) {
                 gp[0] = gi[0];
                 gp[1] = gi[1];
                 gp[2] = gi[2];
@@ -826,9 +863,11 @@ __global__ void k_contact_reset(NView<T> nd) {
 // Node normal from surface particles with (x_i - x_p) . g_p > 0 (:191-210);
 // the reference overwrites in index order, so the largest index wins.
 template <typename T>
-__global__ void k_contact_normal(PView<T> P, NView<T> nd, Geom g, const unsigned* __restrict__ keys, int apply) {
-    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (p >= P.n || !(P.pflags[p] & 16u)) return;
+__global__ void k_contact_normal(PView<T> P, NView<T> nd, Geom g, const unsigned* __restrict__ keys,
+                                 const unsigned* __restrict__ surf, int nsurf, int apply) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nsurf) return;
+    const long long p = surf[t];
     const long long np = P.n, nn = nd.nn;
     unsigned key = keys[p];
     if (key >= g.key_max) return;
@@ -836,14 +875,29 @@ __global__ void k_contact_normal(PView<T> P, NView<T> nd, Geom g, const unsigned
     key_to_base(key, g, b);
     double x[3] = {P.pos[p], P.pos[np + p], P.pos[2 * np + p]};
     double gp[3] = {P.mp_mg[p], P.mp_mg[np + p], P.mp_mg[2 * np + p]};
+    float gpf[3] = {(float)gp[0], (float)gp[1], (float)gp[2]};
+    float u[3];
+    if constexpr (sizeof(T) == 4) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) u[c] = (float)(x[c] - node_coord(g, c, b[c]));  // offset from the base node
+    }
     for (int k = 0; k < 8; ++k) {
         long long nid = corner_node(g, b, k);
         if (nid < 0) continue;
-        int n3[3] = {b[0] + ((k >> 2) & 1), b[1] + ((k >> 1) & 1), b[2] + (k & 1)};
-        double d[3];
+        int o3[3] = {(k >> 2) & 1, (k >> 1) & 1, k & 1};
+        bool facing;
+        if constexpr (sizeof(T) == 8) {
+            double d[3];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) d[c] = __dadd_rn(node_coord(g, c, n3[c]), -x[c]);
-        if (!(dot3_rn(d, gp) > 0.0)) continue;
+            for (int c = 0; c < 3; ++c) d[c] = __dadd_rn(node_coord(g, c, b[c] + o3[c]), -x[c]);
+            facing = dot3_rn(d, gp) > 0.0;
+        } else {
+            float d[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) d[c] = (o3[c] ? (float)g.h[c] : 0.0f) - u[c];
+            facing = dot3f(d, gpf) > 0.0f;
+        }
+        if (!facing) continue;
         if (!apply) {
             atomicMax(&nd.nowner[nid], (unsigned)p + 1u);
         } else if (nd.nowner[nid] == (unsigned)p + 1u) {
@@ -855,25 +909,44 @@ __global__ void k_contact_normal(PView<T> P, NView<T> nd, Geom g, const unsigned
 
 // Contact flags (:215-237): g_i . g_p >= 0.001 |g_i| |g_p| -> positive, <= -tol -> negative.
 template <typename T>
-__global__ void k_contact_flags(PView<T> P, NView<T> nd, Geom g, const unsigned* __restrict__ keys) {
-    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (p >= P.n || !(P.pflags[p] & 16u)) return;
+__global__ void k_contact_flags(PView<T> P, NView<T> nd, Geom g, const unsigned* __restrict__ keys,
+                                const unsigned* __restrict__ surf, int nsurf) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nsurf) return;
+    const long long p = surf[t];
     const long long np = P.n, nn = nd.nn;
     unsigned key = keys[p];
     if (key >= g.key_max) return;
     int b[3];
     key_to_base(key, g, b);
     double gp[3] = {P.mp_mg[p], P.mp_mg[np + p], P.mp_mg[2 * np + p]};
-    const double lp = len3_rn(gp);
+    const float gpf[3] = {(float)gp[0], (float)gp[1], (float)gp[2]};
+    double lp = 0.0;
+    float lpf = 0.0f;
+    if constexpr (sizeof(T) == 8)
+        lp = len3_rn(gp);
+    else
+        lpf = sqrtf(dot3f(gpf, gpf));
     for (int k = 0; k < 8; ++k) {
         long long nid = corner_node(g, b, k);
         if (nid < 0) continue;
         double gi[3] = {nd.mg[nid], nd.mg[nn + nid], nd.mg[2 * nn + nid]};
-        double tol = __dmul_rn(__dmul_rn(0.001, len3_rn(gi)), lp);
-        double dd = dot3_rn(gi, gp);
-        if (dd >= tol)
+        bool pos, neg;
+        if constexpr (sizeof(T) == 8) {
+            double tol = __dmul_rn(__dmul_rn(0.001, len3_rn(gi)), lp);
+            double dd = dot3_rn(gi, gp);
+            pos = dd >= tol;
+            neg = !pos && dd <= -tol;
+        } else {
+            float gif[3] = {(float)gi[0], (float)gi[1], (float)gi[2]};
+            float tol = 0.001f * sqrtf(dot3f(gif, gif)) * lpf;
+            float dd = dot3f(gif, gpf);
+            pos = dd >= tol;
+            neg = !pos && dd <= -tol;
+        }
+        if (pos)
             atomicOr(&nd.state[nid], 4u);
-        else if (dd <= -tol)
+        else if (neg)
             atomicOr(&nd.state[nid], 8u);
     }
 }

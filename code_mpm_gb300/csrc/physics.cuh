@@ -28,14 +28,39 @@ __device__ __forceinline__ void axis_bases(const Geom& g, int a, double x, int b
     }
 }
 
+// FP32 (chosen) form: one FP64 subtraction and product per axis give the
+// cell-local coordinate u = (x - X_b)/h in [0, 1); both nodes' bases follow
+// in FP32 (d/h = u and u - 1).  FP64 instructions cost ~60 FP32 ones on this
+// part, so the chosen form keeps them to this one pair per axis.
+__device__ __forceinline__ void axis_bases_local(const Geom& g, int a, double x, int b, float N[2], float gf[2]) {
+    const float u = (float)((x - node_coord(g, a, b)) * g.inv_h[a]);
+    const float r[2] = {u, u - 1.0f};
+    const float ih = (float)g.inv_h[a];
+#pragma unroll
+    for (int o = 0; o < 2; ++o) {
+        float ar = fabsf(r[o]);
+        float nv = 1.0f - ar;
+        if (nv < 0.0f || nv > 1.0f) nv = 0.0f;
+        N[o] = nv;
+        float s = (float)((r[o] > 0.0f) - (r[o] < 0.0f));
+        gf[o] = (ar > 1.0e-12f && ar < (float)(1.0 - 1.0e-12)) ? s * ih : 0.0f;
+    }
+}
+
 template <typename T>
 struct Bases {
     T Nx[2], Ny[2], Nz[2];
     T gx[2], gy[2], gz[2];
     __device__ __forceinline__ void init(const Geom& g, const double x[3], const int b[3]) {
-        axis_bases<T>(g, 0, x[0], b[0], Nx, gx);
-        axis_bases<T>(g, 1, x[1], b[1], Ny, gy);
-        axis_bases<T>(g, 2, x[2], b[2], Nz, gz);
+        if constexpr (sizeof(T) == 4) {
+            axis_bases_local(g, 0, x[0], b[0], Nx, gx);
+            axis_bases_local(g, 1, x[1], b[1], Ny, gy);
+            axis_bases_local(g, 2, x[2], b[2], Nz, gz);
+        } else {
+            axis_bases<T>(g, 0, x[0], b[0], Nx, gx);
+            axis_bases<T>(g, 1, x[1], b[1], Ny, gy);
+            axis_bases<T>(g, 2, x[2], b[2], Nz, gz);
+        }
     }
     // corner k = 4*ix + 2*iy + iz
     __device__ __forceinline__ void corner(int k, T& N, T G[3]) const {
