@@ -55,6 +55,8 @@ def parse():
                     help="fp32: the chosen form, timed beside the plain FP64 form; fp64: the plain form alone")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip timing the plain FP64 form beside the chosen one")
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--block", default="0.08,0.08,0.04",
                     help="block size in m (smaller blocks only for profiling captures; the metric uses the default)")
     return ap.parse_args()
@@ -194,7 +196,7 @@ def timed_form(st, form, args, dist, contact, floor, tune=True):
     e = engine.Engine.from_state(st, form)
     e.set_option(engine.OPT_FLOOR_FRICTION, floor)
     dt = st.dt_max
-    tune_res = e.autotune(steps=2, dt=dt, contact=bool(contact)) if tune else None
+    tune_res = e.autotune(steps=2, dt=dt, contact=bool(contact)) if (tune and not args.no_autotune) else None
     e.advance(args.warmup, dt, contact)
     e.synchronize()
     dist.barrier()
@@ -224,7 +226,7 @@ def run_gb300(args, dist: Dist):
     # plain FP64 form: the reference method on the GPU (parity-pinned to the oracle)
     plain = None
     plain_state = None
-    if chosen_form != engine.FORM_FP64:
+    if chosen_form != engine.FORM_FP64 and not args.no_plain:
         ep, ms_p, launches_p, clocks_p, tune_p = timed_form(st, engine.FORM_FP64, args, dist, contact, floor)
         plain_state = ep.download_state(st)
         ep.close()

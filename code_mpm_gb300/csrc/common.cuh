@@ -15,24 +15,38 @@ constexpr unsigned ERR_BAD_MATERIAL = 2u;
 // Internal particle flag: member of the displacement-control list.
 constexpr unsigned PF_IN_DC = 32u;
 
-// Grid geometry, by value in every kernel.  Node coordinates come from the
-// padded per-axis tables xtab (axis a at xtab + xoff[a], entry n+1 for node
-// index n in [-1, nn[a]]), each computed as (i*L)/cells like
-// GridPoint_Factory::createGrid (GridPoint_Factory.h:53-55).
+// Grid geometry of one specimen.  A context holds one or more specimens,
+// each with its own regular grid (GridPoint_Factory::createGrid,
+// GridPoint_Factory.h:33-68); their nodes and cell keys are numbered one
+// after the other (node_off, key_off).  Kernels receive specimen 0's record
+// by value; with several specimens, `tab` holds every record in device
+// memory and a particle's record is tab[specimen id].  Node coordinates come
+// from the padded per-axis tables xtab (axis a at xtab + xoff[a], entry n+1
+// for node index n in [-1, nn[a]]), each computed as (i*L)/cells like
+// createGrid (GridPoint_Factory.h:53-55).
 struct Geom {
     double h[3];      // cell size = length/cells (GridPoint_Mediator d3_Length_Cell)
-    double inv_h[3];  // 1/h, used where the result only has to be within tolerance
+    double inv_h[3];  // RN(1/h)
     int nn[3];        // nodes per axis = cells + 1
     int kd[3];        // cell-key extents = cells + 2 (base cells -1..cells)
-    unsigned key_max; // kd0*kd1*kd2: the key of a particle with no grid node in range
-    long long n_nodes;
+    unsigned key_max; // total key count over all specimens: the key of a particle with no node in range
+    long long n_nodes;  // total node count over all specimens
     const double* xtab;
     int xoff[3];
+    unsigned key_off;    // this specimen's first cell key
+    long long node_off;  // this specimen's first node index
+    const struct Geom* tab;  // all specimens (device), or null with one specimen
+    int nspec;
 };
 
-// Decode a cell key into the base (bottom-left-far) cell index.
+// The geometry of particle p's specimen.
+__device__ __forceinline__ const Geom& spec_geom(const Geom& g, const uint16_t* __restrict__ sid, long long p) {
+    return (g.nspec > 1) ? g.tab[sid[p]] : g;
+}
+
+// Decode a cell key into the base (bottom-left-far) cell index of its specimen.
 __device__ __forceinline__ void key_to_base(unsigned key, const Geom& g, int b[3]) {
-    unsigned k = key;
+    unsigned k = key - g.key_off;
     b[0] = (int)(k % (unsigned)g.kd[0]) - 1;
     k /= (unsigned)g.kd[0];
     b[1] = (int)(k % (unsigned)g.kd[1]) - 1;
@@ -46,7 +60,21 @@ __device__ __forceinline__ double node_coord(const Geom& g, int a, int n) { retu
 __device__ __forceinline__ long long corner_node(const Geom& g, const int b[3], int k) {
     int nx = b[0] + ((k >> 2) & 1), ny = b[1] + ((k >> 1) & 1), nz = b[2] + (k & 1);
     if (nx < 0 || ny < 0 || nz < 0 || nx > g.nn[0] - 1 || ny > g.nn[1] - 1 || nz > g.nn[2] - 1) return -1;
-    return (long long)nx + (long long)ny * g.nn[0] + (long long)nz * g.nn[0] * g.nn[1];
+    return g.node_off + (long long)nx + (long long)ny * g.nn[0] + (long long)nz * g.nn[0] * g.nn[1];
+}
+
+// Specimen owning global node i (binary search over the node offsets).
+__device__ __forceinline__ const Geom& node_geom(const Geom& g, long long i) {
+    if (g.nspec <= 1) return g;
+    int lo = 0, hi = g.nspec - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (g.tab[mid].node_off <= i)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return g.tab[lo];
 }
 
 // Material constants, precomputed on the host with the reference's own
@@ -87,6 +115,8 @@ struct PView {
     int32_t* material;
     uint8_t* pflags;
     float* dc_mult;
+    float* loc;  // FP32 form: cell-local coordinate (x - X_b)/h of the current base cell, 3 x n
+    const uint16_t* sid;  // specimen of each particle (null with one specimen)
     long long n;
 };
 
@@ -106,7 +136,17 @@ struct NView {
     T* q;              // scratch: remap accumulator sum N m_p v_p
     unsigned* owner;   // scratch: displacement-control last-writer claims, 3 x nn
     unsigned* nowner;  // scratch: contact-normal last-writer claims, nn
+    const unsigned* alist;   // active nodes of this step (null: sweep every node)
+    const unsigned* acount;  // their number (device)
     long long nn;
 };
+
+// The nodes a node kernel works on, grid-stride: the active-node list when
+// one is given, else every node.  The body may `continue`, not `return`.
+#define NODE_LOOP(nd, i)                                                                        \
+    for (long long t_ = blockIdx.x * (long long)blockDim.x + threadIdx.x,                        \
+                   n_ = (nd).alist ? (long long)*(nd).acount : (nd).nn;                         \
+         t_ < n_; t_ += (long long)gridDim.x * blockDim.x)                                      \
+        if (const long long i = (nd).alist ? (long long)(nd).alist[t_] : t_; true)
 
 }  // namespace mpm

@@ -57,6 +57,11 @@ struct mpm_ctx {
     long long nn = 0;
     int nmat = 0;
     int ndc = 0;
+    int nspec = 1;
+    std::vector<Geom> geoms;
+    DevBuf geom_tab, sid, alist, acount;
+    bool have_alist = false;  // alist holds the active nodes of the last step
+    bool use_alist = false;
     std::vector<double> tl_t, tl_v;
     bool have_particles = false, have_nodes = false;
     // device buffers
@@ -72,8 +77,9 @@ struct mpm_ctx {
     DevBuf cstart, cend;
     // sort
     DevBuf keys0, vals0, keys1, vals1, keys_copy, counts;
-    DevBuf dclist, mats, staging, tune_backup, surf;
+    DevBuf dclist, mats, staging, tune_backup, surf, mon_mask, mon_acc;
     int nsurf = 0;
+    bool have_mon = false;
     // host pinned staging for the error word
     unsigned* h_err = nullptr;
     // profiling
@@ -84,13 +90,17 @@ struct mpm_ctx {
     std::vector<long long> prof_cnt;
     long long launches = 0;
     const unsigned* last_perm = nullptr;
+    const unsigned* last_skeys = nullptr;
+    bool keys_valid = false;  // keys_copy / keys[key_buf] / loc hold the keys of the current positions
+    int key_buf = 0;
+    DevBuf loc;
 
     mpm_ctx() {
         DevBuf* list[] = {&xtab, &err_word, &pos, &vel, &fext, &mass, &vol, &vol0, &F, &stress, &strain, &eps_p,
                           &e_strain, &e_strain_max, &e_strain_ti, &e_plastic, &backstress, &mp_mg, &strain_rate,
                           &material, &pflags, &dc_mult, &g_mass, &g_mom, &g_vel, &g_force, &g_ftemp, &g_mg,
                           &g_state, &g_fixed, &g_friction, &g_ratio, &g_q, &g_owner, &g_nowner, &g_need, &g_list, &g_count, &rs_chunk, &cstart,
-                          &cend, &keys0, &vals0, &keys1, &vals1, &keys_copy, &counts, &dclist, &mats, &staging, &tune_backup, &surf};
+                          &cend, &keys0, &vals0, &keys1, &vals1, &keys_copy, &counts, &dclist, &mats, &staging, &tune_backup, &surf, &mon_mask, &mon_acc, &loc, &geom_tab, &sid, &alist, &acount};
         all.assign(std::begin(list), std::end(list));
     }
 };
@@ -151,6 +161,8 @@ PView<T> pview(mpm_ctx* c) {
     v.material = (int32_t*)c->material.p;
     v.pflags = (uint8_t*)c->pflags.p;
     v.dc_mult = (float*)c->dc_mult.p;
+    v.loc = (float*)c->loc.p;
+    v.sid = c->nspec > 1 ? (const uint16_t*)c->sid.p : nullptr;
     v.n = c->n;
     return v;
 }
@@ -171,6 +183,8 @@ NView<T> nview(mpm_ctx* c) {
     v.q = (T*)c->g_q.p;
     v.owner = (unsigned*)c->g_owner.p;
     v.nowner = (unsigned*)c->g_nowner.p;
+    v.alist = c->use_alist ? (const unsigned*)c->alist.p : nullptr;
+    v.acount = (const unsigned*)c->acount.p;
     v.nn = c->nn;
     return v;
 }
@@ -321,6 +335,18 @@ __global__ void k_compact_flag(const uint8_t* __restrict__ pflags, long long n, 
     base = __shfl_sync(m, base, leader);
     if (take) list[base + __popc(m & ((1u << lane) - 1u))] = (unsigned)i;
 }
+__global__ void k_compact_state(const unsigned* __restrict__ state, long long n, unsigned bit,
+                                unsigned* __restrict__ list, unsigned* __restrict__ count) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    bool take = i < n && (state[i] & bit);
+    unsigned m = __ballot_sync(0xffffffffu, take);
+    if (!m) return;
+    int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(count, (unsigned)__popc(m));
+    base = __shfl_sync(m, base, leader);
+    if (take) list[base + __popc(m & ((1u << lane) - 1u))] = (unsigned)i;
+}
 __global__ void k_clear_flag(uint8_t* __restrict__ pflags, long long n, uint8_t bits) {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i < n) pflags[i] &= (uint8_t)~bits;
@@ -391,16 +417,25 @@ int step_impl(mpm_ctx* c, double dt, int contact) {
     const Geom& g = c->g;
     unsigned* err = (unsigned*)c->err_word.p;
 
-    LAUNCH("reset_grid", k_reset_grid<T>, blocks_for(nn), NTHREADS, N, contact);
+    // node kernels sweep the active-node list; the reset uses the previous step's
+    const unsigned nodeblocks = (unsigned)std::min<long long>(blocks_for(nn), (long long)c->sm_count * 16);
+    N.alist = c->have_alist ? (const unsigned*)c->alist.p : nullptr;
+    LAUNCH("reset_grid", k_reset_grid<T>, c->have_alist ? nodeblocks : blocks_for(nn), NTHREADS, N, contact);
     if (n > 0) {
-        // cell keys + stable radix sort by key
-        LAUNCH("cell_keys", k_cell_keys, blocks_for(n), NTHREADS, (const double*)c->pos.p, n, g,
-               (unsigned*)c->keys0.p, (unsigned*)c->vals0.p, (unsigned*)c->keys_copy.p, err);
+        // cell keys: written by the previous step's pass 2 (which knows the new
+        // positions), or computed here after an upload; then the stable radix
+        // sort by key, whose first pass takes the identity as input values
+        unsigned* key_src = (unsigned*)(c->key_buf ? c->keys1.p : c->keys0.p);
+        unsigned* key_other = (unsigned*)(c->key_buf ? c->keys0.p : c->keys1.p);
+        if (!c->keys_valid)
+            LAUNCH("cell_keys", k_cell_keys, blocks_for(n), NTHREADS, (const double*)c->pos.p, n, g, key_src,
+                   (unsigned*)nullptr, (unsigned*)c->keys_copy.p, err,
+                   c->form == MPM_FORM_FP32 ? (float*)c->loc.p : (float*)nullptr, P.sid);
         int bits = 1;
         while (bits < 32 && ((unsigned long long)1 << bits) <= (unsigned long long)g.key_max) ++bits;
         const int nblocks = (int)((n + RS_TILE - 1) / RS_TILE);
-        unsigned *kin = (unsigned*)c->keys0.p, *vin = (unsigned*)c->vals0.p;
-        unsigned *kout = (unsigned*)c->keys1.p, *vout = (unsigned*)c->vals1.p;
+        unsigned *kin = key_src, *vin = nullptr;
+        unsigned *kout = key_other, *vout = (unsigned*)c->vals0.p;
         const int hist_total = 256 * nblocks;
         const int nchunks = (hist_total + RS_SCAN_CHUNK - 1) / RS_SCAN_CHUNK;
         for (int shift = 0; shift < bits; shift += 8) {
@@ -414,21 +449,31 @@ int step_impl(mpm_ctx* c, double dt, int contact) {
             } else {
                 LAUNCH("rs_scan", k_rs_scan, 1, 1024, (unsigned*)c->counts.p, hist_total);
             }
-            LAUNCH("rs_scatter", k_rs_scatter, nblocks, RS_THREADS, kin, vin, kout, vout, n, shift,
+            LAUNCH("rs_scatter", k_rs_scatter, nblocks, RS_THREADS, kin, (const unsigned*)vin, kout, vout, n, shift,
                    (const unsigned*)c->counts.p, nblocks, chunk_prefix);
             std::swap(kin, kout);
-            std::swap(vin, vout);
+            vin = vout;
+            vout = (vout == (unsigned*)c->vals0.p) ? (unsigned*)c->vals1.p : (unsigned*)c->vals0.p;
         }
         const unsigned* skeys = kin;
         const unsigned* perm = vin;
         c->last_perm = perm;
+        c->last_skeys = skeys;
+        // pass 2 writes the next step's sort input into the buffer not holding skeys
+        unsigned* keys_next = (skeys == (unsigned*)c->keys0.p) ? (unsigned*)c->keys1.p : (unsigned*)c->keys0.p;
+        c->key_buf = (keys_next == (unsigned*)c->keys1.p) ? 1 : 0;
         const unsigned* keys = (const unsigned*)c->keys_copy.p;
         if (contact) {
             CK(cudaMemsetAsync(c->cstart.p, 0, (size_t)g.key_max * 4, c->stream));
             CK(cudaMemsetAsync(c->cend.p, 0, (size_t)g.key_max * 4, c->stream));
         }
         LAUNCH("cell_ranges", k_cell_ranges, blocks_for(n), NTHREADS, skeys, n, g, N.state,
-               contact ? (unsigned*)c->cstart.p : nullptr, contact ? (unsigned*)c->cend.p : nullptr);
+               contact ? (unsigned*)c->cstart.p : nullptr, contact ? (unsigned*)c->cend.p : nullptr, perm, P.sid);
+        CK(cudaMemsetAsync(c->acount.p, 0, 4, c->stream));
+        LAUNCH("active_list", k_compact_state, blocks_for(nn), NTHREADS, (const unsigned*)N.state, nn, 1u,
+               (unsigned*)c->alist.p, (unsigned*)c->acount.p);
+        N.alist = (const unsigned*)c->alist.p;
+        c->have_alist = true;
         // FP32 form: the contact mass gradient is accumulated by P2G itself
         // (the bit-exact ordered gather below serves the FP64 form).
         const int mg_in_p2g = (contact && c->form == MPM_FORM_FP32) ? 1 : 0;
@@ -441,7 +486,7 @@ int step_impl(mpm_ctx* c, double dt, int contact) {
         if (c->ndc > 0) {
             CK(cudaMemsetAsync(c->g_owner.p, 0, (size_t)3 * nn * 4, c->stream));
             LAUNCH("dc_claim", k_dc_claim, blocks_for(c->ndc), NTHREADS, (const unsigned*)c->dclist.p, c->ndc, keys,
-                   (const uint8_t*)c->pflags.p, g, (unsigned*)c->g_owner.p, nn, contact);
+                   (const uint8_t*)c->pflags.p, g, (unsigned*)c->g_owner.p, nn, contact, P.sid);
         }
         if (contact) {
             const unsigned* surf = (const unsigned*)c->surf.p;
@@ -461,7 +506,7 @@ int step_impl(mpm_ctx* c, double dt, int contact) {
             }
             if (ns > 0)
                 LAUNCH("contact_mp_gradient", k_contact_mp_gradient<T>, sb, NTHREADS, P, N, g, keys, surf, ns);
-            LAUNCH("contact_reset", k_contact_reset<T>, blocks_for(nn), NTHREADS, N);
+            LAUNCH("contact_reset", k_contact_reset<T>, nodeblocks, NTHREADS, N);
             if (ns > 0) {
                 LAUNCH("contact_normal", k_contact_normal<T>, sb, NTHREADS, P, N, g, keys, surf, ns, 0);
                 LAUNCH("contact_normal", k_contact_normal<T>, sb, NTHREADS, P, N, g, keys, surf, ns, 1);
@@ -471,37 +516,37 @@ int step_impl(mpm_ctx* c, double dt, int contact) {
         if (!contact && c->ndc > 0)
             LAUNCH("dc_apply", k_dc_apply<T>, blocks_for(c->ndc), NTHREADS, (const unsigned*)c->dclist.p, c->ndc,
                    keys, P, N, g, contact);
-        LAUNCH("grid_update", k_grid_update<T>, blocks_for(nn), NTHREADS, N, (T)dt, c->sim.damping, contact,
+        LAUNCH("grid_update", k_grid_update<T>, nodeblocks, NTHREADS, N, (T)dt, c->sim.damping, contact,
                c->floor_friction);
         if (contact && c->ndc > 0)
             LAUNCH("dc_apply", k_dc_apply<T>, blocks_for(c->ndc), NTHREADS, (const unsigned*)c->dclist.p, c->ndc,
                    keys, P, N, g, contact);
-        LAUNCH("node_ratio", k_node_ratio<T>, blocks_for(nn), NTHREADS, N, (const T*)c->g_force.p, c->sim.mass_min,
+        LAUNCH("node_ratio", k_node_ratio<T>, nodeblocks, NTHREADS, N, (const T*)c->g_force.p, c->sim.mass_min,
                1);
         LAUNCH("pass1_remap", k_pass1_remap<T>, blocks_for(n), NTHREADS, P, N, g, skeys, perm, n, (T)dt,
                c->sim.mass_min, contact);
-        LAUNCH("node_remap", k_node_remap<T>, blocks_for(nn), NTHREADS, N, c->sim.mass_min);
+        LAUNCH("node_remap", k_node_remap<T>, nodeblocks, NTHREADS, N, c->sim.mass_min);
         if (!contact) {
             if (c->ndc > 0)
                 LAUNCH("dc_apply", k_dc_apply<T>, blocks_for(c->ndc), NTHREADS, (const unsigned*)c->dclist.p,
                        c->ndc, keys, P, N, g, contact);
-            LAUNCH("node_bc", k_node_bc<T>, blocks_for(nn), NTHREADS, N);
+            LAUNCH("node_bc", k_node_bc<T>, nodeblocks, NTHREADS, N);
         } else {
-            LAUNCH("node_bc", k_node_bc<T>, blocks_for(nn), NTHREADS, N);
+            LAUNCH("node_bc", k_node_bc<T>, nodeblocks, NTHREADS, N);
             if (c->ndc > 0)
                 LAUNCH("dc_apply", k_dc_apply<T>, blocks_for(c->ndc), NTHREADS, (const unsigned*)c->dclist.p,
                        c->ndc, keys, P, N, g, contact);
         }
-        LAUNCH("node_ratio", k_node_ratio<T>, blocks_for(nn), NTHREADS, N, (const T*)c->g_mom.p, c->sim.mass_min, 0);
+        LAUNCH("node_ratio", k_node_ratio<T>, nodeblocks, NTHREADS, N, (const T*)c->g_mom.p, c->sim.mass_min, 0);
         StepArgs a;
         a.dt = dt;
         a.mass_min = c->sim.mass_min;
         timeline_velocity(c, c->sim.time, a.tv);
         a.has_timeline = c->tl_t.empty() ? 0 : 1;
         a.contact = contact;
-        LAUNCH("pass2", k_pass2<T>, blocks_for(n, c->pass_block), c->pass_block, P, N, g, keys,
-               (const MatConst*)c->mats.p, c->nmat, a,
-               err);
+        LAUNCH("pass2", k_pass2<T>, blocks_for(n, c->pass_block), c->pass_block, P, N, g,
+               (unsigned*)c->keys_copy.p, keys_next, (const MatConst*)c->mats.p, c->nmat, a, err);
+        c->keys_valid = true;
     }
     CK(cudaGetLastError());
     // d_Time += dTimeIncrement; i_TimeCycle++ (…MPLocks.cpp:802-803)
@@ -525,7 +570,7 @@ int alloc_particles(mpm_ctx* c, long long n) {
                 {&c->e_strain_ti, 8}, {&c->e_plastic, 8},      {&c->backstress, t},      {&c->mp_mg, 3 * 8},
                 {&c->strain_rate, 6 * t}, {&c->material, 4},   {&c->pflags, 1},          {&c->dc_mult, 4},
                 {&c->keys0, 4},       {&c->vals0, 4},          {&c->keys1, 4},           {&c->vals1, 4},
-                {&c->keys_copy, 4}};
+                {&c->keys_copy, 4},   {&c->loc, c->form == MPM_FORM_FP32 ? 12u : 0u}};
     for (auto& e : plan) {
         int rc = ensure(c, *e.b, (size_t)n * e.bytes);
         if (rc) return rc;
@@ -565,16 +610,25 @@ int mpm_device_info(char* name, int name_len, int* sm_count, int* cc_major, int*
     return MPM_OK;
 }
 
-int mpm_create(const mpm_grid_desc* grid, int form, mpm_ctx** out) {
+int mpm_create(const mpm_grid_desc* grid, int form, mpm_ctx** out) { return mpm_create_batch(grid, 1, form, out); }
+
+int mpm_create_batch(const mpm_grid_desc* grids, int32_t nspec, int form, mpm_ctx** out) {
     if (!out) return MPM_ERR_ARG;
     *out = nullptr;
-    if (!grid || (form != MPM_FORM_FP64 && form != MPM_FORM_FP32)) return MPM_ERR_ARG;
-    long long keyspace = 1;
-    for (int a = 0; a < 3; ++a) {
-        if (!(grid->length[a] > 0.0) || !std::isfinite(grid->length[a]) || grid->cells[a] < 1) return MPM_ERR_ARG;
-        keyspace *= (long long)grid->cells[a] + 2;
+    if (!grids || nspec < 1 || nspec > 65535 || (form != MPM_FORM_FP64 && form != MPM_FORM_FP32)) return MPM_ERR_ARG;
+    long long keyspace = 0, nodes = 0;
+    for (int s = 0; s < nspec; ++s) {
+        long long ks = 1, ns = 1;
+        for (int a = 0; a < 3; ++a) {
+            const mpm_grid_desc& gd = grids[s];
+            if (!(gd.length[a] > 0.0) || !std::isfinite(gd.length[a]) || gd.cells[a] < 1) return MPM_ERR_ARG;
+            ks *= (long long)gd.cells[a] + 2;
+            ns *= (long long)gd.cells[a] + 1;
+        }
+        keyspace += ks;
+        nodes += ns;
     }
-    if (keyspace >= 0xffffffffLL) return MPM_ERR_ARG;
+    if (keyspace >= 0xffffffffLL || nodes >= 0xffffffffLL) return MPM_ERR_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         cudaGetLastError();
@@ -583,28 +637,43 @@ int mpm_create(const mpm_grid_desc* grid, int form, mpm_ctx** out) {
     mpm_ctx* c = new mpm_ctx();
     c->form = form;
     c->tsize = form == MPM_FORM_FP64 ? 8 : 4;
+    c->nspec = nspec;
     cudaGetDevice(&c->device);
     cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
     if (c->sm_count <= 0) c->sm_count = 152;
-    Geom& g = c->g;
-    for (int a = 0; a < 3; ++a) {
-        c->length[a] = grid->length[a];
-        c->cells[a] = grid->cells[a];
-        // d3_Length_Cell = d3Length_Grid / dvec3(i3Cells)
-        g.h[a] = grid->length[a] / (double)grid->cells[a];
-        g.inv_h[a] = 1.0 / g.h[a];
-        g.nn[a] = grid->cells[a] + 1;
-        g.kd[a] = grid->cells[a] + 2;
-    }
-    g.key_max = (unsigned)keyspace;
-    g.n_nodes = (long long)g.nn[0] * g.nn[1] * g.nn[2];
-    c->nn = g.n_nodes;
-    // padded node coordinate tables: entry n+1 for node n in [-1, nn]
+    // per-specimen geometry, nodes and cell keys numbered one specimen after the other
     std::vector<double> tab;
-    for (int a = 0; a < 3; ++a) {
-        g.xoff[a] = (int)tab.size();
-        for (int i = -1; i <= g.nn[a]; ++i) tab.push_back(i * grid->length[a] / grid->cells[a]);
+    c->geoms.resize(nspec);
+    unsigned key_off = 0;
+    long long node_off = 0;
+    for (int s = 0; s < nspec; ++s) {
+        const mpm_grid_desc& gd = grids[s];
+        Geom& g = c->geoms[s];
+        memset(&g, 0, sizeof(g));
+        long long ks = 1, ns = 1;
+        for (int a = 0; a < 3; ++a) {
+            // d3_Length_Cell = d3Length_Grid / dvec3(i3Cells)
+            g.h[a] = gd.length[a] / (double)gd.cells[a];
+            g.inv_h[a] = 1.0 / g.h[a];
+            g.nn[a] = gd.cells[a] + 1;
+            g.kd[a] = gd.cells[a] + 2;
+            ks *= g.kd[a];
+            ns *= g.nn[a];
+            // padded node coordinate table: entry n+1 for node n in [-1, nn], (i*L)/cells
+            g.xoff[a] = (int)tab.size();
+            for (int i = -1; i <= g.nn[a]; ++i) tab.push_back(i * gd.length[a] / gd.cells[a]);
+        }
+        g.key_off = key_off;
+        g.node_off = node_off;
+        key_off += (unsigned)ks;
+        node_off += ns;
+        if (s == 0)
+            for (int a = 0; a < 3; ++a) {
+                c->length[a] = gd.length[a];
+                c->cells[a] = gd.cells[a];
+            }
     }
+    c->nn = node_off;
     int rc = MPM_OK;
     auto bail = [&](int code) {
         mpm_destroy(c);
@@ -615,7 +684,20 @@ int mpm_create(const mpm_grid_desc* grid, int form, mpm_ctx** out) {
     if ((rc = ensure(c, c->xtab, tab.size() * 8))) return bail(rc);
     if (cudaMemcpy(c->xtab.p, tab.data(), tab.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess)
         return bail(MPM_ERR_CUDA);
-    g.xtab = (const double*)c->xtab.p;
+    for (Geom& g : c->geoms) {
+        g.key_max = key_off;
+        g.n_nodes = node_off;
+        g.xtab = (const double*)c->xtab.p;
+        g.nspec = nspec;
+    }
+    if (nspec > 1) {
+        if ((rc = ensure(c, c->geom_tab, sizeof(Geom) * nspec))) return bail(rc);
+        for (Geom& g : c->geoms) g.tab = (const Geom*)c->geom_tab.p;
+        if (cudaMemcpy(c->geom_tab.p, c->geoms.data(), sizeof(Geom) * nspec, cudaMemcpyHostToDevice) != cudaSuccess)
+            return bail(MPM_ERR_CUDA);
+    }
+    c->g = c->geoms[0];
+    Geom& g = c->g;
     if ((rc = ensure(c, c->err_word, 4))) return bail(rc);
     cudaMemset(c->err_word.p, 0, 4);
     if (cudaMallocHost((void**)&c->h_err, sizeof(unsigned)) != cudaSuccess) return bail(MPM_ERR_CUDA);
@@ -628,13 +710,24 @@ int mpm_create(const mpm_grid_desc* grid, int form, mpm_ctx** out) {
                 {&c->g_state, nn * 4},     {&c->g_fixed, nn},        {&c->g_friction, nn * 8},
                 {&c->g_ratio, 3 * nn * t}, {&c->g_q, 3 * nn * t},    {&c->g_owner, 3 * nn * 4},
                 {&c->g_nowner, nn * 4},    {&c->g_need, nn * 4},     {&c->g_list, nn * 4},
-                {&c->g_count, 4},          {&c->cstart, (size_t)g.key_max * 4},
+                {&c->g_count, 4},          {&c->alist, nn * 4},       {&c->acount, 4},
+                {&c->cstart, (size_t)g.key_max * 4},
                 {&c->cend, (size_t)g.key_max * 4}};
     for (auto& e : plan) {
         if ((rc = ensure(c, *e.b, e.bytes))) return bail(rc);
         if (cudaMemset(e.b->p, 0, e.bytes) != cudaSuccess) return bail(MPM_ERR_CUDA);
     }
     *out = c;
+    return MPM_OK;
+}
+
+int mpm_batch_info(const mpm_ctx* c, int64_t* node_offsets, int32_t* nspec) {
+    if (!c) return MPM_ERR_ARG;
+    if (nspec) *nspec = c->nspec;
+    if (node_offsets) {
+        for (int s = 0; s < c->nspec; ++s) node_offsets[s] = c->geoms[s].node_off;
+        node_offsets[c->nspec] = c->nn;
+    }
     return MPM_OK;
 }
 
@@ -717,9 +810,23 @@ int mpm_upload_particles(mpm_ctx* c, const mpm_particles* p, int64_t n) {
     if (!c) return MPM_ERR_ARG;
     if (!p || n < 0 || n >= 0x7fffffffLL) return fail(c, MPM_ERR_ARG, "bad particle upload (n=%lld)", (long long)n);
     const bool f64 = c->form == MPM_FORM_FP64;
+    std::vector<uint16_t> sid16;
+    if (c->nspec > 1) {
+        if (!p->specimen && n > 0) return fail(c, MPM_ERR_ARG, "a batch of specimens needs the specimen of each particle");
+        sid16.resize((size_t)std::max<int64_t>(1, n));
+        for (int64_t i = 0; i < n; ++i) {
+            if (p->specimen[i] < 0 || p->specimen[i] >= c->nspec)
+                return fail(c, MPM_ERR_ARG, "particle %lld: specimen %d out of range", (long long)i, p->specimen[i]);
+            sid16[i] = (uint16_t)p->specimen[i];
+        }
+    }
     int rc = alloc_particles(c, n);
     if (rc) return rc;
     c->n = n;
+    if (c->nspec > 1) {
+        if ((rc = ensure(c, c->sid, sid16.size() * 2))) return rc;
+        CK(cudaMemcpy(c->sid.p, sid16.data(), sid16.size() * 2, cudaMemcpyHostToDevice));
+    }
     struct {
         DevBuf* b;
         const double* h;
@@ -783,6 +890,7 @@ int mpm_upload_particles(mpm_ctx* c, const mpm_particles* p, int64_t n) {
     CK(cudaStreamSynchronize(c->stream));
     c->nsurf = (int)*c->h_err;
     c->have_particles = true;
+    c->keys_valid = false;
     return MPM_OK;
 }
 
@@ -840,6 +948,7 @@ int mpm_upload_nodes(mpm_ctx* c, const mpm_nodes* nd) {
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(c->stream));
     c->have_nodes = true;
+    c->have_alist = false;
     return MPM_OK;
 }
 
@@ -1001,11 +1110,66 @@ int mpm_cell_order(mpm_ctx* c, uint32_t* keys, uint32_t* sorted_order, int64_t n
     if (!c) return MPM_ERR_ARG;
     if (n != c->n) return fail(c, MPM_ERR_ARG, "n = %lld, engine holds %lld particles", (long long)n, c->n);
     if (!c->last_perm && n > 0) return fail(c, MPM_ERR_STATE, "no step has run yet");
-    if (n > 0 && keys) CK(cudaMemcpyAsync(keys, c->keys_copy.p, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
-    if (n > 0 && sorted_order)
-        CK(cudaMemcpyAsync(sorted_order, c->last_perm, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
+    std::vector<uint32_t> perm((size_t)std::max<int64_t>(1, n)), skeys((size_t)std::max<int64_t>(1, n));
+    if (n > 0) {
+        CK(cudaMemcpyAsync(perm.data(), c->last_perm, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaMemcpyAsync(skeys.data(), c->last_skeys, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
+    }
     CK(cudaStreamSynchronize(c->stream));
+    // the last step's key of particle perm[s] is its sorted key skeys[s]
+    if (keys)
+        for (int64_t s = 0; s < n; ++s) keys[perm[s]] = skeys[s];
+    if (sorted_order && n > 0) memcpy(sorted_order, perm.data(), (size_t)n * 4);
     return MPM_OK;
+}
+
+int mpm_upload_monitor_mask(mpm_ctx* c, const uint8_t* mask, int64_t n) {
+    if (!c) return MPM_ERR_ARG;
+    if (n != c->n || (n > 0 && !mask)) return fail(c, MPM_ERR_ARG, "monitor mask must have one entry per particle");
+    int rc = ensure(c, c->mon_mask, (size_t)std::max<int64_t>(1, n));
+    if (rc) return rc;
+    if (n > 0) CK(cudaMemcpyAsync(c->mon_mask.p, mask, (size_t)n, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->have_mon = true;
+    return MPM_OK;
+}
+
+int mpm_monitors_read(mpm_ctx* c, mpm_monitors* out) {
+    if (!c || !out) return MPM_ERR_ARG;
+    if (!c->have_mon && c->n > 0) return fail(c, MPM_ERR_STATE, "no monitor mask uploaded");
+    int rc = ensure(c, c->mon_acc, MON_SLOTS * 8);
+    if (rc) return rc;
+    CK(cudaMemsetAsync(c->mon_acc.p, 0, MON_SLOTS * 8, c->stream));
+    double* acc = (double*)c->mon_acc.p;
+    const uint8_t* mask = (const uint8_t*)c->mon_mask.p;
+    if (c->form == MPM_FORM_FP64) {
+        if (c->n > 0) LAUNCH("monitors", k_monitors<double>, blocks_for(c->n), NTHREADS, pview<double>(c), mask, acc);
+        LAUNCH("monitors", k_monitor_force<double>, blocks_for(c->nn), NTHREADS, nview<double>(c), acc);
+    } else {
+        if (c->n > 0) LAUNCH("monitors", k_monitors<float>, blocks_for(c->n), NTHREADS, pview<float>(c), mask, acc);
+        LAUNCH("monitors", k_monitor_force<float>, blocks_for(c->nn), NTHREADS, nview<float>(c), acc);
+    }
+    double a[MON_SLOTS];
+    CK(cudaMemcpyAsync(a, c->mon_acc.p, MON_SLOTS * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    int64_t cnt[5];
+    memcpy(cnt, &a[24], sizeof(cnt));
+    memset(out, 0, sizeof(*out));
+    out->time = c->sim.time;
+    for (int k = 0; k < 5; ++k) out->count[k] = cnt[k];
+    for (int i = 0; i < 3; ++i) {
+        out->position_mean[i] = cnt[0] ? a[i] / (double)cnt[0] : 0.0;
+        out->momentum[i] = a[3 + i];
+        out->stress_mean[i] = cnt[3] ? a[8 + i] / (double)cnt[3] : 0.0;
+        out->strain_mean[i] = cnt[3] ? a[11 + i] / (double)cnt[3] : 0.0;
+        out->force_sum[i] = a[17 + i];
+    }
+    out->strain_p_max = a[6];
+    out->stress_p_max = a[7];
+    out->kinetic = a[14];
+    out->strain_energy = a[15];
+    out->plastic_energy = a[16];
+    return check_device_error(c);
 }
 
 int mpm_autotune(mpm_ctx* c, int32_t steps, double dt, int contact, mpm_tune_result* out) {
@@ -1067,6 +1231,8 @@ int mpm_autotune(mpm_ctx* c, int32_t steps, double dt, int contact, mpm_tune_res
                 }
                 worst_ms = std::max(worst_ms, per);
                 if (copy_all(false) != MPM_OK) rc = MPM_ERR_CUDA;
+                c->keys_valid = false;  // positions restored: keys are recomputed next step
+                c->have_alist = false;
                 c->sim = sim0;
             }
     cudaEventDestroy(a);

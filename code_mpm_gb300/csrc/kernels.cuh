@@ -29,20 +29,20 @@ namespace mpm {
 // ---------------------------------------------------------------------------
 template <typename T>
 __global__ void k_reset_grid(NView<T> nd, int contact) {
-    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= nd.nn) return;
-    unsigned st = nd.state[i];
-    if (!(st & 1u)) return;
     const long long nn = nd.nn;
-    nd.state[i] = contact ? 0u : (st & ~1u);
-    nd.mass[i] = (T)0;
+    NODE_LOOP(nd, i) {
+        unsigned st = nd.state[i];
+        if (!(st & 1u)) continue;
+        nd.state[i] = contact ? 0u : (st & ~1u);
+        nd.mass[i] = (T)0;
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        if (contact) nd.mg[c * nn + i] = 0.0;
-        nd.vel[c * nn + i] = (T)0;
-        nd.mom[c * nn + i] = (T)0;
-        nd.force[c * nn + i] = (T)0;
-        nd.ftemp[c * nn + i] = (T)0;
+        for (int c = 0; c < 3; ++c) {
+            if (contact) nd.mg[c * nn + i] = 0.0;
+            nd.vel[c * nn + i] = (T)0;
+            nd.mom[c * nn + i] = (T)0;
+            nd.force[c * nn + i] = (T)0;
+            nd.ftemp[c * nn + i] = (T)0;
+        }
     }
 }
 
@@ -53,29 +53,39 @@ __global__ void k_reset_grid(NView<T> nd, int contact) {
 // reference.  Particles whose base cell lies outside [-1, cells] have no node
 // in range and get key_max.
 // ---------------------------------------------------------------------------
-static __global__ void k_cell_keys(const double* __restrict__ pos, long long n, Geom g, unsigned* __restrict__ keys,
-                            unsigned* __restrict__ vals, unsigned* __restrict__ keys_copy, unsigned* err) {
-    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (p >= n) return;
+__device__ __forceinline__ unsigned particle_key(const Geom& g, const double x[3], float u[3], unsigned* err) {
     bool ok = true;
     int b[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        double q = div_rn_by(pos[a * n + p], g.h[a], g.inv_h[a]);
-        if (!isfinite(q)) {
+        double f;
+        if (!cell_and_local(g, a, x[a], f, u[a])) {
             atomicOr(err, ERR_NONFINITE_POSITION);
             ok = false;
             b[a] = 0;
             continue;
         }
-        double f = floor(q);
         if (f < -1.0 || f > (double)(g.nn[a] - 1)) ok = false;
         b[a] = ok ? (int)f : 0;
     }
-    unsigned key = ok ? (unsigned)((b[0] + 1) + g.kd[0] * ((b[1] + 1) + g.kd[1] * (b[2] + 1))) : g.key_max;
+    return ok ? g.key_off + (unsigned)((b[0] + 1) + g.kd[0] * ((b[1] + 1) + g.kd[1] * (b[2] + 1))) : g.key_max;
+}
+
+static __global__ void k_cell_keys(const double* __restrict__ pos, long long n, Geom g, unsigned* __restrict__ keys,
+                            unsigned* __restrict__ vals, unsigned* __restrict__ keys_copy, unsigned* err,
+                            float* __restrict__ loc, const uint16_t* __restrict__ sid) {
+    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const double x[3] = {pos[p], pos[n + p], pos[2 * n + p]};
+    float u[3];
+    const unsigned key = particle_key(spec_geom(g, sid, p), x, u, err);
     keys[p] = key;
     keys_copy[p] = key;
-    vals[p] = (unsigned)p;
+    if (vals) vals[p] = (unsigned)p;
+    if (loc) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) loc[a * n + p] = u[a];
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -83,18 +93,20 @@ static __global__ void k_cell_keys(const double* __restrict__ pos, long long n, 
 // per-cell [start, end) ranges in sorted order.
 // ---------------------------------------------------------------------------
 static __global__ void k_cell_ranges(const unsigned* __restrict__ skeys, long long n, Geom g, unsigned* __restrict__ state,
-                              unsigned* __restrict__ cstart, unsigned* __restrict__ cend) {
+                              unsigned* __restrict__ cstart, unsigned* __restrict__ cend,
+                              const unsigned* __restrict__ perm, const uint16_t* __restrict__ sid) {
     long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (s >= n) return;
     unsigned key = skeys[s];
     if (key >= g.key_max) return;
     if (s == 0 || skeys[s - 1] != key) {
         if (cstart) cstart[key] = (unsigned)s;
+        const Geom& gs = (g.nspec > 1) ? g.tab[sid[perm[s]]] : g;
         int b[3];
-        key_to_base(key, g, b);
+        key_to_base(key, gs, b);
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
-            long long nid = corner_node(g, b, k);
+            long long nid = corner_node(gs, b, k);
             if (nid >= 0) atomicOr(&state[nid], 1u);
         }
     }
@@ -128,6 +140,21 @@ struct Runs {
     }
 };
 
+// Bases of particle p: FP64 form from the position, FP32 form from the
+// cell-local coordinate the previous step stored (no FP64 instructions).
+template <typename T>
+__device__ __forceinline__ void particle_bases(const PView<T>& P, const Geom& g, long long p, const int b[3],
+                                               Bases<T>& B) {
+    const long long np = P.n;
+    if constexpr (sizeof(T) == 4) {
+        const float u[3] = {P.loc[p], P.loc[np + p], P.loc[2 * np + p]};
+        B.init_local(g, u);
+    } else {
+        const double x[3] = {P.pos[p], P.pos[np + p], P.pos[2 * np + p]};
+        B.init(g, x, b);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // P2G (M2G, …MPLocks.cpp:48-89): per particle and corner, mass N m, momentum
 // N (m v), force -V (grad N . sigma) + N f_ext (Voigt order xx yy zz xy yz zx,
@@ -152,11 +179,12 @@ __global__ void __launch_bounds__(512) k_p2g(PView<T> P, NView<T> nd, Geom g, co
     int b[3] = {0, 0, 0};
     Bases<T> B;
     T m = 0, vs[6] = {0, 0, 0, 0, 0, 0}, mv[3] = {0, 0, 0}, fe[3] = {0, 0, 0};
+    const Geom* gsp = &g;
     if (valid) {
         long long p = perm[s];
-        key_to_base(key, g, b);
-        double x[3] = {P.pos[p], P.pos[np + p], P.pos[2 * np + p]};
-        B.init(g, x, b);
+        gsp = &spec_geom(g, P.sid, p);
+        key_to_base(key, *gsp, b);
+        particle_bases<T>(P, *gsp, p, b, B);
         m = P.mass[p];
         const T V = P.vol[p];
 #pragma unroll
@@ -192,7 +220,7 @@ __global__ void __launch_bounds__(512) k_p2g(PView<T> P, NView<T> nd, Geom g, co
             }
         }
         if (valid && (!REDUCE || run.tail)) {
-            long long nid = corner_node(g, b, k);
+            long long nid = corner_node(*gsp, b, k);
             if (nid >= 0) {
                 atomicAdd(&nd.mass[nid], c[0]);
                 atomicAdd(&nd.mom[nid], c[1]);
@@ -220,17 +248,18 @@ __global__ void __launch_bounds__(512) k_p2g(PView<T> P, NView<T> nd, Geom g, co
 // ---------------------------------------------------------------------------
 static __global__ void k_dc_claim(const unsigned* __restrict__ dclist, int ndc, const unsigned* __restrict__ keys,
                            const uint8_t* __restrict__ pflags, Geom g, unsigned* __restrict__ owner, long long nn,
-                           int contact) {
+                           int contact, const uint16_t* __restrict__ sid) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= ndc) return;
     unsigned p = dclist[k];
     unsigned key = keys[p];
     if (key >= g.key_max) return;
+    const Geom& gs = spec_geom(g, sid, p);
     unsigned axes = contact ? 7u : (pflags[p] & 7u);
     int b[3];
-    key_to_base(key, g, b);
+    key_to_base(key, gs, b);
     for (int c8 = 0; c8 < 8; ++c8) {
-        long long nid = corner_node(g, b, c8);
+        long long nid = corner_node(gs, b, c8);
         if (nid < 0) continue;
         for (int a = 0; a < 3; ++a)
             if (axes & (1u << a)) atomicMax(&owner[a * nn + nid], (unsigned)k + 1u);
@@ -245,12 +274,13 @@ __global__ void k_dc_apply(const unsigned* __restrict__ dclist, int ndc, const u
     unsigned p = dclist[k];
     unsigned key = keys[p];
     if (key >= g.key_max) return;
+    const Geom& gs = spec_geom(g, P.sid, p);
     const long long nn = nd.nn, np = P.n;
     unsigned axes = contact ? 7u : (P.pflags[p] & 7u);
     int b[3];
-    key_to_base(key, g, b);
+    key_to_base(key, gs, b);
     for (int c8 = 0; c8 < 8; ++c8) {
-        long long nid = corner_node(g, b, c8);
+        long long nid = corner_node(gs, b, c8);
         if (nid < 0) continue;
         for (int a = 0; a < 3; ++a) {
             if (!(axes & (1u << a)) || nd.owner[a * nn + nid] != (unsigned)k + 1u) continue;
@@ -280,9 +310,9 @@ __device__ __forceinline__ void coulomb(T p_t, T& f_t, T fn, T mu, T dt) {
 }
 
 template <typename T>
-__global__ void k_grid_update(NView<T> nd, T dt, double damping, int contact, int floor_friction) {
-    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= nd.nn || !(nd.state[i] & 1u)) return;
+__device__ __forceinline__ void grid_update_node(const NView<T>& nd, long long i, T dt, double damping, int contact,
+                                                 int floor_friction) {
+    if (!(nd.state[i] & 1u)) return;
     const long long nn = nd.nn;
     T p[3], f[3];
 #pragma unroll
@@ -354,13 +384,17 @@ __global__ void k_grid_update(NView<T> nd, T dt, double damping, int contact, in
     if (fx & 2u) nd.ftemp[nn + i] += ft_y;
 }
 
+template <typename T>
+__global__ void k_grid_update(NView<T> nd, T dt, double damping, int contact, int floor_friction) {
+    NODE_LOOP(nd, i) grid_update_node<T>(nd, i, dt, damping, contact, floor_friction);
+}
+
 // ratio = src / m for nodes with m > mass_min (else 0).  src = force before
 // pass 1 (the f_i/m_i of …MPLocks.cpp:508), momentum before pass 2 (:198).
 // Also clears the remap accumulator when asked.
 template <typename T>
-__global__ void k_node_ratio(NView<T> nd, const T* __restrict__ src, double mass_min, int clear_q) {
-    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= nd.nn) return;
+__device__ __forceinline__ void node_ratio(const NView<T>& nd, long long i, const T* __restrict__ src,
+                                           double mass_min, int clear_q) {
     const long long nn = nd.nn;
     if (!(nd.state[i] & 1u)) return;
     T m = nd.mass[i];
@@ -370,6 +404,11 @@ __global__ void k_node_ratio(NView<T> nd, const T* __restrict__ src, double mass
         nd.ratio[c * nn + i] = has ? src[c * nn + i] / m : (T)0;
         if (clear_q) nd.q[c * nn + i] = (T)0;
     }
+}
+
+template <typename T>
+__global__ void k_node_ratio(NView<T> nd, const T* __restrict__ src, double mass_min, int clear_q) {
+    NODE_LOOP(nd, i) node_ratio<T>(nd, i, src, mass_min, clear_q);
 }
 
 // ---------------------------------------------------------------------------
@@ -387,26 +426,30 @@ __global__ void __launch_bounds__(256) k_pass1_remap(PView<T> P, NView<T> nd, Ge
     unsigned key = (s < n) ? skeys[s] : 0xffffffffu;
     Runs run;
     run.init(key);
-    bool valid = key < g.key_max;
+    // key_ok: the run has grid nodes (its tail lane issues the atomics even
+    // when its own particle is skipped); valid: this particle takes part
+    const bool key_ok = key < g.key_max;
+    bool valid = key_ok;
     const long long np = P.n, nn = nd.nn;
     long long p = 0;
-    if (valid) {
+    const Geom* gsp = &g;
+    int b[3] = {0, 0, 0};
+    if (key_ok) {
         p = perm[s];
         if (contact && (P.pflags[p] & 8u)) valid = false;
+        gsp = &spec_geom(g, P.sid, p);
+        key_to_base(key, *gsp, b);
     }
-    int b[3] = {0, 0, 0};
     Bases<T> B;
     T m = 0, v[3] = {0, 0, 0};
     if (valid) {
-        key_to_base(key, g, b);
-        double x[3] = {P.pos[p], P.pos[np + p], P.pos[2 * np + p]};
-        B.init(g, x, b);
+        particle_bases<T>(P, *gsp, p, b, B);
         m = P.mass[p];
 #pragma unroll
         for (int c = 0; c < 3; ++c) v[c] = P.vel[c * np + p];
 #pragma unroll 1
         for (int k = 0; k < 8; ++k) {
-            long long nid = corner_node(g, b, k);
+            long long nid = corner_node(*gsp, b, k);
             if (nid < 0) continue;
             if (!((double)nd.mass[nid] > mass_min)) continue;
             T N, G[3];
@@ -425,8 +468,8 @@ __global__ void __launch_bounds__(256) k_pass1_remap(PView<T> P, NView<T> nd, Ge
         T q0 = run.sum(N * mv[0]);
         T q1 = run.sum(N * mv[1]);
         T q2 = run.sum(N * mv[2]);
-        if (valid && run.tail) {
-            long long nid = corner_node(g, b, k);
+        if (key_ok && run.tail) {
+            long long nid = corner_node(*gsp, b, k);
             if (nid >= 0) {
                 atomicAdd(&nd.q[nid], q0);
                 atomicAdd(&nd.q[nn + nid], q1);
@@ -438,9 +481,8 @@ __global__ void __launch_bounds__(256) k_pass1_remap(PView<T> P, NView<T> nd, Ge
 
 // Remap finish: v_i += q_i / m_i on nodes with m_i > mass_min (:559-560).
 template <typename T>
-__global__ void k_node_remap(NView<T> nd, double mass_min) {
-    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= nd.nn || !(nd.state[i] & 1u)) return;
+__device__ __forceinline__ void node_remap(const NView<T>& nd, long long i, double mass_min) {
+    if (!(nd.state[i] & 1u)) return;
     const long long nn = nd.nn;
     T m = nd.mass[i];
     if (!((double)m > mass_min)) return;
@@ -448,11 +490,15 @@ __global__ void k_node_remap(NView<T> nd, double mass_min) {
     for (int c = 0; c < 3; ++c) nd.vel[c * nn + i] += nd.q[c * nn + i] / m;
 }
 
+template <typename T>
+__global__ void k_node_remap(NView<T> nd, double mass_min) {
+    NODE_LOOP(nd, i) node_remap<T>(nd, i, mass_min);
+}
+
 // BC reapply (:573-599): zero the fixed components of v, p and f.
 template <typename T>
-__global__ void k_node_bc(NView<T> nd) {
-    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= nd.nn || !(nd.state[i] & 1u)) return;
+__device__ __forceinline__ void node_bc(const NView<T>& nd, long long i) {
+    if (!(nd.state[i] & 1u)) return;
     const long long nn = nd.nn;
     unsigned fx = nd.fixed[i];
 #pragma unroll
@@ -463,6 +509,11 @@ __global__ void k_node_bc(NView<T> nd) {
             nd.force[c * nn + i] = (T)0;
         }
     }
+}
+
+template <typename T>
+__global__ void k_node_bc(NView<T> nd) {
+    NODE_LOOP(nd, i) node_bc<T>(nd, i);
 }
 
 // TimeLine::getVelocity (TimeLine.h:33-46) is evaluated on the host each step
@@ -478,18 +529,23 @@ struct StepArgs {
 // ---------------------------------------------------------------------------
 // G2P pass 2 + constitutive update + platen (G2P_P2_SmallStrain,
 // …MPLocks.cpp:175-280; contact …_Contact.cpp:438-525 and :531-540).
-// One thread per particle in index order (coalesced particle streams).
+// One thread per particle in index order (coalesced particle streams).  At
+// the end each particle also computes the cell key (and, in the FP32 form,
+// the cell-local coordinate) of its new position for the next step, so the
+// next step needs no separate key pass: `keys` is read (this step) and
+// rewritten (next step), `keys_next` receives the next step's sort input.
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(512) k_pass2(PView<T> P, NView<T> nd, Geom g, const unsigned* __restrict__ keys,
-                                               const MatConst* __restrict__ mats, int nmat, StepArgs a,
-                                               unsigned* err) {
+__global__ void __launch_bounds__(512) k_pass2(PView<T> P, NView<T> nd, Geom g, unsigned* __restrict__ keys,
+                                               unsigned* __restrict__ keys_next, const MatConst* __restrict__ mats,
+                                               int nmat, StepArgs a, unsigned* err) {
     long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long np = P.n, nn = nd.nn;
     if (p >= np) return;
     const unsigned fl = P.pflags[p];
     const T dt = (T)a.dt;
     const bool skip = a.contact && (fl & 8u);
+    const Geom& gs = spec_geom(g, P.sid, p);
     if (!skip) {
         unsigned key = keys[p];
         double x[3] = {P.pos[p], P.pos[np + p], P.pos[2 * np + p]};
@@ -498,9 +554,9 @@ __global__ void __launch_bounds__(512) k_pass2(PView<T> P, NView<T> nd, Geom g, 
         for (int k = 0; k < 9; ++k) L[k] = 0;
         if (key < g.key_max) {
             int b[3];
-            key_to_base(key, g, b);
+            key_to_base(key, gs, b);
             Bases<T> B;
-            B.init(g, x, b);
+            particle_bases<T>(P, gs, p, b, B);
             const double ddt = a.dt;
             // FP32 form: the displacement sum N (p/m) is formed in FP32 and
             // added to the FP64 position once; FP64 form: added per corner
@@ -508,7 +564,7 @@ __global__ void __launch_bounds__(512) k_pass2(PView<T> P, NView<T> nd, Geom g, 
             T disp[3] = {0, 0, 0};
 #pragma unroll 1
             for (int k = 0; k < 8; ++k) {
-                long long nid = corner_node(g, b, k);
+                long long nid = corner_node(gs, b, k);
                 if (nid < 0) continue;
                 T N, G[3];
                 B.corner(k, N, G);
@@ -629,6 +685,16 @@ __global__ void __launch_bounds__(512) k_pass2(PView<T> P, NView<T> nd, Geom g, 
             }
         }
     }
+    // the next step's cell key (and FP32 cell-local coordinate) from the new position
+    const double xn[3] = {P.pos[p], P.pos[np + p], P.pos[2 * np + p]};
+    float u[3];
+    const unsigned nk = particle_key(gs, xn, u, err);
+    keys[p] = nk;
+    keys_next[p] = nk;
+    if constexpr (sizeof(T) == 4) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) P.loc[c * np + p] = u[c];
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -648,10 +714,11 @@ __global__ void k_contact_need(PView<T> P, const unsigned* __restrict__ keys, Ge
     const long long p = surf[t];
     unsigned key = keys[p];
     if (key >= g.key_max) return;
+    const Geom& gs = spec_geom(g, P.sid, p);
     int b[3];
-    key_to_base(key, g, b);
+    key_to_base(key, gs, b);
     for (int k = 0; k < 8; ++k) {
-        long long nid = corner_node(g, b, k);
+        long long nid = corner_node(gs, b, k);
         if (nid >= 0) need[nid] = 1u;
     }
 }
@@ -724,15 +791,17 @@ __global__ void __launch_bounds__(CG_WARPS * 32) k_contact_mass_gradient(PView<T
     const unsigned total_nodes = *count;
     for (unsigned item = blockIdx.x * CG_WARPS + w; item < total_nodes; item += gridDim.x * CG_WARPS) {
         const long long i = list[item];
+        const Geom& gs = node_geom(g, i);
+        const long long il = i - gs.node_off;
         int node[3];
-        node[0] = (int)(i % g.nn[0]);
-        node[1] = (int)((i / g.nn[0]) % g.nn[1]);
-        node[2] = (int)(i / ((long long)g.nn[0] * g.nn[1]));
+        node[0] = (int)(il % gs.nn[0]);
+        node[1] = (int)((il / gs.nn[0]) % gs.nn[1]);
+        node[2] = (int)(il / ((long long)gs.nn[0] * gs.nn[1]));
         // lanes 0..7: the eight surrounding cells (cell = node - {0,1}^3)
         unsigned s0 = 0, len = 0;
         if (lane < 8) {
             int cb[3] = {node[0] - ((lane >> 2) & 1), node[1] - ((lane >> 1) & 1), node[2] - (lane & 1)};
-            unsigned key = (unsigned)((cb[0] + 1) + g.kd[0] * ((cb[1] + 1) + g.kd[1] * (cb[2] + 1)));
+            unsigned key = gs.key_off + (unsigned)((cb[0] + 1) + gs.kd[0] * ((cb[1] + 1) + gs.kd[1] * (cb[2] + 1)));
             s0 = cstart[key];
             unsigned s1 = cend[key];
             len = s1 > s0 ? s1 - s0 : 0u;
@@ -760,7 +829,7 @@ __global__ void __launch_bounds__(CG_WARPS * 32) k_contact_mass_gradient(PView<T
                     cs[k] = segs[k];
                     ce[k] = segs[k] + ((k < 7 ? offs[k + 1] : total) - offs[k]);
                 }
-                mass_gradient_merge<T>(P, g, node, perm, cs, ce, gsum);
+                mass_gradient_merge<T>(P, gs, node, perm, cs, ce, gsum);
             }
         } else {
             for (unsigned e = lane; e < total; e += 32) {
@@ -777,7 +846,7 @@ __global__ void __launch_bounds__(CG_WARPS * 32) k_contact_mass_gradient(PView<T
                 for (unsigned j = 0; j < total; ++j) rank += s_id[w][j] < id ? 1u : 0u;
                 double x[3] = {P.pos[id], P.pos[np + id], P.pos[2 * np + id]};
                 double G[3];
-                exact_gradient(g, x, node, G);
+                exact_gradient(gs, x, node, G);
                 const double m = (double)P.mass[id];
                 s_c[w][rank][0] = __dmul_rn(G[0], m);
                 s_c[w][rank][1] = __dmul_rn(G[1], m);
@@ -817,15 +886,16 @@ __global__ void k_contact_mp_gradient(PView<T> P, NView<T> nd, Geom g, const uns
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nsurf) return;
     const long long p = surf[t];
+    const Geom& gs = spec_geom(g, P.sid, p);
     const long long np = P.n, nn = nd.nn;
     double gp[3] = {0.0, 0.0, 0.0};
     unsigned key = keys[p];
     if (key < g.key_max) {
         int b[3];
-        key_to_base(key, g, b);
+        key_to_base(key, gs, b);
         float best2 = 0.0f;
         for (int k = 0; k < 8; ++k) {
-            long long nid = corner_node(g, b, k);
+            long long nid = corner_node(gs, b, k);
             if (nid < 0) continue;
             double gi[3] = {nd.mg[nid], nd.mg[nn + nid], nd.mg[2 * nn + nid]};
             bool take;
@@ -850,14 +920,17 @@ __global__ void k_contact_mp_gradient(PView<T> P, NView<T> nd, Geom g, const uns
 
 // Reset the node mass gradient of active nodes (:177-186) and the normal claims.
 template <typename T>
-__global__ void k_contact_reset(NView<T> nd) {
-    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= nd.nn) return;
+__device__ __forceinline__ void contact_reset_node(const NView<T>& nd, long long i) {
     nd.nowner[i] = 0u;
     if (!(nd.state[i] & 1u)) return;
     const long long nn = nd.nn;
 #pragma unroll
     for (int c = 0; c < 3; ++c) nd.mg[c * nn + i] = 0.0;
+}
+
+template <typename T>
+__global__ void k_contact_reset(NView<T> nd) {
+    NODE_LOOP(nd, i) contact_reset_node<T>(nd, i);
 }
 
 // Node normal from surface particles with (x_i - x_p) . g_p > 0 (:191-210);
@@ -868,33 +941,34 @@ __global__ void k_contact_normal(PView<T> P, NView<T> nd, Geom g, const unsigned
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nsurf) return;
     const long long p = surf[t];
+    const Geom& gs = spec_geom(g, P.sid, p);
     const long long np = P.n, nn = nd.nn;
     unsigned key = keys[p];
     if (key >= g.key_max) return;
     int b[3];
-    key_to_base(key, g, b);
+    key_to_base(key, gs, b);
     double x[3] = {P.pos[p], P.pos[np + p], P.pos[2 * np + p]};
     double gp[3] = {P.mp_mg[p], P.mp_mg[np + p], P.mp_mg[2 * np + p]};
     float gpf[3] = {(float)gp[0], (float)gp[1], (float)gp[2]};
     float u[3];
     if constexpr (sizeof(T) == 4) {
 #pragma unroll
-        for (int c = 0; c < 3; ++c) u[c] = (float)(x[c] - node_coord(g, c, b[c]));  // offset from the base node
+        for (int c = 0; c < 3; ++c) u[c] = (float)(x[c] - node_coord(gs, c, b[c]));  // offset from the base node
     }
     for (int k = 0; k < 8; ++k) {
-        long long nid = corner_node(g, b, k);
+        long long nid = corner_node(gs, b, k);
         if (nid < 0) continue;
         int o3[3] = {(k >> 2) & 1, (k >> 1) & 1, k & 1};
         bool facing;
         if constexpr (sizeof(T) == 8) {
             double d[3];
 #pragma unroll
-            for (int c = 0; c < 3; ++c) d[c] = __dadd_rn(node_coord(g, c, b[c] + o3[c]), -x[c]);
+            for (int c = 0; c < 3; ++c) d[c] = __dadd_rn(node_coord(gs, c, b[c] + o3[c]), -x[c]);
             facing = dot3_rn(d, gp) > 0.0;
         } else {
             float d[3];
 #pragma unroll
-            for (int c = 0; c < 3; ++c) d[c] = (o3[c] ? (float)g.h[c] : 0.0f) - u[c];
+            for (int c = 0; c < 3; ++c) d[c] = (o3[c] ? (float)gs.h[c] : 0.0f) - u[c];
             facing = dot3f(d, gpf) > 0.0f;
         }
         if (!facing) continue;
@@ -914,11 +988,12 @@ __global__ void k_contact_flags(PView<T> P, NView<T> nd, Geom g, const unsigned*
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nsurf) return;
     const long long p = surf[t];
+    const Geom& gs = spec_geom(g, P.sid, p);
     const long long np = P.n, nn = nd.nn;
     unsigned key = keys[p];
     if (key >= g.key_max) return;
     int b[3];
-    key_to_base(key, g, b);
+    key_to_base(key, gs, b);
     double gp[3] = {P.mp_mg[p], P.mp_mg[np + p], P.mp_mg[2 * np + p]};
     const float gpf[3] = {(float)gp[0], (float)gp[1], (float)gp[2]};
     double lp = 0.0;
@@ -928,7 +1003,7 @@ __global__ void k_contact_flags(PView<T> P, NView<T> nd, Geom g, const unsigned*
     else
         lpf = sqrtf(dot3f(gpf, gpf));
     for (int k = 0; k < 8; ++k) {
-        long long nid = corner_node(g, b, k);
+        long long nid = corner_node(gs, b, k);
         if (nid < 0) continue;
         double gi[3] = {nd.mg[nid], nd.mg[nn + nid], nd.mg[2 * nn + nid]};
         bool pos, neg;
@@ -948,6 +1023,141 @@ __global__ void k_contact_flags(PView<T> P, NView<T> nd, Geom g, const unsigned*
             atomicOr(&nd.state[nid], 4u);
         else if (neg)
             atomicOr(&nd.state[nid], 8u);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Console monitors (PhysicsEngine::reportConsole, PhysicsEngine.cpp:40-183).
+// acc layout (doubles): 0-2 position sum, 3-5 momentum, 6 max |principal
+// strain|, 7 max |principal stress|, 8-10 stress sum, 11-13 strain sum,
+// 14 kinetic, 15 strain energy, 16 plastic energy, 17-19 reaction-force sum;
+// counts (u64) follow at 24-28.
+// ---------------------------------------------------------------------------
+constexpr int MON_SLOTS = 32;
+
+// ConstitutiveRelation::getPrincipal (ConstitutiveRelation_calculateState.cpp:160-196),
+// largest |principal value|; NaN (hydrostatic or zero states) or Q > 0 give 0,
+// as the reference's max update skips them.
+__device__ __forceinline__ double principal_abs_max(const double s[6]) {
+    const double I1 = s[0] + s[1] + s[2];
+    double I2 = 0.0;
+    I2 += s[0] * s[1];
+    I2 += s[1] * s[2];
+    I2 += s[0] * s[2];
+    I2 -= s[3] * s[3];
+    I2 -= s[4] * s[4];
+    I2 -= s[5] * s[5];
+    // symmetric matrix [[s0 s3 s5] [s3 s1 s4] [s5 s4 s2]], glm cofactor determinant
+    const double m[9] = {s[0], s[3], s[5], s[3], s[1], s[4], s[5], s[4], s[2]};
+    const double I3 = Kinematics<double>::det(m);
+    const double Q = (3.0 * I2 - I1 * I1) / 9.0;
+    const double R = (2.0 * I1 * I1 * I1 - 9.0 * I1 * I2 + 27.0 * I3) / 54.0;
+    if (Q > 0.0) return 0.0;
+    double T = R / sqrt(-Q * Q * Q);
+    if (!(T == T)) return 0.0;
+    T = fmin(fmax(T, -1.0), 1.0);
+    const double th = acos(T), pi = 3.14159265359;  // _PI, Definitions.h:12
+    double best = 0.0;
+    for (int k = 0; k < 3; ++k) {
+        double v = fabs(2.0 * sqrt(-Q) * cos((th + 2.0 * k * pi) / 3.0) + 1.0 / 3.0 * I1);
+        if (v == v && v > best) best = v;
+    }
+    return best;
+}
+
+__device__ __forceinline__ void atomic_max_nonneg(double* a, double v) {
+    atomicMax((unsigned long long*)a, (unsigned long long)__double_as_longlong(v));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_monitors(PView<T> P, const uint8_t* __restrict__ mask, double* acc) {
+    __shared__ double sh[8][17];
+    __shared__ unsigned long long shc[8][5];
+    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long np = P.n;
+    double v[17];
+#pragma unroll
+    for (int k = 0; k < 17; ++k) v[k] = 0.0;
+    unsigned long long cnt[5] = {0, 0, 0, 0, 0};
+    if (p < np) {
+        const unsigned mk = mask[p];
+        const double m = (double)P.mass[p];
+        double vel[3] = {(double)P.vel[p], (double)P.vel[np + p], (double)P.vel[2 * np + p]};
+        if (mk & 1u) {
+            for (int c = 0; c < 3; ++c) v[c] = P.pos[c * np + p];
+            cnt[0] = 1;
+        }
+        if (mk & 2u) {
+            for (int c = 0; c < 3; ++c) v[3 + c] = vel[c] * m;
+            cnt[1] = 1;
+        }
+        double sg[6], ep[6];
+        for (int c = 0; c < 6; ++c) {
+            sg[c] = (double)P.stress[c * np + p];
+            ep[c] = (double)P.strain[c * np + p];
+        }
+        if (mk & 4u) {
+            v[6] = principal_abs_max(ep);
+            v[7] = principal_abs_max(sg);
+            cnt[2] = 1;
+        }
+        if (mk & 8u) {
+            for (int c = 0; c < 3; ++c) {
+                v[8 + c] = sg[c];
+                v[11 + c] = ep[c];
+            }
+            cnt[3] = 1;
+        }
+        if (mk & 16u) {
+            double sp = sqrt(vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]);
+            v[14] = 0.5 * m * (sp * sp);
+            v[15] = P.e_strain[p];
+            v[16] = P.e_plastic[p];
+            cnt[4] = 1;
+        }
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 17; ++k) {
+        for (int off = 16; off > 0; off >>= 1) {
+            double o = __shfl_down_sync(FULL_MASK, v[k], off);
+            v[k] = (k == 6 || k == 7) ? fmax(v[k], o) : v[k] + o;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+        for (int off = 16; off > 0; off >>= 1) cnt[k] += __shfl_down_sync(FULL_MASK, cnt[k], off);
+    if (lane == 0) {
+        for (int k = 0; k < 17; ++k) sh[w][k] = v[k];
+        for (int k = 0; k < 5; ++k) shc[w][k] = cnt[k];
+    }
+    __syncthreads();
+    if (threadIdx.x < 17) {
+        const int k = threadIdx.x;
+        double s = sh[0][k];
+        for (int ww = 1; ww < (int)(blockDim.x >> 5); ++ww) s = (k == 6 || k == 7) ? fmax(s, sh[ww][k]) : s + sh[ww][k];
+        if (k == 6 || k == 7)
+            atomic_max_nonneg(&acc[k], s);
+        else
+            atomicAdd(&acc[k], s);
+    } else if (threadIdx.x >= 32 && threadIdx.x < 37) {
+        const int k = threadIdx.x - 32;
+        unsigned long long s = 0;
+        for (int ww = 0; ww < (int)(blockDim.x >> 5); ++ww) s += shc[ww][k];
+        atomicAdd((unsigned long long*)&acc[24 + k], s);
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_monitor_force(NView<T> nd, double* acc) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long nn = nd.nn;
+    double f[3] = {0.0, 0.0, 0.0};
+    if (i < nn)
+        for (int c = 0; c < 3; ++c) f[c] = (double)nd.ftemp[c * nn + i];
+    for (int c = 0; c < 3; ++c) {
+        for (int off = 16; off > 0; off >>= 1) f[c] += __shfl_down_sync(FULL_MASK, f[c], off);
+        if ((threadIdx.x & 31) == 0) atomicAdd(&acc[17 + c], f[c]);
     }
 }
 

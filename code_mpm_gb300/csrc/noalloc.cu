@@ -94,7 +94,7 @@ extern "C" int mpm_cell_order_noalloc(const mpm_grid_desc* grid, const double* d
     // the scratch keeps the previous call's contents: clear the error word
     if (cudaMemsetAsync(err, 0, sizeof(unsigned), st) != cudaSuccess) return MPM_ERR_CUDA;
     const unsigned nb = (unsigned)((n + 255) / 256);
-    k_cell_keys<<<nb, 256, 0, st>>>(d_pos, n, g, keysA, valsA, d_keys, err);
+    k_cell_keys<<<nb, 256, 0, st>>>(d_pos, n, g, keysA, valsA, d_keys, err, nullptr, nullptr);
     int bits = 1;
     while (bits < 32 && ((unsigned long long)1 << bits) <= (unsigned long long)g.key_max) ++bits;
     const int nblocks = (int)((n + RS_TILE - 1) / RS_TILE);

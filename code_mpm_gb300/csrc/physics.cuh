@@ -47,6 +47,20 @@ __device__ __forceinline__ void axis_bases_local(const Geom& g, int a, double x,
     }
 }
 
+// FP32 form, from the stored cell-local coordinate u (no FP64 at all).
+__device__ __forceinline__ void axis_bases_u(float u, float ih, float N[2], float gf[2]) {
+    const float r[2] = {u, u - 1.0f};
+#pragma unroll
+    for (int o = 0; o < 2; ++o) {
+        float ar = fabsf(r[o]);
+        float nv = 1.0f - ar;
+        if (nv < 0.0f || nv > 1.0f) nv = 0.0f;
+        N[o] = nv;
+        float s = (float)((r[o] > 0.0f) - (r[o] < 0.0f));
+        gf[o] = (ar > 1.0e-12f && ar < (float)(1.0 - 1.0e-12)) ? s * ih : 0.0f;
+    }
+}
+
 template <typename T>
 struct Bases {
     T Nx[2], Ny[2], Nz[2];
@@ -61,6 +75,12 @@ struct Bases {
             axis_bases<T>(g, 1, x[1], b[1], Ny, gy);
             axis_bases<T>(g, 2, x[2], b[2], Nz, gz);
         }
+    }
+    // FP32 form: bases from the cell-local coordinate stored by the previous step
+    __device__ __forceinline__ void init_local(const Geom& g, const float u[3]) {
+        axis_bases_u(u[0], (float)g.inv_h[0], (float*)Nx, (float*)gx);
+        axis_bases_u(u[1], (float)g.inv_h[1], (float*)Ny, (float*)gy);
+        axis_bases_u(u[2], (float)g.inv_h[2], (float*)Nz, (float*)gz);
     }
     // corner k = 4*ix + 2*iy + iz
     __device__ __forceinline__ void corner(int k, T& N, T G[3]) const {
@@ -84,6 +104,37 @@ __device__ __forceinline__ double div_rn_by(double a, double b, double y) {
     double q = __dmul_rn(a, y);
     double r = __fma_rn(-q, b, a);
     return __fma_rn(r, y, q);
+}
+
+// ---------------------------------------------------------------------------
+// Base cell b = floor(x/h) along axis a, bit-identical to the floor of the
+// correctly rounded quotient (GridPoint_Mediator.cpp:8), and the cell-local
+// coordinate u = x/h - b as a float.  Fast path: q = RN(x * RN(1/h)) is
+// within 2.3e-16 |q| of x/h and RN(x/h) within 1.2e-16 |q|; if q's float
+// image sits more than 2e-4 from an integer and |q| < 1024 (float half-ulp
+// <= 6.1e-5 there), no rounded quotient can cross an integer, so
+// floor(q) = floor(RN(x/h)).  Otherwise the corrected quotient decides.
+// Returns false for a non-finite quotient.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool cell_and_local(const Geom& g, int a, double x, double& f, float& u) {
+    const double q = __dmul_rn(x, g.inv_h[a]);
+    const float qf = (float)q;
+    const float ff = floorf(qf);
+    const float frf = qf - ff;
+    if (frf > 2.0e-4f && frf < 1.0f - 2.0e-4f && fabsf(qf) < 1024.0f) {
+        f = (double)ff;
+        u = (float)(q - f);
+        return true;
+    }
+    const double qe = div_rn_by(x, g.h[a], g.inv_h[a]);
+    if (!isfinite(qe)) {
+        f = 0.0;
+        u = 0.0f;
+        return false;
+    }
+    f = floor(qe);
+    u = (float)(qe - f);
+    return true;
 }
 
 // ---------------------------------------------------------------------------

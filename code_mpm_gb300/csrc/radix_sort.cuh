@@ -129,7 +129,7 @@ static __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const unsigned
         long long idx = base + c * 32 + lane;
         bool ok = idx < n;
         unsigned key = ok ? kin[idx] : 0u;
-        unsigned val = ok ? vin[idx] : 0u;
+        unsigned val = ok ? (vin ? vin[idx] : (unsigned)idx) : 0u;  // no input values: the identity
         unsigned d = ok ? ((key >> shift) & 255u) : (256u + lane);  // invalid lanes never match a digit
         unsigned peers = __match_any_sync(0xffffffffu, d);
         unsigned rank = 0;

@@ -61,7 +61,7 @@ _PFIELDS = ("pos", "vel", "fext", "mass", "vol", "vol0", "F", "stress", "strain"
 
 class Particles(C.Structure):
     _fields_ = [(k, C.c_void_p) for k in _PFIELDS] + [("material", C.c_void_p), ("pflags", C.c_void_p),
-                                                      ("dc_mult", C.c_void_p)]
+                                                      ("dc_mult", C.c_void_p), ("specimen", C.c_void_p)]
 
 
 _NMAP = (("fixed", "fixed"), ("friction", "friction"), ("mass", "g_mass"), ("mom", "g_mom"), ("vel", "g_vel"),
@@ -82,6 +82,15 @@ class TuneResult(C.Structure):
                 ("candidates", C.c_int32), ("best_ms_per_step", C.c_double), ("worst_ms_per_step", C.c_double)]
 
 
+class Monitors(C.Structure):
+    _fields_ = [("time", C.c_double), ("position_mean", C.c_double * 3), ("force_sum", C.c_double * 3),
+                ("momentum", C.c_double * 3), ("strain_p_max", C.c_double), ("stress_p_max", C.c_double),
+                ("stress_mean", C.c_double * 3), ("strain_mean", C.c_double * 3), ("kinetic", C.c_double),
+                ("strain_energy", C.c_double), ("plastic_energy", C.c_double), ("count", C.c_int64 * 5)]
+
+
+MON_DISPLACEMENT, MON_MOMENTUM, MON_PRINCIPAL, MON_STRESS, MON_ENERGY = 1, 2, 4, 8, 16
+
 OPT_P2G_REDUCE = 3
 OPT_P2G_BLOCK = 4
 OPT_PASS_BLOCK = 5
@@ -101,6 +110,8 @@ def lib():
         vp, i32, i64, dbl = C.c_void_p, C.c_int32, C.c_int64, C.c_double
         sig = {
             "mpm_create": ([C.POINTER(GridDesc), C.c_int, C.POINTER(vp)], C.c_int),
+            "mpm_create_batch": ([C.POINTER(GridDesc), i32, C.c_int, C.POINTER(vp)], C.c_int),
+            "mpm_batch_info": ([vp, C.POINTER(i64), C.POINTER(i32)], C.c_int),
             "mpm_destroy": ([vp], None),
             "mpm_last_error": ([vp], C.c_char_p),
             "mpm_device_info": ([C.c_char_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)],
@@ -126,6 +137,8 @@ def lib():
             "mpm_cell_order": ([vp, vp, vp, i64], C.c_int),
             "mpm_cell_order_noalloc": ([C.POINTER(GridDesc), vp, i64, vp, vp, vp], C.c_int),
             "mpm_autotune": ([vp, i32, dbl, C.c_int, C.POINTER(TuneResult)], C.c_int),
+            "mpm_upload_monitor_mask": ([vp, vp, i64], C.c_int),
+            "mpm_monitors_read": ([vp, C.POINTER(Monitors)], C.c_int),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -170,23 +183,46 @@ def cell_order_noalloc(length, cells, d_pos: int, n: int, d_keys: int, d_order: 
 class Engine:
     """One GPU engine instance (an ``mpm_ctx``)."""
 
-    def __init__(self, length, cells, form: int = FORM_FP64):
+    def __init__(self, length, cells, form: int = FORM_FP64, grids=None):
+        """One grid (length, cells), or a batch of specimen grids [(length, cells), ...]."""
         self._L = lib()
-        g = GridDesc()
-        for a in range(3):
-            g.length[a] = float(length[a])
-            g.cells[a] = int(cells[a])
+        if grids is None:
+            grids = [(length, cells)]
+        tab = (GridDesc * len(grids))()
+        for i, (ln, cl) in enumerate(grids):
+            for a in range(3):
+                tab[i].length[a] = float(ln[a])
+                tab[i].cells[a] = int(cl[a])
         h = C.c_void_p()
-        rc = self._L.mpm_create(C.byref(g), int(form), C.byref(h))
+        rc = self._L.mpm_create_batch(tab, len(grids), int(form), C.byref(h))
         if rc != 0 or not h.value:
             raise MPMError(rc, "mpm_create failed (no usable CUDA device or bad grid)")
         self._h = h
         self.form = int(form)
-        self.length = np.asarray(length, dtype=np.float64)
-        self.cells = np.asarray(cells, dtype=np.int32)
+        self.length = np.asarray(grids[0][0], dtype=np.float64)
+        self.cells = np.asarray(grids[0][1], dtype=np.int32)
+        self.n_spec = len(grids)
         self.n_particles = 0
-        self.n_nodes = int(np.prod(self.cells.astype(np.int64) + 1))
+        self.n_nodes = int(sum(np.prod(np.asarray(cl, dtype=np.int64) + 1) for _, cl in grids))
         self._keep = []
+
+    @classmethod
+    def from_batch(cls, states, form: int = FORM_FP64, time_end: float = 1.0e300):
+        """An engine advancing every specimen of `states` together (see code_mpm_gb300.batch)."""
+        from . import batch
+
+        pk = batch.pack(states)
+        e = cls(None, None, form, grids=pk.grids)
+        e.upload_state(pk.state, time_end=time_end)
+        e.packed = pk
+        return e
+
+    def download_batch(self, states):
+        """Per-specimen states after the batch has advanced."""
+        from . import batch
+
+        full = self.download_state(self.packed.state)
+        return batch.unpack(full, states, self.packed.particle_offsets, self.packed.node_offsets)
 
     # -- plumbing -------------------------------------------------------------------
     def _check(self, rc: int) -> None:
@@ -240,6 +276,8 @@ class Engine:
         arrs["material"] = np.ascontiguousarray(st["material"], dtype=np.int32)
         arrs["pflags"] = np.ascontiguousarray(st["pflags"], dtype=np.uint8)
         arrs["dc_mult"] = np.ascontiguousarray(st["dc_mult"], dtype=np.float32)
+        if "specimen" in st.arrays:
+            arrs["specimen"] = np.ascontiguousarray(st["specimen"], dtype=np.int32)
         p = Particles(**{k: _ptr(v) for k, v in arrs.items()})
         self._check(self._L.mpm_upload_particles(self._h, C.byref(p), st.n_particles))
         self.n_particles = st.n_particles
@@ -282,6 +320,13 @@ class Engine:
                 time_end: float = 1.0e300) -> None:
         s = Sim(float(time), float(dt_max), float(mass_min), float(damping), float(time_end), int(step))
         self._check(self._L.mpm_set_sim(self._h, C.byref(s)))
+
+    def batch_info(self) -> np.ndarray:
+        """First node of each specimen, then the total node count."""
+        offs = (C.c_int64 * (self.n_spec + 1))()
+        ns = C.c_int32(0)
+        self._check(self._L.mpm_batch_info(self._h, offs, C.byref(ns)))
+        return np.array(list(offs), dtype=np.int64)
 
     def get_sim(self) -> Dict[str, float]:
         s = Sim()
@@ -339,6 +384,19 @@ class Engine:
 
     def getCount_GridPoint(self) -> int:
         return self.n_nodes
+
+    def upload_monitor_mask(self, mask: np.ndarray) -> None:
+        m = np.ascontiguousarray(mask, dtype=np.uint8)
+        self._check(self._L.mpm_upload_monitor_mask(self._h, _ptr(m), len(m)))
+
+    def monitors(self) -> Dict[str, object]:
+        """The reportConsole quantities (PhysicsEngine.cpp:40-183), reduced on the GPU."""
+        r = Monitors()
+        self._check(self._L.mpm_monitors_read(self._h, C.byref(r)))
+        return {"time": r.time, "position_mean": list(r.position_mean), "force_sum": list(r.force_sum),
+                "momentum": list(r.momentum), "strain_p_max": r.strain_p_max, "stress_p_max": r.stress_p_max,
+                "stress_mean": list(r.stress_mean), "strain_mean": list(r.strain_mean), "kinetic": r.kinetic,
+                "strain_energy": r.strain_energy, "plastic_energy": r.plastic_energy, "count": list(r.count)}
 
     def cell_order(self):
         """(cell key per particle, particle order sorted by key) of the last step."""

@@ -243,6 +243,85 @@ def mixed_small(seed: int = 1, h: float = 1.0e-3, ncell=(8, 10, 6), vscale: floa
     return st
 
 
+def honeycomb(wall: float, pitch: float, ncell: int, target: int, speed: float, h: float = 0.25e-3,
+              E: float = 200.0e9, nu: float = 0.3, rho: float = 7850.0, yield_: float = 250.0e6,
+              H: float = 2.0e9, C1: float = 1.0e12, friction: float = 0.1, pad: int = 2,
+              headroom: int = 3) -> State:
+    """A square honeycomb crushed in-plane by a rigid platen (contact path).
+
+    Cross-section in the x-z plane: ncell x ncell square cells of pitch
+    `pitch` with walls `wall` thick, (ncell*pitch + wall) wide; extruded
+    along y by as many particle layers as bring the count near `target`.
+    Particles sit at the centres of an h/2 lattice (8 per grid cell) inside
+    the walls; those with an empty lattice neighbour in x or z are surface
+    particles.  A one-layer platen above the top moves down at `speed`
+    (multiplier -speed on a unit timeline, so a batch can give each specimen
+    its own speed); the floor nodes are fixed in z with Coulomb friction.
+    """
+    s = 0.5 * h
+    W = ncell * pitch + wall
+    n1 = int(np.ceil(W / s))
+    c = (np.arange(n1) + 0.5) * s
+    inx = (np.mod(c, pitch) < wall) & (c < W)
+    X, Z = np.meshgrid(c, c, indexing="ij")
+    wall_xz = (inx[:, None] | inx[None, :]) & (X < W) & (Z < W)
+    per_layer = int(wall_xz.sum())
+    ny = max(2, int(round(target / max(per_layer, 1))))
+    nbx = n1 // 2 + 1
+    cells = np.array([nbx + 2 * pad, ny // 2 + 1 + 2 * pad, nbx + pad + headroom], dtype=np.int32)
+    length = cells * h
+    org = np.array([pad * h, pad * h, pad * h])
+    ix, iz = np.nonzero(wall_xz)
+    # surface: a wall lattice site with an empty neighbour in x or z
+    padm = np.pad(wall_xz, 1)
+    surf2 = ~(padm[2:, 1:-1] & padm[:-2, 1:-1] & padm[1:-1, 2:] & padm[1:-1, :-2])[ix, iz]
+    yy = (np.arange(ny) + 0.5) * s
+    body = np.stack([np.repeat(org[0] + c[ix], ny), np.tile(org[1] + yy, len(ix)),
+                     np.repeat(org[2] + c[iz], ny)], axis=1)
+    bsurf = np.repeat(surf2, ny)
+    ztop = org[2] + W + 0.5 * h
+    px = org[0] + np.arange(-h + 0.5 * s, W + h, s)
+    py = org[1] + np.arange(-h + 0.5 * s, ny * s + h, s)
+    PX, PY = np.meshgrid(px, py, indexing="ij")
+    platen = np.stack([PX.ravel(), PY.ravel(), np.full(PX.size, ztop)], axis=1)
+    pos = np.concatenate([body, platen], axis=0)
+    nbody = body.shape[0]
+    dt = 0.2 * h / math.sqrt(E / rho)
+    st = _alloc(length, cells, pos.shape[0], dt, 2, 2, platen.shape[0])
+    _material(st, 0, VONMISESHARDENING, rho, E, nu, yield_, H / C1, C1)
+    _material(st, 1, ELASTIC, rho, E, nu)
+    mat = np.zeros(pos.shape[0], dtype=np.int32)
+    mat[nbody:] = 1
+    _finish_particles(st, pos, s * s * s, mat)
+    st["pflags"][:nbody][bsurf] |= PF_SURFACE
+    st["pflags"][nbody:] = PF_DC_X | PF_DC_Y | PF_DC_Z | PF_DC_SKIP | PF_SURFACE
+    st["dc_mult"][nbody:] = -float(speed)
+    st["vel"][nbody:, 2] = -float(speed)
+    st["dc_list"][:] = np.arange(nbody, pos.shape[0], dtype=np.uint32)
+    st["tl_time"][:] = [0.0, 10.0]
+    st["tl_vel"][:] = [[0.0, 0.0, 1.0], [0.0, 0.0, 1.0]]
+    xn = node_positions(st)
+    floor = np.abs(xn[:, 2] - org[2]) < 0.5 * h
+    st["fixed"][floor] |= NF_FIX_Z
+    st["friction"][floor] = friction
+    return st
+
+
+def honeycomb_batch(n: int = 256, seed: int = 4, total: float = 40.0e6, nmin: int = 10_000, nmax: int = 500_000,
+                    h: float = 0.25e-3):
+    """The batched cellular workload: n honeycombs with walls U(0.4, 1.2) mm, pitch U(4, 8) mm,
+    4-10 cells per side, particle counts log-uniform in [nmin, nmax] scaled so the batch holds
+    about `total` particles, platen speed U(1, 10) m/s per specimen."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    wall = rng.uniform(0.4e-3, 1.2e-3, n)
+    pitch = rng.uniform(4.0e-3, 8.0e-3, n)
+    ncell = rng.integers(4, 11, n)
+    counts = np.exp(rng.uniform(np.log(nmin), np.log(nmax), n))
+    counts = np.clip(counts * total / counts.sum(), nmin, nmax)
+    speed = rng.uniform(1.0, 10.0, n)
+    return [honeycomb(wall[i], pitch[i], int(ncell[i]), int(counts[i]), speed[i], h=h) for i in range(n)]
+
+
 def contact_small(seed: int = 2, h: float = 1.0e-3, nb=(6, 5, 4), speed: float = 30.0) -> State:
     """Small platen_block variant with jittered particles, for contact-path parity."""
     st = platen_block(size=(nb[0] * h, nb[1] * h, nb[2] * h), h=h, ppc=2, yield_=150.0e6, H=2.0e9,

@@ -115,6 +115,7 @@ typedef struct mpm_particles {
     int32_t* material;               /* n, index into the uploaded material table (<0: none) */
     uint8_t* pflags;                 /* n, MPM_PF_* */
     float* dc_mult;                  /* n, f_DisplacementControl_Multiplier */
+    int32_t* specimen;               /* n, specimen of each particle (batches only; upload only) */
 } mpm_particles;
 
 /* Host views of the node state (GridPoint.h:6-45), n_nodes entries each. */
@@ -138,6 +139,15 @@ typedef struct mpm_kernel_stat {
  * (GridPoint_Factory::createGrid, GridPoint_Factory.h:33-68, and the mediator
  * geometry, e.g. PhysicsEngine_initializeWorld_Classic_Bar.cpp:15-27). */
 int mpm_create(const mpm_grid_desc* grid, int form, mpm_ctx** out);
+/* A batch of independent specimens, each with its own grid, advanced together
+ * by every launch (no counterpart in the reference, which runs one scene per
+ * engine).  Their nodes are numbered one specimen after the other (node
+ * arrays in mpm_upload_nodes / mpm_download_nodes are the concatenation);
+ * each particle names its specimen (mpm_particles.specimen).  Specimens never
+ * share nodes, so each evolves exactly as it would alone. */
+int mpm_create_batch(const mpm_grid_desc* grids, int32_t nspec, int form, mpm_ctx** out);
+/* node_offsets[0..nspec]: first node of each specimen, then the total. */
+int mpm_batch_info(const mpm_ctx* ctx, int64_t* node_offsets, int32_t* nspec);
 void mpm_destroy(mpm_ctx* ctx); /* PhysicsEngine::~PhysicsEngine, PhysicsEngine.cpp:4-38 */
 const char* mpm_last_error(const mpm_ctx* ctx);
 int mpm_device_info(char* name, int name_len, int* sm_count, int* cc_major, int* cc_minor);
@@ -230,6 +240,33 @@ int mpm_cell_order(mpm_ctx* ctx, uint32_t* keys, uint32_t* sorted_order, int64_t
 #define MPM_NOALLOC_MAX_PARTICLES (1 << 20)
 int mpm_cell_order_noalloc(const mpm_grid_desc* grid, const double* d_pos, int64_t n, uint32_t* d_keys,
                            uint32_t* d_order, void* stream);
+
+/* --- console monitors ---------------------------------------------------------
+ * The quantities PhysicsEngine::reportConsole (PhysicsEngine.cpp:40-183)
+ * reduces over its marked particle lists, computed on the GPU in FP64 so a
+ * host need not download the particles at every console interval.  Particle
+ * membership in the reference's lists is given by a per-particle mask. */
+#define MPM_MON_DISPLACEMENT 1u /* v_MarkedMaterialPoints_Displacement_Monitor */
+#define MPM_MON_MOMENTUM 2u     /* v_MarkedMaterialPoints_Momentum */
+#define MPM_MON_PRINCIPAL 4u    /* v_MarkedMaterialPoints_Principal_Monitor */
+#define MPM_MON_STRESS 8u       /* v_MarkedMaterialPoints_Stress_Monitor */
+#define MPM_MON_ENERGY 16u      /* v_MarkedMaterialPoints_Monitor_Energy */
+typedef struct mpm_monitors {
+    double time;
+    double position_mean[3];  /* displacement list: mean position (:48-59) */
+    double force_sum[3];      /* all nodes: sum of d3_Force_Temp (:61-70) */
+    double momentum[3];       /* momentum list: sum of m v (:72-80) */
+    double strain_p_max;      /* principal list: max |principal strain| (:82-120) */
+    double stress_p_max;      /* principal list: max |principal stress| */
+    double stress_mean[3];    /* stress list: mean sigma_xx, sigma_yy, sigma_zz (:122-138) */
+    double strain_mean[3];    /* stress list: mean eps_xx, eps_yy, eps_zz */
+    double kinetic;           /* energy list: sum 0.5 m |v|^2 (:140-156) */
+    double strain_energy;     /* energy list: sum of d_Energy_Strain */
+    double plastic_energy;    /* energy list: sum of d_Energy_Plastic */
+    int64_t count[5];         /* members of each list, in the order of the MPM_MON_* bits */
+} mpm_monitors;
+int mpm_upload_monitor_mask(mpm_ctx* ctx, const uint8_t* mask, int64_t n);
+int mpm_monitors_read(mpm_ctx* ctx, mpm_monitors* out);
 
 /* --- profiling ---------------------------------------------------------------
  * Per-kernel CUDA-event timers (the reference's a_Runtime, PhysicsEngine.h:87). */
