@@ -1,15 +1,21 @@
 #!/usr/bin/env python
 """Benchmark: particle-updates/s of the explicit-MPM double-pass step on GB300.
 
-Workload: the J2 block crushed by a rigid platen on the contact path (the
-configuration the headline metric is quoted on): block 0.08 x 0.08 x 0.04 m,
-h = 1 mm, 8 particles per cell (2,048,000 block particles) plus a one-layer
-platen (26,896 particles) moving at -5 m/s, von Mises hardening steel
-(E 200 GPa, nu 0.3, rho 7850, yield 250 MPa, H 2 GPa), fixed floor with
-Coulomb friction 0.1.  One particle-update = one particle advanced through
-one full step; a step is one pass of every kernel of the step over the
-whole particle set.  Inputs are synthetic (seeded generators), resident in
-HBM and larger than L2 (~0.8 GB of particle state).
+Workload (default, "batch"): 256 independent square-honeycomb specimens, each
+with its own grid, crushed in-plane by rigid platens on the contact path and
+advanced together by one engine: walls U(0.4, 1.2) mm, pitch U(4, 8) mm,
+4-10 cells per side, h = 0.25 mm, 8 particles per cell, particle counts
+log-uniform in 10k-500k (about 40.7M particles in total, 59M nodes), platen
+speed U(1, 10) m/s per specimen, von Mises hardening steel (E 200 GPa, nu 0.3,
+rho 7850, yield 250 MPa, H 2 GPa), fixed floor with Coulomb friction 0.1.
+The chosen form (FP32 transfers and grid, FP64 positions and energies, the
+batch in one engine, autotuned launch shapes) is timed against the plain FP64
+form run the reference's way, one specimen per engine; the batched FP64 rate
+is reported beside it.  "--workload block" is the single J2 block crushed by a
+platen (0.08 x 0.08 x 0.04 m, h = 1 mm, 2,074,896 particles).
+
+One particle-update = one particle advanced through one full step.  Inputs are
+synthetic (seeded generators), resident in HBM and larger than L2.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--form fp64|fp32]
 
@@ -43,6 +49,13 @@ ALG_BYTES = {
     "fp64": {"p2g": 136, "pass1_remap": 80, "pass2": 580},
     "fp32": {"p2g": 80, "pass1_remap": 52, "pass2": 348},
 }
+# Grid bytes per active node of each sweep: P2G writes mass, momentum and force
+# (7 values), pass 1 + remap reads f and m and writes the remap sum (4 + 3),
+# pass 2 reads momentum, velocity and mass (3 + 3 + 1).
+ALG_GRID_BYTES = {
+    "fp64": {"p2g": 56, "pass1_remap": 56, "pass2": 56},
+    "fp32": {"p2g": 28, "pass1_remap": 28, "pass2": 28},
+}
 
 
 def parse():
@@ -53,12 +66,14 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--form", default="fp32", choices=["fp64", "fp32"],
                     help="fp32: the chosen form, timed beside the plain FP64 form; fp64: the plain form alone")
+    ap.add_argument("--workload", default="batch", choices=["batch", "block"])
+    ap.add_argument("--specimens", type=int, default=256, help="batch workload: specimen count")
+    ap.add_argument("--total", type=float, default=40.0e6, help="batch workload: target particle count")
+    ap.add_argument("--block", default="0.08,0.08,0.04", help="block workload: block size in m")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip timing the plain FP64 form beside the chosen one")
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--block", default="0.08,0.08,0.04",
-                    help="block size in m (smaller blocks only for profiling captures; the metric uses the default)")
     return ap.parse_args()
 
 
@@ -155,208 +170,402 @@ def peaks():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def workload(block="0.08,0.08,0.04"):
+def workload(args):
+    """(specimen states, config record).  One state for the block workload."""
     from code_mpm_gb300 import scenes
 
-    size = [float(v) for v in block.split(",")]
-    st = scenes.platen_block(size=size)  # default 0.08 x 0.08 x 0.04 m, h = 1 mm, 8 ppc, platen -5 m/s, friction 0.1
-    cfg = {"workload": "J2 block crushed by rigid platen, contact path", "block_m": size,
-           "h_m": 1.0e-3, "particles_per_cell": 8, "n_particles": st.n_particles, "n_nodes": st.n_nodes,
+    if args.workload == "block":
+        size = [float(v) for v in args.block.split(",")]
+        st = scenes.platen_block(size=size)  # h = 1 mm, 8 ppc, platen -5 m/s, friction 0.1
+        cfg = {"workload": "J2 block crushed by rigid platen, contact path", "block_m": size,
+               "h_m": 1.0e-3, "particles_per_cell": 8, "n_particles": st.n_particles, "n_nodes": st.n_nodes,
+               "material": "von Mises hardening E=200GPa nu=0.3 rho=7850 yield=250MPa H=2GPa",
+               "platen_speed_mps": 5.0, "floor_friction": 0.1, "dt_s": st.dt_max,
+               "l2_policy": "inputs larger than L2 (~0.8 GB particle state)"}
+        return [st], cfg
+    sts = scenes.honeycomb_batch(n=args.specimens, total=args.total)
+    counts = [st.n_particles for st in sts]
+    cfg = {"workload": f"{len(sts)} square-honeycomb specimens crushed by rigid platens, one grid each, "
+                       "contact path, batched in one engine",
+           "n_specimens": len(sts), "n_particles": int(sum(counts)), "n_nodes": int(sum(st.n_nodes for st in sts)),
+           "particles_per_specimen": [int(min(counts)), int(max(counts))], "h_m": 0.25e-3, "particles_per_cell": 8,
+           "wall_m": [0.4e-3, 1.2e-3], "pitch_m": [4.0e-3, 8.0e-3], "cells_per_side": [4, 10],
+           "platen_speed_mps": [1.0, 10.0], "floor_friction": 0.1, "dt_s": sts[0].dt_max,
            "material": "von Mises hardening E=200GPa nu=0.3 rho=7850 yield=250MPa H=2GPa",
-           "platen_speed_mps": 5.0, "floor_friction": 0.1, "dt_s": st.dt_max,
-           "l2_policy": "inputs larger than L2 (~0.8 GB particle state)"}
-    return st, cfg
+           "l2_policy": "inputs larger than L2 (~10 GB particle state)"}
+    return sts, cfg
 
 
-def cpu_baseline(st, contact: int, floor_friction: int, budget_s: float = 12.0):
-    """The CPU restatement (OpenMP, all host threads) on a bounded sample of the same workload."""
+def subset(sts, k):
+    """k specimens spread over the size distribution (quantiles of the particle count)."""
+    if len(sts) <= k:
+        return list(range(len(sts)))
+    order = sorted(range(len(sts)), key=lambda i: sts[i].n_particles)
+    return sorted({order[round(q * (len(sts) - 1) / (k - 1))] for q in range(k)})
+
+
+def cpu_rate(sts, idx, contact, floor, budget_s, max_steps=50):
+    """The CPU restatement (OpenMP, all host threads) over specimens idx: steps until the budget is spent."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
 
     pyoracle.build()
     threads = os.cpu_count() or 1
-    s = st.copy()
+    work = [sts[i].copy() for i in idx]
+    n = sum(s.n_particles for s in work)
     steps_done, secs = 0, 0.0
     t0 = time.perf_counter()
     while True:
-        secs += pyoracle.advance(s, 1, contact, floor_friction=floor_friction, threads=threads, omp=True)
+        for s in work:
+            secs += pyoracle.advance(s, 1, contact, floor_friction=floor, threads=threads, omp=True)
         steps_done += 1
-        if time.perf_counter() - t0 > budget_s or steps_done >= 50:
+        if time.perf_counter() - t0 > budget_s or steps_done >= max_steps:
             break
-    rate = st.n_particles * steps_done / secs
+    return n * steps_done / secs, steps_done, secs, n, threads
+
+
+def cpu_baseline(sts, contact, floor, budget_s=12.0):
+    idx = subset(sts, 16)
+    rate, steps, secs, n, threads = cpu_rate(sts, idx, contact, floor, budget_s)
     return {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{steps_done} full steps of the same workload ({st.n_particles} particles), "
-                      f"OpenMP restatement with per-node locks, {threads} threads, {secs:.2f} s"}
+            "sample": f"{steps} full steps of {len(idx)} of the {len(sts)} specimens ({n} particles, spread over "
+                      f"the size range), OpenMP restatement with per-node locks, {threads} threads, {secs:.2f} s"}
 
 
-def timed_form(st, form, args, dist, contact, floor, tune=True):
-    """Autotune, warm up and time one form on `st`; returns (engine, ms, launches, clocks, tune result)."""
+def make_engine(sts, pk, form):
     from code_mpm_gb300 import engine
 
-    e = engine.Engine.from_state(st, form)
-    e.set_option(engine.OPT_FLOOR_FRICTION, floor)
-    dt = st.dt_max
-    tune_res = e.autotune(steps=2, dt=dt, contact=bool(contact)) if (tune and not args.no_autotune) else None
-    e.advance(args.warmup, dt, contact)
+    if pk is None:
+        return engine.Engine.from_state(sts[0], form)
+    e = engine.Engine(None, None, form, grids=pk.grids)
+    e.upload_state(pk.state)
+    return e
+
+
+def apply_tune(e, tune):
+    from code_mpm_gb300 import engine
+
+    if tune:
+        e.set_option(engine.OPT_P2G_REDUCE, tune["p2g_reduce"])
+        e.set_option(engine.OPT_P2G_BLOCK, tune["p2g_block"])
+        e.set_option(engine.OPT_PASS_BLOCK, tune["pass_block"])
+
+
+def timed(e, steps, warmup, dt, contact, dist):
+    """Warm up and time `steps` steps of engine e (CUDA events on its stream); (ms, launches, clocks)."""
+    e.advance(warmup, dt, contact)
     e.synchronize()
     dist.barrier()
     clocks = Clocks(dist.local)
     clocks.start()
     time.sleep(0.25)
     l0 = e.launch_count()
-    ms = e.advance_timed(args.steps, dt, contact)
+    ms = e.advance_timed(steps, dt, contact)
     launches = e.launch_count() - l0
     rec = clocks.stop()
     dist.barrier()
-    return e, dist.max(ms), launches, rec, tune_res
+    return dist.max(ms), launches, rec
 
 
-def run_gb300(args, dist: Dist):
-    from code_mpm_gb300 import build, engine, metrics
+def plain_per_specimen(sts, args, dist, contact, floor, steps):
+    """The plain FP64 form run the reference's way: one engine per specimen, launched one after the other."""
+    from code_mpm_gb300 import engine
 
-    if dist.rank == 0 or not os.path.exists(build.LIB):
-        build.build()
+    big = max(range(len(sts)), key=lambda i: sts[i].n_particles)
+    with engine.Engine.from_state(sts[big], engine.FORM_FP64) as e:
+        e.set_option(engine.OPT_FLOOR_FRICTION, floor)
+        tune = None if args.no_autotune else e.autotune(steps=2, dt=sts[big].dt_max, contact=bool(contact))
     dist.barrier()
-    st, cfg = workload(args.block)
-    contact, floor = 1, 1
-    n = st.n_particles
-    dt = st.dt_max
-    chosen_form = engine.FORM_FP64 if args.form == "fp64" else engine.FORM_FP32
+    clocks = Clocks(dist.local)
+    clocks.start()
+    ms, launches, n_upd = 0.0, 0, 0
+    for st in sts:
+        with engine.Engine.from_state(st, engine.FORM_FP64) as e:
+            e.set_option(engine.OPT_FLOOR_FRICTION, floor)
+            apply_tune(e, tune)
+            e.advance(min(args.warmup, 3), st.dt_max, contact)
+            l0 = e.launch_count()
+            ms += e.advance_timed(steps, st.dt_max, contact)
+            launches += e.launch_count() - l0
+            n_upd += st.n_particles * steps
+    rec = clocks.stop()
+    ms = dist.max(ms)
+    return {"value": n_upd * dist.world / (ms / 1e3), "ms_per_step": ms / steps, "steps": steps, "dtype": "f64",
+            "gpu_launches": launches, "clocks": rec, "autotune": tune,
+            "how": f"one FP64 engine per specimen, {steps} timed steps each after warm-up, device times summed "
+                   "over specimens (engine creation and upload excluded); launch shapes autotuned on the "
+                   "largest specimen"}
 
-    # plain FP64 form: the reference method on the GPU (parity-pinned to the oracle)
-    plain = None
-    plain_state = None
-    if chosen_form != engine.FORM_FP64 and not args.no_plain:
-        ep, ms_p, launches_p, clocks_p, tune_p = timed_form(st, engine.FORM_FP64, args, dist, contact, floor)
-        plain_state = ep.download_state(st)
-        ep.close()
-        plain = {"value": n * args.steps * dist.world / (ms_p / 1e3), "ms_per_step": ms_p / args.steps,
-                 "dtype": "f64", "gpu_launches": launches_p, "clocks": clocks_p, "autotune": tune_p}
 
-    e, ms, launches, clocks_rec, tune = timed_form(st, chosen_form, args, dist, contact, floor)
-    value = n * args.steps * dist.world / (ms / 1e3)
-    accuracy = None
-    if plain_state is not None:
-        err = metrics.form_errors(e.download_state(st), plain_state)
-        accuracy = dict(err, steps=args.warmup + args.steps,
-                        versus="plain FP64 GPU form after the same steps (itself within 1e-9 of the FP64 oracle)",
-                        bars={"vm_stress_rel": 1e-2, "strain_energy_rel": 5e-3})
+ACC_FIELDS = {"pos": 3, "vel": 3, "stress": 6, "e_strain": 1, "e_plastic": 1}
 
-    # per-kernel device times (CUDA events on the engine's stream), separate pass
-    kprof = min(args.steps, 30)
+
+def download_fields(e, n, names=ACC_FIELDS):
+    import numpy as np
+
+    out = {k: np.empty((n, c) if c > 1 else (n,), dtype=np.float64) for k, c in names.items()}
+    e.download_particles(out)
+    return out
+
+
+def perturbed(st, rel, seed=1):
+    """A copy of st with every particle position scaled by 1 + U(-rel, rel)."""
+    import numpy as np
+
+    s = st.copy()
+    rng = np.random.Generator(np.random.PCG64(seed))
+    s["pos"][:] *= 1.0 + rng.uniform(-rel, rel, size=s["pos"].shape)
+    return s
+
+
+def accuracy_vs_plain(sts, pk, idx, chosen, steps, contact, floor, tune_plain):
+    """Chosen-form errors against the plain FP64 form run alone on specimens idx for the same steps, and the
+    conditioning floor: the plain FP64 form against itself with positions perturbed by 1e-7 relative (the size
+    of an FP32 rounding)."""
+    from code_mpm_gb300 import engine, metrics
+
+    def plain_run(st):
+        with engine.Engine.from_state(st, engine.FORM_FP64) as e:
+            e.set_option(engine.OPT_FLOOR_FRICTION, floor)
+            apply_tune(e, tune_plain)
+            e.advance(steps, st.dt_max, contact)
+            return download_fields(e, st.n_particles)
+
+    per, floor_per = [], []
+    for i in idx:
+        st = sts[i]
+        ref = plain_run(st)
+        lo, hi = (0, st.n_particles) if pk is None else (int(pk.particle_offsets[i]), int(pk.particle_offsets[i + 1]))
+        err = metrics.form_errors({k: v[lo:hi] for k, v in chosen.items()}, ref)
+        per.append(dict(err, specimen=int(i), n_particles=int(st.n_particles)))
+        floor_per.append(dict(metrics.form_errors(plain_run(perturbed(st, 1e-7)), ref), specimen=int(i)))
+    keys = ("vm_stress_rel_l2", "vm_stress_rel", "strain_energy_rel", "plastic_energy_rel", "pos_abs_max",
+            "vel_rel")
+    worst = {k: max(p[k] for p in per) for k in keys}
+    bars = {"vm_stress_rel_l2": 1e-2, "strain_energy_rel": 5e-3}
+    return dict(worst, steps=steps, specimens=per, bars=bars, within_bars=all(worst[k] <= v for k, v in bars.items()),
+                conditioning_floor={k: max(p[k] for p in floor_per) for k in keys},
+                versus="plain FP64 GPU form (itself within 1e-9 of the FP64 oracle) run alone on each listed "
+                       "specimen for the same steps; worst over the listed specimens.  conditioning_floor: the "
+                       "plain FP64 form against itself with positions perturbed by 1e-7 relative")
+
+
+def kernel_table(e, steps, dt, contact):
+    from code_mpm_gb300 import engine
+
     e.set_option(engine.OPT_PROFILE, 1)
     e.profile_reset()
-    e.advance(kprof, dt, contact)
+    e.advance(steps, dt, contact)
     prof = e.profile()
     e.set_option(engine.OPT_PROFILE, 0)
     total = sum(v["ms"] for v in prof.values())
     kernels = {k: {"launches": v["launches"], "avg_us": 1e3 * v["ms"] / max(1, v["launches"]),
                    "share": v["ms"] / total if total else 0.0} for k, v in prof.items()}
-    top = max(prof.items(), key=lambda kv: kv[1]["ms"])[0]
+    return prof, kernels
+
+
+def active_nodes(e, n_nodes):
+    import numpy as np
+
+    from code_mpm_gb300 import engine
+
+    state = np.zeros(n_nodes, dtype=np.uint8)
+    nd = engine.Nodes(state=state.ctypes.data)
+    e._check(e._L.mpm_download_nodes(e._h, engine.C.byref(nd)))
+    return int(np.count_nonzero(state & 1))
+
+
+def roofline_of(prof, formkey, n, n_active, workload_name):
     hbm, peak_kind = peaks()
-    formkey = "fp64" if chosen_form == engine.FORM_FP64 else "fp32"
-    alg = ALG_BYTES[formkey]
+    alg, galg = ALG_BYTES[formkey], ALG_GRID_BYTES[formkey]
+    top = max(prof.items(), key=lambda kv: kv[1]["ms"])[0]
     dom = top if top in alg else max(alg, key=lambda k: prof.get(k, {"ms": 0})["ms"])
-    avg_s = prof[dom]["ms"] / prof[dom]["launches"] / 1e3
-    achieved = alg[dom] * n / avg_s / 1e9
-    traffic = None
-    tfile = os.path.join(ROOT, "profiles", f"traffic_{formkey}.json")
+    tj = {}
+    tfile = os.path.join(ROOT, "profiles", f"traffic_{workload_name}_{formkey}.json")
     if os.path.exists(tfile):
         with open(tfile) as f:
             tj = json.load(f)
-        if dom in tj:
-            traffic = tj[dom]["bytes_per_particle"] * n
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "traffic": traffic, "peak_kind": f"{peak_kind} copy bandwidth",
-                "alg_bytes_per_particle": alg[dom], "top_kernel_by_time": top}
+    per = {}
+    for k in alg:
+        if k not in prof or not prof[k]["launches"]:
+            continue
+        avg_s = prof[k]["ms"] / prof[k]["launches"] / 1e3
+        bytes_ = alg[k] * n + galg[k] * n_active
+        per[k] = {"achieved": bytes_ / avg_s / 1e9, "frac": bytes_ / avg_s / 1e9 / hbm, "avg_us": avg_s * 1e6,
+                  "alg_bytes": bytes_,
+                  "traffic": tj[k]["bytes_per_particle"] * n if k in tj else None}
+    d = per[dom]
+    return {"bound": "hbm", "kernel": dom, "achieved": d["achieved"], "peak": hbm, "unit": "GB/s",
+            "frac": d["frac"], "traffic": d["traffic"], "peak_kind": f"{peak_kind} copy bandwidth",
+            "alg_bytes_per_launch": d["alg_bytes"],
+            "alg_bytes_formula": f"{alg[dom]} B x particles + {galg[dom]} B x active nodes",
+            "n_active_nodes": n_active, "top_kernel_by_time": top, "per_kernel": per}
 
-    # end to end through the C ABI with host buffers: H2D of the particle state,
-    # K steps, D2H of the particle state, on one stream, timed with CUDA events.
+
+def e2e_leg(e, pk, sts, n, k_e2e, dt, contact, dist):
+    """The drop-in call with host buffers: H2D of the full particle state from pinned memory, k steps, D2H of the
+    full particle state, on one stream, timed with CUDA events."""
+    import torch
+
+    src = pk.state if pk is not None else sts[0]
+    fields = {"pos": 3, "vel": 3, "fext": 3, "mass": 1, "vol": 1, "vol0": 1, "F": 9, "stress": 6, "strain": 6,
+              "eps_p": 6, "e_strain": 1, "e_strain_max": 1, "e_strain_ti": 1, "e_plastic": 1, "backstress": 1,
+              "mp_mass_gradient": 3, "strain_rate": 6}
+    host = {}
+    for k, c in fields.items():
+        t = torch.empty((n, c) if c > 1 else (n,), dtype=torch.float64, pin_memory=True)
+        t.numpy()[...] = src[k]
+        host[k] = t
+    for k, dt_ in (("material", torch.int32), ("pflags", torch.uint8), ("dc_mult", torch.float32)):
+        t = torch.empty((n,), dtype=dt_, pin_memory=True)
+        t.numpy()[...] = src[k]
+        host[k] = t
+    views = {k: v.numpy() for k, v in host.items()}
+    if pk is not None:
+        t = torch.empty((n,), dtype=torch.int32, pin_memory=True)
+        t.numpy()[...] = pk.state["specimen"]
+        host["specimen"] = t
+        views["specimen"] = t.numpy()
+    stream = torch.cuda.Stream()
+    e.set_stream(stream.cuda_stream)
+    h2d = sum(v.nbytes for v in views.values())
+    outs = {k: views[k] for k in fields}
+    d2h = sum(v.nbytes for v in outs.values())
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    e.upload_particles(views, n)
+    e.advance(k_e2e, dt, contact)
+    e.download_particles(outs)
+    ev1.record(stream)
+    ev1.synchronize()
+    ms = dist.max(ev0.elapsed_time(ev1))
+    return {"value": n * k_e2e * dist.world / (ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d / k_e2e,
+            "d2h_bytes_per_step": d2h / k_e2e, "steps_per_call": k_e2e,
+            "how": "one drop-in call: H2D of the full particle state from pinned host memory, "
+                   f"{k_e2e} steps, D2H of the full particle state; CUDA events on the call's stream"}
+
+
+def run_gb300(args, dist: Dist):
+    from code_mpm_gb300 import batch, build, engine
+
+    if dist.rank == 0 or not os.path.exists(build.LIB):
+        build.build()
+    dist.barrier()
+    sts, cfg = workload(args)
+    pk = batch.pack(sts) if len(sts) > 1 else None
+    contact, floor = 1, 1
+    n = sum(st.n_particles for st in sts)
+    n_nodes = sum(st.n_nodes for st in sts)
+    dt = sts[0].dt_max
+    chosen_form = engine.FORM_FP64 if args.form == "fp64" else engine.FORM_FP32
+    formkey = "fp64" if chosen_form == engine.FORM_FP64 else "fp32"
+    compare = chosen_form != engine.FORM_FP64 and not args.no_plain
+
+    # plain FP64 form: the reference method on the GPU (parity-pinned to the oracle)
+    plain, plain_batched = None, None
+    if compare and pk is not None:
+        plain = plain_per_specimen(sts, args, dist, contact, floor, steps=max(1, min(args.steps, 20)))
+        with make_engine(sts, pk, engine.FORM_FP64) as ep:
+            ep.set_option(engine.OPT_FLOOR_FRICTION, floor)
+            tune_b = None if args.no_autotune else ep.autotune(steps=2, dt=dt, contact=bool(contact))
+            kb = max(1, min(args.steps, 20))
+            ms_b, launches_b, clocks_b = timed(ep, kb, args.warmup, dt, contact, dist)
+        plain_batched = {"value": n * kb * dist.world / (ms_b / 1e3), "ms_per_step": ms_b / kb, "steps": kb,
+                         "dtype": "f64", "gpu_launches": launches_b, "clocks": clocks_b, "autotune": tune_b,
+                         "how": "the plain FP64 form with every specimen in one engine"}
+
+    e = make_engine(sts, pk, chosen_form)
+    e.set_option(engine.OPT_FLOOR_FRICTION, floor)
+    tune = None if args.no_autotune else e.autotune(steps=2, dt=dt, contact=bool(contact))
+    ms, launches, clocks_rec = timed(e, args.steps, args.warmup, dt, contact, dist)
+    value = n * args.steps * dist.world / (ms / 1e3)
+
+    accuracy = None
+    if compare:
+        chosen_out = download_fields(e, n)
+        idx = subset(sts, 8)
+        tune_plain = plain["autotune"] if plain else None
+        accuracy = accuracy_vs_plain(sts, pk, idx, chosen_out, args.warmup + args.steps, contact, floor, tune_plain)
+        del chosen_out
+        if pk is None:  # single specimen: the plain form timed on the same state
+            with make_engine(sts, pk, engine.FORM_FP64) as ep:
+                ep.set_option(engine.OPT_FLOOR_FRICTION, floor)
+                tune_p = None if args.no_autotune else ep.autotune(steps=2, dt=dt, contact=bool(contact))
+                ms_p, launches_p, clocks_p = timed(ep, args.steps, args.warmup, dt, contact, dist)
+            plain = {"value": n * args.steps * dist.world / (ms_p / 1e3), "ms_per_step": ms_p / args.steps,
+                     "steps": args.steps, "dtype": "f64", "gpu_launches": launches_p, "clocks": clocks_p,
+                     "autotune": tune_p}
+
+    prof, kernels = kernel_table(e, min(args.steps, 30), dt, contact)
+    n_active = active_nodes(e, n_nodes)
+    roofline = roofline_of(prof, formkey, n, n_active, args.workload)
+
     e2e = None
-    try:
-        if args.no_e2e:
-            raise RuntimeError("skipped (--no-e2e)")
-        import torch
-
-        fields = {"pos": 3, "vel": 3, "fext": 3, "mass": 1, "vol": 1, "vol0": 1, "F": 9, "stress": 6, "strain": 6,
-                  "eps_p": 6, "e_strain": 1, "e_strain_max": 1, "e_strain_ti": 1, "e_plastic": 1, "backstress": 1,
-                  "mp_mass_gradient": 3, "strain_rate": 6}
-        host = {}
-        for k, c in fields.items():
-            t = torch.empty((n, c) if c > 1 else (n,), dtype=torch.float64, pin_memory=True)
-            a = t.numpy()
-            a[...] = st[k]
-            host[k] = (t, a)
-        for k, dt_ in (("material", torch.int32), ("pflags", torch.uint8), ("dc_mult", torch.float32)):
-            t = torch.empty((n,), dtype=dt_, pin_memory=True)
-            a = t.numpy()
-            a[...] = st[k]
-            host[k] = (t, a)
-        stream = torch.cuda.Stream()
-        e.set_stream(stream.cuda_stream)
-        k_e2e = max(1, min(args.steps, 50))
-        views = {k: v[1] for k, v in host.items()}
-        h2d = sum(v.nbytes for v in views.values())
-        d2h = sum(views[k].nbytes for k in fields)
-        outs = {k: views[k] for k in fields}
-        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        ev0.record(stream)
-        e.upload_particles(views, n)
-        e.advance(k_e2e, dt, contact)
-        e.download_particles(outs)
-        ev1.record(stream)
-        ev1.synchronize()
-        e2e_ms = dist.max(ev0.elapsed_time(ev1))
-        e2e = {"value": n * k_e2e * dist.world / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d / k_e2e,
-               "d2h_bytes_per_step": d2h / k_e2e, "steps_per_call": k_e2e,
-               "how": "one drop-in call: H2D of the full particle state from pinned host memory, "
-                      f"{k_e2e} steps, D2H of the full particle state; CUDA events on the call's stream"}
-    except Exception as ex:  # reported, not hidden
+    if args.no_e2e:
         e2e = {"value": None, "unit": UNIT, "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
-               "error": f"{type(ex).__name__}: {ex}"}
+               "error": "skipped (--no-e2e)"}
+    else:
+        try:
+            e2e = e2e_leg(e, pk, sts, n, max(1, min(args.steps, 50)), dt, contact, dist)
+        except Exception as ex:  # reported, not hidden
+            e2e = {"value": None, "unit": UNIT, "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
+                   "error": f"{type(ex).__name__}: {ex}"}
     e.close()
 
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if formkey == "fp64" else "f32+f64",
-           "data": "synthetic (seeded scene generator, reference scene conventions)",
+           "data": "synthetic (seeded scene generators)",
            "config": dict(cfg, form=("plain FP64" if formkey == "fp64" else "chosen: FP32 transfers/grid, FP64 "
-                                     "positions and energies"), parallelism=f"replicas x{dist.world}"),
+                                     "positions and energies, batched, autotuned"),
+                          parallelism=f"replicas x{dist.world}"),
            "clocks": clocks_rec, "gpu_launches": launches, "autotune": tune, "roofline": roofline,
            "kernels": kernels, "e2e": e2e}
     if plain is not None:
         out["plain_fp64"] = plain
         out["chosen_over_plain"] = value / plain["value"]
+    if plain_batched is not None:
+        out["plain_fp64_batched"] = plain_batched
+        out["chosen_over_plain_batched"] = value / plain_batched["value"]
+    if accuracy is not None:
         out["accuracy"] = accuracy
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(st, contact, floor)
+        out["cpu_baseline"] = cpu_baseline(sts, contact, floor)
     return out
 
 
 def run_reference(args, dist: Dist):
-    """The reference's CPU implementation of the path (the restatement of it), all host threads."""
+    """The reference's CPU implementation of the path (the restatement of it), all host threads, on a bounded
+    sample of the workload: the same specimens every step, steps capped to about two minutes."""
     if dist.rank != 0:
         return None
+    sts, cfg = workload(args)
+    idx = subset(sts, 16)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
 
     pyoracle.build()
-    st, cfg = workload(args.block)
     threads = os.cpu_count() or 1
-    s = st.copy()
-    # bounded: warm-up and timed steps on the full workload, at most ~a few minutes in total
-    w = min(args.warmup, 1)
-    pyoracle.advance(s, w, 1, floor_friction=1, threads=threads, omp=True)
-    one = pyoracle.advance(s, 1, 1, floor_friction=1, threads=threads, omp=True)
+    work = [sts[i].copy() for i in idx]
+    n = sum(s.n_particles for s in work)
+
+    def step():
+        return sum(pyoracle.advance(s, 1, 1, floor_friction=1, threads=threads, omp=True) for s in work)
+
+    w = max(1, min(args.warmup, 1))
+    for _ in range(w):
+        step()
+    one = step()
     k = max(1, min(args.steps, int(120.0 / max(one, 1e-3))))
-    secs = pyoracle.advance(s, k, 1, floor_friction=1, threads=threads, omp=True)
-    rate = st.n_particles * k / secs
-    sample = (f"{k} timed steps (+{w + 1} warm-up) of the full workload ({st.n_particles} particles); "
-              f"CPU restatement of the reference path, OpenMP with per-node locks, {threads} threads")
+    secs = sum(step() for _ in range(k))
+    rate = n * k / secs
+    sample = (f"{k} timed steps (+{w + 1} warm-up) of {len(idx)} of the {len(sts)} specimens ({n} particles, "
+              f"spread over the size range); CPU restatement of the reference path, OpenMP with per-node locks, "
+              f"{threads} threads")
     return {"metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": dist.world, "steps": k, "warmup": w + 1,
             "ms_per_step": 1e3 * secs / k, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic (seeded scene generator)", "config": dict(cfg, form="reference-cpu"),
+            "dtype": "f64", "data": "synthetic (seeded scene generators)", "config": dict(cfg, form="reference-cpu"),
             "impl": "reference",
             "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

@@ -256,6 +256,11 @@ int prof_resolve(mpm_ctx* c) {
         Launch l_(c, name);                                                \
         kernel<<<(grid), (block), 0, c->stream>>>(__VA_ARGS__);            \
     } while (0)
+#define LAUNCH_SMEM(name, kernel, grid, block, smem, ...)                  \
+    do {                                                                   \
+        Launch l_(c, name);                                                \
+        kernel<<<(grid), (block), (smem), c->stream>>>(__VA_ARGS__);       \
+    } while (0)
 
 // ---- host-side timeline (TimeLine::getVelocity, TimeLine.h:33-46) ----------
 void timeline_velocity(const mpm_ctx* c, double t, double out[3]) {
@@ -477,7 +482,10 @@ int step_impl(mpm_ctx* c, double dt, int contact) {
         // FP32 form: the contact mass gradient is accumulated by P2G itself
         // (the bit-exact ordered gather below serves the FP64 form).
         const int mg_in_p2g = (contact && c->form == MPM_FORM_FP32) ? 1 : 0;
-        if (c->p2g_reduce)
+        if (c->p2g_reduce == 2)
+            LAUNCH_SMEM("p2g", k_p2g_cells<T>, blocks_for(n, c->p2g_block), c->p2g_block,
+                        p2g_cells_smem<T>(c->p2g_block), P, N, g, skeys, perm, n, mg_in_p2g);
+        else if (c->p2g_reduce == 1)
             LAUNCH("p2g", (k_p2g<T, 1>), blocks_for(n, c->p2g_block), c->p2g_block, P, N, g, skeys, perm, n,
                    mg_in_p2g);
         else
@@ -641,6 +649,15 @@ int mpm_create_batch(const mpm_grid_desc* grids, int32_t nspec, int form, mpm_ct
     cudaGetDevice(&c->device);
     cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
     if (c->sm_count <= 0) c->sm_count = 152;
+    // cell-centric P2G stages up to 512 slots in shared memory (109 KB in FP64)
+    if (cudaFuncSetAttribute(k_p2g_cells<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)p2g_cells_smem<double>(512)) != cudaSuccess ||
+        cudaFuncSetAttribute(k_p2g_cells<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)p2g_cells_smem<float>(512)) != cudaSuccess) {
+        cudaGetLastError();
+        delete c;
+        return MPM_ERR_DEVICE;
+    }
     // per-specimen geometry, nodes and cell keys numbered one specimen after the other
     std::vector<double> tab;
     c->geoms.resize(nspec);
@@ -762,7 +779,10 @@ int mpm_set_option(mpm_ctx* c, int key, double value) {
     switch (key) {
         case MPM_OPT_FLOOR_FRICTION: c->floor_friction = value != 0.0; return MPM_OK;
         case MPM_OPT_PROFILE: c->profile = value != 0.0; return MPM_OK;
-        case MPM_OPT_P2G_REDUCE: c->p2g_reduce = value != 0.0; return MPM_OK;
+        case MPM_OPT_P2G_REDUCE:
+            if (value != 0.0 && value != 1.0 && value != 2.0) return fail(c, MPM_ERR_ARG, "P2G mode must be 0, 1 or 2");
+            c->p2g_reduce = (int)value;
+            return MPM_OK;
         case MPM_OPT_P2G_BLOCK:
         case MPM_OPT_PASS_BLOCK: {
             int b = (int)value;
@@ -1208,7 +1228,7 @@ int mpm_autotune(mpm_ctx* c, int32_t steps, double dt, int contact, mpm_tune_res
     CK(cudaEventCreate(&a));
     CK(cudaEventCreate(&b));
     const int blocks[3] = {128, 256, 512};
-    for (int red = 0; red < 2 && rc == MPM_OK; ++red)
+    for (int red = 0; red < 3 && rc == MPM_OK; ++red)
         for (int pb = 0; pb < 3 && rc == MPM_OK; ++pb)
             for (int qb = 0; qb < 3 && rc == MPM_OK; ++qb) {
                 c->p2g_reduce = red;

@@ -240,6 +240,141 @@ __global__ void __launch_bounds__(512) k_p2g(PView<T> P, NView<T> nd, Geom g, co
 }
 
 // ---------------------------------------------------------------------------
+// P2G, cell-centric (P2G_REDUCE = 2).  A block takes blockDim.x consecutive
+// sorted slots.  Phase 1: each slot's thread stages its particle's per-axis
+// bases (N and dN/du for both nodes of each axis) and transfer quantities
+// (m, m v, -V sigma, f_ext) in shared memory.  Phase 2: one thread per
+// (run of equal cell keys, corner) sums that corner's contributions over the
+// run's particles in slot order and issues one atomic per field.  Same
+// per-particle arithmetic as k_p2g; the cross-lane shuffles of REDUCE = 1
+// become shared-memory reads, and the atomics are issued by full warps.
+// Shared memory: (12 + 13) values per slot plus the keys, particle indices
+// and run starts (p2g_cells_smem).
+// ---------------------------------------------------------------------------
+template <typename T>
+__host__ __device__ constexpr size_t p2g_cells_smem(int bs) {
+    return (size_t)25 * bs * sizeof(T) + (size_t)bs * 8 + (size_t)(bs + 1) * 4 + 64 * 4;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(512) k_p2g_cells(PView<T> P, NView<T> nd, Geom g, const unsigned* __restrict__ skeys,
+                                                   const unsigned* __restrict__ perm, long long n, int with_mg) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int bs = blockDim.x, t = threadIdx.x, lane = t & 31, w = t >> 5;
+    T* sw = reinterpret_cast<T*>(smem_raw);        // 12 x bs: Nx0 Nx1 Ny0 Ny1 Nz0 Nz1 gx0 gx1 gy0 gy1 gz0 gz1
+    T* sq = sw + 12 * bs;                          // 13 x bs: m, m v (3), -V sigma (6), f_ext (3)
+    unsigned* skey = reinterpret_cast<unsigned*>(sq + 13 * bs);
+    unsigned* sperm = skey + bs;
+    int* run_start = reinterpret_cast<int*>(sperm + bs);  // bs + 1
+    int* wsum = run_start + bs + 1;                        // 32 warp counts + total
+    const long long s = blockIdx.x * (long long)bs + t;
+    const unsigned key = (s < n) ? skeys[s] : 0xffffffffu;
+    const bool valid = key < g.key_max;
+    const long long np = P.n, nn = nd.nn;
+    if (valid) {
+        const long long p = perm[s];
+        const Geom& gs = spec_geom(g, P.sid, p);
+        int b[3];
+        key_to_base(key, gs, b);
+        Bases<T> B;
+        particle_bases<T>(P, gs, p, b, B);
+        sw[0 * bs + t] = B.Nx[0];
+        sw[1 * bs + t] = B.Nx[1];
+        sw[2 * bs + t] = B.Ny[0];
+        sw[3 * bs + t] = B.Ny[1];
+        sw[4 * bs + t] = B.Nz[0];
+        sw[5 * bs + t] = B.Nz[1];
+        sw[6 * bs + t] = B.gx[0];
+        sw[7 * bs + t] = B.gx[1];
+        sw[8 * bs + t] = B.gy[0];
+        sw[9 * bs + t] = B.gy[1];
+        sw[10 * bs + t] = B.gz[0];
+        sw[11 * bs + t] = B.gz[1];
+        const T m = P.mass[p], V = P.vol[p];
+        sq[t] = m;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            sq[(1 + c) * bs + t] = m * P.vel[c * np + p];
+            sq[(10 + c) * bs + t] = P.fext[c * np + p];
+        }
+#pragma unroll
+        for (int c = 0; c < 6; ++c) sq[(4 + c) * bs + t] = -V * P.stress[c * np + p];
+        sperm[t] = (unsigned)p;
+    }
+    skey[t] = key;
+    __syncthreads();
+    // runs: a valid slot whose key differs from its predecessor's starts one
+    // (invalid keys sort last, so the valid slots are a prefix of the block)
+    const bool head = valid && (t == 0 || skey[t - 1] != key);
+    const unsigned bal = __ballot_sync(FULL_MASK, head);
+    if (lane == 0) wsum[w] = __popc(bal);
+    const int nvalid = __syncthreads_count(valid);
+    if (t < 32) {
+        const int nw = bs >> 5;
+        int v = (t < nw) ? wsum[t] : 0;
+        int incl = v;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            int o = __shfl_up_sync(FULL_MASK, incl, off);
+            if (t >= off) incl += o;
+        }
+        if (t < nw) wsum[t] = incl - v;
+        if (t == 31) wsum[32] = incl;
+    }
+    __syncthreads();
+    if (head) run_start[wsum[w] + __popc(bal & ((1u << lane) - 1u))] = t;
+    const int R = wsum[32];
+    if (t == 0) run_start[R] = nvalid;
+    __syncthreads();
+    for (int item = t; item < R * 8; item += bs) {
+        const int r = item >> 3, k = item & 7;
+        const int ix = (k >> 2) & 1, iy = (k >> 1) & 1, iz = k & 1;
+        const int a = run_start[r], e = run_start[r + 1];
+        T am = 0, ap0 = 0, ap1 = 0, ap2 = 0, af0 = 0, af1 = 0, af2 = 0, g0 = 0, g1 = 0, g2 = 0;
+        for (int i = a; i < e; ++i) {
+            const T nx = sw[ix * bs + i], ny = sw[(2 + iy) * bs + i], nz = sw[(4 + iz) * bs + i];
+            const T N = nx * ny * nz;
+            const T G0 = -(ny * nz) * sw[(6 + ix) * bs + i];
+            const T G1 = -(nx * nz) * sw[(8 + iy) * bs + i];
+            const T G2 = -(nx * ny) * sw[(10 + iz) * bs + i];
+            const T m = sq[i];
+            am += N * m;
+            ap0 += N * sq[1 * bs + i];
+            ap1 += N * sq[2 * bs + i];
+            ap2 += N * sq[3 * bs + i];
+            const T v0 = sq[4 * bs + i], v1 = sq[5 * bs + i], v2 = sq[6 * bs + i];
+            const T v3 = sq[7 * bs + i], v4 = sq[8 * bs + i], v5 = sq[9 * bs + i];
+            af0 += G0 * v0 + G1 * v3 + G2 * v5 + N * sq[10 * bs + i];
+            af1 += G1 * v1 + G0 * v3 + G2 * v4 + N * sq[11 * bs + i];
+            af2 += G2 * v2 + G0 * v5 + G1 * v4 + N * sq[12 * bs + i];
+            if (with_mg) {
+                g0 += G0 * m;
+                g1 += G1 * m;
+                g2 += G2 * m;
+            }
+        }
+        const Geom& gs = spec_geom(g, P.sid, sperm[a]);
+        int b[3];
+        key_to_base(skey[a], gs, b);
+        const long long nid = corner_node(gs, b, k);
+        if (nid >= 0) {
+            atomicAdd(&nd.mass[nid], am);
+            atomicAdd(&nd.mom[nid], ap0);
+            atomicAdd(&nd.mom[nn + nid], ap1);
+            atomicAdd(&nd.mom[2 * nn + nid], ap2);
+            atomicAdd(&nd.force[nid], af0);
+            atomicAdd(&nd.force[nn + nid], af1);
+            atomicAdd(&nd.force[2 * nn + nid], af2);
+            if (with_mg) {
+                atomicAdd(&nd.mg[nid], (double)g0);
+                atomicAdd(&nd.mg[nn + nid], (double)g1);
+                atomicAdd(&nd.mg[2 * nn + nid], (double)g2);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Displacement control (…MPLocks.cpp:143-174; contact :283-297, :416-432).
 // The reference overwrites node velocity/momentum/force from each controlled
 // particle in list order, so a node shared by several keeps the last one's.

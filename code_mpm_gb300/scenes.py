@@ -313,13 +313,31 @@ def honeycomb_batch(n: int = 256, seed: int = 4, total: float = 40.0e6, nmin: in
     4-10 cells per side, particle counts log-uniform in [nmin, nmax] scaled so the batch holds
     about `total` particles, platen speed U(1, 10) m/s per specimen."""
     rng = np.random.Generator(np.random.PCG64(seed))
-    wall = rng.uniform(0.4e-3, 1.2e-3, n)
-    pitch = rng.uniform(4.0e-3, 8.0e-3, n)
-    ncell = rng.integers(4, 11, n)
     counts = np.exp(rng.uniform(np.log(nmin), np.log(nmax), n))
     counts = np.clip(counts * total / counts.sum(), nmin, nmax)
     speed = rng.uniform(1.0, 10.0, n)
-    return [honeycomb(wall[i], pitch[i], int(ncell[i]), int(counts[i]), speed[i], h=h) for i in range(n)]
+    out = []
+    for i in range(n):
+        # A cross-section whose two thinnest extrusion layers already exceed the count cannot meet it: draw the
+        # geometry again (the smallest one, 4 cells of 4 mm with 0.4 mm walls, holds about 6,600 particles).
+        for _ in range(10_000):
+            wall, pitch, ncell = rng.uniform(0.4e-3, 1.2e-3), rng.uniform(4.0e-3, 8.0e-3), int(rng.integers(4, 11))
+            if 2 * honeycomb_layer_count(wall, pitch, ncell, h) <= counts[i]:
+                break
+        else:
+            wall, pitch, ncell = 0.4e-3, 4.0e-3, 4
+        out.append(honeycomb(wall, pitch, ncell, int(counts[i]), speed[i], h=h))
+    return out
+
+
+def honeycomb_layer_count(wall: float, pitch: float, ncell: int, h: float) -> int:
+    """Particles in one y-layer of honeycomb()'s cross-section."""
+    s = 0.5 * h
+    W = ncell * pitch + wall
+    c = (np.arange(int(np.ceil(W / s))) + 0.5) * s
+    m = int((c < W).sum())
+    k = int(((np.mod(c, pitch) < wall) & (c < W)).sum())
+    return m * m - (m - k) * (m - k)
 
 
 def contact_small(seed: int = 2, h: float = 1.0e-3, nb=(6, 5, 4), speed: float = 30.0) -> State:

@@ -70,7 +70,7 @@ extern "C" {
 /* Options for mpm_set_option. */
 #define MPM_OPT_FLOOR_FRICTION 1 /* contact path: Coulomb friction on x/y of z-fixed nodes (extension; default 0) */
 #define MPM_OPT_PROFILE 2        /* 1: time every kernel with CUDA events (default 0) */
-#define MPM_OPT_P2G_REDUCE 3     /* P2G: 1 = sum each cell's run of particles across lanes before the atomics, 0 = one atomic per particle */
+#define MPM_OPT_P2G_REDUCE 3     /* P2G: 0 = one atomic per particle, 1 = sum each cell's run across lanes first, 2 = stage the block in shared memory and sum each (cell, corner) in one thread */
 #define MPM_OPT_P2G_BLOCK 4      /* P2G threads per block (128, 256 or 512) */
 #define MPM_OPT_PASS_BLOCK 5     /* G2P pass-2 threads per block (128, 256 or 512) */
 
