@@ -249,6 +249,7 @@ def apply_tune(e, tune):
         e.set_option(engine.OPT_P2G_REDUCE, tune["p2g_reduce"])
         e.set_option(engine.OPT_P2G_BLOCK, tune["p2g_block"])
         e.set_option(engine.OPT_PASS_BLOCK, tune["pass_block"])
+        e.set_option(engine.OPT_GATHER, tune["gather_batch"])
 
 
 def timed(e, steps, warmup, dt, contact, dist):

@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "fpsplit.h"
+
 namespace mpm {
 
 constexpr unsigned FULL_MASK = 0xffffffffu;
@@ -27,6 +29,9 @@ constexpr unsigned PF_IN_DC = 32u;
 struct Geom {
     double h[3];      // cell size = length/cells (GridPoint_Mediator d3_Length_Cell)
     double inv_h[3];  // RN(1/h)
+    float hf[3];      // RN32(h)
+    float inv_hf[3];  // RN32(inv_h)
+    float ih_lo[3];   // RN32(inv_h - inv_hf): inv_hf + ih_lo is inv_h to 2^-48
     int nn[3];        // nodes per axis = cells + 1
     int kd[3];        // cell-key extents = cells + 2 (base cells -1..cells)
     unsigned key_max; // total key count over all specimens: the key of a particle with no node in range
@@ -38,6 +43,13 @@ struct Geom {
     const struct Geom* tab;  // all specimens (device), or null with one specimen
     int nspec;
 };
+
+// Float images of a specimen's cell size (set on the host after h, inv_h).
+inline void set_float_geometry(Geom& g, int a) {
+    g.hf[a] = (float)g.h[a];
+    g.inv_hf[a] = (float)g.inv_h[a];
+    g.ih_lo[a] = (float)(g.inv_h[a] - (double)g.inv_hf[a]);
+}
 
 // The geometry of particle p's specimen.
 __device__ __forceinline__ const Geom& spec_geom(const Geom& g, const uint16_t* __restrict__ sid, long long p) {
@@ -90,7 +102,34 @@ struct MatConst {
     double k0;     // Y/sqrt(3)
     double s23C1;  // sqrt(2/3)*C1
     double inv_E, nu_over_E, inv_G;
+    // RN32 images of the constants the FP32 form uses
+    float fC, fone_m_nu, fnu, fhalf_m_nu, fk0, fs23C1, fC0, finv_E, fnu_over_E, finv_G;
 };
+
+inline void set_float_constants(MatConst& k) {
+    k.fC = (float)k.C;
+    k.fone_m_nu = (float)k.one_m_nu;
+    k.fnu = (float)k.nu;
+    k.fhalf_m_nu = (float)k.half_m_nu;
+    k.fk0 = (float)k.k0;
+    k.fs23C1 = (float)k.s23C1;
+    k.fC0 = (float)k.C0;
+    k.finv_E = (float)k.inv_E;
+    k.fnu_over_E = (float)k.nu_over_E;
+    k.finv_G = (float)k.inv_G;
+}
+
+// An increment of the form's type as a double (exact in both forms).
+__device__ __forceinline__ double fps_f2d_form(double v) { return v; }
+__device__ __forceinline__ double fps_f2d_form(float v) { return fps_f2d(v); }
+
+// The form's copy of a constant: the double itself, or its float image.
+template <typename T>
+__device__ __forceinline__ T form_const(double d, float f);
+template <>
+__device__ __forceinline__ double form_const<double>(double d, float) { return d; }
+template <>
+__device__ __forceinline__ float form_const<float>(double, float f) { return f; }
 
 // Particle arrays: structure of arrays, component a of particle p at [a*n + p].
 template <typename T>
@@ -110,7 +149,7 @@ struct PView {
     double* e_strain_ti;
     double* e_plastic;
     T* backstress;
-    double* mp_mg;
+    T* mp_mg;  // particle mass gradient (contact path), the form's type
     T* strain_rate;
     int32_t* material;
     uint8_t* pflags;
@@ -128,11 +167,12 @@ struct NView {
     T* vel;
     T* force;
     T* ftemp;
-    double* mg;        // mass gradient (contact path)
+    T* mg;             // mass gradient (contact path), the form's type
     unsigned* state;   // MPM_NS_* bits
     uint8_t* fixed;
     double* friction;
-    T* ratio;          // scratch: f/m before pass 1, p/m before pass 2
+    T* rec;            // scratch: per node 8 values {r, has, v, 0}: r = f/m before pass 1, p/m before
+                       // pass 2; has = 1 when m > mass_min; v = node velocity (pass 2 only)
     T* q;              // scratch: remap accumulator sum N m_p v_p
     unsigned* owner;   // scratch: displacement-control last-writer claims, 3 x nn
     unsigned* nowner;  // scratch: contact-normal last-writer claims, nn
@@ -140,6 +180,17 @@ struct NView {
     const unsigned* acount;  // their number (device)
     long long nn;
 };
+
+// Four values loaded or stored as one aligned vector.
+template <typename T>
+struct alignas(4 * sizeof(T)) Quad {
+    T x, y, z, w;
+};
+
+template <typename T>
+__device__ __forceinline__ Quad<T> ld_quad(const T* __restrict__ p) {
+    return *reinterpret_cast<const Quad<T>*>(p);
+}
 
 // The nodes a node kernel works on, grid-stride: the active-node list when
 // one is given, else every node.  The body may `continue`, not `return`.

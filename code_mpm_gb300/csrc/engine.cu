@@ -49,7 +49,7 @@ struct mpm_ctx {
     // options
     int floor_friction = 0;
     int profile = 0;
-    int p2g_reduce = 1, p2g_block = 256, pass_block = 256;
+    int p2g_reduce = 2, p2g_block = 128, pass_block = 128, gather_batch = 0;
     // simulation scalars
     mpm_sim sim{0.0, 1.0e-3, 0.0, 0.0, 10.0, 0};
     // counts
@@ -156,7 +156,7 @@ PView<T> pview(mpm_ctx* c) {
     v.e_strain_ti = (double*)c->e_strain_ti.p;
     v.e_plastic = (double*)c->e_plastic.p;
     v.backstress = (T*)c->backstress.p;
-    v.mp_mg = (double*)c->mp_mg.p;
+    v.mp_mg = (T*)c->mp_mg.p;
     v.strain_rate = (T*)c->strain_rate.p;
     v.material = (int32_t*)c->material.p;
     v.pflags = (uint8_t*)c->pflags.p;
@@ -175,11 +175,11 @@ NView<T> nview(mpm_ctx* c) {
     v.vel = (T*)c->g_vel.p;
     v.force = (T*)c->g_force.p;
     v.ftemp = (T*)c->g_ftemp.p;
-    v.mg = (double*)c->g_mg.p;
+    v.mg = (T*)c->g_mg.p;
     v.state = (unsigned*)c->g_state.p;
     v.fixed = (uint8_t*)c->g_fixed.p;
     v.friction = (double*)c->g_friction.p;
-    v.ratio = (T*)c->g_ratio.p;
+    v.rec = (T*)c->g_ratio.p;
     v.q = (T*)c->g_q.p;
     v.owner = (unsigned*)c->g_owner.p;
     v.nowner = (unsigned*)c->g_nowner.p;
@@ -340,17 +340,37 @@ __global__ void k_compact_flag(const uint8_t* __restrict__ pflags, long long n, 
     base = __shfl_sync(m, base, leader);
     if (take) list[base + __popc(m & ((1u << lane) - 1u))] = (unsigned)i;
 }
-__global__ void k_compact_state(const unsigned* __restrict__ state, long long n, unsigned bit,
-                                unsigned* __restrict__ list, unsigned* __restrict__ count) {
-    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    bool take = i < n && (state[i] & bit);
-    unsigned m = __ballot_sync(0xffffffffu, take);
-    if (!m) return;
-    int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
-    unsigned base = 0;
-    if (lane == leader) base = atomicAdd(count, (unsigned)__popc(m));
-    base = __shfl_sync(m, base, leader);
-    if (take) list[base + __popc(m & ((1u << lane) - 1u))] = (unsigned)i;
+// Active-node list: a block of CS_THREADS compacts a tile of CS_THREADS x
+// CS_ROUNDS consecutive nodes into shared memory in node order, then
+// reserves its range with one atomic (a counter shared by every warp would
+// serialise tens of thousands of atomics at one L2 address).
+constexpr int CS_THREADS = 256, CS_ROUNDS = 16;
+__global__ void __launch_bounds__(CS_THREADS) k_compact_state(const unsigned* __restrict__ state, long long n,
+                                                              unsigned bit, unsigned* __restrict__ list,
+                                                              unsigned* __restrict__ count) {
+    __shared__ unsigned buf[CS_THREADS * CS_ROUNDS];
+    __shared__ unsigned wcnt[CS_THREADS / 32];
+    __shared__ unsigned total, base;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const long long tile = blockIdx.x * (long long)(CS_THREADS * CS_ROUNDS);
+    if (t == 0) total = 0;
+    __syncthreads();
+    for (int r = 0; r < CS_ROUNDS; ++r) {
+        const long long i = tile + (long long)r * CS_THREADS + t;
+        const bool take = i < n && (state[i] & bit);
+        const unsigned m = __ballot_sync(0xffffffffu, take);
+        if (lane == 0) wcnt[w] = __popc(m);
+        __syncthreads();
+        unsigned off = total;
+        for (int k = 0; k < w; ++k) off += wcnt[k];
+        if (take) buf[off + __popc(m & ((1u << lane) - 1u))] = (unsigned)i;
+        __syncthreads();
+        if (t == CS_THREADS - 1) total = off + __popc(m);
+        __syncthreads();
+    }
+    if (t == 0) base = total ? atomicAdd(count, total) : 0u;
+    __syncthreads();
+    for (unsigned k = t; k < total; k += CS_THREADS) list[base + k] = buf[k];
 }
 __global__ void k_clear_flag(uint8_t* __restrict__ pflags, long long n, uint8_t bits) {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -475,8 +495,8 @@ int step_impl(mpm_ctx* c, double dt, int contact) {
         LAUNCH("cell_ranges", k_cell_ranges, blocks_for(n), NTHREADS, skeys, n, g, N.state,
                contact ? (unsigned*)c->cstart.p : nullptr, contact ? (unsigned*)c->cend.p : nullptr, perm, P.sid);
         CK(cudaMemsetAsync(c->acount.p, 0, 4, c->stream));
-        LAUNCH("active_list", k_compact_state, blocks_for(nn), NTHREADS, (const unsigned*)N.state, nn, 1u,
-               (unsigned*)c->alist.p, (unsigned*)c->acount.p);
+        LAUNCH("active_list", k_compact_state, (unsigned)((nn + CS_THREADS * CS_ROUNDS - 1) / (CS_THREADS * CS_ROUNDS)),
+               CS_THREADS, (const unsigned*)N.state, nn, 1u, (unsigned*)c->alist.p, (unsigned*)c->acount.p);
         N.alist = (const unsigned*)c->alist.p;
         c->have_alist = true;
         // FP32 form: the contact mass gradient is accumulated by P2G itself
@@ -529,11 +549,16 @@ int step_impl(mpm_ctx* c, double dt, int contact) {
         if (contact && c->ndc > 0)
             LAUNCH("dc_apply", k_dc_apply<T>, blocks_for(c->ndc), NTHREADS, (const unsigned*)c->dclist.p, c->ndc,
                    keys, P, N, g, contact);
-        LAUNCH("node_ratio", k_node_ratio<T>, nodeblocks, NTHREADS, N, (const T*)c->g_force.p, c->sim.mass_min,
-               1);
-        LAUNCH("pass1_remap", k_pass1_remap<T>, blocks_for(n), NTHREADS, P, N, g, skeys, perm, n, (T)dt,
-               c->sim.mass_min, contact);
-        LAUNCH("node_remap", k_node_remap<T>, nodeblocks, NTHREADS, N, c->sim.mass_min);
+        // the mass threshold in the form's type (FP32: rounded down, so float masses compare exactly)
+        const T mm = sizeof(T) == 4 ? (T)fps_float_threshold(c->sim.mass_min) : (T)c->sim.mass_min;
+        LAUNCH("node_ratio", k_node_ratio<T>, nodeblocks, NTHREADS, N, (const T*)c->g_force.p, mm, 1, 0);
+        if (c->gather_batch)
+            LAUNCH("pass1_remap", (k_pass1_remap<T, 1>), blocks_for(n), NTHREADS, P, N, g, skeys, perm, n, (T)dt, mm,
+                   contact);
+        else
+            LAUNCH("pass1_remap", (k_pass1_remap<T, 0>), blocks_for(n), NTHREADS, P, N, g, skeys, perm, n, (T)dt, mm,
+                   contact);
+        LAUNCH("node_remap", k_node_remap<T>, nodeblocks, NTHREADS, N, mm);
         if (!contact) {
             if (c->ndc > 0)
                 LAUNCH("dc_apply", k_dc_apply<T>, blocks_for(c->ndc), NTHREADS, (const unsigned*)c->dclist.p,
@@ -545,15 +570,21 @@ int step_impl(mpm_ctx* c, double dt, int contact) {
                 LAUNCH("dc_apply", k_dc_apply<T>, blocks_for(c->ndc), NTHREADS, (const unsigned*)c->dclist.p,
                        c->ndc, keys, P, N, g, contact);
         }
-        LAUNCH("node_ratio", k_node_ratio<T>, nodeblocks, NTHREADS, N, (const T*)c->g_mom.p, c->sim.mass_min, 0);
+        LAUNCH("node_ratio", k_node_ratio<T>, nodeblocks, NTHREADS, N, (const T*)c->g_mom.p, mm, 0, 1);
         StepArgs a;
         a.dt = dt;
         a.mass_min = c->sim.mass_min;
+        a.dt_f = (float)dt;
+        a.mass_min_f = fps_float_threshold(c->sim.mass_min);
         timeline_velocity(c, c->sim.time, a.tv);
         a.has_timeline = c->tl_t.empty() ? 0 : 1;
         a.contact = contact;
-        LAUNCH("pass2", k_pass2<T>, blocks_for(n, c->pass_block), c->pass_block, P, N, g,
-               (unsigned*)c->keys_copy.p, keys_next, (const MatConst*)c->mats.p, c->nmat, a, err);
+        if (c->gather_batch)
+            LAUNCH("pass2", (k_pass2<T, 1>), blocks_for(n, c->pass_block), c->pass_block, P, N, g,
+                   (unsigned*)c->keys_copy.p, keys_next, (const MatConst*)c->mats.p, c->nmat, a, err);
+        else
+            LAUNCH("pass2", (k_pass2<T, 0>), blocks_for(n, c->pass_block), c->pass_block, P, N, g,
+                   (unsigned*)c->keys_copy.p, keys_next, (const MatConst*)c->mats.p, c->nmat, a, err);
         c->keys_valid = true;
     }
     CK(cudaGetLastError());
@@ -575,7 +606,7 @@ int alloc_particles(mpm_ctx* c, long long n) {
     } plan[] = {{&c->pos, 3 * 8},     {&c->vel, 3 * t},        {&c->fext, 3 * t},        {&c->mass, t},
                 {&c->vol, t},         {&c->vol0, t},           {&c->F, 9 * t},           {&c->stress, 6 * t},
                 {&c->strain, 6 * t},  {&c->eps_p, 6 * t},      {&c->e_strain, 8},        {&c->e_strain_max, 8},
-                {&c->e_strain_ti, 8}, {&c->e_plastic, 8},      {&c->backstress, t},      {&c->mp_mg, 3 * 8},
+                {&c->e_strain_ti, 8}, {&c->e_plastic, 8},      {&c->backstress, t},      {&c->mp_mg, 3 * t},
                 {&c->strain_rate, 6 * t}, {&c->material, 4},   {&c->pflags, 1},          {&c->dc_mult, 4},
                 {&c->keys0, 4},       {&c->vals0, 4},          {&c->keys1, 4},           {&c->vals1, 4},
                 {&c->keys_copy, 4},   {&c->loc, c->form == MPM_FORM_FP32 ? 12u : 0u}};
@@ -672,6 +703,7 @@ int mpm_create_batch(const mpm_grid_desc* grids, int32_t nspec, int form, mpm_ct
             // d3_Length_Cell = d3Length_Grid / dvec3(i3Cells)
             g.h[a] = gd.length[a] / (double)gd.cells[a];
             g.inv_h[a] = 1.0 / g.h[a];
+            set_float_geometry(g, a);
             g.nn[a] = gd.cells[a] + 1;
             g.kd[a] = gd.cells[a] + 2;
             ks *= g.kd[a];
@@ -723,9 +755,9 @@ int mpm_create_batch(const mpm_grid_desc* grids, int32_t nspec, int form, mpm_ct
         DevBuf* b;
         size_t bytes;
     } plan[] = {{&c->g_mass, nn * t},      {&c->g_mom, 3 * nn * t},  {&c->g_vel, 3 * nn * t},
-                {&c->g_force, 3 * nn * t}, {&c->g_ftemp, 3 * nn * t}, {&c->g_mg, 3 * nn * 8},
+                {&c->g_force, 3 * nn * t}, {&c->g_ftemp, 3 * nn * t}, {&c->g_mg, 3 * nn * t},
                 {&c->g_state, nn * 4},     {&c->g_fixed, nn},        {&c->g_friction, nn * 8},
-                {&c->g_ratio, 3 * nn * t}, {&c->g_q, 3 * nn * t},    {&c->g_owner, 3 * nn * 4},
+                {&c->g_ratio, 8 * nn * t}, {&c->g_q, 3 * nn * t},    {&c->g_owner, 3 * nn * 4},
                 {&c->g_nowner, nn * 4},    {&c->g_need, nn * 4},     {&c->g_list, nn * 4},
                 {&c->g_count, 4},          {&c->alist, nn * 4},       {&c->acount, 4},
                 {&c->cstart, (size_t)g.key_max * 4},
@@ -783,6 +815,10 @@ int mpm_set_option(mpm_ctx* c, int key, double value) {
             if (value != 0.0 && value != 1.0 && value != 2.0) return fail(c, MPM_ERR_ARG, "P2G mode must be 0, 1 or 2");
             c->p2g_reduce = (int)value;
             return MPM_OK;
+        case MPM_OPT_GATHER:
+            if (value != 0.0 && value != 1.0) return fail(c, MPM_ERR_ARG, "gather mode must be 0 or 1");
+            c->gather_batch = (int)value;
+            return MPM_OK;
         case MPM_OPT_P2G_BLOCK:
         case MPM_OPT_PASS_BLOCK: {
             int b = (int)value;
@@ -817,6 +853,7 @@ int mpm_upload_materials(mpm_ctx* c, const mpm_material* m, int32_t n) {
         k.inv_E = 1.0 / E;
         k.nu_over_E = nu / E;
         k.inv_G = 1.0 / k.G;
+        set_float_constants(k);
     }
     int rc = ensure(c, c->mats, mc.size() * sizeof(MatConst));
     if (rc) return rc;
@@ -867,7 +904,7 @@ int mpm_upload_particles(mpm_ctx* c, const mpm_particles* p, int64_t n) {
                   {&c->e_strain_ti, p->e_strain_ti, 1, true, 0.0},
                   {&c->e_plastic, p->e_plastic, 1, true, 0.0},
                   {&c->backstress, p->backstress, 1, f64, 0.0},
-                  {&c->mp_mg, p->mp_mass_gradient, 3, true, 0.0},
+                  {&c->mp_mg, p->mp_mass_gradient, 3, f64, 0.0},
                   {&c->strain_rate, p->strain_rate, 6, f64, 0.0}};
     for (auto& f : fields)
         if ((rc = upload_field(c, *f.b, f.h, n, f.k, f.fp64, f.def))) return rc;
@@ -955,7 +992,7 @@ int mpm_upload_nodes(mpm_ctx* c, const mpm_nodes* nd) {
         bool fp64;
     } fields[] = {{&c->g_mass, nd->mass, 1, f64},  {&c->g_mom, nd->mom, 3, f64},
                   {&c->g_vel, nd->vel, 3, f64},    {&c->g_force, nd->force, 3, f64},
-                  {&c->g_ftemp, nd->force_temp, 3, f64}, {&c->g_mg, nd->mass_gradient, 3, true}};
+                  {&c->g_ftemp, nd->force_temp, 3, f64}, {&c->g_mg, nd->mass_gradient, 3, f64}};
     for (auto& f : fields)
         if (f.h && (rc = upload_field(c, *f.b, f.h, nn, f.k, f.fp64, 0.0))) return rc;
     if (nd->state) {
@@ -1017,7 +1054,7 @@ int mpm_download_particles(mpm_ctx* c, mpm_particles* p) {
                   {&c->e_strain_ti, p->e_strain_ti, 1, true},
                   {&c->e_plastic, p->e_plastic, 1, true},
                   {&c->backstress, p->backstress, 1, f64},
-                  {&c->mp_mg, p->mp_mass_gradient, 3, true},
+                  {&c->mp_mg, p->mp_mass_gradient, 3, f64},
                   {&c->strain_rate, p->strain_rate, 6, f64}};
     for (auto& f : fields) {
         if (!f.h) continue;
@@ -1052,7 +1089,7 @@ int mpm_download_nodes(mpm_ctx* c, mpm_nodes* nd) {
         bool fp64;
     } fields[] = {{&c->g_mass, nd->mass, 1, f64},  {&c->g_mom, nd->mom, 3, f64},
                   {&c->g_vel, nd->vel, 3, f64},    {&c->g_force, nd->force, 3, f64},
-                  {&c->g_ftemp, nd->force_temp, 3, f64}, {&c->g_mg, nd->mass_gradient, 3, true}};
+                  {&c->g_ftemp, nd->force_temp, 3, f64}, {&c->g_mg, nd->mass_gradient, 3, f64}};
     for (auto& f : fields) {
         if (!f.h) continue;
         if ((rc = download_field(c, *f.b, f.h, nn, f.k, f.fp64))) return rc;
@@ -1220,8 +1257,8 @@ int mpm_autotune(mpm_ctx* c, int32_t steps, double dt, int contact, mpm_tune_res
     const mpm_sim sim0 = c->sim;
     const int prof0 = c->profile;
     c->profile = 0;
-    const int old[3] = {c->p2g_reduce, c->p2g_block, c->pass_block};
-    int best[3] = {old[0], old[1], old[2]};
+    const int old[4] = {c->p2g_reduce, c->p2g_block, c->pass_block, c->gather_batch};
+    int best[4] = {old[0], old[1], old[2], old[3]};
     double best_ms = 1e300, worst_ms = 0.0;
     int ncand = 0;
     cudaEvent_t a, b;
@@ -1230,10 +1267,12 @@ int mpm_autotune(mpm_ctx* c, int32_t steps, double dt, int contact, mpm_tune_res
     const int blocks[3] = {128, 256, 512};
     for (int red = 0; red < 3 && rc == MPM_OK; ++red)
         for (int pb = 0; pb < 3 && rc == MPM_OK; ++pb)
-            for (int qb = 0; qb < 3 && rc == MPM_OK; ++qb) {
+            for (int qb = 0; qb < 3 && rc == MPM_OK; ++qb)
+            for (int gb = 0; gb < 2 && rc == MPM_OK; ++gb) {
                 c->p2g_reduce = red;
                 c->p2g_block = blocks[pb];
                 c->pass_block = blocks[qb];
+                c->gather_batch = gb;
                 if ((rc = step(c, dt, contact))) break;  // warm-up for this configuration
                 cudaEventRecord(a, c->stream);
                 for (int s = 0; s < steps && rc == MPM_OK; ++s) rc = step(c, dt, contact);
@@ -1248,6 +1287,7 @@ int mpm_autotune(mpm_ctx* c, int32_t steps, double dt, int contact, mpm_tune_res
                     best[0] = red;
                     best[1] = blocks[pb];
                     best[2] = blocks[qb];
+                    best[3] = gb;
                 }
                 worst_ms = std::max(worst_ms, per);
                 if (copy_all(false) != MPM_OK) rc = MPM_ERR_CUDA;
@@ -1263,16 +1303,19 @@ int mpm_autotune(mpm_ctx* c, int32_t steps, double dt, int contact, mpm_tune_res
         c->p2g_reduce = old[0];
         c->p2g_block = old[1];
         c->pass_block = old[2];
+        c->gather_batch = old[3];
         return rc;
     }
     CK(cudaStreamSynchronize(c->stream));
     c->p2g_reduce = best[0];
     c->p2g_block = best[1];
     c->pass_block = best[2];
+    c->gather_batch = best[3];
     if (out) {
         out->p2g_reduce = best[0];
         out->p2g_block = best[1];
         out->pass_block = best[2];
+        out->gather_batch = best[3];
         out->candidates = ncand;
         out->best_ms_per_step = best_ms;
         out->worst_ms_per_step = worst_ms;

@@ -51,13 +51,21 @@ __global__ void k_reset_grid(NView<T> nd, int contact) {
 // quotient, as glm::floor(d3Position / d3_Length_Cell)
 // (GridPoint_Mediator.cpp:8), so the cell index is bit-identical to the
 // reference.  Particles whose base cell lies outside [-1, cells] have no node
-// in range and get key_max.
+// in range and get key_max.  Decided in float-float arithmetic (fps_cell)
+// unless the quotient lies within 1e-4 of an integer, then by the exact FP64
+// quotient (cell_and_local).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ unsigned particle_key(const Geom& g, const double x[3], float u[3], unsigned* err) {
     bool ok = true;
     int b[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
+        float ff;
+        if (fps_cell(x[a], g.inv_hf[a], g.ih_lo[a], &ff, &u[a])) {
+            if (ff < -1.0f || ff > (float)(g.nn[a] - 1)) ok = false;
+            b[a] = ok ? (int)ff : 0;
+            continue;
+        }
         double f;
         if (!cell_and_local(g, a, x[a], f, u[a])) {
             atomicOr(err, ERR_NONFINITE_POSITION);
@@ -230,9 +238,9 @@ __global__ void __launch_bounds__(512) k_p2g(PView<T> P, NView<T> nd, Geom g, co
                 atomicAdd(&nd.force[nn + nid], c[5]);
                 atomicAdd(&nd.force[2 * nn + nid], c[6]);
                 if (nf == 10) {
-                    atomicAdd(&nd.mg[nid], (double)c[7]);
-                    atomicAdd(&nd.mg[nn + nid], (double)c[8]);
-                    atomicAdd(&nd.mg[2 * nn + nid], (double)c[9]);
+                    atomicAdd(&nd.mg[nid], c[7]);
+                    atomicAdd(&nd.mg[nn + nid], c[8]);
+                    atomicAdd(&nd.mg[2 * nn + nid], c[9]);
                 }
             }
         }
@@ -366,9 +374,9 @@ __global__ void __launch_bounds__(512) k_p2g_cells(PView<T> P, NView<T> nd, Geom
             atomicAdd(&nd.force[nn + nid], af1);
             atomicAdd(&nd.force[2 * nn + nid], af2);
             if (with_mg) {
-                atomicAdd(&nd.mg[nid], (double)g0);
-                atomicAdd(&nd.mg[nn + nid], (double)g1);
-                atomicAdd(&nd.mg[2 * nn + nid], (double)g2);
+                atomicAdd(&nd.mg[nid], g0);
+                atomicAdd(&nd.mg[nn + nid], g1);
+                atomicAdd(&nd.mg[2 * nn + nid], g2);
             }
         }
     }
@@ -526,24 +534,41 @@ __global__ void k_grid_update(NView<T> nd, T dt, double damping, int contact, in
 
 // ratio = src / m for nodes with m > mass_min (else 0).  src = force before
 // pass 1 (the f_i/m_i of …MPLocks.cpp:508), momentum before pass 2 (:198).
-// Also clears the remap accumulator when asked.
+// Also clears the remap accumulator when asked.  mass_min is given in the
+// form's type (the FP32 form's is the threshold rounded down to float, which
+// compares every float mass exactly as the double threshold does).
+// The node's record (r, has, v) is written as one or two aligned vectors so
+// the particle passes gather one 32-byte (FP32) sector per corner.
 template <typename T>
 __device__ __forceinline__ void node_ratio(const NView<T>& nd, long long i, const T* __restrict__ src,
-                                           double mass_min, int clear_q) {
+                                           T mass_min, int clear_q, int with_vel) {
     const long long nn = nd.nn;
     if (!(nd.state[i] & 1u)) return;
     T m = nd.mass[i];
-    bool has = (double)m > mass_min;
+    bool has = m > mass_min;
+    Quad<T> r;
+    r.x = has ? src[i] / m : (T)0;
+    r.y = has ? src[nn + i] / m : (T)0;
+    r.z = has ? src[2 * nn + i] / m : (T)0;
+    r.w = has ? (T)1 : (T)0;
+    *reinterpret_cast<Quad<T>*>(nd.rec + 8 * i) = r;
+    if (with_vel) {
+        Quad<T> v;
+        v.x = nd.vel[i];
+        v.y = nd.vel[nn + i];
+        v.z = nd.vel[2 * nn + i];
+        v.w = (T)0;
+        *reinterpret_cast<Quad<T>*>(nd.rec + 8 * i + 4) = v;
+    }
+    if (clear_q) {
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        nd.ratio[c * nn + i] = has ? src[c * nn + i] / m : (T)0;
-        if (clear_q) nd.q[c * nn + i] = (T)0;
+        for (int c = 0; c < 3; ++c) nd.q[c * nn + i] = (T)0;
     }
 }
 
 template <typename T>
-__global__ void k_node_ratio(NView<T> nd, const T* __restrict__ src, double mass_min, int clear_q) {
-    NODE_LOOP(nd, i) node_ratio<T>(nd, i, src, mass_min, clear_q);
+__global__ void k_node_ratio(NView<T> nd, const T* __restrict__ src, T mass_min, int clear_q, int with_vel) {
+    NODE_LOOP(nd, i) node_ratio<T>(nd, i, src, mass_min, clear_q, with_vel);
 }
 
 // ---------------------------------------------------------------------------
@@ -552,11 +577,11 @@ __global__ void k_node_ratio(NView<T> nd, const T* __restrict__ src, double mass
 // each particle then scatters N m_p v_p, summed per run before the atomic.
 // Contact path: particles flagged b_DisplacementControl are skipped.
 // ---------------------------------------------------------------------------
-template <typename T>
+template <typename T, int BATCH>
 __global__ void __launch_bounds__(256) k_pass1_remap(PView<T> P, NView<T> nd, Geom g,
                                                      const unsigned* __restrict__ skeys,
                                                      const unsigned* __restrict__ perm, long long n, T dt,
-                                                     double mass_min, int contact) {
+                                                     T mass_min, int contact) {
     long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     unsigned key = (s < n) ? skeys[s] : 0xffffffffu;
     Runs run;
@@ -582,15 +607,38 @@ __global__ void __launch_bounds__(256) k_pass1_remap(PView<T> P, NView<T> nd, Ge
         m = P.mass[p];
 #pragma unroll
         for (int c = 0; c < 3; ++c) v[c] = P.vel[c * np + p];
-#pragma unroll 1
-        for (int k = 0; k < 8; ++k) {
-            long long nid = corner_node(*gsp, b, k);
-            if (nid < 0) continue;
-            if (!((double)nd.mass[nid] > mass_min)) continue;
-            T N, G[3];
-            B.corner(k, N, G);
+        // BATCH: every corner's record is requested before any is used (one
+        // round trip to memory instead of eight, at more registers); the sum
+        // runs in corner order either way
+        if constexpr (BATCH) {
+            Quad<T> r[8];
 #pragma unroll
-            for (int c = 0; c < 3; ++c) v[c] = v[c] + N * nd.ratio[c * nn + nid] * dt;
+            for (int k = 0; k < 8; ++k) {
+                const long long nid = corner_node(*gsp, b, k);
+                r[k] = nid >= 0 ? ld_quad(nd.rec + 8 * nid) : Quad<T>{(T)0, (T)0, (T)0, (T)0};
+            }
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                if (!(r[k].w != (T)0)) continue;  // out of range or m <= mass_min
+                T N, G[3];
+                B.corner(k, N, G);
+                v[0] = v[0] + N * r[k].x * dt;
+                v[1] = v[1] + N * r[k].y * dt;
+                v[2] = v[2] + N * r[k].z * dt;
+            }
+        } else {
+#pragma unroll 1
+            for (int k = 0; k < 8; ++k) {
+                const long long nid = corner_node(*gsp, b, k);
+                if (nid < 0) continue;
+                const Quad<T> r = ld_quad(nd.rec + 8 * nid);
+                if (!(r.w != (T)0)) continue;
+                T N, G[3];
+                B.corner(k, N, G);
+                v[0] = v[0] + N * r.x * dt;
+                v[1] = v[1] + N * r.y * dt;
+                v[2] = v[2] + N * r.z * dt;
+            }
         }
 #pragma unroll
         for (int c = 0; c < 3; ++c) P.vel[c * np + p] = v[c];
@@ -616,17 +664,17 @@ __global__ void __launch_bounds__(256) k_pass1_remap(PView<T> P, NView<T> nd, Ge
 
 // Remap finish: v_i += q_i / m_i on nodes with m_i > mass_min (:559-560).
 template <typename T>
-__device__ __forceinline__ void node_remap(const NView<T>& nd, long long i, double mass_min) {
+__device__ __forceinline__ void node_remap(const NView<T>& nd, long long i, T mass_min) {
     if (!(nd.state[i] & 1u)) return;
     const long long nn = nd.nn;
     T m = nd.mass[i];
-    if (!((double)m > mass_min)) return;
+    if (!(m > mass_min)) return;
 #pragma unroll
     for (int c = 0; c < 3; ++c) nd.vel[c * nn + i] += nd.q[c * nn + i] / m;
 }
 
 template <typename T>
-__global__ void k_node_remap(NView<T> nd, double mass_min) {
+__global__ void k_node_remap(NView<T> nd, T mass_min) {
     NODE_LOOP(nd, i) node_remap<T>(nd, i, mass_min);
 }
 
@@ -656,6 +704,8 @@ __global__ void k_node_bc(NView<T> nd) {
 struct StepArgs {
     double dt;
     double mass_min;
+    float dt_f;        // RN32(dt)
+    float mass_min_f;  // mass_min rounded down to float (fps_float_threshold)
     double tv[3];
     int has_timeline;
     int contact;
@@ -670,7 +720,7 @@ struct StepArgs {
 // next step needs no separate key pass: `keys` is read (this step) and
 // rewritten (next step), `keys_next` receives the next step's sort input.
 // ---------------------------------------------------------------------------
-template <typename T>
+template <typename T, int BATCH>
 __global__ void __launch_bounds__(512) k_pass2(PView<T> P, NView<T> nd, Geom g, unsigned* __restrict__ keys,
                                                unsigned* __restrict__ keys_next, const MatConst* __restrict__ mats,
                                                int nmat, StepArgs a, unsigned* err) {
@@ -678,7 +728,8 @@ __global__ void __launch_bounds__(512) k_pass2(PView<T> P, NView<T> nd, Geom g, 
     const long long np = P.n, nn = nd.nn;
     if (p >= np) return;
     const unsigned fl = P.pflags[p];
-    const T dt = (T)a.dt;
+    const T dt = form_const<T>(a.dt, a.dt_f);
+    const T mass_min = form_const<T>(a.mass_min, a.mass_min_f);
     const bool skip = a.contact && (fl & 8u);
     const Geom& gs = spec_geom(g, P.sid, p);
     if (!skip) {
@@ -697,31 +748,48 @@ __global__ void __launch_bounds__(512) k_pass2(PView<T> P, NView<T> nd, Geom g, 
             // added to the FP64 position once; FP64 form: added per corner
             // as the reference does (…MPLocks.cpp:197-198).
             T disp[3] = {0, 0, 0};
-#pragma unroll 1
-            for (int k = 0; k < 8; ++k) {
-                long long nid = corner_node(gs, b, k);
-                if (nid < 0) continue;
-                T N, G[3];
-                B.corner(k, N, G);
-                if ((double)nd.mass[nid] > a.mass_min) {
-                    if constexpr (sizeof(T) == 4) {
+            // BATCH: four corners' records are requested before any is used
+            // (two round trips to memory instead of eight, at more registers);
+            // sums run in corner order either way
+#pragma unroll(BATCH ? 2 : 1)
+            for (int h = 0; h < (BATCH ? 2 : 8); ++h) {
+                constexpr int W = BATCH ? 4 : 1;
+                Quad<T> rq[W], vq[W];
+                bool in[W];
 #pragma unroll
-                        for (int c = 0; c < 3; ++c) disp[c] += N * nd.ratio[c * nn + nid];
-                    } else {
-#pragma unroll
-                        for (int c = 0; c < 3; ++c) x[c] = x[c] + (double)(N * nd.ratio[c * nn + nid]) * ddt;
-                    }
+                for (int j = 0; j < W; ++j) {
+                    const long long nid = corner_node(gs, b, W * h + j);
+                    in[j] = nid >= 0;
+                    const Quad<T> z{(T)0, (T)0, (T)0, (T)0};
+                    rq[j] = in[j] ? ld_quad(nd.rec + 8 * nid) : z;
+                    vq[j] = in[j] ? ld_quad(nd.rec + 8 * nid + 4) : z;
                 }
-                T vi[3] = {nd.vel[nid], nd.vel[nn + nid], nd.vel[2 * nn + nid]};
-                // outerProduct(v_i, grad N): column c, row r = v_i[r] * G[c]
 #pragma unroll
-                for (int c = 0; c < 3; ++c)
+                for (int j = 0; j < W; ++j) {
+                    if (!in[j]) continue;
+                    T N, G[3];
+                    B.corner(W * h + j, N, G);
+                    if (rq[j].w != (T)0) {  // m > mass_min
+                        const T rr[3] = {rq[j].x, rq[j].y, rq[j].z};
+                        if constexpr (sizeof(T) == 4) {
 #pragma unroll
-                    for (int r = 0; r < 3; ++r) L[3 * c + r] += vi[r] * G[c];
+                            for (int c = 0; c < 3; ++c) disp[c] += N * rr[c];
+                        } else {
+#pragma unroll
+                            for (int c = 0; c < 3; ++c) x[c] = x[c] + (double)(N * rr[c]) * ddt;
+                        }
+                    }
+                    const T vi[3] = {vq[j].x, vq[j].y, vq[j].z};
+                    // outerProduct(v_i, grad N): column c, row r = v_i[r] * G[c]
+#pragma unroll
+                    for (int c = 0; c < 3; ++c)
+#pragma unroll
+                        for (int r = 0; r < 3; ++r) L[3 * c + r] += vi[r] * G[c];
+                }
             }
             if constexpr (sizeof(T) == 4) {
 #pragma unroll
-                for (int c = 0; c < 3; ++c) x[c] += (double)(disp[c] * dt);
+                for (int c = 0; c < 3; ++c) x[c] += fps_f2d(disp[c] * dt);
             }
 #pragma unroll
             for (int c = 0; c < 3; ++c) P.pos[c * np + p] = x[c];
@@ -790,13 +858,13 @@ __global__ void __launch_bounds__(512) k_pass2(PView<T> P, NView<T> nd, Geom g, 
                     dEp += sn * o.deps_p[k] * V;
                 }
             }
-            double es = P.e_strain[p] + (double)dEs;
+            double es = P.e_strain[p] + fps_f2d_form(dEs);
             P.e_strain[p] = es;
             if (!a.contact) {
                 P.e_strain_ti[p] += es * a.dt;
                 if (es > P.e_strain_max[p]) P.e_strain_max[p] = es;
             }
-            P.e_plastic[p] += (double)dEp;
+            P.e_plastic[p] += fps_f2d_form(dEp);
             P.backstress[p] = R + o.dR;
         } else if (!a.contact) {
             atomicOr(err, ERR_BAD_MATERIAL);
@@ -1023,7 +1091,7 @@ __global__ void k_contact_mp_gradient(PView<T> P, NView<T> nd, Geom g, const uns
     const long long p = surf[t];
     const Geom& gs = spec_geom(g, P.sid, p);
     const long long np = P.n, nn = nd.nn;
-    double gp[3] = {0.0, 0.0, 0.0};
+    T gp[3] = {0, 0, 0};
     unsigned key = keys[p];
     if (key < g.key_max) {
         int b[3];
@@ -1032,13 +1100,12 @@ __global__ void k_contact_mp_gradient(PView<T> P, NView<T> nd, Geom g, const uns
         for (int k = 0; k < 8; ++k) {
             long long nid = corner_node(gs, b, k);
             if (nid < 0) continue;
-            double gi[3] = {nd.mg[nid], nd.mg[nn + nid], nd.mg[2 * nn + nid]};
+            T gi[3] = {nd.mg[nid], nd.mg[nn + nid], nd.mg[2 * nn + nid]};
             bool take;
             if constexpr (sizeof(T) == 8) {
                 take = len3_rn(gi) > len3_rn(gp);
             } else {
-                float f[3] = {(float)gi[0], (float)gi[1], (float)gi[2]};
-                float l2 = dot3f(f, f);
+                float l2 = dot3f(gi, gi);
                 take = l2 > best2;
                 if (take) best2 = l2;
             }
@@ -1082,14 +1149,7 @@ __global__ void k_contact_normal(PView<T> P, NView<T> nd, Geom g, const unsigned
     if (key >= g.key_max) return;
     int b[3];
     key_to_base(key, gs, b);
-    double x[3] = {P.pos[p], P.pos[np + p], P.pos[2 * np + p]};
-    double gp[3] = {P.mp_mg[p], P.mp_mg[np + p], P.mp_mg[2 * np + p]};
-    float gpf[3] = {(float)gp[0], (float)gp[1], (float)gp[2]};
-    float u[3];
-    if constexpr (sizeof(T) == 4) {
-#pragma unroll
-        for (int c = 0; c < 3; ++c) u[c] = (float)(x[c] - node_coord(gs, c, b[c]));  // offset from the base node
-    }
+    const T gp[3] = {P.mp_mg[p], P.mp_mg[np + p], P.mp_mg[2 * np + p]};
     for (int k = 0; k < 8; ++k) {
         long long nid = corner_node(gs, b, k);
         if (nid < 0) continue;
@@ -1098,13 +1158,14 @@ __global__ void k_contact_normal(PView<T> P, NView<T> nd, Geom g, const unsigned
         if constexpr (sizeof(T) == 8) {
             double d[3];
 #pragma unroll
-            for (int c = 0; c < 3; ++c) d[c] = __dadd_rn(node_coord(gs, c, b[c] + o3[c]), -x[c]);
+            for (int c = 0; c < 3; ++c) d[c] = __dadd_rn(node_coord(gs, c, b[c] + o3[c]), -P.pos[c * np + p]);
             facing = dot3_rn(d, gp) > 0.0;
         } else {
+            // node minus particle from the cell-local coordinate: (o - u) h per axis
             float d[3];
 #pragma unroll
-            for (int c = 0; c < 3; ++c) d[c] = (o3[c] ? (float)gs.h[c] : 0.0f) - u[c];
-            facing = dot3f(d, gpf) > 0.0f;
+            for (int c = 0; c < 3; ++c) d[c] = ((float)o3[c] - P.loc[c * np + p]) * gs.hf[c];
+            facing = dot3f(d, gp) > 0.0f;
         }
         if (!facing) continue;
         if (!apply) {
@@ -1129,18 +1190,17 @@ __global__ void k_contact_flags(PView<T> P, NView<T> nd, Geom g, const unsigned*
     if (key >= g.key_max) return;
     int b[3];
     key_to_base(key, gs, b);
-    double gp[3] = {P.mp_mg[p], P.mp_mg[np + p], P.mp_mg[2 * np + p]};
-    const float gpf[3] = {(float)gp[0], (float)gp[1], (float)gp[2]};
+    const T gp[3] = {P.mp_mg[p], P.mp_mg[np + p], P.mp_mg[2 * np + p]};
     double lp = 0.0;
     float lpf = 0.0f;
     if constexpr (sizeof(T) == 8)
         lp = len3_rn(gp);
     else
-        lpf = sqrtf(dot3f(gpf, gpf));
+        lpf = sqrtf(dot3f(gp, gp));
     for (int k = 0; k < 8; ++k) {
         long long nid = corner_node(gs, b, k);
         if (nid < 0) continue;
-        double gi[3] = {nd.mg[nid], nd.mg[nn + nid], nd.mg[2 * nn + nid]};
+        const T gi[3] = {nd.mg[nid], nd.mg[nn + nid], nd.mg[2 * nn + nid]};
         bool pos, neg;
         if constexpr (sizeof(T) == 8) {
             double tol = __dmul_rn(__dmul_rn(0.001, len3_rn(gi)), lp);
@@ -1148,9 +1208,8 @@ __global__ void k_contact_flags(PView<T> P, NView<T> nd, Geom g, const unsigned*
             pos = dd >= tol;
             neg = !pos && dd <= -tol;
         } else {
-            float gif[3] = {(float)gi[0], (float)gi[1], (float)gi[2]};
-            float tol = 0.001f * sqrtf(dot3f(gif, gif)) * lpf;
-            float dd = dot3f(gif, gpf);
+            float tol = 0.001f * sqrtf(dot3f(gi, gi)) * lpf;
+            float dd = dot3f(gi, gp);
             pos = dd >= tol;
             neg = !pos && dd <= -tol;
         }

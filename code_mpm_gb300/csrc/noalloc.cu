@@ -75,6 +75,7 @@ extern "C" int mpm_cell_order_noalloc(const mpm_grid_desc* grid, const double* d
         if (!(grid->length[a] > 0.0) || grid->cells[a] < 1) return MPM_ERR_ARG;
         g.h[a] = grid->length[a] / (double)grid->cells[a];
         g.inv_h[a] = 1.0 / g.h[a];
+        set_float_geometry(g, a);
         g.nn[a] = grid->cells[a] + 1;
         g.kd[a] = grid->cells[a] + 2;
         keyspace *= (long long)g.kd[a];

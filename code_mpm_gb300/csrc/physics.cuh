@@ -78,18 +78,19 @@ struct Bases {
     }
     // FP32 form: bases from the cell-local coordinate stored by the previous step
     __device__ __forceinline__ void init_local(const Geom& g, const float u[3]) {
-        axis_bases_u(u[0], (float)g.inv_h[0], (float*)Nx, (float*)gx);
-        axis_bases_u(u[1], (float)g.inv_h[1], (float*)Ny, (float*)gy);
-        axis_bases_u(u[2], (float)g.inv_h[2], (float*)Nz, (float*)gz);
+        axis_bases_u(u[0], g.inv_hf[0], (float*)Nx, (float*)gx);
+        axis_bases_u(u[1], g.inv_hf[1], (float*)Ny, (float*)gy);
+        axis_bases_u(u[2], g.inv_hf[2], (float*)Nz, (float*)gz);
     }
-    // corner k = 4*ix + 2*iy + iz
+    // corner k = 4*ix + 2*iy + iz (selects, not indexing, so the bases stay
+    // in registers when k is a loop variable)
     __device__ __forceinline__ void corner(int k, T& N, T G[3]) const {
-        int ix = (k >> 2) & 1, iy = (k >> 1) & 1, iz = k & 1;
-        T nx = Nx[ix], ny = Ny[iy], nz = Nz[iz];
+        const bool ix = (k >> 2) & 1, iy = (k >> 1) & 1, iz = k & 1;
+        const T nx = ix ? Nx[1] : Nx[0], ny = iy ? Ny[1] : Ny[0], nz = iz ? Nz[1] : Nz[0];
         N = nx * ny * nz;
-        G[0] = -(ny * nz) * gx[ix];
-        G[1] = -(nx * nz) * gy[iy];
-        G[2] = -(nx * ny) * gz[iz];
+        G[0] = -(ny * nz) * (ix ? gx[1] : gx[0]);
+        G[1] = -(nx * nz) * (iy ? gy[1] : gy[0]);
+        G[2] = -(nx * ny) * (iz ? gz[1] : gz[0]);
     }
 };
 
@@ -255,7 +256,8 @@ struct CrOut {
 
 template <typename T>
 __device__ __forceinline__ void trial_increment(const MatConst& m, const T e[6], T d[6]) {
-    const T C = (T)m.C, a = (T)m.one_m_nu, nu = (T)m.nu, hb = (T)m.half_m_nu;
+    const T C = form_const<T>(m.C, m.fC), a = form_const<T>(m.one_m_nu, m.fone_m_nu),
+            nu = form_const<T>(m.nu, m.fnu), hb = form_const<T>(m.half_m_nu, m.fhalf_m_nu);
     d[0] = C * (a * e[0] + nu * e[1] + nu * e[2]);
     d[1] = C * (a * e[1] + nu * e[0] + nu * e[2]);
     d[2] = C * (a * e[2] + nu * e[0] + nu * e[1]);
@@ -292,7 +294,7 @@ __device__ __forceinline__ void cr_increment(const MatConst& m, T R, const T sig
     J2 += tr[3] * tr[3];
     J2 += tr[4] * tr[4];
     J2 += tr[5] * tr[5];
-    T rad = (T)m.k0;
+    T rad = form_const<T>(m.k0, m.fk0);
     if (hard) rad = rad + R * (T)0.70710678118654752440;  // R / sqrt(2)
     if (J2 <= rad * rad) {
 #pragma unroll
@@ -311,7 +313,8 @@ __device__ __forceinline__ void cr_increment(const MatConst& m, T R, const T sig
     o.dsig[0] += hyd;
     o.dsig[1] += hyd;
     o.dsig[2] += hyd;
-    const T iE = (T)m.inv_E, nE = (T)m.nu_over_E, iG = (T)m.inv_G;
+    const T iE = form_const<T>(m.inv_E, m.finv_E), nE = form_const<T>(m.nu_over_E, m.fnu_over_E),
+            iG = form_const<T>(m.inv_G, m.finv_G);
     T ee[6];
     ee[0] = o.dsig[0] * iE - o.dsig[1] * nE - o.dsig[2] * nE;
     ee[1] = o.dsig[1] * iE - o.dsig[0] * nE - o.dsig[2] * nE;
@@ -326,8 +329,8 @@ __device__ __forceinline__ void cr_increment(const MatConst& m, T R, const T sig
 #pragma unroll
     for (int i = 0; i < 6; ++i) ep += o.deps_p[i] * o.deps_p[i];
     ep = sqrt(ep * (T)(2.0 / 3.0));
-    const T sat = (T)m.s23C1 - R;
-    o.dR = (sat > (T)0) ? (T)m.C0 * sat * ep : (T)0;
+    const T sat = form_const<T>(m.s23C1, m.fs23C1) - R;
+    o.dR = (sat > (T)0) ? form_const<T>(m.C0, m.fC0) * sat * ep : (T)0;
 }
 
 }  // namespace mpm

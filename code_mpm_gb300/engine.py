@@ -79,7 +79,8 @@ class KernelStat(C.Structure):
 
 class TuneResult(C.Structure):
     _fields_ = [("p2g_reduce", C.c_int32), ("p2g_block", C.c_int32), ("pass_block", C.c_int32),
-                ("candidates", C.c_int32), ("best_ms_per_step", C.c_double), ("worst_ms_per_step", C.c_double)]
+                ("candidates", C.c_int32), ("best_ms_per_step", C.c_double), ("worst_ms_per_step", C.c_double),
+                ("gather_batch", C.c_int32)]
 
 
 class Monitors(C.Structure):
@@ -94,6 +95,7 @@ MON_DISPLACEMENT, MON_MOMENTUM, MON_PRINCIPAL, MON_STRESS, MON_ENERGY = 1, 2, 4,
 OPT_P2G_REDUCE = 3
 OPT_P2G_BLOCK = 4
 OPT_PASS_BLOCK = 5
+OPT_GATHER = 6
 
 
 def library_path() -> str:
@@ -357,6 +359,7 @@ class Engine:
         r = TuneResult()
         self._check(self._L.mpm_autotune(self._h, int(steps), float(dt), 1 if contact else 0, C.byref(r)))
         return {"p2g_reduce": r.p2g_reduce, "p2g_block": r.p2g_block, "pass_block": r.pass_block,
+                "gather_batch": r.gather_batch,
                 "candidates": r.candidates, "best_ms_per_step": r.best_ms_per_step,
                 "worst_ms_per_step": r.worst_ms_per_step}
 

@@ -73,6 +73,7 @@ extern "C" {
 #define MPM_OPT_P2G_REDUCE 3     /* P2G: 0 = one atomic per particle, 1 = sum each cell's run across lanes first, 2 = stage the block in shared memory and sum each (cell, corner) in one thread */
 #define MPM_OPT_P2G_BLOCK 4      /* P2G threads per block (128, 256 or 512) */
 #define MPM_OPT_PASS_BLOCK 5     /* G2P pass-2 threads per block (128, 256 or 512) */
+#define MPM_OPT_GATHER 6         /* G2P node gathers: 0 = one corner at a time, 1 = several corners' loads issued together */
 
 typedef struct mpm_ctx mpm_ctx;
 
@@ -200,6 +201,7 @@ int mpm_advance_timed(mpm_ctx* ctx, int32_t nsteps, double dt, int contact, floa
 typedef struct mpm_tune_result {
     int32_t p2g_reduce, p2g_block, pass_block, candidates;
     double best_ms_per_step, worst_ms_per_step;
+    int32_t gather_batch;
 } mpm_tune_result;
 int mpm_autotune(mpm_ctx* ctx, int32_t steps, double dt, int contact, mpm_tune_result* out);
 

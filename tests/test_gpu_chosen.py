@@ -56,7 +56,7 @@ def test_autotune_restores_state_and_picks_valid_options(golden, form):
         before = e.download_state(st)
         res = e.autotune(steps=2, contact=True)
         after = e.download_state(st)
-        assert res["candidates"] == 27 and res["p2g_block"] in (128, 256, 512) and res["pass_block"] in (128, 256, 512)
+        assert res["candidates"] == 54 and res["gather_batch"] in (0, 1) and res["p2g_block"] in (128, 256, 512) and res["pass_block"] in (128, 256, 512)
         assert res["best_ms_per_step"] <= res["worst_ms_per_step"]
         for k in ("pos", "vel", "stress", "F", "g_mass", "g_state"):
             assert np.array_equal(before[k], after[k]), k
@@ -69,6 +69,7 @@ def test_plain_form_parity_holds_for_every_launch_configuration(golden):
     for red in (0, 1, 2):
         for blk in (128, 512):
             with engine.Engine.from_state(st) as e:
+                e.set_option(engine.OPT_GATHER, 1 if blk == 512 else 0)
                 e.set_option(engine.OPT_P2G_REDUCE, red)
                 e.set_option(engine.OPT_P2G_BLOCK, blk)
                 e.set_option(engine.OPT_PASS_BLOCK, blk)
