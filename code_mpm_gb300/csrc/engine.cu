@@ -16,7 +16,9 @@
 
 #include "kernels.cuh"
 #include "mpm_gb300.h"
+#include "mpm_surrogate.h"
 #include "radix_sort.cuh"
+#include "surrogate.cuh"
 
 using namespace mpm;
 
@@ -94,13 +96,27 @@ struct mpm_ctx {
     bool keys_valid = false;  // keys_copy / keys[key_buf] / loc hold the keys of the current positions
     int key_buf = 0;
     DevBuf loc;
+    // return-map network (FP32 form)
+    mpm_net* net = nullptr;
+    float sg_band = 0.02f, sg_recheck = 0.01f;
+    unsigned sg_mats = 0;
+    std::vector<MatConst> mats_host;
+    DevBuf q_in, q_out, q_vol, q_pidx, q_count, sg_acc;
+    // harvesting of return-map inputs
+    int hv_on = 0;
+    unsigned hv_mats = 0;
+    float hv_band = 0.02f;
+    float* hv_rows = nullptr;
+    long long hv_cap = 0;
+    DevBuf hv_count;
 
     mpm_ctx() {
         DevBuf* list[] = {&xtab, &err_word, &pos, &vel, &fext, &mass, &vol, &vol0, &F, &stress, &strain, &eps_p,
                           &e_strain, &e_strain_max, &e_strain_ti, &e_plastic, &backstress, &mp_mg, &strain_rate,
                           &material, &pflags, &dc_mult, &g_mass, &g_mom, &g_vel, &g_force, &g_ftemp, &g_mg,
                           &g_state, &g_fixed, &g_friction, &g_ratio, &g_q, &g_owner, &g_nowner, &g_need, &g_list, &g_count, &rs_chunk, &cstart,
-                          &cend, &keys0, &vals0, &keys1, &vals1, &keys_copy, &counts, &dclist, &mats, &staging, &tune_backup, &surf, &mon_mask, &mon_acc, &loc, &geom_tab, &sid, &alist, &acount};
+                          &cend, &keys0, &vals0, &keys1, &vals1, &keys_copy, &counts, &dclist, &mats, &staging, &tune_backup, &surf, &mon_mask, &mon_acc, &loc, &geom_tab, &sid, &alist, &acount,
+                          &q_in, &q_out, &q_vol, &q_pidx, &q_count, &sg_acc, &hv_count};
         all.assign(std::begin(list), std::end(list));
     }
 };
@@ -579,12 +595,51 @@ int step_impl(mpm_ctx* c, double dt, int contact) {
         timeline_velocity(c, c->sim.time, a.tv);
         a.has_timeline = c->tl_t.empty() ? 0 : 1;
         a.contact = contact;
+        a.sg_on = 0;
+        a.sg_mats = 0;
+        a.sg_band = 0.0f;
+        a.q = SurrogateQueue{};
+        a.sg_acc = nullptr;
+        a.hv_on = c->hv_on;
+        a.hv_mats = c->hv_mats;
+        a.hv_band = c->hv_band;
+        a.hv_rows = c->hv_rows;
+        a.hv_count = (unsigned*)c->hv_count.p;
+        a.hv_cap = c->hv_cap;
+        const bool use_net = sizeof(T) == 4 && c->net && c->sg_mats;
+        if (use_net) {
+            int rq;
+            if ((rq = ensure(c, c->q_in, (size_t)n * 13 * 4)) || (rq = ensure(c, c->q_out, (size_t)n * 7 * 4)) ||
+                (rq = ensure(c, c->q_vol, (size_t)n * 4)) || (rq = ensure(c, c->q_pidx, (size_t)n * 4)) ||
+                (rq = ensure(c, c->q_count, 64)))
+                return rq;
+            CK(cudaMemsetAsync(c->q_count.p, 0, 4, c->stream));
+            a.sg_on = 1;
+            a.sg_mats = c->sg_mats;
+            a.sg_band = c->sg_band;
+            a.q = SurrogateQueue{(float*)c->q_in.p, (float*)c->q_out.p, (float*)c->q_vol.p, (unsigned*)c->q_pidx.p,
+                                 (unsigned*)c->q_count.p, n};
+            a.sg_acc = (SurrogateAcc*)c->sg_acc.p;
+        }
         if (c->gather_batch)
             LAUNCH("pass2", (k_pass2<T, 1>), blocks_for(n, c->pass_block), c->pass_block, P, N, g,
                    (unsigned*)c->keys_copy.p, keys_next, (const MatConst*)c->mats.p, c->nmat, a, err);
         else
             LAUNCH("pass2", (k_pass2<T, 0>), blocks_for(n, c->pass_block), c->pass_block, P, N, g,
                    (unsigned*)c->keys_copy.p, keys_next, (const MatConst*)c->mats.p, c->nmat, a, err);
+        if constexpr (sizeof(T) == 4) {
+            if (use_net) {
+                int rq;
+                {
+                    Launch l_(c, "net_infer");
+                    rq = net_run_queue(c->net, a.q, c->stream, err);
+                }
+                if (rq) return rq;
+                LAUNCH("net_finish", k_sg_finish, (unsigned)c->sm_count * 8, 256, P, a.q, net_material(c->net),
+                       contact, dt, 1.0f / net_yield(c->net), c->sg_recheck, (unsigned long long)c->sim.step,
+                       a.sg_acc);
+            }
+        }
         c->keys_valid = true;
     }
     CK(cudaGetLastError());
@@ -854,6 +909,15 @@ int mpm_upload_materials(mpm_ctx* c, const mpm_material* m, int32_t n) {
         k.nu_over_E = nu / E;
         k.inv_G = 1.0 / k.G;
         set_float_constants(k);
+    }
+    c->mats_host = mc;
+    c->sg_mats = 0;
+    if (c->net) {
+        const MatConst& nm = net_material(c->net);
+        for (int i = 0; i < n && i < 32; ++i)
+            if (mc[i].type == 4 && mc[i].E == nm.E && mc[i].nu == nm.nu && mc[i].Y == nm.Y && mc[i].C0 == nm.C0 &&
+                mc[i].C1 == nm.C1)
+                c->sg_mats |= 1u << i;
     }
     int rc = ensure(c, c->mats, mc.size() * sizeof(MatConst));
     if (rc) return rc;
@@ -1344,6 +1408,77 @@ int mpm_profile_reset(mpm_ctx* c) {
     if (rc) return rc;
     std::fill(c->prof_ms.begin(), c->prof_ms.end(), 0.0);
     std::fill(c->prof_cnt.begin(), c->prof_cnt.end(), 0LL);
+    return MPM_OK;
+}
+
+int mpm_attach_surrogate(mpm_ctx* c, mpm_net* net, double band, double recheck) {
+    if (!c) return MPM_ERR_ARG;
+    if (net && c->form != MPM_FORM_FP32) return fail(c, MPM_ERR_ARG, "the return-map network serves the FP32 form");
+    if (net && !(band >= 0.0 && band < 10.0 && recheck >= 0.0 && recheck <= 1.0))
+        return fail(c, MPM_ERR_ARG, "band must be in [0, 10), recheck in [0, 1]");
+    c->net = net;
+    c->sg_band = (float)band;
+    c->sg_recheck = (float)recheck;
+    c->sg_mats = 0;
+    if (net) {
+        const MatConst& nm = net_material(net);
+        for (size_t i = 0; i < c->mats_host.size() && i < (size_t)c->nmat && i < 32; ++i) {
+            const MatConst& m = c->mats_host[i];
+            if (m.type == 4 && m.E == nm.E && m.nu == nm.nu && m.Y == nm.Y && m.C0 == nm.C0 && m.C1 == nm.C1)
+                c->sg_mats |= 1u << i;
+        }
+        int rc = ensure(c, c->sg_acc, sizeof(SurrogateAcc));
+        if (rc) return rc;
+        CK(cudaMemsetAsync(c->sg_acc.p, 0, sizeof(SurrogateAcc), c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    return MPM_OK;
+}
+
+int mpm_harvest_begin(mpm_ctx* c, float* d_rows, int64_t cap, uint32_t mat_mask, double band) {
+    if (!c) return MPM_ERR_ARG;
+    if (!d_rows || cap < 1 || !(band >= 0.0)) return fail(c, MPM_ERR_ARG, "harvest needs rows, cap >= 1, band >= 0");
+    int rc = ensure(c, c->hv_count, 64);
+    if (rc) return rc;
+    CK(cudaMemsetAsync(c->hv_count.p, 0, 4, c->stream));
+    c->hv_on = 1;
+    c->hv_rows = d_rows;
+    c->hv_cap = cap;
+    c->hv_mats = mat_mask;
+    c->hv_band = (float)band;
+    return MPM_OK;
+}
+
+int mpm_harvest_end(mpm_ctx* c, int64_t* rows) {
+    if (!c || !rows) return MPM_ERR_ARG;
+    *rows = 0;
+    if (!c->hv_on) return MPM_OK;
+    unsigned h = 0;
+    CK(cudaMemcpyAsync(&h, c->hv_count.p, 4, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    *rows = (int64_t)h;
+    c->hv_on = 0;
+    c->hv_rows = nullptr;
+    c->hv_cap = 0;
+    return MPM_OK;
+}
+
+int mpm_surrogate_stats_read(mpm_ctx* c, mpm_surrogate_stats* out, int reset) {
+    if (!c || !out) return MPM_ERR_ARG;
+    memset(out, 0, sizeof(*out));
+    if (!c->sg_acc.p) return MPM_OK;
+    SurrogateAcc h;
+    CK(cudaMemcpyAsync(&h, c->sg_acc.p, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    out->queued = (int64_t)h.queued;
+    out->band = (int64_t)h.band;
+    out->rechecked = (int64_t)h.rechecked;
+    out->recheck_rms = h.rechecked ? std::sqrt(h.sq_err / (double)h.rechecked) : 0.0;
+    out->recheck_max = h.max_err;
+    if (reset) {
+        CK(cudaMemsetAsync(c->sg_acc.p, 0, sizeof(SurrogateAcc), c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    }
     return MPM_OK;
 }
 

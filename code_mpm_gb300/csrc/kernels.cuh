@@ -20,6 +20,7 @@
 
 #include "common.cuh"
 #include "physics.cuh"
+#include "surrogate.cuh"
 
 namespace mpm {
 
@@ -709,7 +710,83 @@ struct StepArgs {
     double tv[3];
     int has_timeline;
     int contact;
+    // return-map network (FP32 form): materials it stands in for (bit per
+    // material index), the fallback half-width (fraction of k0), the queue
+    int sg_on;
+    unsigned sg_mats;
+    float sg_band;
+    SurrogateQueue q;
+    SurrogateAcc* sg_acc;
+    // harvesting of return-map inputs (either form)
+    int hv_on;
+    unsigned hv_mats;
+    float hv_band;
+    float* hv_rows;
+    unsigned* hv_count;
+    long long hv_cap;
 };
+
+// Apply a constitutive increment o to particle p (stress, plastic strain,
+// back stress, energies; …MPLocks.cpp:246-270, contact …_Contact.cpp:486-525).
+// The step's energy increments are summed in the form's type and added once
+// to the FP64 energy accumulators.
+template <typename T>
+__device__ __forceinline__ void apply_increment(const PView<T>& P, long long p, const T sig[6], const T e[6],
+                                                const CrOut<T>& o, T V, T R, int contact, double dt) {
+    const long long np = P.n;
+    T dEs = 0, dEp = 0;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        T sn = sig[k] + o.dsig[k];
+        P.stress[k * np + p] = sn;
+        P.eps_p[k * np + p] += o.deps_p[k];
+        if (!contact) {
+            T mid = sn - (T)0.5 * o.dsig[k];
+            dEs += mid * e[k] * V;
+            dEp += mid * o.deps_p[k] * V;
+        } else {
+            dEs += sn * e[k] * V;
+            dEp += sn * o.deps_p[k] * V;
+        }
+    }
+    double es = P.e_strain[p] + fps_f2d_form(dEs);
+    P.e_strain[p] = es;
+    if (!contact) {
+        P.e_strain_ti[p] += es * dt;
+        if (es > P.e_strain_max[p]) P.e_strain_max[p] = es;
+    }
+    P.e_plastic[p] += fps_f2d_form(dEp);
+    P.backstress[p] = R + o.dR;
+}
+
+// Trial yield function of the von Mises hardening map (…_VonMisesHardening.cpp:20-46):
+// sqrt(J2) of the elastic trial stress minus the radius k0 + R/sqrt 2.
+template <typename T>
+__device__ __forceinline__ T vmh_trial(const MatConst& m, T R, const T sig[6], const T e[6]) {
+    T d[6];
+    trial_increment<T>(m, e, d);
+    T tr[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) tr[i] = sig[i] + d[i];
+    const T a01 = tr[0] - tr[1], a12 = tr[1] - tr[2], a20 = tr[2] - tr[0];
+    T J2 = (T)(1.0 / 6.0) * a01 * a01;
+    J2 += (T)(1.0 / 6.0) * a12 * a12;
+    J2 += (T)(1.0 / 6.0) * a20 * a20;
+    J2 += tr[3] * tr[3];
+    J2 += tr[4] * tr[4];
+    J2 += tr[5] * tr[5];
+    return sqrt(J2) - (form_const<T>(m.k0, m.fk0) + R * (T)0.70710678118654752440);
+}
+
+// warp-aggregated increment of a device counter; returns this lane's slot
+__device__ __forceinline__ unsigned warp_slot(unsigned* counter) {
+    const unsigned m = __activemask();
+    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(counter, (unsigned)__popc(m));
+    base = __shfl_sync(m, base, leader);
+    return base + __popc(m & ((1u << lane) - 1u));
+}
 
 // ---------------------------------------------------------------------------
 // G2P pass 2 + constitutive update + platen (G2P_P2_SmallStrain,
@@ -827,7 +904,33 @@ __global__ void __launch_bounds__(512) k_pass2(PView<T> P, NView<T> nd, Geom g, 
             for (int k = 0; k < 6; ++k) sig[k] = P.stress[k * np + p];
             T R = P.backstress[p];
             CrOut<T> o;
-            cr_increment<T>(M, R, sig, e, o);
+            // the network takes clearly plastic trial states of the materials it
+            // was trained for; the band near the surface and elastic states stay exact
+            bool queued = false;
+            if constexpr (sizeof(T) == 4) {
+                if (a.sg_on && mi < 32 && ((a.sg_mats >> mi) & 1u)) {
+                    const float f = vmh_trial<float>(M, R, sig, e);
+                    queued = f >= a.sg_band * M.fk0;
+                    if (!queued && f > 0.0f) {
+                        const unsigned m = __activemask();
+                        if ((threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(&a.sg_acc->band, (unsigned long long)__popc(m));
+                    }
+                }
+            }
+            if (a.hv_on && mi < 32 && ((a.hv_mats >> mi) & 1u) && M.type == 4 &&
+                vmh_trial<T>(M, R, sig, e) >= (T)a.hv_band * form_const<T>(M.k0, M.fk0)) {
+                const unsigned slot = warp_slot(a.hv_count);
+                if (slot < (unsigned long long)a.hv_cap) {
+                    float* hr = a.hv_rows + (long long)slot * 13;
+#pragma unroll
+                    for (int k = 0; k < 6; ++k) {
+                        hr[k] = (float)sig[k];
+                        hr[7 + k] = (float)e[k];
+                    }
+                    hr[6] = (float)R;
+                }
+            }
+            if (!queued) cr_increment<T>(M, R, sig, e, o);
             T V;
             if (!a.contact) {
 #pragma unroll
@@ -841,31 +944,24 @@ __global__ void __launch_bounds__(512) k_pass2(PView<T> P, NView<T> nd, Geom g, 
 #pragma unroll
                 for (int k = 0; k < 6; ++k) P.strain_rate[k * np + p] = e[k] / dt;
             }
-            // the step's energy increments are summed in the form's type and
-            // added once to the FP64 energy accumulators
-            T dEs = 0, dEp = 0;
+            if (queued) {
+                if constexpr (sizeof(T) == 4) {
+                    const unsigned slot = warp_slot(a.q.count);
+                    if (slot < (unsigned long long)a.q.cap) {
+                        float* qi = a.q.in + (long long)slot * 13;
 #pragma unroll
-            for (int k = 0; k < 6; ++k) {
-                T sn = sig[k] + o.dsig[k];
-                P.stress[k * np + p] = sn;
-                P.eps_p[k * np + p] += o.deps_p[k];
-                if (!a.contact) {
-                    T mid = sn - (T)0.5 * o.dsig[k];
-                    dEs += mid * e[k] * V;
-                    dEp += mid * o.deps_p[k] * V;
-                } else {
-                    dEs += sn * e[k] * V;
-                    dEp += sn * o.deps_p[k] * V;
+                        for (int k = 0; k < 6; ++k) {
+                            qi[k] = sig[k];
+                            qi[7 + k] = e[k];
+                        }
+                        qi[6] = R;
+                        a.q.vol[slot] = V;
+                        a.q.pidx[slot] = (unsigned)p;
+                    }
                 }
+            } else {
+                apply_increment<T>(P, p, sig, e, o, V, R, a.contact, a.dt);
             }
-            double es = P.e_strain[p] + fps_f2d_form(dEs);
-            P.e_strain[p] = es;
-            if (!a.contact) {
-                P.e_strain_ti[p] += es * a.dt;
-                if (es > P.e_strain_max[p]) P.e_strain_max[p] = es;
-            }
-            P.e_plastic[p] += fps_f2d_form(dEp);
-            P.backstress[p] = R + o.dR;
         } else if (!a.contact) {
             atomicOr(err, ERR_BAD_MATERIAL);
         }
@@ -1352,6 +1448,62 @@ __global__ void __launch_bounds__(256) k_monitor_force(NView<T> nd, double* acc)
     for (int c = 0; c < 3; ++c) {
         for (int off = 16; off > 0; off >>= 1) f[c] += __shfl_down_sync(FULL_MASK, f[c], off);
         if ((threadIdx.x & 31) == 0) atomicAdd(&acc[17 + c], f[c]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Return-map network, finishing pass: apply the network's stress increment
+// and dR to each queued particle (dR kept non-negative, as the hardening law
+// gives), with the plastic strain increment recovered as de - C^-1 dsigma
+// (the compliance of …_VonMisesHardening.cpp:64-71), and re-check a hashed
+// fraction of the particles against the exact map (the error is recorded;
+// the network's result is kept).
+// ---------------------------------------------------------------------------
+static __global__ void k_sg_finish(PView<float> P, SurrogateQueue q, MatConst M, int contact, double dt, float inv_yield,
+                            float recheck, unsigned long long step, SurrogateAcc* acc) {
+    const unsigned cnt = (unsigned)min((unsigned long long)*q.count, (unsigned long long)q.cap);
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&acc->queued, (unsigned long long)cnt);
+    const unsigned thr = (unsigned)(recheck * 4294967296.0f);
+    for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < cnt; s += gridDim.x * blockDim.x) {
+        const long long p = q.pidx[s];
+        const float* qi = q.in + (long long)s * 13;
+        const float* qo = q.out + (long long)s * 7;
+        float sig[6], e[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            sig[k] = qi[k];
+            e[k] = qi[7 + k];
+        }
+        const float R = qi[6];
+        CrOut<float> o;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) o.dsig[k] = qo[k];
+        o.dR = fmaxf(qo[6], 0.0f);
+        const float iE = M.finv_E, nE = M.fnu_over_E, iG = M.finv_G;
+        o.deps_p[0] = e[0] - (o.dsig[0] * iE - o.dsig[1] * nE - o.dsig[2] * nE);
+        o.deps_p[1] = e[1] - (o.dsig[1] * iE - o.dsig[0] * nE - o.dsig[2] * nE);
+        o.deps_p[2] = e[2] - (o.dsig[2] * iE - o.dsig[0] * nE - o.dsig[1] * nE);
+        o.deps_p[3] = e[3] - o.dsig[3] * iG;
+        o.deps_p[4] = e[4] - o.dsig[4] * iG;
+        o.deps_p[5] = e[5] - o.dsig[5] * iG;
+        // recheck: a hash of (step, particle) below the fraction
+        unsigned long long h = (step + 1) * 0x9e3779b97f4a7c15ULL ^ ((unsigned long long)p * 0xbf58476d1ce4e5b9ULL);
+        h = (h ^ (h >> 31)) * 0x94d049bb133111ebULL;
+        if ((unsigned)(h >> 32) < thr) {
+            CrOut<float> x;
+            cr_increment<float>(M, R, sig, e, x);
+            float sq = 0.0f, mx = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                const float d = fabsf(o.dsig[k] - x.dsig[k]) * inv_yield;
+                sq += d * d;
+                mx = fmaxf(mx, d);
+            }
+            atomicAdd(&acc->rechecked, 1ULL);
+            atomicAdd(&acc->sq_err, (double)sq / 6.0);
+            atomicMax(reinterpret_cast<unsigned long long*>(&acc->max_err), (unsigned long long)__double_as_longlong((double)mx));
+        }
+        apply_increment<float>(P, p, sig, e, o, q.vol[s], R, contact, dt);
     }
 }
 

@@ -1,0 +1,1223 @@
+// Learned von Mises hardening return map: training samples from the exact
+// FP64 map, FP32 training kernels (forward, backward, Adam), and the BF16
+// tcgen05 inference kernel.  The network replaces
+// ConstitutiveRelation::calculateIncrement_VonMisesHardening
+// (ConstitutiveRelation_calculateIncrement_VonMisesHardening.cpp:4-92) for
+// clearly plastic trial states; it is this library's addition.
+//
+// Network: x (13 inputs, padded to 16) -> 128 -> 128 -> 128 (SiLU) -> 8 (7
+// used).  Inputs are scaled to O(1): stress and R by 1/yield, the strain
+// increment by 1/deps_sigma; outputs are standardised by the training set's
+// mean and standard deviation.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <vector>
+
+#include "common.cuh"
+#include "mpm_surrogate.h"
+#include "physics.cuh"
+#include "surrogate.cuh"
+
+namespace mpm {
+namespace net {
+
+constexpr int IN = 16, NIN = 13, HID = 128, OUT = 8, NOUT = 7;
+constexpr long long OW1 = 0, OB1 = OW1 + HID * IN, OW2 = OB1 + HID, OB2 = OW2 + HID * HID, OW3 = OB2 + HID,
+                    OB3 = OW3 + HID * HID, OW4 = OB3 + HID, OB4 = OW4 + OUT * HID, NPARAM = OB4 + OUT;
+
+#define NCK(x)                                      \
+    do {                                            \
+        cudaError_t e_ = (x);                       \
+        if (e_ != cudaSuccess) {                    \
+            cudaGetLastError();                     \
+            return MPM_ERR_CUDA;                    \
+        }                                           \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// counter-based random numbers (splitmix64 finaliser of (seed, sample, draw))
+// ---------------------------------------------------------------------------
+__host__ __device__ inline uint64_t mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    return z ^ (z >> 31);
+}
+__device__ inline float uni(uint64_t seed, uint64_t i, uint32_t j) {
+    uint64_t h = mix64(seed + 0x9e3779b97f4a7c15ULL * (i * 64 + j + 1));
+    return ((float)(h >> 40) + 0.5f) * (1.0f / 16777216.0f);  // (0, 1)
+}
+__device__ inline float gauss(uint64_t seed, uint64_t i, uint32_t j) {
+    float u1 = uni(seed, i, 2 * j + 32), u2 = uni(seed, i, 2 * j + 33);
+    return sqrtf(-2.0f * logf(u1)) * cospif(2.0f * u2);
+}
+
+struct SampleCfg {
+    double yield, range, epmax, dsig, C0, C1;
+    uint64_t seed;
+    int sampling;
+};
+
+// One sample: prior stress U(+-range yield), R from the closed form of the
+// hardening law for a uniform equivalent plastic strain
+// (R = sqrt(2/3) C1 (1 - exp(-C0 epbar)), the solution of dR = C0 (sqrt(2/3)
+// C1 - R) depbar), strain increment N(0, dsig); target = the exact FP64
+// return map (cr_increment<double>).  x: normalised inputs (16, zero padded),
+// raw: physical inputs (13), t: physical outputs (7) and f_trial / k0.
+__device__ void label_sample(long long i, const double sig[6], double R, const double e[6], const SampleCfg& sc,
+                             const MatConst& M, float* __restrict__ x, float* __restrict__ t);
+
+__global__ void k_generate(long long n, long long i0, SampleCfg sc, MatConst M, float* __restrict__ x,
+                           float* __restrict__ t) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint64_t gi = (uint64_t)(i0 + i);
+    double sig[6], e[6];
+    const double ep = uni(sc.seed, gi, 6) * sc.epmax;
+    const double R = sqrt(2.0 / 3.0) * sc.C1 * (1.0 - exp(-sc.C0 * ep));
+    if (sc.sampling == 0) {
+        for (int c = 0; c < 6; ++c) sig[c] = (2.0 * uni(sc.seed, gi, c) - 1.0) * sc.range * sc.yield;
+    } else {
+        // a random deviator scaled to sqrt J2 = U(0.85, 1) (k0 + R/sqrt 2), plus a hydrostatic part
+        double d[6];
+        for (int c = 0; c < 6; ++c) d[c] = gauss(sc.seed, gi, 8 + c);
+        const double h = (d[0] + d[1] + d[2]) / 3.0;
+        for (int c = 0; c < 3; ++c) d[c] -= h;
+        const double j2 = ((d[0] - d[1]) * (d[0] - d[1]) + (d[1] - d[2]) * (d[1] - d[2]) + (d[2] - d[0]) * (d[2] - d[0])) /
+                              6.0 + d[3] * d[3] + d[4] * d[4] + d[5] * d[5];
+        const double rad = M.k0 + R * 0.70710678118654752440;
+        const double sc2 = (0.85 + 0.15 * uni(sc.seed, gi, 7)) * rad / sqrt(j2);
+        const double p = (2.0 * uni(sc.seed, gi, 5) - 1.0) * sc.yield;
+        for (int c = 0; c < 6; ++c) sig[c] = d[c] * sc2 + (c < 3 ? p : 0.0);
+    }
+    for (int c = 0; c < 6; ++c) e[c] = gauss(sc.seed, gi, c) * sc.dsig;
+    label_sample(i, sig, R, e, sc, M, x, t);
+}
+
+// Samples given as physical input rows (e.g. harvested from a run of the
+// plain method): labelled by the exact FP64 map like generated ones.
+__global__ void k_label_rows(long long n, const float* __restrict__ in, SampleCfg sc, MatConst M,
+                             float* __restrict__ x, float* __restrict__ t) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double sig[6], e[6];
+    for (int c = 0; c < 6; ++c) {
+        sig[c] = in[i * NIN + c];
+        e[c] = in[i * NIN + 7 + c];
+    }
+    label_sample(i, sig, (double)in[i * NIN + 6], e, sc, M, x, t);
+}
+
+// normalised inputs x[i] (16) and targets t[i] (plastic correction, dR, f_trial / k0)
+__device__ void label_sample(long long i, const double sig[6], double R, const double e[6], const SampleCfg& sc,
+                             const MatConst& M, float* __restrict__ x, float* __restrict__ t) {
+    CrOut<double> o;
+    cr_increment<double>(M, R, sig, e, o);
+    // trial yield function (…_VonMisesHardening.cpp:35-46)
+    double dtr[6];
+    trial_increment<double>(M, e, dtr);
+    double tr[6];
+    for (int c = 0; c < 6; ++c) tr[c] = sig[c] + dtr[c];
+    const double a01 = tr[0] - tr[1], a12 = tr[1] - tr[2], a20 = tr[2] - tr[0];
+    const double J2 = (a01 * a01 + a12 * a12 + a20 * a20) / 6.0 + tr[3] * tr[3] + tr[4] * tr[4] + tr[5] * tr[5];
+    const double f = sqrt(J2) - (M.k0 + R * 0.70710678118654752440);
+    float* xi = x + i * IN;
+    for (int c = 0; c < 6; ++c) {
+        xi[c] = (float)(sig[c] / sc.yield);
+        xi[7 + c] = (float)(e[c] / sc.dsig);
+    }
+    xi[6] = (float)(R / sc.yield);
+    xi[13] = xi[14] = xi[15] = 0.0f;
+    // targets: the plastic correction dsigma - D de (the kernels add D de back)
+    float* ti = t + i * OUT;
+    for (int c = 0; c < 6; ++c) ti[c] = (float)(o.dsig[c] - dtr[c]);
+    ti[6] = (float)o.dR;
+    ti[7] = (float)(f / M.k0);
+}
+
+// per-output sums of the targets (mean and standard deviation)
+__global__ void k_moments(long long n, const float* __restrict__ t, double* __restrict__ acc) {
+    __shared__ double s[2 * NOUT];
+    if (threadIdx.x < 2 * NOUT) s[threadIdx.x] = 0.0;
+    __syncthreads();
+    double a[NOUT] = {}, b[NOUT] = {};
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        for (int c = 0; c < NOUT; ++c) {
+            double v = t[i * OUT + c];
+            a[c] += v;
+            b[c] += v * v;
+        }
+    for (int c = 0; c < NOUT; ++c) {
+        atomicAdd(&s[c], a[c]);
+        atomicAdd(&s[NOUT + c], b[c]);
+    }
+    __syncthreads();
+    if (threadIdx.x < 2 * NOUT) atomicAdd(&acc[threadIdx.x], s[threadIdx.x]);
+}
+
+__global__ void k_normalise_targets(long long n, const float* __restrict__ t, const float* __restrict__ shift,
+                                    const float* __restrict__ inv_scale, float* __restrict__ tn) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int c = 0; c < NOUT; ++c) tn[i * OUT + c] = (t[i * OUT + c] - shift[c]) * inv_scale[c];
+    tn[i * OUT + 7] = 0.0f;
+}
+
+// ---------------------------------------------------------------------------
+// FP32 GEMM for training: C[M x N] = op(A)[M x K] op(B)[K x N], 64 x 64 tiles,
+// 16-deep k slices, 4 x 4 outputs per thread.  op(A) = A (row-major, lda) or
+// A^T (A stored K x M); op(B) = B (row-major K x N) or B^T (B stored N x K,
+// the layer weights W[out][in]).  Epilogues: store (+bias), bias + SiLU
+// (keeps the pre-activation in aux), times SiLU'(aux) (backward), and atomic
+// accumulation of split-K partial sums (weight gradients; blockIdx.z picks
+// the k range).
+// ---------------------------------------------------------------------------
+enum { EPI_STORE = 0, EPI_SILU = 1, EPI_DSILU = 2, EPI_ATOMIC = 3 };
+
+__device__ __forceinline__ float silu_f(float z) { return z / (1.0f + __expf(-z)); }
+__device__ __forceinline__ float dsilu_f(float z) {
+    const float s = 1.0f / (1.0f + __expf(-z));
+    return s * (1.0f + z * (1.0f - s));
+}
+
+template <bool TA, bool TB, int EPI>
+__global__ void __launch_bounds__(256) k_sgemm(int M, int N, int K, const float* __restrict__ A, int lda,
+                                               const float* __restrict__ B, int ldb, float* __restrict__ C, int ldc,
+                                               const float* __restrict__ bias, float* __restrict__ aux, int kchunk) {
+    __shared__ __align__(16) float As[16][68];
+    __shared__ __align__(16) float Bs[16][68];
+    const int tid = threadIdx.x;
+    const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
+    const int kbeg = blockIdx.z * kchunk, kend = min(K, kbeg + kchunk);
+    const int tm = (tid >> 4) * 4, tn = (tid & 15) * 4;
+    float acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.0f;
+    for (int k0 = kbeg; k0 < kend; k0 += 16) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int e = tid + r * 256;
+            int mm, kk;
+            if (!TA) {
+                mm = e >> 4;
+                kk = e & 15;
+            } else {
+                kk = e >> 6;
+                mm = e & 63;
+            }
+            const int gm = m0 + mm, gk = k0 + kk;
+            float v = 0.0f;
+            if (gm < M && gk < kend) v = TA ? A[(long long)gk * lda + gm] : A[(long long)gm * lda + gk];
+            As[kk][mm] = v;
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int e = tid + r * 256;
+            int kk, nn;
+            if (!TB) {
+                kk = e >> 6;
+                nn = e & 63;
+            } else {
+                nn = e >> 4;
+                kk = e & 15;
+            }
+            const int gn = n0 + nn, gk = k0 + kk;
+            float v = 0.0f;
+            if (gn < N && gk < kend) v = TB ? B[(long long)gn * ldb + gk] : B[(long long)gk * ldb + gn];
+            Bs[kk][nn] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < 16; ++kk) {
+            const float4 a = *reinterpret_cast<const float4*>(&As[kk][tm]);
+            const float4 b = *reinterpret_cast<const float4*>(&Bs[kk][tn]);
+            const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int m = m0 + tm + i, n = n0 + tn + j;
+            if (m >= M || n >= N) continue;
+            float v = acc[i][j];
+            const long long o = (long long)m * ldc + n;
+            if constexpr (EPI == EPI_STORE) {
+                if (bias) v += bias[n];
+                C[o] = v;
+            } else if constexpr (EPI == EPI_SILU) {
+                v += bias[n];
+                aux[o] = v;
+                C[o] = silu_f(v);
+            } else if constexpr (EPI == EPI_DSILU) {
+                C[o] = v * dsilu_f(aux[o]);
+            } else {
+                atomicAdd(&C[o], v);
+            }
+        }
+}
+
+template <bool TA, bool TB, int EPI>
+static void sgemm(cudaStream_t s, int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C,
+                  int ldc, const float* bias = nullptr, float* aux = nullptr, int splits = 1) {
+    const int kchunk = ((K + splits - 1) / splits + 15) / 16 * 16;
+    splits = (K + kchunk - 1) / kchunk;
+    dim3 grid((N + 63) / 64, (M + 63) / 64, splits);
+    k_sgemm<TA, TB, EPI><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, bias, aux, kchunk);
+}
+
+// column sums of an n x N row-major matrix into g (atomic; N divides 256)
+template <int N>
+__global__ void k_colsum(long long n, const float* __restrict__ d, float* __restrict__ g) {
+    static_assert(256 % N == 0, "N must divide 256");
+    constexpr int RPI = 256 / N;
+    const int col = threadIdx.x % N, r0 = threadIdx.x / N;
+    const long long base = blockIdx.x * 1024LL;
+    float s = 0.0f;
+    for (int r = r0; r < 1024; r += RPI) {
+        const long long i = base + r;
+        if (i < n) s += d[i * N + col];
+    }
+    atomicAdd(&g[col], s);
+}
+
+// loss (mean over samples and the 7 used outputs) and its gradient
+__global__ void k_loss(long long n, const float* __restrict__ y, const float* __restrict__ t, float* __restrict__ dy,
+                       double* __restrict__ loss) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    double l = 0.0;
+    if (i < n) {
+        const float sc = 2.0f / (float)(n * NOUT);
+        for (int c = 0; c < OUT; ++c) {
+            const float d = c < NOUT ? y[i * OUT + c] - t[i * OUT + c] : 0.0f;
+            dy[i * OUT + c] = sc * d;
+            l += (double)d * d;
+        }
+    }
+    for (int o = 16; o; o >>= 1) l += __shfl_down_sync(0xffffffffu, l, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(loss, l / (double)(n * NOUT));
+}
+
+__global__ void k_adam(long long n, float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v, float lr, float b1, float b2, float eps, float c1, float c2) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+// rows of the training set in a pseudo-random order: row j of the epoch is
+// (a j + c) mod n with a coprime to n (a full-period affine permutation)
+__global__ void k_gather(long long n, const float* __restrict__ x, const float* __restrict__ t, long long a,
+                         long long c, long long j0, int rows, float* __restrict__ xb, float* __restrict__ tb) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    const unsigned long long j = (unsigned long long)(j0 + r);
+    const long long i = (long long)(((unsigned __int128)a * j + (unsigned long long)c) % (unsigned long long)n);
+    const float4* xs = reinterpret_cast<const float4*>(x + i * IN);
+    float4* xd = reinterpret_cast<float4*>(xb + (long long)r * IN);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) xd[k] = xs[k];
+    const float4* ts = reinterpret_cast<const float4*>(t + i * OUT);
+    float4* td = reinterpret_cast<float4*>(tb + (long long)r * OUT);
+    td[0] = ts[0];
+    td[1] = ts[1];
+}
+
+// validation errors in physical units: sums of squared dstress/yield errors
+// (all samples, and those outside the fallback band), max outside the band,
+// squared dR/yield errors
+__global__ void k_val_errors(long long n, const float* __restrict__ yn, const float* __restrict__ t,
+                             const float* __restrict__ shift, const float* __restrict__ scale, float inv_yield,
+                             float band, double* __restrict__ acc, unsigned* __restrict__ maxbits) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    double s_all = 0, s_out = 0, s_r = 0, cnt_out = 0;
+    float mx = 0.0f;
+    if (i < n) {
+        const bool outside = fabsf(t[i * OUT + 7]) >= band;
+        for (int c = 0; c < 6; ++c) {
+            const float y = yn[i * OUT + c] * scale[c] + shift[c];
+            const float d = (y - t[i * OUT + c]) * inv_yield;
+            s_all += (double)d * d;
+            if (outside) {
+                s_out += (double)d * d;
+                mx = fmaxf(mx, fabsf(d));
+            }
+        }
+        const float yr = yn[i * OUT + 6] * scale[6] + shift[6];
+        const float dr = (yr - t[i * OUT + 6]) * inv_yield;
+        s_r = (double)dr * dr;
+        cnt_out = outside ? 1.0 : 0.0;
+    }
+    for (int o = 16; o; o >>= 1) {
+        s_all += __shfl_down_sync(0xffffffffu, s_all, o);
+        s_out += __shfl_down_sync(0xffffffffu, s_out, o);
+        s_r += __shfl_down_sync(0xffffffffu, s_r, o);
+        cnt_out += __shfl_down_sync(0xffffffffu, cnt_out, o);
+        mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&acc[0], s_all);
+        atomicAdd(&acc[1], s_out);
+        atomicAdd(&acc[2], s_r);
+        atomicAdd(&acc[3], cnt_out);
+        atomicMax(maxbits, __float_as_uint(mx));
+    }
+}
+
+// physical inputs (n x 13) -> normalised rows (n x 16)
+__global__ void k_norm_inputs(long long n, const float* __restrict__ in, const float* __restrict__ inv_scale,
+                              float* __restrict__ x) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int c = 0; c < NIN; ++c) x[i * IN + c] = in[i * NIN + c] * inv_scale[c];
+    x[i * IN + 13] = x[i * IN + 14] = x[i * IN + 15] = 0.0f;
+}
+
+// the elastic predictor D de of physical input row `in` (trial_increment, FP32)
+__device__ __forceinline__ void elastic_predictor(const MatConst& M, const float* in, float d[6]) {
+    float e[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) e[c] = in[7 + c];
+    trial_increment<float>(M, e, d);
+}
+
+// normalised outputs (n x 8) -> physical (n x 7): correction + D de, dR
+__global__ void k_denorm_outputs(long long n, const float* __restrict__ yn, const float* __restrict__ scale,
+                                 const float* __restrict__ shift, const float* __restrict__ in, MatConst M,
+                                 float* __restrict__ out) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float d[6];
+    elastic_predictor(M, in + i * NIN, d);
+    for (int c = 0; c < NOUT; ++c) out[i * NOUT + c] = yn[i * OUT + c] * scale[c] + shift[c] + (c < 6 ? d[c] : 0.0f);
+}
+
+// the exact return map in FP32 on physical rows: the method without the network
+__global__ void k_exact_fp32(long long n, const float* __restrict__ in, MatConst M, float* __restrict__ out) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float sig[6], e[6];
+    for (int c = 0; c < 6; ++c) {
+        sig[c] = in[i * NIN + c];
+        e[c] = in[i * NIN + 7 + c];
+    }
+    CrOut<float> o;
+    cr_increment<float>(M, in[i * NIN + 6], sig, e, o);
+    for (int c = 0; c < 6; ++c) out[i * NOUT + c] = o.dsig[c];
+    out[i * NOUT + 6] = o.dR;
+}
+
+// ---------------------------------------------------------------------------
+// BF16 tcgen05 inference.  One CTA of 128 threads (4 warps) per SM-slot loops
+// over tiles of 128 samples.  Per layer, thread 0 issues tcgen05.mma
+// (kind::f16, BF16 x BF16 -> FP32, M = 128) with the activations (A, M x K)
+// and the weights (B = W[out][in], N x K) in shared memory, both K-major
+// without swizzle; the accumulator D (128 lanes x N columns FP32) sits in
+// tensor memory.  tcgen05.commit signals an mbarrier; each warp then reads
+// its 32 lanes (tcgen05.ld 32x32b: thread t of warp w <-> lane 32w + t =
+// sample), adds the bias, applies SiLU, rounds to BF16 and writes the next
+// layer's A operand.
+//
+// Shared-memory operand layout (K-major, no swizzle): 8-row x 16-byte core
+// matrices; element (r, k) of an R-row operand at byte
+//   ((k / 8) * (R / 8) + r / 8) * 128 + (r % 8) * 16 + (k % 8) * 2,
+// so core matrices adjacent in K are R/8 * 128 bytes apart (the leading
+// byte offset) and 8-row groups 128 bytes apart (the stride byte offset).
+// ---------------------------------------------------------------------------
+__host__ __device__ constexpr uint32_t kmajor_off(int r, int k, int R) {
+    return (uint32_t)(((k >> 3) * (R >> 3) + (r >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+// shared-memory matrix descriptor: start address, leading and stride byte
+// offsets (>> 4), descriptor version 1 (bits 46-47), no swizzle (bits 61-63 = 0)
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// instruction descriptor, kind::f16: D FP32 (bits 4-5 = 1), A and B BF16
+// (bits 7-9, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits
+// 17-22, M >> 4 at bits 24-28
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// shared-memory image of the packed weights (bytes)
+constexpr uint32_t SW1 = 0, SW2 = SW1 + HID * IN * 2, SW3 = SW2 + HID * HID * 2, SW4 = SW3 + HID * HID * 2,
+                   WBYTES = SW4 + 16 * HID * 2;  // W4 padded to 16 rows
+// biases (FP32): b1, b2, b3 (128 each), b4 (16)
+constexpr uint32_t NBIAS = 3 * HID + 16;
+// kernel shared memory: weights, bias, A0 (128 x 16), A1 (128 x 128), mbarrier, TMEM address
+constexpr uint32_t S_BIAS = WBYTES, S_A0 = (S_BIAS + NBIAS * 4 + 1023) / 1024 * 1024, S_A1 = S_A0 + 128 * IN * 2,
+                   S_BAR = S_A1 + 128 * HID * 2, S_TADDR = S_BAR + 8, SMEM_TC = S_TADDR + 8 + 1024;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+// bounded wait on an mbarrier phase; false (and the error bit) on timeout
+__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity, unsigned* err) {
+    for (int it = 0; it < (1 << 22); ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    atomicOr(err, 4u);
+    return false;
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float v[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ float tanh_approx(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+// SiLU z * sigmoid(z) with sigmoid(z) = (1 + tanh(z/2)) / 2
+__device__ __forceinline__ float silu_tc(float z) { return z * fmaf(0.5f, tanh_approx(0.5f * z), 0.5f); }
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+    __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t*>(&h);
+}
+
+// issue one layer: D = A (128 x K) . W^T (W: N x K), K in steps of 16
+__device__ __forceinline__ void issue_layer(uint32_t tmem, uint32_t a_addr, int K, uint32_t w_addr, int N) {
+    const uint32_t lbo_a = 128 / 8 * 128, lbo_b = (uint32_t)(N / 8) * 128;
+    const uint32_t id = idesc_bf16(128, N);
+    for (int k = 0; k < K; k += 16) {
+        const uint64_t a = smem_desc(a_addr + (uint32_t)(k / 8) * lbo_a, lbo_a, 128);
+        const uint64_t b = smem_desc(w_addr + (uint32_t)(k / 8) * lbo_b, lbo_b, 128);
+        mma_bf16(tmem, a, b, id, k > 0 ? 1u : 0u);
+    }
+}
+
+// hidden-layer epilogue: thread t reads sample t's 128 accumulators, adds
+// the bias, applies SiLU, and writes BF16 row t of the next A operand
+__device__ __forceinline__ void hidden_epilogue(uint32_t taddr_row, const float* bias, unsigned char* a1) {
+    const int r = threadIdx.x;
+#pragma unroll 1
+    for (int c0 = 0; c0 < HID; c0 += 32) {
+        float v[32];
+        tmem_ld32(taddr_row + (uint32_t)c0, v);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            uint4 pk;
+            const int k = c0 + 8 * q;
+            pk.x = pack_bf16(silu_tc(v[8 * q + 0] + bias[k + 0]), silu_tc(v[8 * q + 1] + bias[k + 1]));
+            pk.y = pack_bf16(silu_tc(v[8 * q + 2] + bias[k + 2]), silu_tc(v[8 * q + 3] + bias[k + 3]));
+            pk.z = pack_bf16(silu_tc(v[8 * q + 4] + bias[k + 4]), silu_tc(v[8 * q + 5] + bias[k + 5]));
+            pk.w = pack_bf16(silu_tc(v[8 * q + 6] + bias[k + 6]), silu_tc(v[8 * q + 7] + bias[k + 7]));
+            *reinterpret_cast<uint4*>(a1 + kmajor_off(r, k, 128)) = pk;
+        }
+    }
+}
+
+struct TcArgs {
+    const uint4* wpack;        // WBYTES of packed BF16 weights (the shared-memory image)
+    const float* bias;         // NBIAS
+    float in_inv_scale[NIN];
+    float out_scale[NOUT], out_shift[NOUT];
+    const float* in;           // n x 13 physical
+    float* out;                // n x 7 physical
+    const unsigned* count;     // device sample count (queue), or null
+    long long n;               // sample count (or queue capacity)
+    unsigned* err;
+    MatConst mat;              // for the elastic predictor D de
+};
+
+__global__ void __launch_bounds__(128, 1) k_mlp_tc(TcArgs a) {
+    extern __shared__ __align__(1024) unsigned char sm[];
+    const int t = threadIdx.x, w = t >> 5;
+    unsigned char* s = sm + ((1024 - (smem_u32(sm) & 1023u)) & 1023u);  // 1024-byte aligned base
+    const uint32_t sbase = smem_u32(s);
+    // weights and biases into shared memory (once per CTA)
+    for (uint32_t i = t; i < WBYTES / 16; i += 128) reinterpret_cast<uint4*>(s)[i] = a.wpack[i];
+    float* bias = reinterpret_cast<float*>(s + S_BIAS);
+    for (uint32_t i = t; i < NBIAS; i += 128) bias[i] = a.bias[i];
+    uint32_t* taddr_slot = reinterpret_cast<uint32_t*>(s + S_TADDR);
+    const uint32_t bar = sbase + S_BAR;
+    if (t == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (w == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(smem_u32(taddr_slot))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *taddr_slot;
+    const uint32_t trow = tmem + ((uint32_t)(32 * w) << 16);  // this warp's lane quarter
+    const long long n = a.count ? (long long)min((unsigned long long)*a.count, (unsigned long long)a.n) : a.n;
+    const long long ntiles = (n + 127) / 128;
+    uint32_t phase = 0;
+    bool ok = true;
+    for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const long long i = tile * 128 + t;
+        // inputs -> A0 (128 x 16 BF16)
+        float x[16];
+#pragma unroll
+        for (int c = 0; c < 16; ++c) x[c] = 0.0f;
+        if (i < n) {
+#pragma unroll
+            for (int c = 0; c < NIN; ++c) x[c] = a.in[i * NIN + c] * a.in_inv_scale[c];
+        }
+        uint4 p0, p1;
+        p0.x = pack_bf16(x[0], x[1]);
+        p0.y = pack_bf16(x[2], x[3]);
+        p0.z = pack_bf16(x[4], x[5]);
+        p0.w = pack_bf16(x[6], x[7]);
+        p1.x = pack_bf16(x[8], x[9]);
+        p1.y = pack_bf16(x[10], x[11]);
+        p1.z = pack_bf16(x[12], x[13]);
+        p1.w = pack_bf16(x[14], x[15]);
+        *reinterpret_cast<uint4*>(s + S_A0 + kmajor_off(t, 0, 128)) = p0;
+        *reinterpret_cast<uint4*>(s + S_A0 + kmajor_off(t, 8, 128)) = p1;
+        for (int layer = 0; layer < 4 && ok; ++layer) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncthreads();
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            if (t == 0) {
+                if (layer == 0)
+                    issue_layer(tmem, sbase + S_A0, IN, sbase + SW1, HID);
+                else if (layer < 3)
+                    issue_layer(tmem, sbase + S_A1, HID, sbase + (layer == 1 ? SW2 : SW3), HID);
+                else
+                    issue_layer(tmem, sbase + S_A1, HID, sbase + SW4, 16);
+                mma_commit(bar);
+            }
+            // every thread decides alike, so no thread leaves a barrier the others reach
+            ok = __syncthreads_and(bar_wait(bar, phase, a.err) ? 1 : 0) != 0;
+            if (!ok) {
+                bar_wait(bar, phase, a.err);  // once more (bounded) for the MMAs in flight
+                break;
+            }
+            phase ^= 1u;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            if (layer < 3) {
+                hidden_epilogue(trow, bias + layer * HID, s + S_A1);
+            } else {
+                float v[16];
+                tmem_ld16(trow, v);
+                if (i < n) {
+                    float d[6];
+                    elastic_predictor(a.mat, a.in + i * NIN, d);
+#pragma unroll
+                    for (int c = 0; c < NOUT; ++c)
+                        a.out[i * NOUT + c] =
+                            (v[c] + bias[3 * HID + c]) * a.out_scale[c] + a.out_shift[c] + (c < 6 ? d[c] : 0.0f);
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (w == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem) : "memory");
+}
+
+}  // namespace net
+}  // namespace mpm
+
+using namespace mpm;
+using namespace mpm::net;
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+struct mpm_net {
+    mpm_net_config cfg;
+    MatConst mat;
+    int sm_count = 152;
+    float* p = nullptr;      // NPARAM master parameters
+    float* wpack = nullptr;  // packed BF16 weight image (WBYTES) + biases (NBIAS floats)
+    float* scratch = nullptr;
+    size_t scratch_bytes = 0;
+    unsigned* err = nullptr;
+    float in_inv_scale[NIN];
+    float out_scale[NOUT], out_shift[NOUT];
+    bool packed = false;
+};
+
+static MatConst make_mat(const mpm_net_config& c) {
+    MatConst k;
+    memset(&k, 0, sizeof(k));
+    const double E = c.E, nu = c.nu;
+    k.type = 4;
+    k.E = E;
+    k.nu = nu;
+    k.Y = c.yield;
+    k.C0 = c.C0;
+    k.C1 = c.C1;
+    k.C = E / (1.0 + nu) / (1.0 - 2.0 * nu);
+    k.one_m_nu = 1.0 - nu;
+    k.half_m_nu = 0.5 - nu;
+    k.G = 0.5 * E / (1.0 + nu);
+    k.k0 = c.yield / std::sqrt(3.0);
+    k.s23C1 = std::sqrt(2.0 / 3.0) * c.C1;
+    k.inv_E = 1.0 / E;
+    k.nu_over_E = nu / E;
+    k.inv_G = 1.0 / k.G;
+    set_float_constants(k);
+    return k;
+}
+
+static int ensure_scratch(mpm_net* net, size_t bytes) {
+    if (net->scratch_bytes >= bytes) return MPM_OK;
+    if (net->scratch) cudaFree(net->scratch);
+    net->scratch = nullptr;
+    net->scratch_bytes = 0;
+    if (cudaMalloc(&net->scratch, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return MPM_ERR_NOMEM;
+    }
+    net->scratch_bytes = bytes;
+    return MPM_OK;
+}
+
+// BF16 image of the weights in the inference kernel's shared-memory layout
+static int pack_weights(mpm_net* net) {
+    std::vector<float> p(NPARAM);
+    NCK(cudaMemcpy(p.data(), net->p, NPARAM * 4, cudaMemcpyDeviceToHost));
+    std::vector<uint16_t> img(WBYTES / 2, 0);
+    auto bf = [](float f) -> uint16_t {
+        uint32_t u;
+        memcpy(&u, &f, 4);
+        if ((u & 0x7fffffffu) > 0x7f800000u) return (uint16_t)((u >> 16) | 0x40u);
+        u += 0x7fffu + ((u >> 16) & 1u);
+        return (uint16_t)(u >> 16);
+    };
+    auto put = [&](uint32_t base, int R, int K, long long off, int rows_valid) {
+        for (int r = 0; r < R; ++r)
+            for (int k = 0; k < K; ++k) {
+                const float v = r < rows_valid ? p[off + (long long)r * K + k] : 0.0f;
+                img[(base + kmajor_off(r, k, R)) / 2] = bf(v);
+            }
+    };
+    put(SW1, HID, IN, OW1, HID);
+    put(SW2, HID, HID, OW2, HID);
+    put(SW3, HID, HID, OW3, HID);
+    put(SW4, 16, HID, OW4, OUT);
+    std::vector<float> bias(NBIAS, 0.0f);
+    for (int i = 0; i < HID; ++i) {
+        bias[i] = p[OB1 + i];
+        bias[HID + i] = p[OB2 + i];
+        bias[2 * HID + i] = p[OB3 + i];
+    }
+    for (int i = 0; i < OUT; ++i) bias[3 * HID + i] = p[OB4 + i];
+    if (!net->wpack && cudaMalloc(&net->wpack, WBYTES + NBIAS * 4) != cudaSuccess) {
+        cudaGetLastError();
+        return MPM_ERR_NOMEM;
+    }
+    NCK(cudaMemcpy(net->wpack, img.data(), WBYTES, cudaMemcpyHostToDevice));
+    NCK(cudaMemcpy((char*)net->wpack + WBYTES, bias.data(), NBIAS * 4, cudaMemcpyHostToDevice));
+    net->packed = true;
+    return MPM_OK;
+}
+
+// forward pass on normalised rows x (n x 16) with the FP32 kernels; y (n x 8);
+// z1..z3/h1..h3 scratch (n x 128 each)
+static void forward_fp32(mpm_net* net, cudaStream_t s, long long n, const float* x, float* z1, float* h1, float* z2,
+                         float* h2, float* z3, float* h3, float* y) {
+    const float* p = net->p;
+    sgemm<false, true, EPI_SILU>(s, (int)n, HID, IN, x, IN, p + OW1, IN, h1, HID, p + OB1, z1);
+    sgemm<false, true, EPI_SILU>(s, (int)n, HID, HID, h1, HID, p + OW2, HID, h2, HID, p + OB2, z2);
+    sgemm<false, true, EPI_SILU>(s, (int)n, HID, HID, h2, HID, p + OW3, HID, h3, HID, p + OB3, z3);
+    sgemm<false, true, EPI_STORE>(s, (int)n, OUT, HID, h3, HID, p + OW4, HID, y, OUT, p + OB4);
+}
+
+// gradient of the loss into g (NPARAM, zeroed here); dy already holds dL/dy
+static void backward_fp32(mpm_net* net, cudaStream_t s, long long n, const float* x, const float* z1,
+                          const float* h1, const float* z2, const float* h2, const float* z3, const float* h3,
+                          const float* dy, float* d1, float* d2, float* g) {
+    const float* p = net->p;
+    cudaMemsetAsync(g, 0, NPARAM * 4, s);
+    const int splits = (int)std::max(1LL, std::min(256LL, n / 256));
+    const unsigned cb = (unsigned)((n + 1023) / 1024);
+    // layer 4
+    sgemm<true, false, EPI_ATOMIC>(s, OUT, HID, (int)n, dy, OUT, h3, HID, g + OW4, HID, nullptr, nullptr, splits);
+    k_colsum<OUT><<<cb, 256, 0, s>>>(n, dy, g + OB4);
+    sgemm<false, false, EPI_DSILU>(s, (int)n, HID, OUT, dy, OUT, p + OW4, HID, d1, HID, nullptr, (float*)z3);
+    // layer 3
+    sgemm<true, false, EPI_ATOMIC>(s, HID, HID, (int)n, d1, HID, h2, HID, g + OW3, HID, nullptr, nullptr, splits);
+    k_colsum<HID><<<cb, 256, 0, s>>>(n, d1, g + OB3);
+    sgemm<false, false, EPI_DSILU>(s, (int)n, HID, HID, d1, HID, p + OW3, HID, d2, HID, nullptr, (float*)z2);
+    // layer 2
+    sgemm<true, false, EPI_ATOMIC>(s, HID, HID, (int)n, d2, HID, h1, HID, g + OW2, HID, nullptr, nullptr, splits);
+    k_colsum<HID><<<cb, 256, 0, s>>>(n, d2, g + OB2);
+    sgemm<false, false, EPI_DSILU>(s, (int)n, HID, HID, d2, HID, p + OW2, HID, d1, HID, nullptr, (float*)z1);
+    // layer 1
+    sgemm<true, false, EPI_ATOMIC>(s, HID, IN, (int)n, d1, HID, x, IN, g + OW1, IN, nullptr, nullptr, splits);
+    k_colsum<HID><<<cb, 256, 0, s>>>(n, d1, g + OB1);
+}
+
+extern "C" {
+
+int64_t mpm_net_param_count(void) { return NPARAM; }
+
+int mpm_net_create(const mpm_net_config* cfg, mpm_net** out) {
+    if (!cfg || !out) return MPM_ERR_ARG;
+    *out = nullptr;
+    if (!(cfg->E > 0) || !(cfg->nu > -1.0 && cfg->nu < 0.5) || !(cfg->yield > 0) || cfg->n_samples < 1 ||
+        cfg->batch < 64 || cfg->epochs < 0 || !(cfg->deps_sigma > 0) || !(cfg->stress_range > 0) ||
+        (cfg->sampling != 0 && cfg->sampling != 1))
+        return MPM_ERR_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return MPM_ERR_CUDA;
+    }
+    mpm_net* net = new (std::nothrow) mpm_net();
+    if (!net) return MPM_ERR_NOMEM;
+    net->cfg = *cfg;
+    net->mat = make_mat(*cfg);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&net->sm_count, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaMalloc(&net->p, NPARAM * 4) != cudaSuccess || cudaMalloc(&net->err, 4) != cudaSuccess ||
+        cudaFuncSetAttribute(k_mlp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_TC) != cudaSuccess) {
+        cudaGetLastError();
+        mpm_net_destroy(net);
+        return MPM_ERR_NOMEM;
+    }
+    cudaMemset(net->err, 0, 4);
+    // initial parameters: U(-1/sqrt(fan_in), 1/sqrt(fan_in)) (padded input columns zero)
+    std::vector<float> p(NPARAM, 0.0f);
+    uint64_t st = cfg->seed * 0x2545F4914F6CDD1DULL + 12345;
+    auto u = [&]() {
+        st += 0x9e3779b97f4a7c15ULL;
+        return (double)(mix64(st) >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
+    };
+    for (int r = 0; r < HID; ++r)
+        for (int k = 0; k < NIN; ++k) p[OW1 + r * IN + k] = (float)(u() / std::sqrt((double)NIN));
+    for (int r = 0; r < HID; ++r) p[OB1 + r] = (float)(u() / std::sqrt((double)NIN));
+    for (long long i = 0; i < HID * HID; ++i) p[OW2 + i] = (float)(u() / std::sqrt((double)HID));
+    for (int r = 0; r < HID; ++r) p[OB2 + r] = (float)(u() / std::sqrt((double)HID));
+    for (long long i = 0; i < HID * HID; ++i) p[OW3 + i] = (float)(u() / std::sqrt((double)HID));
+    for (int r = 0; r < HID; ++r) p[OB3 + r] = (float)(u() / std::sqrt((double)HID));
+    for (long long i = 0; i < OUT * HID; ++i) p[OW4 + i] = i < NOUT * HID ? (float)(u() / std::sqrt((double)HID)) : 0.0f;
+    for (int r = 0; r < NOUT; ++r) p[OB4 + r] = (float)(u() / std::sqrt((double)HID));
+    if (cudaMemcpy(net->p, p.data(), NPARAM * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaGetLastError();
+        mpm_net_destroy(net);
+        return MPM_ERR_CUDA;
+    }
+    for (int c = 0; c < 6; ++c) {
+        net->in_inv_scale[c] = (float)(1.0 / cfg->yield);
+        net->in_inv_scale[7 + c] = (float)(1.0 / cfg->deps_sigma);
+    }
+    net->in_inv_scale[6] = (float)(1.0 / cfg->yield);
+    for (int c = 0; c < NOUT; ++c) {
+        net->out_scale[c] = 1.0f;
+        net->out_shift[c] = 0.0f;
+    }
+    *out = net;
+    return MPM_OK;
+}
+
+void mpm_net_destroy(mpm_net* net) {
+    if (!net) return;
+    if (net->p) cudaFree(net->p);
+    if (net->wpack) cudaFree(net->wpack);
+    if (net->scratch) cudaFree(net->scratch);
+    if (net->err) cudaFree(net->err);
+    delete net;
+}
+
+int mpm_net_get_params(mpm_net* net, float* host, int64_t n) {
+    if (!net || !host || n != NPARAM) return MPM_ERR_ARG;
+    NCK(cudaMemcpy(host, net->p, NPARAM * 4, cudaMemcpyDeviceToHost));
+    return MPM_OK;
+}
+
+int mpm_net_set_params(mpm_net* net, const float* host, int64_t n) {
+    if (!net || !host || n != NPARAM) return MPM_ERR_ARG;
+    NCK(cudaMemcpy(net->p, host, NPARAM * 4, cudaMemcpyHostToDevice));
+    return pack_weights(net);
+}
+
+int mpm_net_scales(mpm_net* net, double in_scale[13], double out_scale[7], double out_shift[7]) {
+    if (!net) return MPM_ERR_ARG;
+    for (int c = 0; c < NIN; ++c)
+        if (in_scale) in_scale[c] = 1.0 / (double)net->in_inv_scale[c];
+    for (int c = 0; c < NOUT; ++c) {
+        if (out_scale) out_scale[c] = net->out_scale[c];
+        if (out_shift) out_shift[c] = net->out_shift[c];
+    }
+    return MPM_OK;
+}
+
+int mpm_net_loss_grad(mpm_net* net, const float* x, const float* t, int64_t n, float* grad, double* loss) {
+    if (!net || !x || !t || !grad || n < 1) return MPM_ERR_ARG;
+    const size_t fb = 4;
+    const size_t need = fb * ((size_t)n * (IN + OUT + OUT + OUT) + (size_t)n * HID * 8 + NPARAM) + 64;
+    int rc = ensure_scratch(net, need);
+    if (rc) return rc;
+    float* xs = net->scratch;
+    float* ts = xs + n * IN;
+    float* y = ts + n * OUT;
+    float* dy = y + n * OUT;
+    float* z1 = dy + n * OUT;
+    float* h1 = z1 + n * HID;
+    float* z2 = h1 + n * HID;
+    float* h2 = z2 + n * HID;
+    float* z3 = h2 + n * HID;
+    float* h3 = z3 + n * HID;
+    float* d1 = h3 + n * HID;
+    float* d2 = d1 + n * HID;
+    float* g = d2 + n * HID;
+    double* dl = reinterpret_cast<double*>(((uintptr_t)(g + NPARAM) + 7) & ~(uintptr_t)7);
+    cudaStream_t s = 0;
+    NCK(cudaMemcpy(xs, x, (size_t)n * IN * 4, cudaMemcpyHostToDevice));
+    NCK(cudaMemcpy(ts, t, (size_t)n * OUT * 4, cudaMemcpyHostToDevice));
+    NCK(cudaMemset(dl, 0, 8));
+    forward_fp32(net, s, n, xs, z1, h1, z2, h2, z3, h3, y);
+    k_loss<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, y, ts, dy, dl);
+    backward_fp32(net, s, n, xs, z1, h1, z2, h2, z3, h3, dy, d1, d2, g);
+    NCK(cudaGetLastError());
+    NCK(cudaMemcpy(grad, g, NPARAM * 4, cudaMemcpyDeviceToHost));
+    if (loss) NCK(cudaMemcpy(loss, dl, 8, cudaMemcpyDeviceToHost));
+    return MPM_OK;
+}
+
+static int train_impl(mpm_net* net, const float* d_rows, long long n_rows, mpm_net_report* rep) {
+    const mpm_net_config& c = net->cfg;
+    const long long nval = d_rows ? std::max(1LL, std::min(65536LL, n_rows / 20)) : std::max(65536LL, (long long)c.n_samples / 100);
+    const long long n = d_rows ? n_rows - nval : (long long)c.n_samples, B = std::min<long long>(c.batch, n);
+    if (n < 64) return MPM_ERR_ARG;
+    mpm_net_report r;
+    memset(&r, 0, sizeof(r));
+    // data: x (n x 16), t (n x 8 physical), tn (n x 8 normalised), raw inputs (n x 13)
+    float *x = nullptr, *t = nullptr, *tn = nullptr, *xv = nullptr, *tv = nullptr;
+    auto freeall = [&]() {
+        for (float* q : {x, t, tn, xv, tv})
+            if (q) cudaFree(q);
+    };
+    if (cudaMalloc(&x, (size_t)n * IN * 4) != cudaSuccess || cudaMalloc(&t, (size_t)n * OUT * 4) != cudaSuccess ||
+        cudaMalloc(&tn, (size_t)n * OUT * 4) != cudaSuccess || cudaMalloc(&xv, (size_t)nval * IN * 4) != cudaSuccess ||
+        cudaMalloc(&tv, (size_t)nval * OUT * 4) != cudaSuccess) {
+        cudaGetLastError();
+        freeall();
+        return MPM_ERR_NOMEM;
+    }
+    SampleCfg sc{c.yield, c.stress_range, c.epbar_max, c.deps_sigma, c.C0, c.C1, c.seed, c.sampling};
+    auto t0 = std::chrono::steady_clock::now();
+    if (d_rows) {
+        k_label_rows<<<(unsigned)((n + 255) / 256), 256>>>(n, d_rows, sc, net->mat, x, t);
+        k_label_rows<<<(unsigned)((nval + 255) / 256), 256>>>(nval, d_rows + n * NIN, sc, net->mat, xv, tv);
+    } else {
+        k_generate<<<(unsigned)((n + 255) / 256), 256>>>(n, 0, sc, net->mat, x, t);
+        k_generate<<<(unsigned)((nval + 255) / 256), 256>>>(nval, n, sc, net->mat, xv, tv);
+    }
+    // output normalisation from the training set
+    double* acc = nullptr;
+    float* dvec = nullptr;
+    if (cudaMalloc(&acc, 64 * 8) != cudaSuccess || cudaMalloc(&dvec, 64 * 4) != cudaSuccess) {
+        cudaGetLastError();
+        freeall();
+        return MPM_ERR_NOMEM;
+    }
+    cudaMemset(acc, 0, 64 * 8);
+    k_moments<<<net->sm_count * 4, 256>>>(n, t, acc);
+    double h[2 * NOUT];
+    cudaMemcpy(h, acc, sizeof(h), cudaMemcpyDeviceToHost);
+    float fs[2 * NOUT];
+    for (int k = 0; k < NOUT; ++k) {
+        const double mean = h[k] / n, var = std::max(h[NOUT + k] / n - mean * mean, 1e-30);
+        net->out_shift[k] = (float)mean;
+        net->out_scale[k] = (float)std::sqrt(var);
+        fs[k] = net->out_shift[k];
+        fs[NOUT + k] = 1.0f / net->out_scale[k];
+        r.out_shift[k] = net->out_shift[k];
+        r.out_scale[k] = net->out_scale[k];
+    }
+    cudaMemcpy(dvec, fs, sizeof(fs), cudaMemcpyHostToDevice);
+    k_normalise_targets<<<(unsigned)((n + 255) / 256), 256>>>(n, t, dvec, dvec + NOUT, tn);
+    if (cudaDeviceSynchronize() != cudaSuccess) {
+        cudaGetLastError();
+        freeall();
+        cudaFree(acc);
+        cudaFree(dvec);
+        return MPM_ERR_CUDA;
+    }
+    auto t1 = std::chrono::steady_clock::now();
+    r.seconds_generate = std::chrono::duration<double>(t1 - t0).count();
+    // training buffers
+    const size_t need = 4 * ((size_t)B * (IN + 3 * OUT) + (size_t)B * HID * 8 + 3 * NPARAM) + 1024;
+    int rc = ensure_scratch(net, need);
+    if (rc) {
+        freeall();
+        cudaFree(acc);
+        cudaFree(dvec);
+        return rc;
+    }
+    float* xb = net->scratch;
+    float* tb = xb + B * IN;
+    float* y = tb + B * OUT;
+    float* dy = y + B * OUT;
+    float* z1 = dy + B * OUT;
+    float* h1 = z1 + B * HID;
+    float* z2 = h1 + B * HID;
+    float* h2 = z2 + B * HID;
+    float* z3 = h2 + B * HID;
+    float* h3 = z3 + B * HID;
+    float* d1 = h3 + B * HID;
+    float* d2 = d1 + B * HID;
+    float* g = d2 + B * HID;
+    float* m1 = g + NPARAM;
+    float* m2 = m1 + NPARAM;
+    cudaMemset(m1, 0, 2 * NPARAM * 4);
+    const long long per_epoch = n / B;
+    const long long total = per_epoch * c.epochs;
+    static const long long primes[] = {1000003, 2750159, 4256249, 7368787, 9999991, 15485863, 32452843,
+                                       49979687, 67867967, 86028121, 104395301, 122949823};
+    long long step = 0;
+    cudaStream_t s = 0;
+    for (int ep = 0; ep < c.epochs; ++ep) {
+        long long a = primes[ep % 12];
+        while (std::gcd(a, n) != 1) a += 2;
+        const long long cc = (long long)(mix64(c.seed + ep) % (uint64_t)n);
+        cudaMemsetAsync(acc + 32, 0, 8, s);
+        for (long long b = 0; b < per_epoch; ++b, ++step) {
+            k_gather<<<(unsigned)((B + 255) / 256), 256, 0, s>>>(n, x, tn, a, cc, b * B, (int)B, xb, tb);
+            forward_fp32(net, s, B, xb, z1, h1, z2, h2, z3, h3, y);
+            k_loss<<<(unsigned)((B + 255) / 256), 256, 0, s>>>(B, y, tb, dy, acc + 32);
+            backward_fp32(net, s, B, xb, z1, h1, z2, h2, z3, h3, dy, d1, d2, g);
+            // Adam, cosine-decayed step size after a short warm-up
+            const double tt = (double)(step + 1);
+            const double warm = std::min(1.0, tt / (double)std::max(1LL, std::min(200LL, total / 10)));
+            const double lr = c.lr * warm * (0.02 + 0.98 * 0.5 * (1.0 + std::cos(3.14159265358979323846 * (double)step / (double)total)));
+            const float c1 = (float)(1.0 - std::pow(0.9, tt)), c2 = (float)(1.0 - std::pow(0.999, tt));
+            k_adam<<<(unsigned)((NPARAM + 255) / 256), 256, 0, s>>>(NPARAM, net->p, g, m1, m2, (float)lr, 0.9f, 0.999f,
+                                                                    1e-8f, c1, c2);
+        }
+        double lsum = 0.0;
+        cudaMemcpy(&lsum, acc + 32, 8, cudaMemcpyDeviceToHost);
+        const double lmean = per_epoch ? lsum / per_epoch : 0.0;
+        if (ep == 0) r.loss_first = lmean;
+        r.loss_last = lmean;
+    }
+    if (cudaDeviceSynchronize() != cudaSuccess) {
+        cudaGetLastError();
+        freeall();
+        cudaFree(acc);
+        cudaFree(dvec);
+        return MPM_ERR_CUDA;
+    }
+    auto t2 = std::chrono::steady_clock::now();
+    r.seconds_train = std::chrono::duration<double>(t2 - t1).count();
+    r.steps = step;
+    // held-out errors with the FP32 forward pass
+    rc = MPM_OK;
+    {
+        const long long chunk = std::min(nval, B);
+        float fsh[2 * NOUT];
+        for (int k = 0; k < NOUT; ++k) {
+            fsh[k] = net->out_shift[k];
+            fsh[NOUT + k] = net->out_scale[k];
+        }
+        cudaMemcpy(dvec, fsh, sizeof(fsh), cudaMemcpyHostToDevice);
+        cudaMemset(acc, 0, 16 * 8);
+        unsigned* maxbits = reinterpret_cast<unsigned*>(acc + 8);
+        for (long long o = 0; o < nval; o += chunk) {
+            const long long m = std::min(chunk, nval - o);
+            forward_fp32(net, s, m, xv + o * IN, z1, h1, z2, h2, z3, h3, y);
+            k_val_errors<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(m, y, tv + o * OUT, dvec, dvec + NOUT,
+                                                                    (float)(1.0 / c.yield), 0.02f, acc, maxbits);
+        }
+        double v[4];
+        unsigned mb = 0;
+        cudaMemcpy(v, acc, sizeof(v), cudaMemcpyDeviceToHost);
+        cudaMemcpy(&mb, maxbits, 4, cudaMemcpyDeviceToHost);
+        float mx;
+        memcpy(&mx, &mb, 4);
+        r.n_val = nval;
+        r.val_rms_dsig = std::sqrt(v[0] / (6.0 * nval));
+        r.val_rms_dsig_outside = v[3] > 0 ? std::sqrt(v[1] / (6.0 * v[3])) : 0.0;
+        r.val_max_dsig = mx;
+        r.val_rms_dR = std::sqrt(v[2] / nval);
+        if (cudaDeviceSynchronize() != cudaSuccess) {
+            cudaGetLastError();
+            rc = MPM_ERR_CUDA;
+        }
+    }
+    freeall();
+    cudaFree(acc);
+    cudaFree(dvec);
+    if (rc) return rc;
+    rc = pack_weights(net);
+    if (rep) *rep = r;
+    return rc;
+}
+
+int mpm_net_train(mpm_net* net, mpm_net_report* rep) {
+    if (!net) return MPM_ERR_ARG;
+    return train_impl(net, nullptr, 0, rep);
+}
+
+int mpm_net_train_rows(mpm_net* net, const float* d_rows, int64_t n, mpm_net_report* rep) {
+    if (!net || !d_rows || n < 128) return MPM_ERR_ARG;
+    return train_impl(net, d_rows, n, rep);
+}
+
+int mpm_net_infer(mpm_net* net, const float* d_in, float* d_out, int64_t n, int kernel, void* stream) {
+    if (!net || n < 0 || kernel < 0 || kernel > 2) return MPM_ERR_ARG;
+    if (n == 0) return MPM_OK;
+    if (!d_in || !d_out) return MPM_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (kernel == 2) {
+        k_exact_fp32<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, d_in, net->mat, d_out);
+        NCK(cudaGetLastError());
+        return MPM_OK;
+    }
+    if (!net->packed) {
+        int rc = pack_weights(net);
+        if (rc) return rc;
+    }
+    if (kernel == 0) {
+        TcArgs a;
+        a.wpack = reinterpret_cast<const uint4*>(net->wpack);
+        a.bias = reinterpret_cast<const float*>((const char*)net->wpack + WBYTES);
+        for (int c = 0; c < NIN; ++c) a.in_inv_scale[c] = net->in_inv_scale[c];
+        for (int c = 0; c < NOUT; ++c) {
+            a.out_scale[c] = net->out_scale[c];
+            a.out_shift[c] = net->out_shift[c];
+        }
+        a.in = d_in;
+        a.out = d_out;
+        a.count = nullptr;
+        a.n = n;
+        a.err = net->err;
+        a.mat = net->mat;
+        const long long tiles = (n + 127) / 128;
+        const unsigned grid = (unsigned)std::min<long long>(tiles, (long long)net->sm_count);
+        k_mlp_tc<<<grid, 128, SMEM_TC, s>>>(a);
+        NCK(cudaGetLastError());
+        return MPM_OK;
+    }
+    // FP32 reference: normalise, the training forward pass in chunks, de-normalise
+    const long long chunk = std::min<long long>(n, 1 << 20);
+    const size_t need = 4 * ((size_t)chunk * (IN + OUT) + (size_t)chunk * HID * 6 + 2 * NIN + 2 * NOUT) + 256;
+    int rc = ensure_scratch(net, need);
+    if (rc) return rc;
+    float* x = net->scratch;
+    float* y = x + chunk * IN;
+    float* z1 = y + chunk * OUT;
+    float* h1 = z1 + chunk * HID;
+    float* z2 = h1 + chunk * HID;
+    float* h2 = z2 + chunk * HID;
+    float* z3 = h2 + chunk * HID;
+    float* h3 = z3 + chunk * HID;
+    float* sc = h3 + chunk * HID;
+    float hs[NIN + 2 * NOUT];
+    for (int c = 0; c < NIN; ++c) hs[c] = net->in_inv_scale[c];
+    for (int c = 0; c < NOUT; ++c) {
+        hs[NIN + c] = net->out_scale[c];
+        hs[NIN + NOUT + c] = net->out_shift[c];
+    }
+    NCK(cudaMemcpyAsync(sc, hs, sizeof(hs), cudaMemcpyHostToDevice, s));
+    for (long long o = 0; o < n; o += chunk) {
+        const long long m = std::min(chunk, n - o);
+        k_norm_inputs<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(m, d_in + o * NIN, sc, x);
+        forward_fp32(net, s, m, x, z1, h1, z2, h2, z3, h3, y);
+        k_denorm_outputs<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(m, y, sc + NIN, sc + NIN + NOUT,
+                                                                     d_in + o * NIN, net->mat, d_out + o * NOUT);
+    }
+    NCK(cudaStreamSynchronize(s));
+    return MPM_OK;
+}
+
+}  // extern "C"
+
+namespace mpm {
+int net_run_queue(mpm_net* net, const SurrogateQueue& q, cudaStream_t s, unsigned* err) {
+    if (!net->packed) {
+        int rc = pack_weights(net);
+        if (rc) return rc;
+    }
+    TcArgs a;
+    a.wpack = reinterpret_cast<const uint4*>(net->wpack);
+    a.bias = reinterpret_cast<const float*>((const char*)net->wpack + WBYTES);
+    for (int c = 0; c < NIN; ++c) a.in_inv_scale[c] = net->in_inv_scale[c];
+    for (int c = 0; c < NOUT; ++c) {
+        a.out_scale[c] = net->out_scale[c];
+        a.out_shift[c] = net->out_shift[c];
+    }
+    a.in = q.in;
+    a.out = q.out;
+    a.count = q.count;
+    a.n = q.cap;
+    a.err = err;
+    a.mat = net->mat;
+    k_mlp_tc<<<(unsigned)net->sm_count, 128, SMEM_TC, s>>>(a);
+    return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_ERR_CUDA;
+}
+
+float net_yield(const mpm_net* net) { return (float)net->cfg.yield; }
+const MatConst& net_material(const mpm_net* net) { return net->mat; }
+}  // namespace mpm

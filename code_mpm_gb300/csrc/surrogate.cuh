@@ -1,0 +1,38 @@
+// Internal interface between the engine and the return-map network
+// (surrogate.cu): the pieces pass 2 and the step driver need.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+struct mpm_net;
+
+namespace mpm {
+
+// A particle whose return map the network computes: its inputs in physical
+// units (stress, R, strain increment), what the finishing kernel needs to
+// apply the result (volume, particle index), and the network's outputs.
+struct SurrogateQueue {
+    float* in;         // cap x 13
+    float* out;        // cap x 7
+    float* vol;        // cap
+    unsigned* pidx;    // cap
+    unsigned* count;   // device counter (pass 2 appends)
+    long long cap;
+};
+
+// Counters of the in-loop use (device, doubles/u64 as laid out here).
+struct SurrogateAcc {
+    unsigned long long queued, band, rechecked, pad;
+    double sq_err, max_err;  // over rechecks, |dsigma error| / yield
+};
+
+// Run the network over the queue (device-side count; no host sync).
+int net_run_queue(mpm_net* net, const SurrogateQueue& q, cudaStream_t s, unsigned* err);
+// The material the network was trained for, and its yield stress.
+const MatConst& net_material(const mpm_net* net);
+float net_yield(const mpm_net* net);
+
+}  // namespace mpm

@@ -73,6 +73,25 @@ class Nodes(C.Structure):
     _fields_ = [(k, C.c_void_p) for k, _ in _NMAP]
 
 
+class NetConfig(C.Structure):
+    _fields_ = [("E", C.c_double), ("nu", C.c_double), ("yield_", C.c_double), ("C0", C.c_double),
+                ("C1", C.c_double), ("n_samples", C.c_int64), ("batch", C.c_int32), ("epochs", C.c_int32),
+                ("lr", C.c_double), ("stress_range", C.c_double), ("epbar_max", C.c_double),
+                ("deps_sigma", C.c_double), ("seed", C.c_uint64), ("sampling", C.c_int32), ("pad", C.c_int32)]
+
+
+class NetReport(C.Structure):
+    _fields_ = [("loss_first", C.c_double), ("loss_last", C.c_double), ("val_rms_dsig", C.c_double),
+                ("val_rms_dsig_outside", C.c_double), ("val_max_dsig", C.c_double), ("val_rms_dR", C.c_double),
+                ("seconds_generate", C.c_double), ("seconds_train", C.c_double), ("steps", C.c_int64),
+                ("n_val", C.c_int64), ("out_scale", C.c_double * 8), ("out_shift", C.c_double * 8)]
+
+
+class SurrogateStats(C.Structure):
+    _fields_ = [("queued", C.c_int64), ("band", C.c_int64), ("rechecked", C.c_int64), ("recheck_rms", C.c_double),
+                ("recheck_max", C.c_double)]
+
+
 class KernelStat(C.Structure):
     _fields_ = [("name", C.c_char * 32), ("launches", C.c_int64), ("total_ms", C.c_double)]
 
@@ -141,6 +160,20 @@ def lib():
             "mpm_autotune": ([vp, i32, dbl, C.c_int, C.POINTER(TuneResult)], C.c_int),
             "mpm_upload_monitor_mask": ([vp, vp, i64], C.c_int),
             "mpm_monitors_read": ([vp, C.POINTER(Monitors)], C.c_int),
+            "mpm_net_create": ([C.POINTER(NetConfig), C.POINTER(vp)], C.c_int),
+            "mpm_net_destroy": ([vp], None),
+            "mpm_net_train": ([vp, C.POINTER(NetReport)], C.c_int),
+            "mpm_net_param_count": ([], i64),
+            "mpm_net_get_params": ([vp, vp, i64], C.c_int),
+            "mpm_net_set_params": ([vp, vp, i64], C.c_int),
+            "mpm_net_loss_grad": ([vp, vp, vp, i64, vp, C.POINTER(dbl)], C.c_int),
+            "mpm_net_infer": ([vp, vp, vp, i64, C.c_int, vp], C.c_int),
+            "mpm_net_scales": ([vp, vp, vp, vp], C.c_int),
+            "mpm_attach_surrogate": ([vp, vp, dbl, dbl], C.c_int),
+            "mpm_surrogate_stats_read": ([vp, C.POINTER(SurrogateStats), C.c_int], C.c_int),
+            "mpm_net_train_rows": ([vp, vp, i64, C.POINTER(NetReport)], C.c_int),
+            "mpm_harvest_begin": ([vp, vp, i64, C.c_uint32, dbl], C.c_int),
+            "mpm_harvest_end": ([vp, C.POINTER(i64)], C.c_int),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -423,3 +456,110 @@ class Engine:
         c = C.c_int64(0)
         self._check(self._L.mpm_launch_count(self._h, C.byref(c)))
         return int(c.value)
+
+    # -- return-map network ------------------------------------------------------------
+    def attach_surrogate(self, net: Optional["Net"], band: float = 0.02, recheck: float = 0.01) -> None:
+        """Let the network compute the return map of clearly plastic von Mises hardening particles (FP32 form)."""
+        self._check(self._L.mpm_attach_surrogate(self._h, net.handle if net else None, float(band), float(recheck)))
+        self._keep.append(net)
+
+    def harvest_begin(self, d_rows: int, cap: int, mat_mask: int = 1, band: float = 0.02) -> None:
+        """Record return-map inputs of clearly plastic particles into device rows (n x 13 floats) while stepping."""
+        self._check(self._L.mpm_harvest_begin(self._h, C.c_void_p(d_rows), int(cap), int(mat_mask), float(band)))
+
+    def harvest_end(self) -> int:
+        r = C.c_int64(0)
+        self._check(self._L.mpm_harvest_end(self._h, C.byref(r)))
+        return int(r.value)
+
+    def surrogate_stats(self, reset: bool = False) -> Dict[str, float]:
+        r = SurrogateStats()
+        self._check(self._L.mpm_surrogate_stats_read(self._h, C.byref(r), 1 if reset else 0))
+        return {"queued": r.queued, "band": r.band, "rechecked": r.rechecked, "recheck_rms": r.recheck_rms,
+                "recheck_max": r.recheck_max}
+
+
+INFER_TC, INFER_FP32, INFER_EXACT = 0, 1, 2
+
+
+class Net:
+    """The learned von Mises hardening return map (include/mpm_surrogate.h)."""
+
+    def __init__(self, E=200.0e9, nu=0.3, yield_=250.0e6, C0=2.0e-3, C1=1.0e12, n_samples=20_000_000,
+                 batch=65536, epochs=20, lr=2.0e-3, stress_range=1.5, epbar_max=0.2, deps_sigma=2.0e-4, seed=7,
+                 sampling=0):
+        self._L = lib()
+        self.cfg = NetConfig(float(E), float(nu), float(yield_), float(C0), float(C1), int(n_samples), int(batch),
+                             int(epochs), float(lr), float(stress_range), float(epbar_max), float(deps_sigma),
+                             int(seed), int(sampling), 0)
+        h = C.c_void_p()
+        rc = self._L.mpm_net_create(C.byref(self.cfg), C.byref(h))
+        if rc != 0 or not h.value:
+            raise MPMError(rc, "mpm_net_create failed")
+        self._h = h
+        self.report = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._L.mpm_net_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != 0:
+            raise MPMError(rc, "mpm_net call failed")
+
+    def train(self) -> Dict[str, float]:
+        r = NetReport()
+        self._check(self._L.mpm_net_train(self._h, C.byref(r)))
+        self.report = {k: getattr(r, k) for k, _ in NetReport._fields_ if k not in ("out_scale", "out_shift")}
+        self.report["out_scale"] = list(r.out_scale)[:7]
+        self.report["out_shift"] = list(r.out_shift)[:7]
+        return self.report
+
+    def train_rows(self, d_rows: int, n: int) -> Dict[str, float]:
+        """Train on device input rows (n x 13 physical), labelled by the exact FP64 map."""
+        r = NetReport()
+        self._check(self._L.mpm_net_train_rows(self._h, C.c_void_p(d_rows), int(n), C.byref(r)))
+        self.report = {k: getattr(r, k) for k, _ in NetReport._fields_ if k not in ("out_scale", "out_shift")}
+        return self.report
+
+    def params(self) -> np.ndarray:
+        n = int(self._L.mpm_net_param_count())
+        a = np.zeros(n, dtype=np.float32)
+        self._check(self._L.mpm_net_get_params(self._h, _ptr(a), n))
+        return a
+
+    def set_params(self, a: np.ndarray) -> None:
+        a = np.ascontiguousarray(a, dtype=np.float32)
+        self._check(self._L.mpm_net_set_params(self._h, _ptr(a), a.size))
+
+    def loss_grad(self, x: np.ndarray, t: np.ndarray):
+        """(loss, gradient) of the training kernels on normalised rows x (n x 16), t (n x 8)."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        g = np.zeros(int(self._L.mpm_net_param_count()), dtype=np.float32)
+        loss = C.c_double(0.0)
+        self._check(self._L.mpm_net_loss_grad(self._h, _ptr(x), _ptr(t), x.shape[0], _ptr(g), C.byref(loss)))
+        return loss.value, g
+
+    def scales(self):
+        i = (C.c_double * 13)()
+        s = (C.c_double * 7)()
+        h = (C.c_double * 7)()
+        self._check(self._L.mpm_net_scales(self._h, i, s, h))
+        return np.array(list(i)), np.array(list(s)), np.array(list(h))
+
+    def infer_device(self, d_in: int, d_out: int, n: int, kernel: int = INFER_TC, stream: int = 0) -> None:
+        """Inference on device rows (pointers): inputs n x 13, outputs n x 7, physical units."""
+        self._check(self._L.mpm_net_infer(self._h, C.c_void_p(d_in), C.c_void_p(d_out), int(n), int(kernel),
+                                          C.c_void_p(stream)))

@@ -1,4 +1,4 @@
-"""The C-ABI library builds for sm_103a, loads without a GPU, and exports every entry point of include/mpm_gb300.h."""
+"""The C-ABI library builds for sm_103a, loads without a GPU, and exports every entry point of include/*.h."""
 import ctypes
 import os
 import re
@@ -11,9 +11,14 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def declared_functions():
-    src = open(os.path.join(ROOT, "include", "mpm_gb300.h")).read()
-    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"^\s*(?:int|void|const char\*)\s+(mpm_\w+)\s*\(", src, flags=re.M)))
+    names = set()
+    inc = os.path.join(ROOT, "include")
+    for f in sorted(os.listdir(inc)):
+        if not f.endswith(".h") or not f.startswith("mpm_"):
+            continue
+        src = re.sub(r"/\*.*?\*/", "", open(os.path.join(inc, f)).read(), flags=re.S)
+        names |= set(re.findall(r"^\s*(?:int|void|int64_t|const char\*)\s+(mpm_\w+)\s*\(", src, flags=re.M))
+    return sorted(names)
 
 
 @pytest.fixture(scope="module")
