@@ -102,6 +102,14 @@ struct mpm_ctx {
     unsigned sg_mats = 0;
     std::vector<MatConst> mats_host;
     DevBuf q_in, q_out, q_vol, q_pidx, q_count, sg_acc;
+    // CUDA graph of two steps, replayed while nothing it captured changes
+    int use_graph = 1;
+    cudaGraphExec_t gexec = nullptr;
+    double g_dt = 0.0;
+    int g_contact = -1;
+    long long g_launches = 0;
+    DevBuf dsim, tl_dev;
+    double* h_sim = nullptr;  // pinned: time, dt, step (as double bits), tv[3]
     // harvesting of return-map inputs
     int hv_on = 0;
     unsigned hv_mats = 0;
@@ -116,7 +124,8 @@ struct mpm_ctx {
                           &material, &pflags, &dc_mult, &g_mass, &g_mom, &g_vel, &g_force, &g_ftemp, &g_mg,
                           &g_state, &g_fixed, &g_friction, &g_ratio, &g_q, &g_owner, &g_nowner, &g_need, &g_list, &g_count, &rs_chunk, &cstart,
                           &cend, &keys0, &vals0, &keys1, &vals1, &keys_copy, &counts, &dclist, &mats, &staging, &tune_backup, &surf, &mon_mask, &mon_acc, &loc, &geom_tab, &sid, &alist, &acount,
-                          &q_in, &q_out, &q_vol, &q_pidx, &q_count, &sg_acc, &hv_count};
+                          &q_in, &q_out, &q_vol, &q_pidx, &q_count, &sg_acc, &hv_count,
+                          &dsim, &tl_dev};
         all.assign(std::begin(list), std::end(list));
     }
 };
@@ -450,14 +459,50 @@ int check_device_error(mpm_ctx* c) {
 }
 
 // ---- one time step -----------------------------------------------------------
+// Device copy of the clock for graph replay: time, dt, step and the
+// timeline velocity at the step's start, computed with the host's exact
+// operations (timeline_velocity), so device and host clocks stay identical.
+struct DevSim {
+    double time, dt;
+    unsigned long long step;
+    double tv[3];
+};
+
+__global__ void k_step_begin(DevSim* d, const double* __restrict__ tl_t, const double* __restrict__ tl_v, int nt) {
+    const double t = d->time;
+    double out[3] = {0.0, 0.0, 0.0};
+    for (int k = 0; k + 1 < nt; ++k) {
+        if (tl_t[k] <= t && t < tl_t[k + 1]) {
+            const double s = __ddiv_rn(__dsub_rn(t, tl_t[k]), __dsub_rn(tl_t[k + 1], tl_t[k]));
+            for (int a = 0; a < 3; ++a)
+                out[a] = __dadd_rn(__dmul_rn(__dsub_rn(1.0, s), tl_v[3 * k + a]), __dmul_rn(s, tl_v[3 * (k + 1) + a]));
+        }
+    }
+    for (int a = 0; a < 3; ++a) d->tv[a] = out[a];
+}
+
+__global__ void k_step_end(DevSim* d) {
+    d->time = __dadd_rn(d->time, d->dt);
+    d->step += 1;
+}
+
+void graph_reset(mpm_ctx* c) {
+    if (c && c->gexec) {
+        cudaGraphExecDestroy(c->gexec);
+        c->gexec = nullptr;
+    }
+}
+
 template <typename T>
-int step_impl(mpm_ctx* c, double dt, int contact) {
+int step_impl(mpm_ctx* c, double dt, int contact, bool graph = false) {
     const long long n = c->n, nn = c->nn;
     PView<T> P = pview<T>(c);
     NView<T> N = nview<T>(c);
     const Geom& g = c->g;
     unsigned* err = (unsigned*)c->err_word.p;
 
+    DevSim* dsim = (DevSim*)c->dsim.p;
+    if (graph) LAUNCH("step_clock", k_step_begin, 1, 1, dsim, (const double*)c->tl_dev.p, (const double*)c->tl_dev.p + c->tl_t.size(), (int)c->tl_t.size());
     // node kernels sweep the active-node list; the reset uses the previous step's
     const unsigned nodeblocks = (unsigned)std::min<long long>(blocks_for(nn), (long long)c->sm_count * 16);
     N.alist = c->have_alist ? (const unsigned*)c->alist.p : nullptr;
@@ -593,6 +638,7 @@ int step_impl(mpm_ctx* c, double dt, int contact) {
         a.dt_f = (float)dt;
         a.mass_min_f = fps_float_threshold(c->sim.mass_min);
         timeline_velocity(c, c->sim.time, a.tv);
+        a.tv_dev = graph ? dsim->tv : nullptr;
         a.has_timeline = c->tl_t.empty() ? 0 : 1;
         a.contact = contact;
         a.sg_on = 0;
@@ -637,11 +683,12 @@ int step_impl(mpm_ctx* c, double dt, int contact) {
                 if (rq) return rq;
                 LAUNCH("net_finish", k_sg_finish, (unsigned)c->sm_count * 8, 256, P, a.q, net_material(c->net),
                        contact, dt, 1.0f / net_yield(c->net), c->sg_recheck, (unsigned long long)c->sim.step,
-                       a.sg_acc);
+                       graph ? &dsim->step : (const unsigned long long*)nullptr, a.sg_acc);
             }
         }
         c->keys_valid = true;
     }
+    if (graph) LAUNCH("step_clock", k_step_end, 1, 1, dsim);
     CK(cudaGetLastError());
     // d_Time += dTimeIncrement; i_TimeCycle++ (…MPLocks.cpp:802-803)
     c->sim.time += dt;
@@ -649,8 +696,76 @@ int step_impl(mpm_ctx* c, double dt, int contact) {
     return MPM_OK;
 }
 
-int step(mpm_ctx* c, double dt, int contact) {
-    return c->form == MPM_FORM_FP64 ? step_impl<double>(c, dt, contact) : step_impl<float>(c, dt, contact);
+int step(mpm_ctx* c, double dt, int contact, bool graph = false) {
+    return c->form == MPM_FORM_FP64 ? step_impl<double>(c, dt, contact, graph)
+                                    : step_impl<float>(c, dt, contact, graph);
+}
+
+// Steps nsteps with the two-step graph where it applies: the steady state
+// (keys from the previous pass 2, an active-node list), no profiling, a
+// stream that can be captured, the same dt and contact flag as the cached
+// graph.  Capturing records two steps without running them while the host
+// state advances by two steps; launching the graph once then brings the
+// device to the same point.
+int advance_graph(mpm_ctx* c, int nsteps, double dt, int contact) {
+    int s = 0;
+    auto plain = [&](int k) -> int {
+        for (int i = 0; i < k; ++i)
+            if (int rc = step(c, dt, contact)) return rc;
+        return MPM_OK;
+    };
+    while (s < nsteps && (!c->keys_valid || !c->have_alist)) {
+        if (int rc = plain(1)) return rc;
+        ++s;
+    }
+    const bool can = c->use_graph && !c->profile && c->stream != nullptr && c->n > 0 && nsteps - s >= 2;
+    if (!can) return plain(nsteps - s);
+    if (c->gexec && (c->g_dt != dt || c->g_contact != contact)) graph_reset(c);
+    int rc;
+    if ((rc = ensure(c, c->dsim, sizeof(DevSim)))) return rc;
+    if (!c->h_sim && cudaMallocHost(&c->h_sim, sizeof(DevSim)) != cudaSuccess) {
+        cudaGetLastError();
+        return plain(nsteps - s);
+    }
+    // the device clock from the host's
+    CK(cudaStreamSynchronize(c->stream));
+    DevSim hs{c->sim.time, dt, (unsigned long long)c->sim.step, {0.0, 0.0, 0.0}};
+    memcpy(c->h_sim, &hs, sizeof(hs));
+    CK(cudaMemcpyAsync(c->dsim.p, c->h_sim, sizeof(DevSim), cudaMemcpyHostToDevice, c->stream));
+    if (!c->gexec) {
+        const long long l0 = c->launches;
+        cudaGraph_t gr = nullptr;
+        CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
+        int r1 = step(c, dt, contact, true);
+        int r2 = r1 ? r1 : step(c, dt, contact, true);
+        cudaError_t ec = cudaStreamEndCapture(c->stream, &gr);
+        if (r2 || ec != cudaSuccess) {
+            cudaGetLastError();
+            if (gr) cudaGraphDestroy(gr);
+            return r2 ? r2 : fail(c, MPM_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(ec));
+        }
+        ec = cudaGraphInstantiate(&c->gexec, gr, 0);
+        cudaGraphDestroy(gr);
+        if (ec != cudaSuccess) {
+            cudaGetLastError();
+            c->gexec = nullptr;
+            return fail(c, MPM_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(ec));
+        }
+        c->g_dt = dt;
+        c->g_contact = contact;
+        c->g_launches = c->launches - l0;
+        CK(cudaGraphLaunch(c->gexec, c->stream));  // the two captured steps (host state already advanced)
+        s += 2;
+    }
+    for (; nsteps - s >= 2; s += 2) {
+        CK(cudaGraphLaunch(c->gexec, c->stream));
+        c->launches += c->g_launches;
+        c->sim.time += dt;
+        c->sim.step += 1;
+        c->sim.time += dt;
+        c->sim.step += 1;
+    }
+    return plain(nsteps - s);
 }
 
 int alloc_particles(mpm_ctx* c, long long n) {
@@ -846,6 +961,8 @@ void mpm_destroy(mpm_ctx* c) {
     for (DevBuf* b : c->all)
         if (b->p) cudaFree(b->p);
     if (c->h_err) cudaFreeHost(c->h_err);
+    if (c->h_sim) cudaFreeHost(c->h_sim);
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -853,6 +970,7 @@ void mpm_destroy(mpm_ctx* c) {
 const char* mpm_last_error(const mpm_ctx* c) { return c ? c->err.c_str() : "null context"; }
 
 int mpm_set_stream(mpm_ctx* c, void* stream) {
+    graph_reset(c);
     if (!c) return MPM_ERR_ARG;
     CK(cudaStreamSynchronize(c->stream));
     if (c->own_stream) cudaStreamDestroy(c->stream);
@@ -862,6 +980,7 @@ int mpm_set_stream(mpm_ctx* c, void* stream) {
 }
 
 int mpm_set_option(mpm_ctx* c, int key, double value) {
+    graph_reset(c);
     if (!c) return MPM_ERR_ARG;
     switch (key) {
         case MPM_OPT_FLOOR_FRICTION: c->floor_friction = value != 0.0; return MPM_OK;
@@ -869,6 +988,9 @@ int mpm_set_option(mpm_ctx* c, int key, double value) {
         case MPM_OPT_P2G_REDUCE:
             if (value != 0.0 && value != 1.0 && value != 2.0) return fail(c, MPM_ERR_ARG, "P2G mode must be 0, 1 or 2");
             c->p2g_reduce = (int)value;
+            return MPM_OK;
+        case MPM_OPT_GRAPH:
+            c->use_graph = value != 0.0;
             return MPM_OK;
         case MPM_OPT_GATHER:
             if (value != 0.0 && value != 1.0) return fail(c, MPM_ERR_ARG, "gather mode must be 0 or 1");
@@ -886,6 +1008,7 @@ int mpm_set_option(mpm_ctx* c, int key, double value) {
 }
 
 int mpm_upload_materials(mpm_ctx* c, const mpm_material* m, int32_t n) {
+    graph_reset(c);
     if (!c || n < 0 || (n > 0 && !m)) return c ? fail(c, MPM_ERR_ARG, "bad material table") : MPM_ERR_ARG;
     std::vector<MatConst> mc((size_t)std::max(1, n));
     for (int i = 0; i < n; ++i) {
@@ -928,6 +1051,7 @@ int mpm_upload_materials(mpm_ctx* c, const mpm_material* m, int32_t n) {
 }
 
 int mpm_upload_particles(mpm_ctx* c, const mpm_particles* p, int64_t n) {
+    graph_reset(c);
     if (!c) return MPM_ERR_ARG;
     if (!p || n < 0 || n >= 0x7fffffffLL) return fail(c, MPM_ERR_ARG, "bad particle upload (n=%lld)", (long long)n);
     const bool f64 = c->form == MPM_FORM_FP64;
@@ -1016,6 +1140,7 @@ int mpm_upload_particles(mpm_ctx* c, const mpm_particles* p, int64_t n) {
 }
 
 int mpm_upload_dc_list(mpm_ctx* c, const uint32_t* idx, int64_t n) {
+    graph_reset(c);
     if (!c) return MPM_ERR_ARG;
     if (n < 0 || (n > 0 && !idx)) return fail(c, MPM_ERR_ARG, "bad displacement-control list");
     if (!c->have_particles && n > 0) return fail(c, MPM_ERR_STATE, "upload particles before the dc list");
@@ -1040,6 +1165,7 @@ int mpm_upload_dc_list(mpm_ctx* c, const uint32_t* idx, int64_t n) {
 }
 
 int mpm_upload_nodes(mpm_ctx* c, const mpm_nodes* nd) {
+    graph_reset(c);
     if (!c) return MPM_ERR_ARG;
     if (!nd) return fail(c, MPM_ERR_ARG, "null node view");
     const long long nn = c->nn;
@@ -1074,14 +1200,22 @@ int mpm_upload_nodes(mpm_ctx* c, const mpm_nodes* nd) {
 }
 
 int mpm_set_timeline(mpm_ctx* c, const double* t, const double* v3, int32_t n) {
+    graph_reset(c);
     if (!c) return MPM_ERR_ARG;
     if (n < 0 || (n > 0 && (!t || !v3))) return fail(c, MPM_ERR_ARG, "bad timeline");
     c->tl_t.assign(t, t + n);
     c->tl_v.assign(v3, v3 + 3 * (size_t)n);
+    if (n > 0) {  // device copy (t[n], v[3n]) for the step graph's clock
+        int rc = ensure(c, c->tl_dev, (size_t)4 * n * 8);
+        if (rc) return rc;
+        CK(cudaMemcpy(c->tl_dev.p, t, (size_t)n * 8, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy((double*)c->tl_dev.p + n, v3, (size_t)3 * n * 8, cudaMemcpyHostToDevice));
+    }
     return MPM_OK;
 }
 
 int mpm_set_sim(mpm_ctx* c, const mpm_sim* s) {
+    graph_reset(c);
     if (!c || !s) return MPM_ERR_ARG;
     c->sim = *s;
     return MPM_OK;
@@ -1177,23 +1311,31 @@ int mpm_advance(mpm_ctx* c, int32_t nsteps, double dt, int contact) {
     if (nsteps < 0 || !(dt > 0.0) || !std::isfinite(dt)) return fail(c, MPM_ERR_ARG, "bad step request");
     if (!c->have_particles) return fail(c, MPM_ERR_STATE, "no particles uploaded");
     if (c->nmat <= 0 && c->n > 0) return fail(c, MPM_ERR_STATE, "no materials uploaded");
-    for (int s = 0; s < nsteps; ++s) {
-        int rc = step(c, dt, contact ? 1 : 0);
-        if (rc) return rc;
-    }
-    return MPM_OK;
+    return advance_graph(c, nsteps, dt, contact ? 1 : 0);
 }
 
 int mpm_run(mpm_ctx* c, double dt_total, int contact, int* done) {
     if (!c) return MPM_ERR_ARG;
     if (!(dt_total >= 0.0)) return fail(c, MPM_ERR_ARG, "bad dt_total");
-    // …MPLocks.cpp:449-458
+    // …MPLocks.cpp:449-458: the step sizes of the chunking loop, run in runs of
+    // equal size (so the full-size steps can replay the step graph)
     double acc = 0.0;
+    double run_dt = 0.0;
+    int run_len = 0;
     while (acc < dt_total) {
         double dt = c->sim.dt_max;
         if (c->sim.dt_max > (dt_total - acc)) dt = dt_total - acc;
         acc += dt;
-        int rc = mpm_advance(c, 1, dt, contact);
+        if (run_len > 0 && dt != run_dt) {
+            int rc = mpm_advance(c, run_len, run_dt, contact);
+            if (rc) return rc;
+            run_len = 0;
+        }
+        run_dt = dt;
+        ++run_len;
+    }
+    if (run_len > 0) {
+        int rc = mpm_advance(c, run_len, run_dt, contact);
         if (rc) return rc;
     }
     int rc = mpm_synchronize(c);
@@ -1245,6 +1387,7 @@ int mpm_cell_order(mpm_ctx* c, uint32_t* keys, uint32_t* sorted_order, int64_t n
 }
 
 int mpm_upload_monitor_mask(mpm_ctx* c, const uint8_t* mask, int64_t n) {
+    graph_reset(c);
     if (!c) return MPM_ERR_ARG;
     if (n != c->n || (n > 0 && !mask)) return fail(c, MPM_ERR_ARG, "monitor mask must have one entry per particle");
     int rc = ensure(c, c->mon_mask, (size_t)std::max<int64_t>(1, n));
@@ -1294,6 +1437,7 @@ int mpm_monitors_read(mpm_ctx* c, mpm_monitors* out) {
 }
 
 int mpm_autotune(mpm_ctx* c, int32_t steps, double dt, int contact, mpm_tune_result* out) {
+    graph_reset(c);
     if (!c) return MPM_ERR_ARG;
     if (steps < 1 || !(dt > 0.0)) return fail(c, MPM_ERR_ARG, "bad autotune request");
     if (!c->have_particles) return fail(c, MPM_ERR_STATE, "no particles uploaded");
@@ -1412,6 +1556,7 @@ int mpm_profile_reset(mpm_ctx* c) {
 }
 
 int mpm_attach_surrogate(mpm_ctx* c, mpm_net* net, double band, double recheck) {
+    graph_reset(c);
     if (!c) return MPM_ERR_ARG;
     if (net && c->form != MPM_FORM_FP32) return fail(c, MPM_ERR_ARG, "the return-map network serves the FP32 form");
     if (net && !(band >= 0.0 && band < 10.0 && recheck >= 0.0 && recheck <= 1.0))
@@ -1436,6 +1581,7 @@ int mpm_attach_surrogate(mpm_ctx* c, mpm_net* net, double band, double recheck) 
 }
 
 int mpm_harvest_begin(mpm_ctx* c, float* d_rows, int64_t cap, uint32_t mat_mask, double band) {
+    graph_reset(c);
     if (!c) return MPM_ERR_ARG;
     if (!d_rows || cap < 1 || !(band >= 0.0)) return fail(c, MPM_ERR_ARG, "harvest needs rows, cap >= 1, band >= 0");
     int rc = ensure(c, c->hv_count, 64);
@@ -1450,6 +1596,7 @@ int mpm_harvest_begin(mpm_ctx* c, float* d_rows, int64_t cap, uint32_t mat_mask,
 }
 
 int mpm_harvest_end(mpm_ctx* c, int64_t* rows) {
+    graph_reset(c);
     if (!c || !rows) return MPM_ERR_ARG;
     *rows = 0;
     if (!c->hv_on) return MPM_OK;

@@ -708,6 +708,7 @@ struct StepArgs {
     float dt_f;        // RN32(dt)
     float mass_min_f;  // mass_min rounded down to float (fps_float_threshold)
     double tv[3];
+    const double* tv_dev;  // graph replay: the timeline velocity computed on the device (else tv)
     int has_timeline;
     int contact;
     // return-map network (FP32 form): materials it stands in for (bit per
@@ -968,17 +969,18 @@ __global__ void __launch_bounds__(512) k_pass2(PView<T> P, NView<T> nd, Geom g, 
     }
     // platen timeline (…MPLocks.cpp:766-789; contact :531-540)
     if (fl & PF_IN_DC) {
+        const double* tv = a.tv_dev ? a.tv_dev : a.tv;
         if (!a.contact) {
             if (a.has_timeline) {
 #pragma unroll
                 for (int c = 0; c < 3; ++c)
-                    if (fl & (1u << c)) P.vel[c * np + p] = (T)((double)P.dc_mult[p] * a.tv[c]);
+                    if (fl & (1u << c)) P.vel[c * np + p] = (T)((double)P.dc_mult[p] * tv[c]);
             }
         } else {
             double vv[3];
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                vv[c] = a.has_timeline ? (double)P.dc_mult[p] * a.tv[c] : (double)P.vel[c * np + p];
+                vv[c] = a.has_timeline ? (double)P.dc_mult[p] * tv[c] : (double)P.vel[c * np + p];
                 P.vel[c * np + p] = (T)vv[c];
                 P.pos[c * np + p] += vv[c] * a.dt;
             }
@@ -1460,7 +1462,9 @@ __global__ void __launch_bounds__(256) k_monitor_force(NView<T> nd, double* acc)
 // the network's result is kept).
 // ---------------------------------------------------------------------------
 static __global__ void k_sg_finish(PView<float> P, SurrogateQueue q, MatConst M, int contact, double dt, float inv_yield,
-                            float recheck, unsigned long long step, SurrogateAcc* acc) {
+                            float recheck, unsigned long long step, const unsigned long long* step_dev,
+                            SurrogateAcc* acc) {
+    if (step_dev) step = *step_dev;
     const unsigned cnt = (unsigned)min((unsigned long long)*q.count, (unsigned long long)q.cap);
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&acc->queued, (unsigned long long)cnt);
     const unsigned thr = (unsigned)(recheck * 4294967296.0f);

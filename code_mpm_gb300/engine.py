@@ -115,6 +115,7 @@ OPT_P2G_REDUCE = 3
 OPT_P2G_BLOCK = 4
 OPT_PASS_BLOCK = 5
 OPT_GATHER = 6
+OPT_GRAPH = 7
 
 
 def library_path() -> str:
