@@ -74,6 +74,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip timing the plain FP64 form beside the chosen one")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-network", action="store_true",
+                    help="run the chosen form without the learned return map (and skip its isolated benchmark)")
     return ap.parse_args()
 
 
@@ -351,6 +353,96 @@ def accuracy_vs_plain(sts, pk, idx, chosen, steps, contact, floor, tune_plain):
                        "plain FP64 form against itself with positions perturbed by 1e-7 relative")
 
 
+def peaks_bf16():
+    try:
+        with open(PEAKS_PATH) as f:
+            p = json.load(f)
+        return float(p["bf16_tflops"]), "measured"
+    except Exception:
+        return 1900.0, "fallback"
+
+
+# algorithmic FLOPs of one sample through 13 -> 128 -> 128 -> 128 -> 7
+NET_FLOPS = 2 * (13 * 128 + 128 * 128 + 128 * 128 + 128 * 7)
+
+
+def network_for_batch(args, contact, floor, steps):
+    """The learned return map for the batch: trained on the return-map inputs that the plain FP64 method meets on
+    a pilot batch (16 other specimens drawn with another seed), labelled by the exact FP64 map."""
+    import torch
+
+    from code_mpm_gb300 import batch, engine, scenes
+
+    pilot = scenes.honeycomb_batch(n=16, seed=99, total=2.5e6)
+    ppk = batch.pack(pilot)
+    cap = 16_000_000
+    rows = torch.zeros((cap, 13), dtype=torch.float32, device="cuda")
+    t0 = time.perf_counter()
+    e = engine.Engine(None, None, engine.FORM_FP64, grids=ppk.grids)
+    e.upload_state(ppk.state)
+    e.set_option(engine.OPT_FLOOR_FRICTION, floor)
+    e.harvest_begin(rows.data_ptr(), cap, mat_mask=1, band=0.0)
+    e.advance(steps, pilot[0].dt_max, contact)
+    n = min(e.harvest_end(), cap)
+    e.close()
+    t1 = time.perf_counter()
+    dsig = float(rows[:n, 7:].std().item())
+    bsz = 8192
+    epochs = int(max(20, math.ceil(5000 * bsz / max(n, 1))))  # about 5000 Adam steps
+    net = engine.Net(E=200.0e9, nu=0.3, yield_=250.0e6, C0=2.0e-3, C1=1.0e12, n_samples=1000, epochs=epochs,
+                     batch=bsz, deps_sigma=dsig, lr=2.0e-3)
+    rep = net.train_rows(rows.data_ptr(), n)
+    del rows
+    info = {"pilot": f"16 honeycomb specimens (seed 99, {ppk.state.n_particles} particles), plain FP64, {steps} steps",
+            "harvested_rows": n, "seconds_pilot": t1 - t0, "training": rep}
+    return net, info
+
+
+def network_isolated(contact_unused=None):
+    """The network as stated for the isolated return map: 20M samples (stress U(+-1.5 yield), R from epbar
+    U(0, 0.2), strain increment N(0, 2e-4)), batch 65536, 20 epochs; inference on 16M samples per call (tensor cores)
+    against the exact FP32 map on the same samples."""
+    import torch
+
+    from code_mpm_gb300 import engine
+
+    net = engine.Net(E=200.0e9, nu=0.3, yield_=250.0e6, C0=2.0e-3, C1=1.0e12, n_samples=20_000_000, epochs=20,
+                     batch=65536, lr=2.0e-3)
+    rep = net.train()
+    n = 16 * 1024 * 1024
+    g = torch.Generator(device="cuda")
+    g.manual_seed(5)
+    Y = 250.0e6
+    x = torch.empty((n, 13), dtype=torch.float32, device="cuda")
+    x[:, :6] = (torch.rand((n, 6), generator=g, device="cuda") * 3.0 - 1.5) * Y
+    ep = torch.rand((n,), generator=g, device="cuda") * 0.2
+    x[:, 6] = (math.sqrt(2.0 / 3.0) * 1.0e12 * (1.0 - torch.exp(-2.0e-3 * ep.double()))).float()
+    x[:, 7:] = torch.randn((n, 6), generator=g, device="cuda") * 2.0e-4
+    out = torch.empty((n, 7), dtype=torch.float32, device="cuda")
+    times = {}
+    for name, k in (("network_tcgen05", engine.INFER_TC), ("exact_map_fp32", engine.INFER_EXACT)):
+        for _ in range(3):
+            net.infer_device(x.data_ptr(), out.data_ptr(), n, k)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(10):
+            net.infer_device(x.data_ptr(), out.data_ptr(), n, k)
+        b.record()
+        b.synchronize()
+        times[name] = a.elapsed_time(b) / 10
+    peak, kind = peaks_bf16()
+    achieved = NET_FLOPS * n / (times["network_tcgen05"] / 1e3) / 1e12
+    net.close()
+    return {"samples_per_call": n, "ms_per_call": times,
+            "samples_per_s": {k: n / (v / 1e3) for k, v in times.items()},
+            "network_over_exact_speed": times["exact_map_fp32"] / times["network_tcgen05"],
+            "roofline": {"bound": "tensor", "kernel": "k_mlp_tc", "achieved": achieved, "peak": peak,
+                         "unit": "TFLOP/s", "frac": achieved / peak, "peak_kind": f"{kind} cuBLAS bf16 burst",
+                         "flops_per_sample": NET_FLOPS},
+            "training": rep}
+
+
 def kernel_table(e, steps, dt, contact):
     from code_mpm_gb300 import engine
 
@@ -476,11 +568,23 @@ def run_gb300(args, dist: Dist):
                          "dtype": "f64", "gpu_launches": launches_b, "clocks": clocks_b, "autotune": tune_b,
                          "how": "the plain FP64 form with every specimen in one engine"}
 
+    # the learned return map (chosen form, batch workload): trained on a pilot batch's plain-method samples
+    net, net_info = None, None
+    use_net = compare and pk is not None and not args.no_network
+    if use_net:
+        net, net_info = network_for_batch(args, contact, floor, steps=min(args.warmup + args.steps, 1000))
+
     e = make_engine(sts, pk, chosen_form)
     e.set_option(engine.OPT_FLOOR_FRICTION, floor)
+    if net is not None:
+        e.attach_surrogate(net, band=0.02, recheck=0.01)
     tune = None if args.no_autotune else e.autotune(steps=2, dt=dt, contact=bool(contact))
+    if net is not None:
+        e.surrogate_stats(reset=True)
     ms, launches, clocks_rec = timed(e, args.steps, args.warmup, dt, contact, dist)
     value = n * args.steps * dist.world / (ms / 1e3)
+    if net is not None:
+        net_info["in_step"] = e.surrogate_stats()
 
     accuracy = None
     if compare:
@@ -501,6 +605,14 @@ def run_gb300(args, dist: Dist):
     prof, kernels = kernel_table(e, min(args.steps, 30), dt, contact)
     n_active = active_nodes(e, n_nodes)
     roofline = roofline_of(prof, formkey, n, n_active, args.workload)
+    without_net = None
+    if net is not None:  # the same engine with the network detached
+        e.attach_surrogate(None)
+        k2 = max(1, min(args.steps, 300))
+        ms2, l2, c2 = timed(e, k2, 2, dt, contact, dist)
+        without_net = {"value": n * k2 * dist.world / (ms2 / 1e3), "ms_per_step": ms2 / k2, "steps": k2,
+                       "gpu_launches": l2}
+        e.attach_surrogate(net, band=0.02, recheck=0.01)  # the e2e call runs the chosen form as timed
 
     e2e = None
     if args.no_e2e:
@@ -519,7 +631,9 @@ def run_gb300(args, dist: Dist):
            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if formkey == "fp64" else "f32+f64",
            "data": "synthetic (seeded scene generators)",
            "config": dict(cfg, form=("plain FP64" if formkey == "fp64" else "chosen: FP32 transfers/grid, FP64 "
-                                     "positions and energies, batched, autotuned"),
+                                     "positions and energies, batched, autotuned" +
+                                     (", learned return map with 2% fallback band and 1% recheck" if use_net
+                                      else "")),
                           parallelism=f"replicas x{dist.world}"),
            "clocks": clocks_rec, "gpu_launches": launches, "autotune": tune, "roofline": roofline,
            "kernels": kernels, "e2e": e2e}
@@ -531,6 +645,12 @@ def run_gb300(args, dist: Dist):
         out["chosen_over_plain_batched"] = value / plain_batched["value"]
     if accuracy is not None:
         out["accuracy"] = accuracy
+    if net_info is not None:
+        out["network"] = net_info
+        out["chosen_without_network"] = without_net
+        net.close()
+    if dist.rank == 0 and dist.world == 1 and use_net:
+        out["network_isolated"] = network_isolated()
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(sts, contact, floor)
     return out

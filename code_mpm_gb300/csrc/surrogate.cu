@@ -553,12 +553,14 @@ __device__ __forceinline__ void issue_layer(uint32_t tmem, uint32_t a_addr, int 
     }
 }
 
-// hidden-layer epilogue: thread t reads sample t's 128 accumulators, adds
-// the bias, applies SiLU, and writes BF16 row t of the next A operand
+// hidden-layer epilogue: warps w and w + 4 share TMEM lane quarter w % 4;
+// their thread t reads sample 32 (w % 4) + t's accumulators in columns
+// [64 (w / 4), 64 (w / 4) + 64), adds the bias, applies SiLU, and writes that
+// part of BF16 row r of the next A operand
 __device__ __forceinline__ void hidden_epilogue(uint32_t taddr_row, const float* bias, unsigned char* a1) {
-    const int r = threadIdx.x;
+    const int w = threadIdx.x >> 5, r = 32 * (w & 3) + (threadIdx.x & 31), half = w >> 2;
 #pragma unroll 1
-    for (int c0 = 0; c0 < HID; c0 += 32) {
+    for (int c0 = 64 * half; c0 < 64 * half + 64; c0 += 32) {
         float v[32];
         tmem_ld32(taddr_row + (uint32_t)c0, v);
 #pragma unroll
@@ -587,15 +589,17 @@ struct TcArgs {
     MatConst mat;              // for the elastic predictor D de
 };
 
-__global__ void __launch_bounds__(128, 1) k_mlp_tc(TcArgs a) {
+constexpr int TC_THREADS = 256;
+
+__global__ void __launch_bounds__(TC_THREADS, 2) k_mlp_tc(TcArgs a) {
     extern __shared__ __align__(1024) unsigned char sm[];
     const int t = threadIdx.x, w = t >> 5;
     unsigned char* s = sm + ((1024 - (smem_u32(sm) & 1023u)) & 1023u);  // 1024-byte aligned base
     const uint32_t sbase = smem_u32(s);
     // weights and biases into shared memory (once per CTA)
-    for (uint32_t i = t; i < WBYTES / 16; i += 128) reinterpret_cast<uint4*>(s)[i] = a.wpack[i];
+    for (uint32_t i = t; i < WBYTES / 16; i += TC_THREADS) reinterpret_cast<uint4*>(s)[i] = a.wpack[i];
     float* bias = reinterpret_cast<float*>(s + S_BIAS);
-    for (uint32_t i = t; i < NBIAS; i += 128) bias[i] = a.bias[i];
+    for (uint32_t i = t; i < NBIAS; i += TC_THREADS) bias[i] = a.bias[i];
     uint32_t* taddr_slot = reinterpret_cast<uint32_t*>(s + S_TADDR);
     const uint32_t bar = sbase + S_BAR;
     if (t == 0) {
@@ -612,18 +616,18 @@ __global__ void __launch_bounds__(128, 1) k_mlp_tc(TcArgs a) {
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *taddr_slot;
-    const uint32_t trow = tmem + ((uint32_t)(32 * w) << 16);  // this warp's lane quarter
+    const uint32_t trow = tmem + ((uint32_t)(32 * (w & 3)) << 16);  // this warp's lane quarter
     const long long n = a.count ? (long long)min((unsigned long long)*a.count, (unsigned long long)a.n) : a.n;
     const long long ntiles = (n + 127) / 128;
     uint32_t phase = 0;
     bool ok = true;
     for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        const long long i = tile * 128 + t;
+        const long long i = tile * 128 + (t & 127);  // warps 0-3 own the samples' inputs and outputs
         // inputs -> A0 (128 x 16 BF16)
         float x[16];
 #pragma unroll
         for (int c = 0; c < 16; ++c) x[c] = 0.0f;
-        if (i < n) {
+        if (t < 128 && i < n) {
 #pragma unroll
             for (int c = 0; c < NIN; ++c) x[c] = a.in[i * NIN + c] * a.in_inv_scale[c];
         }
@@ -636,8 +640,10 @@ __global__ void __launch_bounds__(128, 1) k_mlp_tc(TcArgs a) {
         p1.y = pack_bf16(x[10], x[11]);
         p1.z = pack_bf16(x[12], x[13]);
         p1.w = pack_bf16(x[14], x[15]);
-        *reinterpret_cast<uint4*>(s + S_A0 + kmajor_off(t, 0, 128)) = p0;
-        *reinterpret_cast<uint4*>(s + S_A0 + kmajor_off(t, 8, 128)) = p1;
+        if (t < 128) {
+            *reinterpret_cast<uint4*>(s + S_A0 + kmajor_off(t, 0, 128)) = p0;
+            *reinterpret_cast<uint4*>(s + S_A0 + kmajor_off(t, 8, 128)) = p1;
+        }
         for (int layer = 0; layer < 4 && ok; ++layer) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -664,8 +670,8 @@ __global__ void __launch_bounds__(128, 1) k_mlp_tc(TcArgs a) {
                 hidden_epilogue(trow, bias + layer * HID, s + S_A1);
             } else {
                 float v[16];
-                tmem_ld16(trow, v);
-                if (i < n) {
+                if (w < 4) tmem_ld16(trow, v);
+                if (w < 4 && i < n) {
                     float d[6];
                     elastic_predictor(a.mat, a.in + i * NIN, d);
 #pragma unroll
@@ -1155,8 +1161,8 @@ int mpm_net_infer(mpm_net* net, const float* d_in, float* d_out, int64_t n, int 
         a.err = net->err;
         a.mat = net->mat;
         const long long tiles = (n + 127) / 128;
-        const unsigned grid = (unsigned)std::min<long long>(tiles, (long long)net->sm_count);
-        k_mlp_tc<<<grid, 128, SMEM_TC, s>>>(a);
+        const unsigned grid = (unsigned)std::min<long long>(tiles, 2LL * net->sm_count);
+        k_mlp_tc<<<grid, TC_THREADS, SMEM_TC, s>>>(a);
         NCK(cudaGetLastError());
         return MPM_OK;
     }
@@ -1214,7 +1220,7 @@ int net_run_queue(mpm_net* net, const SurrogateQueue& q, cudaStream_t s, unsigne
     a.n = q.cap;
     a.err = err;
     a.mat = net->mat;
-    k_mlp_tc<<<(unsigned)net->sm_count, 128, SMEM_TC, s>>>(a);
+    k_mlp_tc<<<(unsigned)(2 * net->sm_count), TC_THREADS, SMEM_TC, s>>>(a);
     return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_ERR_CUDA;
 }
 
