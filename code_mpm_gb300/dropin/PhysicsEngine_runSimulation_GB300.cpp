@@ -241,21 +241,41 @@ static int gb300_run(PhysicsEngine* self, double total, int contact, std::vector
         return 0;
     };
 
-    // …MPLocks.cpp:449-458 time chunking, :796-803 console and time advance
+    // …MPLocks.cpp:449-458 time chunking, :796-803 console and time advance.
+    // The steps between two console reports have one size, so each such run
+    // goes to the GPU in one mpm_advance call (which replays the step graph);
+    // the host then repeats the reference's bookkeeping for the run.
+    mpm_sim sim = {time, dt_max, mass_min, damping, time_end, (int64_t)cycle};
+    if ((rc = mpm_set_sim(ctx, &sim))) return fail(ctx, rc);
     double acc = 0.0;
     while (acc < total) {
-        double dt = dt_max;
-        if (dt_max > (total - acc)) dt = total - acc;
-        acc += dt;
-        mpm_sim sim = {time, dt_max, mass_min, damping, time_end, (int64_t)cycle};
-        if ((rc = mpm_set_sim(ctx, &sim)) || (rc = mpm_advance(ctx, 1, dt, contact))) return fail(ctx, rc);
-        if (time - console_last > console_interval) {
-            if ((rc = pull())) return fail(ctx, rc);
-            console_last = time;
-            (self->*report)("");
+        int k = 0;
+        double run_dt = 0.0;
+        {
+            double a = acc, t = time;
+            while (a < total) {
+                double dt = dt_max;
+                if (dt_max > (total - a)) dt = total - a;
+                if (k > 0 && dt != run_dt) break;
+                run_dt = dt;
+                a += dt;
+                ++k;
+                const bool console = t - console_last > console_interval;
+                t += dt;
+                if (console) break;
+            }
         }
-        time += dt;
-        cycle++;
+        if ((rc = mpm_advance(ctx, k, run_dt, contact))) return fail(ctx, rc);
+        for (int i = 0; i < k; ++i) {
+            acc += run_dt;
+            if (time - console_last > console_interval) {  // only the run's last step can report
+                if ((rc = pull())) return fail(ctx, rc);
+                console_last = time;
+                (self->*report)("");
+            }
+            time += run_dt;
+            cycle++;
+        }
     }
     if ((rc = mpm_synchronize(ctx)) || (rc = pull())) return fail(ctx, rc);
     mpm_destroy(ctx);
