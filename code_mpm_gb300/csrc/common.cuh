@@ -156,6 +156,7 @@ struct PView {
     float* dc_mult;
     float* loc;  // FP32 form: cell-local coordinate (x - X_b)/h of the current base cell, 3 x n
     const uint16_t* sid;  // specimen of each particle (null with one specimen)
+    const unsigned* orig; // FP32 form in cell order: the caller's index of each slot (null: slot = index)
     long long n;
 };
 

@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "kernels.cuh"
@@ -117,6 +118,11 @@ struct mpm_ctx {
     float* hv_rows = nullptr;
     long long hv_cap = 0;
     DevBuf hv_count;
+    // particles stored in cell order (FP32 form): orig[slot] = the caller's index
+    DevBuf orig, ptmp;
+    bool have_orig = false, reorder_pending = false;
+    int reorder_interval = 0;  // -1: never; 0: after each particle upload; N: also every N steps
+    long long steps_since_reorder = 0;
 
     mpm_ctx() {
         DevBuf* list[] = {&xtab, &err_word, &pos, &vel, &fext, &mass, &vol, &vol0, &F, &stress, &strain, &eps_p,
@@ -125,7 +131,7 @@ struct mpm_ctx {
                           &g_state, &g_fixed, &g_friction, &g_ratio, &g_q, &g_owner, &g_nowner, &g_need, &g_list, &g_count, &rs_chunk, &cstart,
                           &cend, &keys0, &vals0, &keys1, &vals1, &keys_copy, &counts, &dclist, &mats, &staging, &tune_backup, &surf, &mon_mask, &mon_acc, &loc, &geom_tab, &sid, &alist, &acount,
                           &q_in, &q_out, &q_vol, &q_pidx, &q_count, &sg_acc, &hv_count,
-                          &dsim, &tl_dev};
+                          &dsim, &tl_dev, &orig, &ptmp};
         all.assign(std::begin(list), std::end(list));
     }
 };
@@ -188,6 +194,7 @@ PView<T> pview(mpm_ctx* c) {
     v.dc_mult = (float*)c->dc_mult.p;
     v.loc = (float*)c->loc.p;
     v.sid = c->nspec > 1 ? (const uint16_t*)c->sid.p : nullptr;
+    v.orig = c->have_orig ? (const unsigned*)c->orig.p : nullptr;
     v.n = c->n;
     return v;
 }
@@ -316,15 +323,50 @@ __global__ void k_unpack(const double* __restrict__ src, T* __restrict__ dst, lo
     if (shift_identity && (c == 0 || c == 4 || c == 8)) v -= 1.0;
     dst[(long long)c * n + p] = (T)v;
 }
+// device SoA (slot order) -> host rows; with orig, slot s goes to the caller's row orig[s]
 template <typename T>
-__global__ void k_pack(const T* __restrict__ src, double* __restrict__ dst, long long n, int k, int shift_identity) {
+__global__ void k_pack(const T* __restrict__ src, double* __restrict__ dst, long long n, int k, int shift_identity,
+                       const unsigned* __restrict__ orig) {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= n * k) return;
-    long long p = i / k;
-    int c = (int)(i - p * k);
-    double v = (double)src[(long long)c * n + p];
+    long long s = i / k;
+    int c = (int)(i - s * k);
+    double v = (double)src[(long long)c * n + s];
     if (shift_identity && (c == 0 || c == 4 || c == 8)) v += 1.0;
-    dst[i] = v;
+    dst[(orig ? (long long)orig[s] : s) * k + c] = v;
+}
+// dst[c n + s] = src[c n + perm[s]] for ES-byte elements (a particle field into slot order)
+template <int ES>
+__global__ void k_permute(const void* __restrict__ src, void* __restrict__ dst, const unsigned* __restrict__ perm,
+                          long long n, int k) {
+    using U = typename std::conditional<ES == 8, unsigned long long,
+              typename std::conditional<ES == 4, unsigned, typename std::conditional<ES == 2, unsigned short,
+                                                                                        unsigned char>::type>::type>::type;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n * k;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long c = i / n, s = i - c * n;
+        reinterpret_cast<U*>(dst)[i] = reinterpret_cast<const U*>(src)[c * n + perm[s]];
+    }
+}
+// dst[orig[s]] = src[s] for ES-byte single-component fields (slot order -> the caller's order)
+template <int ES>
+__global__ void k_scatter_orig(const void* __restrict__ src, void* __restrict__ dst, const unsigned* __restrict__ orig,
+                               long long n) {
+    using U = typename std::conditional<ES == 4, unsigned, unsigned char>::type;
+    long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (s < n) reinterpret_cast<U*>(dst)[orig[s]] = reinterpret_cast<const U*>(src)[s];
+}
+__global__ void k_invert(const unsigned* __restrict__ perm, unsigned* __restrict__ inv, long long n) {
+    long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (s < n) inv[perm[s]] = (unsigned)s;
+}
+__global__ void k_remap_list(unsigned* __restrict__ list, long long n, const unsigned* __restrict__ map) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) list[i] = map[list[i]];
+}
+__global__ void k_iota(unsigned* __restrict__ a, long long n) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) a[i] = (unsigned)i;
 }
 template <typename T>
 __global__ void k_fill(T* __restrict__ dst, long long n, T v) {
@@ -434,12 +476,13 @@ int download_field(mpm_ctx* c, const DevBuf& src, double* host, long long n, int
     if (!host || n == 0) return MPM_OK;
     int rc = ensure(c, c->staging, (size_t)n * k * 8);
     if (rc) return rc;
+    const unsigned* orig = c->have_orig ? (const unsigned*)c->orig.p : nullptr;
     if (fp64)
         LAUNCH("pack", k_pack<double>, blocks_for(n * k), NTHREADS, (const double*)src.p, (double*)c->staging.p, n,
-               k, shift_identity);
+               k, shift_identity, orig);
     else
         LAUNCH("pack", k_pack<float>, blocks_for(n * k), NTHREADS, (const float*)src.p, (double*)c->staging.p, n, k,
-               shift_identity);
+               shift_identity, orig);
     CK(cudaMemcpyAsync(host, c->staging.p, (size_t)n * k * 8, cudaMemcpyDeviceToHost, c->stream));
     return MPM_OK;
 }
@@ -459,6 +502,120 @@ int check_device_error(mpm_ctx* c) {
 }
 
 // ---- one time step -----------------------------------------------------------
+// Sort the particles by cell key: the keys of the current positions (written
+// by the previous step's pass 2, or computed here after an upload), then the
+// stable radix sort, whose first pass takes the identity as input values.
+int sort_cells(mpm_ctx* c, const unsigned** skeys_out, const unsigned** perm_out) {
+    const long long n = c->n;
+    const Geom& g = c->g;
+    unsigned* err = (unsigned*)c->err_word.p;
+    const uint16_t* sid = c->nspec > 1 ? (const uint16_t*)c->sid.p : nullptr;
+    // cell keys: written by the previous step's pass 2 (which knows the new
+    // positions), or computed here after an upload; then the stable radix
+    // sort by key, whose first pass takes the identity as input values
+    unsigned* key_src = (unsigned*)(c->key_buf ? c->keys1.p : c->keys0.p);
+    unsigned* key_other = (unsigned*)(c->key_buf ? c->keys0.p : c->keys1.p);
+    if (!c->keys_valid)
+        LAUNCH("cell_keys", k_cell_keys, blocks_for(n), NTHREADS, (const double*)c->pos.p, n, g, key_src,
+               (unsigned*)nullptr, (unsigned*)c->keys_copy.p, err,
+               c->form == MPM_FORM_FP32 ? (float*)c->loc.p : (float*)nullptr, sid);
+    int bits = 1;
+    while (bits < 32 && ((unsigned long long)1 << bits) <= (unsigned long long)g.key_max) ++bits;
+    const int nblocks = (int)((n + RS_TILE - 1) / RS_TILE);
+    unsigned *kin = key_src, *vin = nullptr;
+    unsigned *kout = key_other, *vout = (unsigned*)c->vals0.p;
+    const int hist_total = 256 * nblocks;
+    const int nchunks = (hist_total + RS_SCAN_CHUNK - 1) / RS_SCAN_CHUNK;
+    for (int shift = 0; shift < bits; shift += 8) {
+        LAUNCH("rs_hist", k_rs_hist, nblocks, RS_THREADS, kin, n, shift, (unsigned*)c->counts.p, nblocks);
+        const unsigned* chunk_prefix = nullptr;
+        if (nchunks > 1) {
+            LAUNCH("rs_scan", k_rs_scan_chunks, nchunks, RS_SCAN_THREADS, (unsigned*)c->counts.p, hist_total,
+                   (unsigned*)c->rs_chunk.p);
+            LAUNCH("rs_scan", k_rs_scan, 1, 1024, (unsigned*)c->rs_chunk.p, nchunks);
+            chunk_prefix = (const unsigned*)c->rs_chunk.p;
+        } else {
+            LAUNCH("rs_scan", k_rs_scan, 1, 1024, (unsigned*)c->counts.p, hist_total);
+        }
+        LAUNCH("rs_scatter", k_rs_scatter, nblocks, RS_THREADS, kin, (const unsigned*)vin, kout, vout, n, shift,
+               (const unsigned*)c->counts.p, nblocks, chunk_prefix);
+        std::swap(kin, kout);
+        vin = vout;
+        vout = (vout == (unsigned*)c->vals0.p) ? (unsigned*)c->vals1.p : (unsigned*)c->vals0.p;
+    }
+    const unsigned* skeys = kin;
+    const unsigned* perm = vin;
+    c->last_perm = perm;
+    c->last_skeys = skeys;
+    *skeys_out = skeys;
+    *perm_out = perm;
+    return MPM_OK;
+}
+
+void graph_reset(mpm_ctx* c);
+
+// Store the particles in cell order (FP32 form).  After a sort every
+// particle array is permuted into sorted order and `orig` keeps each slot's
+// index as the caller numbers it; the displacement-control list is remapped
+// and the surface list rebuilt.  Later sorts find the particles nearly in
+// order, so the gathers of P2G and pass 1 through the sort permutation read
+// consecutive memory.  Everything the caller sees (downloads, lists, the cell
+// order, last-writer claims) stays in the caller's order.
+int reorder(mpm_ctx* c) {
+    c->reorder_pending = false;
+    c->steps_since_reorder = 0;
+    const long long n = c->n;
+    if (n <= 0 || c->form != MPM_FORM_FP32) return MPM_OK;
+    graph_reset(c);
+    const unsigned *skeys = nullptr, *perm = nullptr;
+    int rc = sort_cells(c, &skeys, &perm);
+    if (rc) return rc;
+    if ((rc = ensure(c, c->orig, (size_t)n * 4)) || (rc = ensure(c, c->ptmp, (size_t)n * 36))) return rc;
+    if (!c->have_orig) {
+        LAUNCH("reorder", k_iota, blocks_for(n), NTHREADS, (unsigned*)c->orig.p, n);
+        c->have_orig = true;
+    }
+    struct {
+        DevBuf* b;
+        int k, es;
+    } fields[] = {{&c->pos, 3, 8},        {&c->vel, 3, 4},       {&c->fext, 3, 4},         {&c->mass, 1, 4},
+                  {&c->vol, 1, 4},        {&c->vol0, 1, 4},      {&c->F, 9, 4},            {&c->stress, 6, 4},
+                  {&c->strain, 6, 4},     {&c->eps_p, 6, 4},     {&c->e_strain, 1, 8},     {&c->e_strain_max, 1, 8},
+                  {&c->e_strain_ti, 1, 8}, {&c->e_plastic, 1, 8}, {&c->backstress, 1, 4},   {&c->mp_mg, 3, 4},
+                  {&c->strain_rate, 6, 4}, {&c->material, 1, 4}, {&c->pflags, 1, 1},       {&c->dc_mult, 1, 4},
+                  {&c->loc, 3, 4},        {&c->keys_copy, 1, 4}, {&c->orig, 1, 4},         {&c->sid, 1, 2},
+                  {&c->mon_mask, 1, 1}};
+    const unsigned grid = (unsigned)std::min<long long>(blocks_for(n * 3), (long long)c->sm_count * 32);
+    for (auto& f : fields) {
+        if (f.b == &c->sid && c->nspec <= 1) continue;
+        if (f.b == &c->mon_mask && !c->have_mon) continue;
+        void* src = f.b->p;
+        switch (f.es) {
+            case 8: LAUNCH("reorder", k_permute<8>, grid, NTHREADS, src, c->ptmp.p, perm, n, f.k); break;
+            case 4: LAUNCH("reorder", k_permute<4>, grid, NTHREADS, src, c->ptmp.p, perm, n, f.k); break;
+            case 2: LAUNCH("reorder", k_permute<2>, grid, NTHREADS, src, c->ptmp.p, perm, n, f.k); break;
+            default: LAUNCH("reorder", k_permute<1>, grid, NTHREADS, src, c->ptmp.p, perm, n, f.k); break;
+        }
+        CK(cudaMemcpyAsync(src, c->ptmp.p, (size_t)n * f.k * f.es, cudaMemcpyDeviceToDevice, c->stream));
+    }
+    // list entries: old slot -> new slot
+    unsigned* inv = (unsigned*)c->ptmp.p;
+    LAUNCH("reorder", k_invert, blocks_for(n), NTHREADS, perm, inv, n);
+    if (c->ndc > 0) LAUNCH("reorder", k_remap_list, blocks_for(c->ndc), NTHREADS, (unsigned*)c->dclist.p, (long long)c->ndc, inv);
+    CK(cudaMemsetAsync(c->g_count.p, 0, 4, c->stream));
+    LAUNCH("reorder", k_compact_flag, blocks_for(n), NTHREADS, (const uint8_t*)c->pflags.p, n, (uint8_t)MPM_PF_SURFACE,
+           (unsigned*)c->surf.p, (unsigned*)c->g_count.p);
+    // the sorted keys are now the keys of the slots in order: they become the next sort's input
+    c->key_buf = (skeys == (const unsigned*)c->keys1.p) ? 1 : 0;
+    unsigned* ident = (unsigned*)(perm == (const unsigned*)c->vals0.p ? c->vals1.p : c->vals0.p);
+    LAUNCH("reorder", k_iota, blocks_for(n), NTHREADS, ident, n);
+    c->last_perm = ident;
+    c->last_skeys = skeys;
+    c->keys_valid = true;
+    CK(cudaGetLastError());
+    return MPM_OK;
+}
+
 // Device copy of the clock for graph replay: time, dt, step and the
 // timeline velocity at the step's start, computed with the host's exact
 // operations (timeline_velocity), so device and host clocks stay identical.
@@ -508,43 +665,8 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph = false) {
     N.alist = c->have_alist ? (const unsigned*)c->alist.p : nullptr;
     LAUNCH("reset_grid", k_reset_grid<T>, c->have_alist ? nodeblocks : blocks_for(nn), NTHREADS, N, contact);
     if (n > 0) {
-        // cell keys: written by the previous step's pass 2 (which knows the new
-        // positions), or computed here after an upload; then the stable radix
-        // sort by key, whose first pass takes the identity as input values
-        unsigned* key_src = (unsigned*)(c->key_buf ? c->keys1.p : c->keys0.p);
-        unsigned* key_other = (unsigned*)(c->key_buf ? c->keys0.p : c->keys1.p);
-        if (!c->keys_valid)
-            LAUNCH("cell_keys", k_cell_keys, blocks_for(n), NTHREADS, (const double*)c->pos.p, n, g, key_src,
-                   (unsigned*)nullptr, (unsigned*)c->keys_copy.p, err,
-                   c->form == MPM_FORM_FP32 ? (float*)c->loc.p : (float*)nullptr, P.sid);
-        int bits = 1;
-        while (bits < 32 && ((unsigned long long)1 << bits) <= (unsigned long long)g.key_max) ++bits;
-        const int nblocks = (int)((n + RS_TILE - 1) / RS_TILE);
-        unsigned *kin = key_src, *vin = nullptr;
-        unsigned *kout = key_other, *vout = (unsigned*)c->vals0.p;
-        const int hist_total = 256 * nblocks;
-        const int nchunks = (hist_total + RS_SCAN_CHUNK - 1) / RS_SCAN_CHUNK;
-        for (int shift = 0; shift < bits; shift += 8) {
-            LAUNCH("rs_hist", k_rs_hist, nblocks, RS_THREADS, kin, n, shift, (unsigned*)c->counts.p, nblocks);
-            const unsigned* chunk_prefix = nullptr;
-            if (nchunks > 1) {
-                LAUNCH("rs_scan", k_rs_scan_chunks, nchunks, RS_SCAN_THREADS, (unsigned*)c->counts.p, hist_total,
-                       (unsigned*)c->rs_chunk.p);
-                LAUNCH("rs_scan", k_rs_scan, 1, 1024, (unsigned*)c->rs_chunk.p, nchunks);
-                chunk_prefix = (const unsigned*)c->rs_chunk.p;
-            } else {
-                LAUNCH("rs_scan", k_rs_scan, 1, 1024, (unsigned*)c->counts.p, hist_total);
-            }
-            LAUNCH("rs_scatter", k_rs_scatter, nblocks, RS_THREADS, kin, (const unsigned*)vin, kout, vout, n, shift,
-                   (const unsigned*)c->counts.p, nblocks, chunk_prefix);
-            std::swap(kin, kout);
-            vin = vout;
-            vout = (vout == (unsigned*)c->vals0.p) ? (unsigned*)c->vals1.p : (unsigned*)c->vals0.p;
-        }
-        const unsigned* skeys = kin;
-        const unsigned* perm = vin;
-        c->last_perm = perm;
-        c->last_skeys = skeys;
+        const unsigned *skeys = nullptr, *perm = nullptr;
+        if (int rs = sort_cells(c, &skeys, &perm)) return rs;
         // pass 2 writes the next step's sort input into the buffer not holding skeys
         unsigned* keys_next = (skeys == (unsigned*)c->keys0.p) ? (unsigned*)c->keys1.p : (unsigned*)c->keys0.p;
         c->key_buf = (keys_next == (unsigned*)c->keys1.p) ? 1 : 0;
@@ -689,6 +811,7 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph = false) {
         c->keys_valid = true;
     }
     if (graph) LAUNCH("step_clock", k_step_end, 1, 1, dsim);
+    c->steps_since_reorder += 1;
     CK(cudaGetLastError());
     // d_Time += dTimeIncrement; i_TimeCycle++ (…MPLocks.cpp:802-803)
     c->sim.time += dt;
@@ -708,6 +831,23 @@ int step(mpm_ctx* c, double dt, int contact, bool graph = false) {
 // state advances by two steps; launching the graph once then brings the
 // device to the same point.
 int advance_graph(mpm_ctx* c, int nsteps, double dt, int contact) {
+    if (c->reorder_pending && c->have_particles) {
+        int rc = reorder(c);
+        if (rc) return rc;
+    }
+    if (c->reorder_interval > 0 && c->form == MPM_FORM_FP32) {  // periodic: advance in runs between reorders
+        while (nsteps > 0) {
+            const long long left = std::max<long long>(1, c->reorder_interval - c->steps_since_reorder);
+            const int k = (int)std::min<long long>(nsteps, left);
+            c->reorder_interval = -c->reorder_interval;  // no nested reorder inside the run
+            int rc = advance_graph(c, k, dt, contact);
+            c->reorder_interval = -c->reorder_interval;
+            if (rc) return rc;
+            nsteps -= k;
+            if (c->steps_since_reorder >= c->reorder_interval && (rc = reorder(c))) return rc;
+        }
+        return MPM_OK;
+    }
     int s = 0;
     auto plain = [&](int k) -> int {
         for (int i = 0; i < k; ++i)
@@ -760,6 +900,7 @@ int advance_graph(mpm_ctx* c, int nsteps, double dt, int contact) {
     for (; nsteps - s >= 2; s += 2) {
         CK(cudaGraphLaunch(c->gexec, c->stream));
         c->launches += c->g_launches;
+        c->steps_since_reorder += 2;
         c->sim.time += dt;
         c->sim.step += 1;
         c->sim.time += dt;
@@ -992,6 +1133,12 @@ int mpm_set_option(mpm_ctx* c, int key, double value) {
         case MPM_OPT_GRAPH:
             c->use_graph = value != 0.0;
             return MPM_OK;
+        case MPM_OPT_REORDER:
+            if (!(value >= -1.0 && value < 2147483647.0) || value != (double)(long long)value)
+                return fail(c, MPM_ERR_ARG, "reorder interval must be -1, 0 or a step count");
+            c->reorder_interval = (int)value;
+            if (c->reorder_interval < 0) c->reorder_pending = false;
+            return MPM_OK;
         case MPM_OPT_GATHER:
             if (value != 0.0 && value != 1.0) return fail(c, MPM_ERR_ARG, "gather mode must be 0 or 1");
             c->gather_batch = (int)value;
@@ -1136,6 +1283,9 @@ int mpm_upload_particles(mpm_ctx* c, const mpm_particles* p, int64_t n) {
     c->nsurf = (int)*c->h_err;
     c->have_particles = true;
     c->keys_valid = false;
+    c->have_orig = false;  // the upload is in the caller's order
+    c->reorder_pending = c->form == MPM_FORM_FP32 && c->reorder_interval >= 0;
+    c->last_perm = c->last_skeys = nullptr;
     return MPM_OK;
 }
 
@@ -1156,6 +1306,12 @@ int mpm_upload_dc_list(mpm_ctx* c, const uint32_t* idx, int64_t n) {
         LAUNCH("fill", k_clear_flag, blocks_for(c->n), NTHREADS, (uint8_t*)c->pflags.p, c->n, (uint8_t)PF_IN_DC);
     if (n > 0) {
         CK(cudaMemcpyAsync(c->dclist.p, idx, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
+        if (c->have_orig) {  // caller's indices -> slots
+            if ((rc = ensure(c, c->ptmp, (size_t)c->n * 4))) return rc;
+            LAUNCH("fill", k_invert, blocks_for(c->n), NTHREADS, (const unsigned*)c->orig.p, (unsigned*)c->ptmp.p, c->n);
+            LAUNCH("fill", k_remap_list, blocks_for(n), NTHREADS, (unsigned*)c->dclist.p, (long long)n,
+                   (const unsigned*)c->ptmp.p);
+        }
         LAUNCH("fill", k_mark_dc, blocks_for(n), NTHREADS, (const unsigned*)c->dclist.p, (int)n,
                (uint8_t*)c->pflags.p);
     }
@@ -1261,13 +1417,26 @@ int mpm_download_particles(mpm_ctx* c, mpm_particles* p) {
         CK(cudaStreamSynchronize(c->stream));  // staging is reused by the next field
     }
     if (n > 0) {
-        if (p->material)
-            CK(cudaMemcpyAsync(p->material, c->material.p, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
-        if (p->pflags) {
-            CK(cudaMemcpyAsync(p->pflags, c->pflags.p, (size_t)n, cudaMemcpyDeviceToHost, c->stream));
-        }
-        if (p->dc_mult)
-            CK(cudaMemcpyAsync(p->dc_mult, c->dc_mult.p, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
+        // in the caller's order: through the staging buffer when the slots are in cell order
+        auto get = [&](void* host, const DevBuf& b, int es) -> int {
+            if (!host) return MPM_OK;
+            if (!c->have_orig) {
+                CK(cudaMemcpyAsync(host, b.p, (size_t)n * es, cudaMemcpyDeviceToHost, c->stream));
+                return MPM_OK;
+            }
+            int r = ensure(c, c->staging, (size_t)n * 8);
+            if (r) return r;
+            if (es == 4)
+                LAUNCH("pack", k_scatter_orig<4>, blocks_for(n), NTHREADS, b.p, c->staging.p, (const unsigned*)c->orig.p, n);
+            else
+                LAUNCH("pack", k_scatter_orig<1>, blocks_for(n), NTHREADS, b.p, c->staging.p, (const unsigned*)c->orig.p, n);
+            CK(cudaMemcpyAsync(host, c->staging.p, (size_t)n * es, cudaMemcpyDeviceToHost, c->stream));
+            CK(cudaStreamSynchronize(c->stream));
+            return MPM_OK;
+        };
+        if ((rc = get(p->material, c->material, 4)) || (rc = get(p->pflags, c->pflags, 1)) ||
+            (rc = get(p->dc_mult, c->dc_mult, 4)))
+            return rc;
     }
     CK(cudaStreamSynchronize(c->stream));
     if (p->pflags)
@@ -1379,10 +1548,22 @@ int mpm_cell_order(mpm_ctx* c, uint32_t* keys, uint32_t* sorted_order, int64_t n
         CK(cudaMemcpyAsync(skeys.data(), c->last_skeys, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
     }
     CK(cudaStreamSynchronize(c->stream));
-    // the last step's key of particle perm[s] is its sorted key skeys[s]
-    if (keys)
-        for (int64_t s = 0; s < n; ++s) keys[perm[s]] = skeys[s];
-    if (sorted_order && n > 0) memcpy(sorted_order, perm.data(), (size_t)n * 4);
+    // the last step's key of slot perm[s] is its sorted key skeys[s]
+    if (!c->have_orig) {
+        if (keys)
+            for (int64_t s = 0; s < n; ++s) keys[perm[s]] = skeys[s];
+        if (sorted_order && n > 0) memcpy(sorted_order, perm.data(), (size_t)n * 4);
+        return MPM_OK;
+    }
+    // slots in cell order: keys by the caller's index, and the stable order of those indices by key
+    std::vector<uint32_t> orig((size_t)n), k((size_t)n);
+    CK(cudaMemcpy(orig.data(), c->orig.p, (size_t)n * 4, cudaMemcpyDeviceToHost));
+    for (int64_t s = 0; s < n; ++s) k[orig[perm[s]]] = skeys[s];
+    if (keys) memcpy(keys, k.data(), (size_t)n * 4);
+    if (sorted_order) {
+        for (int64_t i = 0; i < n; ++i) sorted_order[i] = (uint32_t)i;
+        std::stable_sort(sorted_order, sorted_order + n, [&](uint32_t a, uint32_t b) { return k[a] < k[b]; });
+    }
     return MPM_OK;
 }
 
@@ -1393,6 +1574,11 @@ int mpm_upload_monitor_mask(mpm_ctx* c, const uint8_t* mask, int64_t n) {
     int rc = ensure(c, c->mon_mask, (size_t)std::max<int64_t>(1, n));
     if (rc) return rc;
     if (n > 0) CK(cudaMemcpyAsync(c->mon_mask.p, mask, (size_t)n, cudaMemcpyHostToDevice, c->stream));
+    if (n > 0 && c->have_orig) {  // slot s takes the caller's entry orig[s]
+        if ((rc = ensure(c, c->ptmp, (size_t)n))) return rc;
+        LAUNCH("fill", k_permute<1>, blocks_for(n), NTHREADS, c->mon_mask.p, c->ptmp.p, (const unsigned*)c->orig.p, n, 1);
+        CK(cudaMemcpyAsync(c->mon_mask.p, c->ptmp.p, (size_t)n, cudaMemcpyDeviceToDevice, c->stream));
+    }
     CK(cudaStreamSynchronize(c->stream));
     c->have_mon = true;
     return MPM_OK;
@@ -1441,6 +1627,11 @@ int mpm_autotune(mpm_ctx* c, int32_t steps, double dt, int contact, mpm_tune_res
     if (!c) return MPM_ERR_ARG;
     if (steps < 1 || !(dt > 0.0)) return fail(c, MPM_ERR_ARG, "bad autotune request");
     if (!c->have_particles) return fail(c, MPM_ERR_STATE, "no particles uploaded");
+    if (c->reorder_pending) {  // the trials time the storage order the run will have
+        int r0 = reorder(c);
+        if (r0) return r0;
+    }
+    const long long since0 = c->steps_since_reorder;
     // everything a step writes that outlives the step
     DevBuf* state[] = {&c->pos,        &c->vel,      &c->F,          &c->stress,  &c->strain,  &c->eps_p,
                        &c->vol,        &c->e_strain, &c->e_strain_max, &c->e_strain_ti, &c->e_plastic,
@@ -1505,6 +1696,7 @@ int mpm_autotune(mpm_ctx* c, int32_t steps, double dt, int contact, mpm_tune_res
             }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
+    c->steps_since_reorder = since0;
     c->profile = prof0;
     c->sim = sim0;
     if (rc) {

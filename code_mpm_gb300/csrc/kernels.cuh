@@ -1266,9 +1266,10 @@ __global__ void k_contact_normal(PView<T> P, NView<T> nd, Geom g, const unsigned
             facing = dot3f(d, gp) > 0.0f;
         }
         if (!facing) continue;
+        const unsigned who = (P.orig ? P.orig[p] : (unsigned)p) + 1u;  // the caller's particle order
         if (!apply) {
-            atomicMax(&nd.nowner[nid], (unsigned)p + 1u);
-        } else if (nd.nowner[nid] == (unsigned)p + 1u) {
+            atomicMax(&nd.nowner[nid], who);
+        } else if (nd.nowner[nid] == who) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) nd.mg[c * nn + nid] = gp[c];
         }

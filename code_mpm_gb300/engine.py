@@ -116,6 +116,7 @@ OPT_P2G_BLOCK = 4
 OPT_PASS_BLOCK = 5
 OPT_GATHER = 6
 OPT_GRAPH = 7
+OPT_REORDER = 8
 
 
 def library_path() -> str:

@@ -75,6 +75,7 @@ extern "C" {
 #define MPM_OPT_PASS_BLOCK 5     /* G2P pass-2 threads per block (128, 256 or 512) */
 #define MPM_OPT_GATHER 6         /* G2P node gathers: 0 = one corner at a time, 1 = several corners' loads issued together */
 #define MPM_OPT_GRAPH 7          /* 1 (default): mpm_advance replays a captured two-step CUDA graph in the steady state; 0: launch every kernel */
+#define MPM_OPT_REORDER 8        /* FP32 form: store particles in cell order after each particle upload (0, default), also every N steps (N > 0), or never (-1); results stay in the caller's order */
 
 typedef struct mpm_ctx mpm_ctx;
 
