@@ -735,7 +735,10 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph = false) {
         // the mass threshold in the form's type (FP32: rounded down, so float masses compare exactly)
         const T mm = sizeof(T) == 4 ? (T)fps_float_threshold(c->sim.mass_min) : (T)c->sim.mass_min;
         LAUNCH("node_ratio", k_node_ratio<T>, nodeblocks, NTHREADS, N, (const T*)c->g_force.p, mm, 1, 0);
-        if (c->gather_batch)
+        if (c->p2g_reduce == 2)  // the same reduction as P2G: shared-memory cell runs
+            LAUNCH_SMEM("pass1_remap", k_pass1_cells<T>, blocks_for(n, c->p2g_block), c->p2g_block,
+                        pass1_cells_smem<T>(c->p2g_block), P, N, g, skeys, perm, n, (T)dt, mm, contact);
+        else if (c->gather_batch)
             LAUNCH("pass1_remap", (k_pass1_remap<T, 1>), blocks_for(n), NTHREADS, P, N, g, skeys, perm, n, (T)dt, mm,
                    contact);
         else

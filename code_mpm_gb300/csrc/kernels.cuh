@@ -164,6 +164,20 @@ __device__ __forceinline__ void particle_bases(const PView<T>& P, const Geom& g,
     }
 }
 
+// Prefetch into L2 the bytes of elements [p0, p0 + cnt) of an array of n
+// ES-byte elements (a bulk prefetch, trimmed to 16-byte boundaries inside
+// the array; a hint with no effect on results).
+__device__ __forceinline__ void prefetch_l2(const void* base, int es, long long n, long long p0, int cnt) {
+    if (!base) return;
+    const unsigned long long lo = (unsigned long long)base, hi = lo + (unsigned long long)n * es;
+    unsigned long long a = lo + (unsigned long long)p0 * es;
+    unsigned long long b = lo + (unsigned long long)min((long long)n, p0 + cnt) * es;
+    a = max(a & ~15ULL, (lo + 15) & ~15ULL);
+    b = min((b + 15) & ~15ULL, hi & ~15ULL);
+    if (b > a)
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"((unsigned)(b - a)) : "memory");
+}
+
 // ---------------------------------------------------------------------------
 // P2G (M2G, …MPLocks.cpp:48-89): per particle and corner, mass N m, momentum
 // N (m v), force -V (grad N . sigma) + N f_ext (Voigt order xx yy zz xy yz zx,
@@ -663,6 +677,124 @@ __global__ void __launch_bounds__(256) k_pass1_remap(PView<T> P, NView<T> nd, Ge
     }
 }
 
+// ---------------------------------------------------------------------------
+// G2P pass 1 + velocity remap, cell-centric (used with P2G mode 2): each slot's
+// thread updates its particle's velocity from the node records (in corner
+// order, as k_pass1_remap) and stages N (per axis) and m v in shared memory;
+// one thread per (cell run, corner) then sums N m v over the run in slot order
+// and issues three atomics.  Skipped particles (platen on the contact path)
+// stay in their run with zero weight.
+// ---------------------------------------------------------------------------
+template <typename T>
+__host__ __device__ constexpr size_t pass1_cells_smem(int bs) {
+    return (size_t)9 * bs * sizeof(T) + (size_t)bs * 8 + (size_t)(bs + 1) * 4 + 64 * 4;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(512) k_pass1_cells(PView<T> P, NView<T> nd, Geom g,
+                                                     const unsigned* __restrict__ skeys,
+                                                     const unsigned* __restrict__ perm, long long n, T dt,
+                                                     T mass_min, int contact) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int bs = blockDim.x, t = threadIdx.x, lane = t & 31, w = t >> 5;
+    T* sn = reinterpret_cast<T*>(smem_raw);  // 6 x bs: Nx0 Nx1 Ny0 Ny1 Nz0 Nz1
+    T* smv = sn + 6 * bs;                    // 3 x bs: m v
+    unsigned* skey = reinterpret_cast<unsigned*>(smv + 3 * bs);
+    unsigned* sperm = skey + bs;
+    int* run_start = reinterpret_cast<int*>(sperm + bs);
+    int* wsum = run_start + bs + 1;
+    const long long s = blockIdx.x * (long long)bs + t;
+    const unsigned key = (s < n) ? skeys[s] : 0xffffffffu;
+    const bool key_ok = key < g.key_max;
+    const long long np = P.n, nn = nd.nn;
+    if (key_ok) {
+        const long long p = perm[s];
+        sperm[t] = (unsigned)p;
+        const bool valid = !(contact && (P.pflags[p] & 8u));
+        T N6[6] = {0, 0, 0, 0, 0, 0}, mv[3] = {0, 0, 0};
+        if (valid) {
+            const Geom& gs = spec_geom(g, P.sid, p);
+            int b[3];
+            key_to_base(key, gs, b);
+            Bases<T> B;
+            particle_bases<T>(P, gs, p, b, B);
+            const T m = P.mass[p];
+            T v[3] = {P.vel[p], P.vel[np + p], P.vel[2 * np + p]};
+#pragma unroll 1
+            for (int k = 0; k < 8; ++k) {
+                const long long nid = corner_node(gs, b, k);
+                if (nid < 0) continue;
+                const Quad<T> r = ld_quad(nd.rec + 8 * nid);
+                if (!(r.w != (T)0)) continue;
+                T N, G[3];
+                B.corner(k, N, G);
+                v[0] = v[0] + N * r.x * dt;
+                v[1] = v[1] + N * r.y * dt;
+                v[2] = v[2] + N * r.z * dt;
+            }
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                P.vel[c * np + p] = v[c];
+                mv[c] = m * v[c];
+            }
+            N6[0] = B.Nx[0];
+            N6[1] = B.Nx[1];
+            N6[2] = B.Ny[0];
+            N6[3] = B.Ny[1];
+            N6[4] = B.Nz[0];
+            N6[5] = B.Nz[1];
+        }
+#pragma unroll
+        for (int c = 0; c < 6; ++c) sn[c * bs + t] = N6[c];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) smv[c * bs + t] = mv[c];
+    }
+    skey[t] = key;
+    __syncthreads();
+    const bool head = key_ok && (t == 0 || skey[t - 1] != key);
+    const unsigned bal = __ballot_sync(FULL_MASK, head);
+    if (lane == 0) wsum[w] = __popc(bal);
+    const int nvalid = __syncthreads_count(key_ok);
+    if (t < 32) {
+        const int nw = bs >> 5;
+        int v = (t < nw) ? wsum[t] : 0;
+        int incl = v;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            int o = __shfl_up_sync(FULL_MASK, incl, off);
+            if (t >= off) incl += o;
+        }
+        if (t < nw) wsum[t] = incl - v;
+        if (t == 31) wsum[32] = incl;
+    }
+    __syncthreads();
+    if (head) run_start[wsum[w] + __popc(bal & ((1u << lane) - 1u))] = t;
+    const int R = wsum[32];
+    if (t == 0) run_start[R] = nvalid;
+    __syncthreads();
+    for (int item = t; item < R * 8; item += bs) {
+        const int r = item >> 3, k = item & 7;
+        const int ix = (k >> 2) & 1, iy = (k >> 1) & 1, iz = k & 1;
+        const int a = run_start[r], e = run_start[r + 1];
+        T q0 = 0, q1 = 0, q2 = 0;
+        for (int i = a; i < e; ++i) {
+            const T N = sn[ix * bs + i] * sn[(2 + iy) * bs + i] * sn[(4 + iz) * bs + i];
+            q0 += N * smv[i];
+            q1 += N * smv[bs + i];
+            q2 += N * smv[2 * bs + i];
+        }
+        const Geom& gs = spec_geom(g, P.sid, sperm[a]);
+        int b[3];
+        key_to_base(skey[a], gs, b);
+        const long long nid = corner_node(gs, b, k);
+        if (nid >= 0) {
+            atomicAdd(&nd.q[nid], q0);
+            atomicAdd(&nd.q[nn + nid], q1);
+            atomicAdd(&nd.q[2 * nn + nid], q2);
+        }
+    }
+}
+
 // Remap finish: v_i += q_i / m_i on nodes with m_i > mass_min (:559-560).
 template <typename T>
 __device__ __forceinline__ void node_remap(const NView<T>& nd, long long i, T mass_min) {
@@ -789,6 +921,60 @@ __device__ __forceinline__ unsigned warp_slot(unsigned* counter) {
     return base + __popc(m & ((1u << lane) - 1u));
 }
 
+// The particle arrays pass 2 reads, one per thread of a block's first warps:
+// prefetched into L2 for the block's particle range while the warps gather
+// the node records.
+template <typename T>
+__device__ __forceinline__ void pass2_prefetch(const PView<T>& P, long long p0, int cnt, int contact) {
+    const int t = threadIdx.x;
+    const long long n = P.n;
+    const void* base = nullptr;
+    int es = (int)sizeof(T);
+    long long comp = 0;
+    if (t < 3) {
+        base = P.pos;
+        es = 8;
+        comp = t;
+    } else if (t < 12) {
+        base = P.F;
+        comp = t - 3;
+    } else if (t < 18) {
+        base = P.stress;
+        comp = t - 12;
+    } else if (t < 24) {
+        base = P.strain;
+        comp = t - 18;
+    } else if (t < 30) {
+        base = P.eps_p;
+        comp = t - 24;
+    } else if (t == 30) {
+        base = P.vol0;
+    } else if (t == 31) {
+        base = P.vol;
+    } else if (t == 32) {
+        base = P.backstress;
+    } else if (t == 33) {
+        base = P.e_strain;
+        es = 8;
+    } else if (t == 34) {
+        base = P.e_plastic;
+        es = 8;
+    } else if (t == 35) {
+        base = P.material;
+        es = 4;
+    } else if (t == 36) {
+        base = P.pflags;
+        es = 1;
+    } else if (t == 37 && !contact) {
+        base = P.e_strain_ti;
+        es = 8;
+    } else if (t == 38 && !contact) {
+        base = P.e_strain_max;
+        es = 8;
+    }
+    if (base) prefetch_l2((const char*)base + comp * n * es, es, n, p0, cnt);
+}
+
 // ---------------------------------------------------------------------------
 // G2P pass 2 + constitutive update + platen (G2P_P2_SmallStrain,
 // …MPLocks.cpp:175-280; contact …_Contact.cpp:438-525 and :531-540).
@@ -804,6 +990,7 @@ __global__ void __launch_bounds__(512) k_pass2(PView<T> P, NView<T> nd, Geom g, 
                                                int nmat, StepArgs a, unsigned* err) {
     long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long np = P.n, nn = nd.nn;
+    if (threadIdx.x < 64) pass2_prefetch<T>(P, blockIdx.x * (long long)blockDim.x, blockDim.x, a.contact);
     if (p >= np) return;
     const unsigned fl = P.pflags[p];
     const T dt = form_const<T>(a.dt, a.dt_f);
