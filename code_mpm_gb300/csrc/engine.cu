@@ -521,13 +521,21 @@ int sort_cells(mpm_ctx* c, const unsigned** skeys_out, const unsigned** perm_out
                c->form == MPM_FORM_FP32 ? (float*)c->loc.p : (float*)nullptr, sid);
     int bits = 1;
     while (bits < 32 && ((unsigned long long)1 << bits) <= (unsigned long long)g.key_max) ++bits;
+    // the fewest passes of at most 10-bit digits (27-bit keys: three 9-bit passes)
+    const int passes = (bits + 9) / 10;
+    const int db = std::max(8, (bits + passes - 1) / passes);
     const int nblocks = (int)((n + RS_TILE - 1) / RS_TILE);
     unsigned *kin = key_src, *vin = nullptr;
     unsigned *kout = key_other, *vout = (unsigned*)c->vals0.p;
-    const int hist_total = 256 * nblocks;
+    const int hist_total = (1 << db) * nblocks;
     const int nchunks = (hist_total + RS_SCAN_CHUNK - 1) / RS_SCAN_CHUNK;
-    for (int shift = 0; shift < bits; shift += 8) {
-        LAUNCH("rs_hist", k_rs_hist, nblocks, RS_THREADS, kin, n, shift, (unsigned*)c->counts.p, nblocks);
+    for (int shift = 0; shift < bits; shift += db) {
+        if (db == 8)
+            LAUNCH("rs_hist", k_rs_hist<8>, nblocks, RS_THREADS, kin, n, shift, (unsigned*)c->counts.p, nblocks);
+        else if (db == 9)
+            LAUNCH("rs_hist", k_rs_hist<9>, nblocks, RS_THREADS, kin, n, shift, (unsigned*)c->counts.p, nblocks);
+        else
+            LAUNCH("rs_hist", k_rs_hist<10>, nblocks, RS_THREADS, kin, n, shift, (unsigned*)c->counts.p, nblocks);
         const unsigned* chunk_prefix = nullptr;
         if (nchunks > 1) {
             LAUNCH("rs_scan", k_rs_scan_chunks, nchunks, RS_SCAN_THREADS, (unsigned*)c->counts.p, hist_total,
@@ -537,8 +545,15 @@ int sort_cells(mpm_ctx* c, const unsigned** skeys_out, const unsigned** perm_out
         } else {
             LAUNCH("rs_scan", k_rs_scan, 1, 1024, (unsigned*)c->counts.p, hist_total);
         }
-        LAUNCH("rs_scatter", k_rs_scatter, nblocks, RS_THREADS, kin, (const unsigned*)vin, kout, vout, n, shift,
-               (const unsigned*)c->counts.p, nblocks, chunk_prefix);
+        if (db == 8)
+            LAUNCH("rs_scatter", k_rs_scatter<8>, nblocks, RS_THREADS, kin, (const unsigned*)vin, kout, vout, n, shift,
+                   (const unsigned*)c->counts.p, nblocks, chunk_prefix);
+        else if (db == 9)
+            LAUNCH("rs_scatter", k_rs_scatter<9>, nblocks, RS_THREADS, kin, (const unsigned*)vin, kout, vout, n, shift,
+                   (const unsigned*)c->counts.p, nblocks, chunk_prefix);
+        else
+            LAUNCH("rs_scatter", k_rs_scatter<10>, nblocks, RS_THREADS, kin, (const unsigned*)vin, kout, vout, n,
+                   shift, (const unsigned*)c->counts.p, nblocks, chunk_prefix);
         std::swap(kin, kout);
         vin = vout;
         vout = (vout == (unsigned*)c->vals0.p) ? (unsigned*)c->vals1.p : (unsigned*)c->vals0.p;
@@ -671,29 +686,33 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph = false) {
         unsigned* keys_next = (skeys == (unsigned*)c->keys0.p) ? (unsigned*)c->keys1.p : (unsigned*)c->keys0.p;
         c->key_buf = (keys_next == (unsigned*)c->keys1.p) ? 1 : 0;
         const unsigned* keys = (const unsigned*)c->keys_copy.p;
-        if (contact) {
-            CK(cudaMemsetAsync(c->cstart.p, 0, (size_t)g.key_max * 4, c->stream));
-            CK(cudaMemsetAsync(c->cend.p, 0, (size_t)g.key_max * 4, c->stream));
+        // FP32 form: the contact mass gradient is accumulated by P2G itself
+        // and P2G marks the active nodes; the FP64 form marks them here and
+        // records the per-cell ranges its bit-exact ordered gather reads.
+        const int fp32 = c->form == MPM_FORM_FP32 ? 1 : 0;
+        const int mg_in_p2g = (contact && fp32) ? 1 : 0;
+        if (!fp32) {
+            if (contact) {
+                CK(cudaMemsetAsync(c->cstart.p, 0, (size_t)g.key_max * 4, c->stream));
+                CK(cudaMemsetAsync(c->cend.p, 0, (size_t)g.key_max * 4, c->stream));
+            }
+            LAUNCH("cell_ranges", k_cell_ranges, blocks_for(n), NTHREADS, skeys, n, g, N.state,
+                   contact ? (unsigned*)c->cstart.p : nullptr, contact ? (unsigned*)c->cend.p : nullptr, perm, P.sid);
         }
-        LAUNCH("cell_ranges", k_cell_ranges, blocks_for(n), NTHREADS, skeys, n, g, N.state,
-               contact ? (unsigned*)c->cstart.p : nullptr, contact ? (unsigned*)c->cend.p : nullptr, perm, P.sid);
+        if (c->p2g_reduce == 2)
+            LAUNCH_SMEM("p2g", k_p2g_cells<T>, blocks_for(n, c->p2g_block), c->p2g_block,
+                        p2g_cells_smem<T>(c->p2g_block), P, N, g, skeys, perm, n, mg_in_p2g, fp32);
+        else if (c->p2g_reduce == 1)
+            LAUNCH("p2g", (k_p2g<T, 1>), blocks_for(n, c->p2g_block), c->p2g_block, P, N, g, skeys, perm, n,
+                   mg_in_p2g, fp32);
+        else
+            LAUNCH("p2g", (k_p2g<T, 0>), blocks_for(n, c->p2g_block), c->p2g_block, P, N, g, skeys, perm, n,
+                   mg_in_p2g, fp32);
         CK(cudaMemsetAsync(c->acount.p, 0, 4, c->stream));
         LAUNCH("active_list", k_compact_state, (unsigned)((nn + CS_THREADS * CS_ROUNDS - 1) / (CS_THREADS * CS_ROUNDS)),
                CS_THREADS, (const unsigned*)N.state, nn, 1u, (unsigned*)c->alist.p, (unsigned*)c->acount.p);
         N.alist = (const unsigned*)c->alist.p;
         c->have_alist = true;
-        // FP32 form: the contact mass gradient is accumulated by P2G itself
-        // (the bit-exact ordered gather below serves the FP64 form).
-        const int mg_in_p2g = (contact && c->form == MPM_FORM_FP32) ? 1 : 0;
-        if (c->p2g_reduce == 2)
-            LAUNCH_SMEM("p2g", k_p2g_cells<T>, blocks_for(n, c->p2g_block), c->p2g_block,
-                        p2g_cells_smem<T>(c->p2g_block), P, N, g, skeys, perm, n, mg_in_p2g);
-        else if (c->p2g_reduce == 1)
-            LAUNCH("p2g", (k_p2g<T, 1>), blocks_for(n, c->p2g_block), c->p2g_block, P, N, g, skeys, perm, n,
-                   mg_in_p2g);
-        else
-            LAUNCH("p2g", (k_p2g<T, 0>), blocks_for(n, c->p2g_block), c->p2g_block, P, N, g, skeys, perm, n,
-                   mg_in_p2g);
         if (c->ndc > 0) {
             CK(cudaMemsetAsync(c->g_owner.p, 0, (size_t)3 * nn * 4, c->stream));
             LAUNCH("dc_claim", k_dc_claim, blocks_for(c->ndc), NTHREADS, (const unsigned*)c->dclist.p, c->ndc, keys,
@@ -929,9 +948,9 @@ int alloc_particles(mpm_ctx* c, long long n) {
         if (rc) return rc;
     }
     const long long nblocks = std::max<long long>(1, (n + RS_TILE - 1) / RS_TILE);
-    int rc = ensure(c, c->counts, (size_t)256 * nblocks * 4);
+    int rc = ensure(c, c->counts, (size_t)1024 * nblocks * 4);
     if (rc) return rc;
-    const long long nchunks = (256 * nblocks + RS_SCAN_CHUNK - 1) / RS_SCAN_CHUNK;
+    const long long nchunks = (1024 * nblocks + RS_SCAN_CHUNK - 1) / RS_SCAN_CHUNK;
     return ensure(c, c->rs_chunk, (size_t)std::max<long long>(1, nchunks) * 4);
 }
 

@@ -191,7 +191,8 @@ __device__ __forceinline__ void prefetch_l2(const void* base, int es, long long 
 // ---------------------------------------------------------------------------
 template <typename T, int REDUCE>
 __global__ void __launch_bounds__(512) k_p2g(PView<T> P, NView<T> nd, Geom g, const unsigned* __restrict__ skeys,
-                                             const unsigned* __restrict__ perm, long long n, int with_mg) {
+                                             const unsigned* __restrict__ perm, long long n, int with_mg,
+                                             int mark_active) {
     long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     unsigned key = (s < n) ? skeys[s] : 0xffffffffu;
     const bool valid = key < g.key_max;
@@ -245,6 +246,7 @@ __global__ void __launch_bounds__(512) k_p2g(PView<T> P, NView<T> nd, Geom g, co
         if (valid && (!REDUCE || run.tail)) {
             long long nid = corner_node(*gsp, b, k);
             if (nid >= 0) {
+                if (mark_active && !(nd.state[nid] & 1u)) atomicOr(&nd.state[nid], 1u);
                 atomicAdd(&nd.mass[nid], c[0]);
                 atomicAdd(&nd.mom[nid], c[1]);
                 atomicAdd(&nd.mom[nn + nid], c[2]);
@@ -281,7 +283,8 @@ __host__ __device__ constexpr size_t p2g_cells_smem(int bs) {
 
 template <typename T>
 __global__ void __launch_bounds__(512) k_p2g_cells(PView<T> P, NView<T> nd, Geom g, const unsigned* __restrict__ skeys,
-                                                   const unsigned* __restrict__ perm, long long n, int with_mg) {
+                                                   const unsigned* __restrict__ perm, long long n, int with_mg,
+                                                   int mark_active) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int bs = blockDim.x, t = threadIdx.x, lane = t & 31, w = t >> 5;
     T* sw = reinterpret_cast<T*>(smem_raw);        // 12 x bs: Nx0 Nx1 Ny0 Ny1 Nz0 Nz1 gx0 gx1 gy0 gy1 gz0 gz1
@@ -381,6 +384,8 @@ __global__ void __launch_bounds__(512) k_p2g_cells(PView<T> P, NView<T> nd, Geom
         key_to_base(skey[a], gs, b);
         const long long nid = corner_node(gs, b, k);
         if (nid >= 0) {
+            // active nodes: the in-range corners of occupied cells (b_Active, …MPLocks.cpp:36)
+            if (mark_active && !(nd.state[nid] & 1u)) atomicOr(&nd.state[nid], 1u);
             atomicAdd(&nd.mass[nid], am);
             atomicAdd(&nd.mom[nid], ap0);
             atomicAdd(&nd.mom[nn + nid], ap1);

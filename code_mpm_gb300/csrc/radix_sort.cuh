@@ -1,4 +1,5 @@
-// Stable LSD radix sort of (32-bit key, 32-bit value) pairs, 8-bit digits.
+// Stable LSD radix sort of (32-bit key, 32-bit value) pairs, DB-bit digits
+// (8 to 10; the caller picks the fewest passes that cover the key bits).
 //
 // Used to order particles by cell key each step.  Stability within a digit
 // pass comes from ranking every key against the keys before it in its tile
@@ -21,19 +22,21 @@ constexpr int RS_ITEMS = 16;  // keys per thread
 constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
 constexpr int RS_WARP_TILE = 32 * RS_ITEMS;
 
+template <int DB = 8>
 static __global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const unsigned* __restrict__ keys, long long n, int shift,
                                                          unsigned* __restrict__ counts, int nblocks) {
-    __shared__ unsigned h[256];
-    for (int i = threadIdx.x; i < 256; i += RS_THREADS) h[i] = 0;
+    constexpr unsigned NB = 1u << DB, MASK = NB - 1u;
+    __shared__ unsigned h[NB];
+    for (int i = threadIdx.x; i < (int)NB; i += RS_THREADS) h[i] = 0;
     __syncthreads();
     long long base = (long long)blockIdx.x * RS_TILE;
 #pragma unroll 4
     for (int j = 0; j < RS_ITEMS; ++j) {
         long long idx = base + (long long)j * RS_THREADS + threadIdx.x;
-        if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & 255u], 1u);
+        if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & MASK], 1u);
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < 256; i += RS_THREADS) counts[(size_t)i * nblocks + blockIdx.x] = h[i];
+    for (int i = threadIdx.x; i < (int)NB; i += RS_THREADS) counts[(size_t)i * nblocks + blockIdx.x] = h[i];
 }
 
 // Exclusive scan of counts[0..total) in place, one block of 1024 threads.
@@ -106,17 +109,19 @@ static __global__ void __launch_bounds__(RS_SCAN_THREADS) k_rs_scan_chunks(unsig
     if (t == RS_SCAN_THREADS - 1) chunk_totals[blockIdx.x] = wsum[31];
 }
 
+template <int DB = 8>
 static __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const unsigned* __restrict__ kin,
                                                             const unsigned* __restrict__ vin,
                                                             unsigned* __restrict__ kout, unsigned* __restrict__ vout,
                                                             long long n, int shift,
                                                             const unsigned* __restrict__ offs, int nblocks,
                                                             const unsigned* __restrict__ chunk_prefix) {
-    __shared__ unsigned wcnt[RS_WARPS][256];
-    __shared__ unsigned gofs[256];
+    constexpr unsigned NB = 1u << DB, MASK = NB - 1u;
+    __shared__ unsigned wcnt[RS_WARPS][NB];
+    __shared__ unsigned gofs[NB];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int i = threadIdx.x; i < RS_WARPS * 256; i += RS_THREADS) (&wcnt[0][0])[i] = 0;
-    for (int i = threadIdx.x; i < 256; i += RS_THREADS) {
+    for (int i = threadIdx.x; i < RS_WARPS * (int)NB; i += RS_THREADS) (&wcnt[0][0])[i] = 0;
+    for (int i = threadIdx.x; i < (int)NB; i += RS_THREADS) {
         size_t j = (size_t)i * nblocks + blockIdx.x;
         gofs[i] = offs[j] + (chunk_prefix ? chunk_prefix[j / RS_SCAN_CHUNK] : 0u);
     }
@@ -130,7 +135,7 @@ static __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const unsigned
         bool ok = idx < n;
         unsigned key = ok ? kin[idx] : 0u;
         unsigned val = ok ? (vin ? vin[idx] : (unsigned)idx) : 0u;  // no input values: the identity
-        unsigned d = ok ? ((key >> shift) & 255u) : (256u + lane);  // invalid lanes never match a digit
+        unsigned d = ok ? ((key >> shift) & MASK) : (NB + lane);  // invalid lanes never match a digit
         unsigned peers = __match_any_sync(0xffffffffu, d);
         unsigned rank = 0;
         if (ok) rank = wcnt[w][d] + __popc(peers & lt);
@@ -142,7 +147,7 @@ static __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const unsigned
         r[c] = rank;
     }
     __syncthreads();
-    for (int d = threadIdx.x; d < 256; d += RS_THREADS) {
+    for (int d = threadIdx.x; d < (int)NB; d += RS_THREADS) {
         unsigned run = 0;
         for (int ww = 0; ww < RS_WARPS; ++ww) {
             unsigned t = wcnt[ww][d];
@@ -155,7 +160,7 @@ static __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const unsigned
     for (int c = 0; c < RS_ITEMS; ++c) {
         long long idx = base + c * 32 + lane;
         if (idx < n) {
-            unsigned d = (k[c] >> shift) & 255u;
+            unsigned d = (k[c] >> shift) & MASK;
             unsigned dst = gofs[d] + wcnt[w][d] + r[c];
             kout[dst] = k[c];
             vout[dst] = v[c];
