@@ -123,6 +123,7 @@ struct mpm_ctx {
     bool have_orig = false, reorder_pending = false;
     int reorder_interval = 0;  // -1: never; 0: after each particle upload; N: also every N steps
     long long steps_since_reorder = 0;
+    bool owner_clean = false;  // displacement-control claims all zero (phase B clears them after use)
 
     mpm_ctx() {
         DevBuf* list[] = {&xtab, &err_word, &pos, &vel, &fext, &mass, &vol, &vol0, &F, &stress, &strain, &eps_p,
@@ -714,7 +715,8 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph = false) {
         N.alist = (const unsigned*)c->alist.p;
         c->have_alist = true;
         if (c->ndc > 0) {
-            CK(cudaMemsetAsync(c->g_owner.p, 0, (size_t)3 * nn * 4, c->stream));
+            if (!c->owner_clean) CK(cudaMemsetAsync(c->g_owner.p, 0, (size_t)3 * nn * 4, c->stream));
+            c->owner_clean = false;  // claims in use until phase B clears them
             LAUNCH("dc_claim", k_dc_claim, blocks_for(c->ndc), NTHREADS, (const unsigned*)c->dclist.p, c->ndc, keys,
                    (const uint8_t*)c->pflags.p, g, (unsigned*)c->g_owner.p, nn, contact, P.sid);
         }
@@ -743,17 +745,11 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph = false) {
                 LAUNCH("contact_flags", k_contact_flags<T>, sb, NTHREADS, P, N, g, keys, surf, ns);
             }
         }
-        if (!contact && c->ndc > 0)
-            LAUNCH("dc_apply", k_dc_apply<T>, blocks_for(c->ndc), NTHREADS, (const unsigned*)c->dclist.p, c->ndc,
-                   keys, P, N, g, contact);
-        LAUNCH("grid_update", k_grid_update<T>, nodeblocks, NTHREADS, N, (T)dt, c->sim.damping, contact,
-               c->floor_friction);
-        if (contact && c->ndc > 0)
-            LAUNCH("dc_apply", k_dc_apply<T>, blocks_for(c->ndc), NTHREADS, (const unsigned*)c->dclist.p, c->ndc,
-                   keys, P, N, g, contact);
         // the mass threshold in the form's type (FP32: rounded down, so float masses compare exactly)
         const T mm = sizeof(T) == 4 ? (T)fps_float_threshold(c->sim.mass_min) : (T)c->sim.mass_min;
-        LAUNCH("node_ratio", k_node_ratio<T>, nodeblocks, NTHREADS, N, (const T*)c->g_force.p, mm, 1, 0);
+        // displacement control, grid update, displacement control, f/m: one pass over the active nodes
+        LAUNCH("node_phase_a", k_node_phase_a<T>, nodeblocks, NTHREADS, N, (T)dt, c->sim.damping, contact,
+               c->floor_friction, (const unsigned*)c->dclist.p, c->ndc, (const T*)c->vel.p, n, mm);
         if (c->p2g_reduce == 2)  // the same reduction as P2G: shared-memory cell runs
             LAUNCH_SMEM("pass1_remap", k_pass1_cells<T>, blocks_for(n, c->p2g_block), c->p2g_block,
                         pass1_cells_smem<T>(c->p2g_block), P, N, g, skeys, perm, n, (T)dt, mm, contact);
@@ -763,19 +759,10 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph = false) {
         else
             LAUNCH("pass1_remap", (k_pass1_remap<T, 0>), blocks_for(n), NTHREADS, P, N, g, skeys, perm, n, (T)dt, mm,
                    contact);
-        LAUNCH("node_remap", k_node_remap<T>, nodeblocks, NTHREADS, N, mm);
-        if (!contact) {
-            if (c->ndc > 0)
-                LAUNCH("dc_apply", k_dc_apply<T>, blocks_for(c->ndc), NTHREADS, (const unsigned*)c->dclist.p,
-                       c->ndc, keys, P, N, g, contact);
-            LAUNCH("node_bc", k_node_bc<T>, nodeblocks, NTHREADS, N);
-        } else {
-            LAUNCH("node_bc", k_node_bc<T>, nodeblocks, NTHREADS, N);
-            if (c->ndc > 0)
-                LAUNCH("dc_apply", k_dc_apply<T>, blocks_for(c->ndc), NTHREADS, (const unsigned*)c->dclist.p,
-                       c->ndc, keys, P, N, g, contact);
-        }
-        LAUNCH("node_ratio", k_node_ratio<T>, nodeblocks, NTHREADS, N, (const T*)c->g_mom.p, mm, 0, 1);
+        // remap, displacement control and BC in the path's order, p/m and v: one pass
+        LAUNCH("node_phase_b", k_node_phase_b<T>, nodeblocks, NTHREADS, N, contact, (const unsigned*)c->dclist.p,
+               c->ndc, (const T*)c->vel.p, n, mm);
+        if (c->ndc > 0) c->owner_clean = true;
         StepArgs a;
         a.dt = dt;
         a.mass_min = c->sim.mass_min;
@@ -1093,8 +1080,9 @@ int mpm_create_batch(const mpm_grid_desc* grids, int32_t nspec, int form, mpm_ct
                 {&c->g_ratio, 8 * nn * t}, {&c->g_q, 3 * nn * t},    {&c->g_owner, 3 * nn * 4},
                 {&c->g_nowner, nn * 4},    {&c->g_need, nn * 4},     {&c->g_list, nn * 4},
                 {&c->g_count, 4},          {&c->alist, nn * 4},       {&c->acount, 4},
-                {&c->cstart, (size_t)g.key_max * 4},
-                {&c->cend, (size_t)g.key_max * 4}};
+                // per-cell particle ranges: the FP64 form's exact contact gather only
+                {&c->cstart, c->form == MPM_FORM_FP64 ? (size_t)g.key_max * 4 : 0},
+                {&c->cend, c->form == MPM_FORM_FP64 ? (size_t)g.key_max * 4 : 0}};
     for (auto& e : plan) {
         if ((rc = ensure(c, *e.b, e.bytes))) return bail(rc);
         if (cudaMemset(e.b->p, 0, e.bytes) != cudaSuccess) return bail(MPM_ERR_CUDA);

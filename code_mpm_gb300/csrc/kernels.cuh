@@ -837,6 +837,62 @@ __global__ void k_node_bc(NView<T> nd) {
     NODE_LOOP(nd, i) node_bc<T>(nd, i);
 }
 
+// Displacement control applied from the node's side: for each axis whose
+// last-writer claim (list position + 1, k_dc_claim) is set, the claiming
+// platen particle's velocity, as k_dc_apply writes it.
+template <typename T>
+__device__ __forceinline__ void node_dc(const NView<T>& nd, long long i, const unsigned* __restrict__ dclist,
+                                        const T* __restrict__ pvel, long long np, bool clear = false) {
+    const long long nn = nd.nn;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const unsigned k1 = nd.owner[a * nn + i];
+        if (!k1) continue;
+        if (clear) nd.owner[a * nn + i] = 0u;  // the claims' last use this step: clean for the next
+        const T vp = pvel[a * np + dclist[k1 - 1]];
+        nd.vel[a * nn + i] = vp;
+        nd.mom[a * nn + i] = nd.mass[i] * vp;
+        nd.force[a * nn + i] = (T)0;
+    }
+}
+
+// The node work between P2G and pass 1, one pass over the active nodes:
+// displacement control (non-contact: before the update), the grid update,
+// displacement control (contact: after it), then the record f/m.
+template <typename T>
+__global__ void k_node_phase_a(NView<T> nd, T dt, double damping, int contact, int floor_friction,
+                               const unsigned* __restrict__ dclist, int ndc, const T* __restrict__ pvel, long long np,
+                               T mass_min) {
+    NODE_LOOP(nd, i) {
+        if (!(nd.state[i] & 1u)) continue;
+        if (!contact && ndc) node_dc<T>(nd, i, dclist, pvel, np);
+        grid_update_node<T>(nd, i, dt, damping, contact, floor_friction);
+        if (contact && ndc) node_dc<T>(nd, i, dclist, pvel, np);
+        node_ratio<T>(nd, i, nd.force, mass_min, 1, 0);
+    }
+}
+
+// The node work between pass 1 and pass 2: the remap v += q/m, displacement
+// control and BC in the path's order, then the record p/m and v.  The claims
+// are cleared after this last use (every claimed node is active: platen
+// particles take part in P2G).
+template <typename T>
+__global__ void k_node_phase_b(NView<T> nd, int contact, const unsigned* __restrict__ dclist, int ndc,
+                               const T* __restrict__ pvel, long long np, T mass_min) {
+    NODE_LOOP(nd, i) {
+        if (!(nd.state[i] & 1u)) continue;
+        node_remap<T>(nd, i, mass_min);
+        if (!contact) {
+            if (ndc) node_dc<T>(nd, i, dclist, pvel, np, true);
+            node_bc<T>(nd, i);
+        } else {
+            node_bc<T>(nd, i);
+            if (ndc) node_dc<T>(nd, i, dclist, pvel, np, true);
+        }
+        node_ratio<T>(nd, i, nd.mom, mass_min, 0, 1);
+    }
+}
+
 // TimeLine::getVelocity (TimeLine.h:33-46) is evaluated on the host each step
 // and passed in as tv.
 struct StepArgs {
