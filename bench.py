@@ -66,7 +66,7 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--form", default="fp32", choices=["fp64", "fp32"],
                     help="fp32: the chosen form, timed beside the plain FP64 form; fp64: the plain form alone")
-    ap.add_argument("--workload", default="batch", choices=["batch", "block"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "block", "foam"])
     ap.add_argument("--specimens", type=int, default=256, help="batch workload: specimen count")
     ap.add_argument("--total", type=float, default=40.0e6, help="batch workload: target particle count")
     ap.add_argument("--block", default="0.08,0.08,0.04", help="block workload: block size in m")
@@ -176,6 +176,16 @@ def workload(args):
     """(specimen states, config record).  One state for the block workload."""
     from code_mpm_gb300 import scenes
 
+    if args.workload == "foam":
+        st = scenes.graded_foam()  # 800 x 800 x 400 cells, 8 x 8 graded cells of 5 mm, platen -20 m/s
+        cfg = {"workload": "density-graded square-cell foam crushed by a rigid platen, contact path, single instance",
+               "block_m": [0.2, 0.2, 0.1], "h_m": 0.25e-3, "grid_cells": [800, 800, 400],
+               "cells_per_side": 8, "pitch_m": 5.0e-3, "wall_m": [0.3e-3, 1.0e-3], "wall_perturbation": 0.1,
+               "n_particles": st.n_particles, "n_nodes": st.n_nodes, "platen_speed_mps": 20.0,
+               "floor_friction": 0.2, "dt_s": st.dt_max,
+               "material": "von Mises hardening aluminium E=70GPa nu=0.33 rho=2700 yield=120MPa H=700MPa",
+               "l2_policy": "inputs larger than L2 (~6 GB particle state)"}
+        return [st], cfg
     if args.workload == "block":
         size = [float(v) for v in args.block.split(",")]
         st = scenes.platen_block(size=size)  # h = 1 mm, 8 ppc, platen -5 m/s, friction 0.1
@@ -226,12 +236,26 @@ def cpu_rate(sts, idx, contact, floor, budget_s, max_steps=50):
     return n * steps_done / secs, steps_done, secs, n, threads
 
 
-def cpu_baseline(sts, contact, floor, budget_s=12.0):
+def cpu_sample(args, sts):
+    """(states, indices, description) of the CPU legs' bounded sample: 16 specimens spread over the size range,
+    or for the foam a reduced foam of the same generator (its 257M-node grid needs ~60 GB of host memory in the
+    CPU restatement)."""
+    if getattr(args, "workload", "batch") == "foam":
+        from code_mpm_gb300 import scenes
+
+        st = scenes.graded_foam(ncell=2, block=(0.02, 0.02, 0.012), seed=5)
+        return [st], [0], f"a reduced foam of the same generator (2 x 2 cells, {st.n_particles} particles)"
     idx = subset(sts, 16)
-    rate, steps, secs, n, threads = cpu_rate(sts, idx, contact, floor, budget_s)
+    n = sum(sts[i].n_particles for i in idx)
+    return sts, idx, f"{len(idx)} of the {len(sts)} specimens ({n} particles, spread over the size range)"
+
+
+def cpu_baseline(args, sts, contact, floor, budget_s=12.0):
+    sts_, idx, what = cpu_sample(args, sts)
+    rate, steps, secs, n, threads = cpu_rate(sts_, idx, contact, floor, budget_s)
     return {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{steps} full steps of {len(idx)} of the {len(sts)} specimens ({n} particles, spread over "
-                      f"the size range), OpenMP restatement with per-node locks, {threads} threads, {secs:.2f} s"}
+            "sample": f"{steps} full steps of {what}, OpenMP restatement with per-node locks, {threads} threads, "
+                      f"{secs:.2f} s"}
 
 
 def make_engine(sts, pk, form):
@@ -396,6 +420,55 @@ def network_for_batch(args, contact, floor, steps):
     info = {"pilot": f"16 honeycomb specimens (seed 99, {ppk.state.n_particles} particles), plain FP64, {steps} steps",
             "harvested_rows": n, "seconds_pilot": t1 - t0, "training": rep}
     return net, info
+
+
+def network_for_foam(args, contact, floor, steps):
+    """The learned return map for the foam's aluminium: trained on the return-map inputs the plain FP64 method
+    meets on a reduced foam (2 x 2 cells, another seed)."""
+    import torch
+
+    from code_mpm_gb300 import engine, scenes
+
+    pilot = scenes.graded_foam(ncell=2, block=(0.02, 0.02, 0.012), seed=9)
+    cap = 8_000_000
+    rows = torch.zeros((cap, 13), dtype=torch.float32, device="cuda")
+    t0 = time.perf_counter()
+    with engine.Engine.from_state(pilot, engine.FORM_FP64) as e:
+        e.set_option(engine.OPT_FLOOR_FRICTION, floor)
+        e.harvest_begin(rows.data_ptr(), cap, mat_mask=1, band=0.0)
+        e.advance(steps, pilot.dt_max, contact)
+        n = min(e.harvest_end(), cap)
+    t1 = time.perf_counter()
+    dsig = float(rows[:n, 7:].std().item())
+    bsz = 8192
+    epochs = int(max(20, math.ceil(5000 * bsz / max(n, 1))))
+    net = engine.Net(E=70.0e9, nu=0.33, yield_=120.0e6, C0=700.0e6 / 1.0e12, C1=1.0e12, n_samples=1000,
+                     epochs=epochs, batch=bsz, deps_sigma=dsig, lr=2.0e-3)
+    rep = net.train_rows(rows.data_ptr(), n)
+    return net, {"pilot": f"reduced foam 2 x 2 cells (seed 9, {pilot.n_particles} particles), plain FP64, "
+                          f"{steps} steps", "harvested_rows": n, "seconds_pilot": t1 - t0, "training": rep}
+
+
+def accuracy_reduced_foam(steps, contact, floor, tune, net):
+    """Foam accuracy: the chosen form (same launch shapes and network) against the plain FP64 form on a reduced
+    foam of the same generator (2 x 2 cells) for the same steps."""
+    from code_mpm_gb300 import engine, metrics, scenes
+
+    st = scenes.graded_foam(ncell=2, block=(0.02, 0.02, 0.012), seed=5)
+    outs = {}
+    for form in (engine.FORM_FP32, engine.FORM_FP64):
+        with engine.Engine.from_state(st, form) as e:
+            e.set_option(engine.OPT_FLOOR_FRICTION, floor)
+            apply_tune(e, tune)
+            if form == engine.FORM_FP32 and net is not None:
+                e.attach_surrogate(net, band=0.02, recheck=0.01)
+            e.advance(steps, st.dt_max, contact)
+            outs[form] = download_fields(e, st.n_particles)
+    err = metrics.form_errors(outs[engine.FORM_FP32], outs[engine.FORM_FP64])
+    bars = {"vm_stress_rel_l2": 1e-2, "strain_energy_rel": 5e-3}
+    return dict(err, steps=steps, bars=bars, within_bars=all(err[k] <= v for k, v in bars.items()),
+                versus=f"plain FP64 form on a reduced foam of the same generator ({st.n_particles} particles), "
+                       "same steps")
 
 
 def network_isolated(contact_unused=None):
@@ -570,9 +643,13 @@ def run_gb300(args, dist: Dist):
 
     # the learned return map (chosen form, batch workload): trained on a pilot batch's plain-method samples
     net, net_info = None, None
-    use_net = compare and pk is not None and not args.no_network
+    use_net = compare and not args.no_network and args.workload in ("batch", "foam")
     if use_net:
-        net, net_info = network_for_batch(args, contact, floor, steps=min(args.warmup + args.steps, 1000))
+        pilot_steps = min(args.warmup + args.steps, 1000)
+        if args.workload == "foam":
+            net, net_info = network_for_foam(args, contact, floor, steps=pilot_steps)
+        else:
+            net, net_info = network_for_batch(args, contact, floor, steps=pilot_steps)
 
     e = make_engine(sts, pk, chosen_form)
     e.set_option(engine.OPT_FLOOR_FRICTION, floor)
@@ -588,18 +665,23 @@ def run_gb300(args, dist: Dist):
 
     accuracy = None
     if compare:
-        chosen_out = download_fields(e, n)
-        idx = subset(sts, 8)
-        tune_plain = plain["autotune"] if plain else None
-        accuracy = accuracy_vs_plain(sts, pk, idx, chosen_out, args.warmup + args.steps, contact, floor, tune_plain)
-        del chosen_out
-        if pk is None:  # single specimen: the plain form timed on the same state
+        if args.workload == "foam":
+            accuracy = accuracy_reduced_foam(args.warmup + args.steps, contact, floor, tune, net)
+        else:
+            chosen_out = download_fields(e, n)
+            idx = subset(sts, 8)
+            tune_plain = plain["autotune"] if plain else None
+            accuracy = accuracy_vs_plain(sts, pk, idx, chosen_out, args.warmup + args.steps, contact, floor,
+                                         tune_plain)
+            del chosen_out
+        if pk is None:  # single instance: the plain form timed on the same state (fewer steps for the foam)
+            kp = args.steps if args.workload == "block" else max(1, min(args.steps, 20))
             with make_engine(sts, pk, engine.FORM_FP64) as ep:
                 ep.set_option(engine.OPT_FLOOR_FRICTION, floor)
                 tune_p = None if args.no_autotune else ep.autotune(steps=2, dt=dt, contact=bool(contact))
-                ms_p, launches_p, clocks_p = timed(ep, args.steps, args.warmup, dt, contact, dist)
-            plain = {"value": n * args.steps * dist.world / (ms_p / 1e3), "ms_per_step": ms_p / args.steps,
-                     "steps": args.steps, "dtype": "f64", "gpu_launches": launches_p, "clocks": clocks_p,
+                ms_p, launches_p, clocks_p = timed(ep, kp, min(args.warmup, 3), dt, contact, dist)
+            plain = {"value": n * kp * dist.world / (ms_p / 1e3), "ms_per_step": ms_p / kp,
+                     "steps": kp, "dtype": "f64", "gpu_launches": launches_p, "clocks": clocks_p,
                      "autotune": tune_p}
 
     prof, kernels = kernel_table(e, min(args.steps, 30), dt, contact)
@@ -652,7 +734,7 @@ def run_gb300(args, dist: Dist):
     if dist.rank == 0 and dist.world == 1 and use_net:
         out["network_isolated"] = network_isolated()
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(sts, contact, floor)
+        out["cpu_baseline"] = cpu_baseline(args, sts, contact, floor)
     return out
 
 
@@ -662,13 +744,13 @@ def run_reference(args, dist: Dist):
     if dist.rank != 0:
         return None
     sts, cfg = workload(args)
-    idx = subset(sts, 16)
+    sts_, idx, what = cpu_sample(args, sts)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
 
     pyoracle.build()
     threads = os.cpu_count() or 1
-    work = [sts[i].copy() for i in idx]
+    work = [sts_[i].copy() for i in idx]
     n = sum(s.n_particles for s in work)
 
     def step():
@@ -681,9 +763,8 @@ def run_reference(args, dist: Dist):
     k = max(1, min(args.steps, int(120.0 / max(one, 1e-3))))
     secs = sum(step() for _ in range(k))
     rate = n * k / secs
-    sample = (f"{k} timed steps (+{w + 1} warm-up) of {len(idx)} of the {len(sts)} specimens ({n} particles, "
-              f"spread over the size range); CPU restatement of the reference path, OpenMP with per-node locks, "
-              f"{threads} threads")
+    sample = (f"{k} timed steps (+{w + 1} warm-up) of {what}; CPU restatement of the reference path, OpenMP with "
+              f"per-node locks, {threads} threads")
     return {"metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": dist.world, "steps": k, "warmup": w + 1,
             "ms_per_step": 1e3 * secs / k, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (seeded scene generators)", "config": dict(cfg, form="reference-cpu"),

@@ -472,12 +472,15 @@ int upload_field(mpm_ctx* c, DevBuf& dst, const double* host, long long n, int k
     return MPM_OK;
 }
 
+// Download one field into host rows.  Particle fields (particles = true) go
+// through the slot -> caller-index map when the slots are in cell order;
+// node fields never do.
 int download_field(mpm_ctx* c, const DevBuf& src, double* host, long long n, int k, bool fp64,
-                   int shift_identity = 0) {
+                   int shift_identity = 0, bool particles = false) {
     if (!host || n == 0) return MPM_OK;
     int rc = ensure(c, c->staging, (size_t)n * k * 8);
     if (rc) return rc;
-    const unsigned* orig = c->have_orig ? (const unsigned*)c->orig.p : nullptr;
+    const unsigned* orig = (particles && c->have_orig) ? (const unsigned*)c->orig.p : nullptr;
     if (fp64)
         LAUNCH("pack", k_pack<double>, blocks_for(n * k), NTHREADS, (const double*)src.p, (double*)c->staging.p, n,
                k, shift_identity, orig);
@@ -1423,7 +1426,7 @@ int mpm_download_particles(mpm_ctx* c, mpm_particles* p) {
     for (auto& f : fields) {
         if (!f.h) continue;
         const int shift = (f.b == &c->F && !f64) ? 1 : 0;
-        if ((rc = download_field(c, *f.b, f.h, n, f.k, f.fp64, shift))) return rc;
+        if ((rc = download_field(c, *f.b, f.h, n, f.k, f.fp64, shift, true))) return rc;
         CK(cudaStreamSynchronize(c->stream));  // staging is reused by the next field
     }
     if (n > 0) {

@@ -320,7 +320,8 @@ class Engine:
         self.n_particles = st.n_particles
         dcl = np.ascontiguousarray(st["dc_list"], dtype=np.uint32)
         self._check(self._L.mpm_upload_dc_list(self._h, _ptr(dcl), len(dcl)))
-        narr = {k: np.ascontiguousarray(st[src]) for k, src in _NMAP}
+        # empty node arrays (a State holding only boundary conditions) stay unset: zero on the device
+        narr = {k: np.ascontiguousarray(st[src]) for k, src in _NMAP if len(st[src]) > 0}
         nd = Nodes(**{k: _ptr(v) for k, v in narr.items()})
         self._check(self._L.mpm_upload_nodes(self._h, C.byref(nd)))
         t = np.ascontiguousarray(st["tl_time"], dtype=np.float64)
@@ -338,7 +339,7 @@ class Engine:
         arrs["dc_mult"] = st["dc_mult"]
         p = Particles(**{k: _ptr(v) for k, v in arrs.items()})
         self._check(self._L.mpm_download_particles(self._h, C.byref(p)))
-        nd = Nodes(**{k: _ptr(st[src]) for k, src in _NMAP})
+        nd = Nodes(**{k: _ptr(st[src]) for k, src in _NMAP if len(st[src]) > 0})
         self._check(self._L.mpm_download_nodes(self._h, C.byref(nd)))
         s = self.get_sim()
         st.time, st.step = s["time"], s["step"]

@@ -340,6 +340,82 @@ def honeycomb_layer_count(wall: float, pitch: float, ncell: int, h: float) -> in
     return m * m - (m - k) * (m - k)
 
 
+def graded_foam(ncell: int = 8, pitch: float = 5.0e-3, t0: float = 0.3e-3, t1: float = 1.0e-3,
+                block=(0.2, 0.2, 0.1), h: float = 0.25e-3, perturb: float = 0.1, seed: int = 5,
+                E: float = 70.0e9, nu: float = 0.33, rho: float = 2700.0, yield_: float = 120.0e6, H: float = 700.0e6,
+                C1: float = 1.0e12, speed: float = 20.0, friction: float = 0.2, pad: int = 2, headroom: int = 4,
+                height: Optional[float] = None) -> State:
+    """Density-graded square-cell foam crushed out of plane by a rigid platen (contact path).
+
+    The grid covers the whole block (block / h cells, 800 x 800 x 400 by default) while the foam occupies
+    ncell x ncell square cells of pitch `pitch` centred in x-y: walls are the planes x, y = x0 + k pitch (k = 0 ..
+    ncell) extruded along z, their thickness growing linearly from t0 at the floor to t1 at the top, each wall's
+    thickness scaled by 1 + U(-perturb, perturb) (seeded).  Particles sit at the centres of an h/2 lattice inside
+    the walls (8 per cell); those with an empty lattice neighbour in x or y are surface particles.  A one-layer
+    platen above the top moves down at `speed`; the floor node plane is fixed in z with Coulomb friction.  Grids
+    above 50M nodes hold only the nodes' boundary conditions on the host (node_fields="bc").
+    """
+    cells = np.array([int(round(block[a] / h)) for a in range(3)], dtype=np.int32)
+    length = cells * h
+    s = 0.5 * h
+    z0 = pad * h
+    if height is None:
+        height = length[2] - (pad + headroom) * h
+    W = ncell * pitch + t1 * (1.0 + perturb)
+    x0 = round(0.5 * (length[0] - W) / h) * h
+    y0 = round(0.5 * (length[1] - W) / h) * h
+    m = int(np.ceil(W / s))
+    c = (np.arange(m) + 0.5) * s
+    nz = int(round(height / s))
+    rng = np.random.Generator(np.random.PCG64(seed))
+    fx = 1.0 + rng.uniform(-perturb, perturb, ncell + 1)
+    fy = 1.0 + rng.uniform(-perturb, perturb, ncell + 1)
+    kx = np.minimum((c // pitch).astype(np.int64), ncell)
+    rel = c - kx * pitch
+    layers, surf_layers = [], []
+    for k in range(nz):
+        zc = (k + 0.5) * s
+        t = t0 + (t1 - t0) * zc / height
+        inx = rel < t * fx[kx]
+        iny = rel < t * fy[kx]
+        wall = inx[:, None] | iny[None, :]
+        ix, iy = np.nonzero(wall)
+        padm = np.pad(wall, 1)
+        surf = ~(padm[2:, 1:-1] & padm[:-2, 1:-1] & padm[1:-1, 2:] & padm[1:-1, :-2])[ix, iy]
+        layers.append(np.stack([x0 + c[ix], y0 + c[iy], np.full(ix.size, z0 + zc)], axis=1))
+        surf_layers.append(surf)
+    body = np.concatenate(layers)
+    bsurf = np.concatenate(surf_layers)
+    ztop = z0 + height + 0.5 * h
+    px = x0 + np.arange(-h + 0.5 * s, W + h, s)
+    py = y0 + np.arange(-h + 0.5 * s, W + h, s)
+    PX, PY = np.meshgrid(px, py, indexing="ij")
+    platen = np.stack([PX.ravel(), PY.ravel(), np.full(PX.size, ztop)], axis=1)
+    pos = np.concatenate([body, platen])
+    nbody = body.shape[0]
+    dt = 0.2 * h / math.sqrt(E / rho)
+    n_nodes = int(np.prod(cells.astype(np.int64) + 1))
+    st = empty_state(length, cells, pos.shape[0], dt, n_materials=2, n_timeline=2, n_dc=platen.shape[0],
+                     node_fields="bc" if n_nodes > 50_000_000 else "all")
+    _material(st, 0, VONMISESHARDENING, rho, E, nu, yield_, H / C1, C1)
+    _material(st, 1, ELASTIC, rho, E, nu)
+    mat = np.zeros(pos.shape[0], dtype=np.int32)
+    mat[nbody:] = 1
+    _finish_particles(st, pos, s * s * s, mat)
+    st["pflags"][:nbody][bsurf] |= PF_SURFACE
+    st["pflags"][nbody:] = PF_DC_X | PF_DC_Y | PF_DC_Z | PF_DC_SKIP | PF_SURFACE
+    st["dc_mult"][nbody:] = -float(speed)
+    st["vel"][nbody:, 2] = -float(speed)
+    st["dc_list"][:] = np.arange(nbody, pos.shape[0], dtype=np.uint32)
+    st["tl_time"][:] = [0.0, 10.0]
+    st["tl_vel"][:] = [[0.0, 0.0, 1.0], [0.0, 0.0, 1.0]]
+    nn = cells + 1
+    floor = pad * nn[0] * nn[1] + np.arange(nn[0] * nn[1], dtype=np.int64)  # node plane iz = pad
+    st["fixed"][floor] |= NF_FIX_Z
+    st["friction"][floor] = friction
+    return st
+
+
 def contact_small(seed: int = 2, h: float = 1.0e-3, nb=(6, 5, 4), speed: float = 30.0) -> State:
     """Small platen_block variant with jittered particles, for contact-path parity."""
     st = platen_block(size=(nb[0] * h, nb[1] * h, nb[2] * h), h=h, ppc=2, yield_=150.0e6, H=2.0e9,

@@ -118,14 +118,18 @@ class State:
 
 
 def empty_state(length, cells, n_particles: int, dt_max: float, n_materials: int = 1,
-                n_timeline: int = 0, n_dc: int = 0, time: float = 0.0) -> State:
-    """A State with every array allocated and zero-filled, F set to identity."""
+                n_timeline: int = 0, n_dc: int = 0, time: float = 0.0, node_fields: str = "all") -> State:
+    """A State with every array allocated and zero-filled, F set to identity.  node_fields="bc" allocates only
+    the nodes' boundary conditions (fixed, friction): the other node arrays are empty, an engine leaves those
+    fields zero, and downloads skip them (for grids of hundreds of millions of nodes)."""
     st = State(length=np.asarray(length, dtype=np.float64), cells=np.asarray(cells, dtype=np.int32),
                time=float(time), dt_max=float(dt_max))
     counts = {"p": n_particles, "n": int(np.prod(np.asarray(cells, dtype=np.int64) + 1)),
               "m": n_materials, "t": n_timeline, "d": n_dc}
     for name, dt, comp, sel in FIELDS:
         n = counts[sel]
+        if sel == "n" and node_fields == "bc" and name not in ("fixed", "friction"):
+            n = 0
         if dt == "mat":
             st.arrays[name] = np.zeros(n, dtype=MATERIAL_DTYPE)
         else:

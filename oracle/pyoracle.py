@@ -92,6 +92,8 @@ def _make_snap(st):
 def advance(st, steps: int, contact: int, floor_friction: int = 0, threads: int = 0, omp: bool = False) -> float:
     """Advance ``st`` in place by ``steps`` steps of ``st.dt_max``; returns loop seconds (OpenMP build only)."""
     lib = _lib(omp)
+    if len(st.arrays["g_mass"]) != st.n_nodes:
+        raise ValueError("the oracle needs every node array (this State holds only the nodes' boundary conditions)")
     s = _make_snap(st)
     sec = C.c_double(0.0)
     rc = lib.oracle_advance(C.byref(s), int(steps), int(contact), int(floor_friction), int(threads), C.byref(sec))
