@@ -26,20 +26,21 @@ d = bench.Dist()
 assert d.world == 2
 d.barrier()
 m = d.max(float(d.rank) * 3.0 + 1.0)
-print(json.dumps({{"rank": d.rank, "max": m}}))
+with open(os.path.join({out!r}, "rank%d.json" % d.rank), "w") as f:
+    f.write(json.dumps({{"rank": d.rank, "max": m}}))
 d.close()
 '''
 
 
 def test_max_over_ranks_with_gloo(tmp_path):
     script = tmp_path / "w.py"
-    script.write_text(WORKER.format(root=ROOT))
+    script.write_text(WORKER.format(root=ROOT, out=str(tmp_path)))
     env = dict(os.environ, MASTER_ADDR="127.0.0.1", CUDA_VISIBLE_DEVICES="")
     r = subprocess.run([sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=2",
                         "--master-addr=127.0.0.1", f"--master-port={free_port()}", str(script)],
                        capture_output=True, text=True, timeout=300, env=env, cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
-    lines = [json.loads(l) for l in r.stdout.splitlines() if l.startswith("{")]
+    lines = [json.loads((tmp_path / f"rank{k}.json").read_text()) for k in (0, 1)]
     assert sorted(l["rank"] for l in lines) == [0, 1]
     assert all(l["max"] == 4.0 for l in lines)
 
