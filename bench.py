@@ -74,6 +74,9 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip timing the plain FP64 form beside the chosen one")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--cell-sort", type=int, default=-1, choices=(-1, 0, 1),
+                    help="FP32 form: 1 sorts the particles by cell every step, 0 takes the storage order "
+                         "(the engine's default when -1)")
     ap.add_argument("--no-network", action="store_true",
                     help="run the chosen form without the learned return map (and skip its isolated benchmark)")
     return ap.parse_args()
@@ -449,7 +452,7 @@ def network_for_foam(args, contact, floor, steps):
                           f"{steps} steps", "harvested_rows": n, "seconds_pilot": t1 - t0, "training": rep}
 
 
-def accuracy_reduced_foam(steps, contact, floor, tune, net):
+def accuracy_reduced_foam(steps, contact, floor, tune, net, cell_sort=-1):
     """Foam accuracy: the chosen form (same launch shapes and network) against the plain FP64 form on a reduced
     foam of the same generator (2 x 2 cells) for the same steps."""
     from code_mpm_gb300 import engine, metrics, scenes
@@ -460,6 +463,8 @@ def accuracy_reduced_foam(steps, contact, floor, tune, net):
         with engine.Engine.from_state(st, form) as e:
             e.set_option(engine.OPT_FLOOR_FRICTION, floor)
             apply_tune(e, tune)
+            if form == engine.FORM_FP32 and cell_sort >= 0:
+                e.set_option(engine.OPT_CELL_SORT, cell_sort)
             if form == engine.FORM_FP32 and net is not None:
                 e.attach_surrogate(net, band=0.02, recheck=0.01)
             e.advance(steps, st.dt_max, contact)
@@ -653,6 +658,8 @@ def run_gb300(args, dist: Dist):
 
     e = make_engine(sts, pk, chosen_form)
     e.set_option(engine.OPT_FLOOR_FRICTION, floor)
+    if args.cell_sort >= 0:
+        e.set_option(engine.OPT_CELL_SORT, args.cell_sort)
     if net is not None:
         e.attach_surrogate(net, band=0.02, recheck=0.01)
     tune = None if args.no_autotune else e.autotune(steps=2, dt=dt, contact=bool(contact))
@@ -666,7 +673,7 @@ def run_gb300(args, dist: Dist):
     accuracy = None
     if compare:
         if args.workload == "foam":
-            accuracy = accuracy_reduced_foam(args.warmup + args.steps, contact, floor, tune, net)
+            accuracy = accuracy_reduced_foam(args.warmup + args.steps, contact, floor, tune, net, args.cell_sort)
         else:
             chosen_out = download_fields(e, n)
             idx = subset(sts, 8)

@@ -122,6 +122,7 @@ struct mpm_ctx {
     DevBuf orig, ptmp;
     bool have_orig = false, reorder_pending = false;
     int reorder_interval = 0;  // -1: never; 0: after each particle upload; N: also every N steps
+    bool cell_sort = false;    // FP32 form, P2G modes 2-4: false = take the storage order as the cell order
     long long steps_since_reorder = 0;
     bool owner_clean = false;  // displacement-control claims all zero (phase B clears them after use)
 
@@ -509,7 +510,7 @@ int check_device_error(mpm_ctx* c) {
 // Sort the particles by cell key: the keys of the current positions (written
 // by the previous step's pass 2, or computed here after an upload), then the
 // stable radix sort, whose first pass takes the identity as input values.
-int sort_cells(mpm_ctx* c, const unsigned** skeys_out, const unsigned** perm_out) {
+int sort_cells(mpm_ctx* c, const unsigned** skeys_out, const unsigned** perm_out, bool sort = true) {
     const long long n = c->n;
     const Geom& g = c->g;
     unsigned* err = (unsigned*)c->err_word.p;
@@ -523,6 +524,13 @@ int sort_cells(mpm_ctx* c, const unsigned** skeys_out, const unsigned** perm_out
         LAUNCH("cell_keys", k_cell_keys, blocks_for(n), NTHREADS, (const double*)c->pos.p, n, g, key_src,
                (unsigned*)nullptr, (unsigned*)c->keys_copy.p, err,
                c->form == MPM_FORM_FP32 ? (float*)c->loc.p : (float*)nullptr, sid);
+    if (!sort) {  // the slots in storage order with their keys (identity permutation)
+        c->last_perm = nullptr;
+        c->last_skeys = key_src;
+        *skeys_out = key_src;
+        *perm_out = nullptr;
+        return MPM_OK;
+    }
     int bits = 1;
     while (bits < 32 && ((unsigned long long)1 << bits) <= (unsigned long long)g.key_max) ++bits;
     // the fewest passes of at most 10-bit digits (27-bit keys: three 9-bit passes)
@@ -684,8 +692,12 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph = false) {
     N.alist = c->have_alist ? (const unsigned*)c->alist.p : nullptr;
     LAUNCH("reset_grid", k_reset_grid<T>, c->have_alist ? nodeblocks : blocks_for(nn), NTHREADS, N, contact);
     if (n > 0) {
+        // The FP32 form's cell-run kernels accept slots out of cell order (a
+        // cell met twice is summed in two runs), so with particles stored in
+        // cell order it can skip the sort and take the storage order as it is.
+        const bool sort = !(c->form == MPM_FORM_FP32 && !c->cell_sort && c->p2g_reduce >= 2);
         const unsigned *skeys = nullptr, *perm = nullptr;
-        if (int rs = sort_cells(c, &skeys, &perm)) return rs;
+        if (int rs = sort_cells(c, &skeys, &perm, sort)) return rs;
         // pass 2 writes the next step's sort input into the buffer not holding skeys
         unsigned* keys_next = (skeys == (unsigned*)c->keys0.p) ? (unsigned*)c->keys1.p : (unsigned*)c->keys0.p;
         c->key_buf = (keys_next == (unsigned*)c->keys1.p) ? 1 : 0;
@@ -703,9 +715,16 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph = false) {
             LAUNCH("cell_ranges", k_cell_ranges, blocks_for(n), NTHREADS, skeys, n, g, N.state,
                    contact ? (unsigned*)c->cstart.p : nullptr, contact ? (unsigned*)c->cend.p : nullptr, perm, P.sid);
         }
-        if (c->p2g_reduce == 2)
-            LAUNCH_SMEM("p2g", k_p2g_cells<T>, blocks_for(n, c->p2g_block), c->p2g_block,
-                        p2g_cells_smem<T>(c->p2g_block), P, N, g, skeys, perm, n, mg_in_p2g, fp32);
+        if (c->p2g_reduce >= 2) {  // shared-memory cell runs, 1 / 2 / 4 corners per thread
+            const unsigned gb = blocks_for(n, c->p2g_block);
+            const size_t sm = p2g_cells_smem<T>(c->p2g_block);
+            if (c->p2g_reduce == 2)
+                LAUNCH_SMEM("p2g", (k_p2g_cells<T, 1>), gb, c->p2g_block, sm, P, N, g, skeys, perm, n, mg_in_p2g, fp32);
+            else if (c->p2g_reduce == 3)
+                LAUNCH_SMEM("p2g", (k_p2g_cells<T, 2>), gb, c->p2g_block, sm, P, N, g, skeys, perm, n, mg_in_p2g, fp32);
+            else
+                LAUNCH_SMEM("p2g", (k_p2g_cells<T, 4>), gb, c->p2g_block, sm, P, N, g, skeys, perm, n, mg_in_p2g, fp32);
+        }
         else if (c->p2g_reduce == 1)
             LAUNCH("p2g", (k_p2g<T, 1>), blocks_for(n, c->p2g_block), c->p2g_block, P, N, g, skeys, perm, n,
                    mg_in_p2g, fp32);
@@ -753,9 +772,19 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph = false) {
         // displacement control, grid update, displacement control, f/m: one pass over the active nodes
         LAUNCH("node_phase_a", k_node_phase_a<T>, nodeblocks, NTHREADS, N, (T)dt, c->sim.damping, contact,
                c->floor_friction, (const unsigned*)c->dclist.p, c->ndc, (const T*)c->vel.p, n, mm);
-        if (c->p2g_reduce == 2)  // the same reduction as P2G: shared-memory cell runs
-            LAUNCH_SMEM("pass1_remap", k_pass1_cells<T>, blocks_for(n, c->p2g_block), c->p2g_block,
-                        pass1_cells_smem<T>(c->p2g_block), P, N, g, skeys, perm, n, (T)dt, mm, contact);
+        if (c->p2g_reduce >= 2) {  // the same reduction as P2G: shared-memory cell runs
+            const unsigned gb = blocks_for(n, c->p2g_block);
+            const size_t sm = pass1_cells_smem<T>(c->p2g_block);
+            if (c->p2g_reduce == 2)
+                LAUNCH_SMEM("pass1_remap", (k_pass1_cells<T, 1>), gb, c->p2g_block, sm, P, N, g, skeys, perm, n, (T)dt,
+                            mm, contact);
+            else if (c->p2g_reduce == 3)
+                LAUNCH_SMEM("pass1_remap", (k_pass1_cells<T, 2>), gb, c->p2g_block, sm, P, N, g, skeys, perm, n, (T)dt,
+                            mm, contact);
+            else
+                LAUNCH_SMEM("pass1_remap", (k_pass1_cells<T, 4>), gb, c->p2g_block, sm, P, N, g, skeys, perm, n, (T)dt,
+                            mm, contact);
+        }
         else if (c->gather_batch)
             LAUNCH("pass1_remap", (k_pass1_remap<T, 1>), blocks_for(n), NTHREADS, P, N, g, skeys, perm, n, (T)dt, mm,
                    contact);
@@ -842,23 +871,34 @@ int step(mpm_ctx* c, double dt, int contact, bool graph = false) {
 // graph.  Capturing records two steps without running them while the host
 // state advances by two steps; launching the graph once then brings the
 // device to the same point.
-int advance_graph(mpm_ctx* c, int nsteps, double dt, int contact) {
-    if (c->reorder_pending && c->have_particles) {
-        int rc = reorder(c);
-        if (rc) return rc;
-    }
-    if (c->reorder_interval > 0 && c->form == MPM_FORM_FP32) {  // periodic: advance in runs between reorders
-        while (nsteps > 0) {
-            const long long left = std::max<long long>(1, c->reorder_interval - c->steps_since_reorder);
-            const int k = (int)std::min<long long>(nsteps, left);
-            c->reorder_interval = -c->reorder_interval;  // no nested reorder inside the run
-            int rc = advance_graph(c, k, dt, contact);
-            c->reorder_interval = -c->reorder_interval;
+// Steps between periodic reorders (FP32 form; 0: none).  Without the
+// per-step sort the storage order is the only cell order, so it is restored
+// every SORT_FREE_REORDER steps unless the caller chose an interval.
+constexpr int SORT_FREE_REORDER = 256;
+int reorder_every(const mpm_ctx* c) {
+    if (c->form != MPM_FORM_FP32 || c->reorder_interval < 0) return 0;
+    if (c->reorder_interval > 0) return c->reorder_interval;
+    return (!c->cell_sort && c->p2g_reduce >= 2) ? SORT_FREE_REORDER : 0;
+}
+
+int advance_graph(mpm_ctx* c, int nsteps, double dt, int contact, bool between_reorders = false) {
+    if (!between_reorders) {
+        if (c->reorder_pending && c->have_particles) {
+            int rc = reorder(c);
             if (rc) return rc;
-            nsteps -= k;
-            if (c->steps_since_reorder >= c->reorder_interval && (rc = reorder(c))) return rc;
         }
-        return MPM_OK;
+        const int every = reorder_every(c);
+        if (every > 0) {  // periodic: advance in runs between reorders
+            while (nsteps > 0) {
+                const long long left = std::max<long long>(1, every - c->steps_since_reorder);
+                const int k = (int)std::min<long long>(nsteps, left);
+                int rc = advance_graph(c, k, dt, contact, true);
+                if (rc) return rc;
+                nsteps -= k;
+                if (c->steps_since_reorder >= every && (rc = reorder(c))) return rc;
+            }
+            return MPM_OK;
+        }
     }
     int s = 0;
     auto plain = [&](int k) -> int {
@@ -1004,10 +1044,14 @@ int mpm_create_batch(const mpm_grid_desc* grids, int32_t nspec, int form, mpm_ct
     cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
     if (c->sm_count <= 0) c->sm_count = 152;
     // cell-centric P2G stages up to 512 slots in shared memory (109 KB in FP64)
-    if (cudaFuncSetAttribute(k_p2g_cells<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)p2g_cells_smem<double>(512)) != cudaSuccess ||
-        cudaFuncSetAttribute(k_p2g_cells<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)p2g_cells_smem<float>(512)) != cudaSuccess) {
+    const int smd = (int)p2g_cells_smem<double>(512), smf = (int)p2g_cells_smem<float>(512);
+    const cudaFuncAttribute dyn = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    if (cudaFuncSetAttribute(k_p2g_cells<double, 1>, dyn, smd) != cudaSuccess ||
+        cudaFuncSetAttribute(k_p2g_cells<double, 2>, dyn, smd) != cudaSuccess ||
+        cudaFuncSetAttribute(k_p2g_cells<double, 4>, dyn, smd) != cudaSuccess ||
+        cudaFuncSetAttribute(k_p2g_cells<float, 1>, dyn, smf) != cudaSuccess ||
+        cudaFuncSetAttribute(k_p2g_cells<float, 2>, dyn, smf) != cudaSuccess ||
+        cudaFuncSetAttribute(k_p2g_cells<float, 4>, dyn, smf) != cudaSuccess) {
         cudaGetLastError();
         delete c;
         return MPM_ERR_DEVICE;
@@ -1140,11 +1184,16 @@ int mpm_set_option(mpm_ctx* c, int key, double value) {
         case MPM_OPT_FLOOR_FRICTION: c->floor_friction = value != 0.0; return MPM_OK;
         case MPM_OPT_PROFILE: c->profile = value != 0.0; return MPM_OK;
         case MPM_OPT_P2G_REDUCE:
-            if (value != 0.0 && value != 1.0 && value != 2.0) return fail(c, MPM_ERR_ARG, "P2G mode must be 0, 1 or 2");
+            if (!(value >= 0.0 && value <= 4.0) || value != (double)(int)value)
+                return fail(c, MPM_ERR_ARG, "P2G mode must be 0 to 4");
             c->p2g_reduce = (int)value;
             return MPM_OK;
         case MPM_OPT_GRAPH:
             c->use_graph = value != 0.0;
+            return MPM_OK;
+        case MPM_OPT_CELL_SORT:
+            if (value != 0.0 && value != 1.0) return fail(c, MPM_ERR_ARG, "cell sort must be 0 or 1");
+            c->cell_sort = value != 0.0;
             return MPM_OK;
         case MPM_OPT_REORDER:
             if (!(value >= -1.0 && value < 2147483647.0) || value != (double)(long long)value)
@@ -1554,13 +1603,24 @@ int mpm_advance_timed(mpm_ctx* c, int32_t nsteps, double dt, int contact, float*
 int mpm_cell_order(mpm_ctx* c, uint32_t* keys, uint32_t* sorted_order, int64_t n) {
     if (!c) return MPM_ERR_ARG;
     if (n != c->n) return fail(c, MPM_ERR_ARG, "n = %lld, engine holds %lld particles", (long long)n, c->n);
-    if (!c->last_perm && n > 0) return fail(c, MPM_ERR_STATE, "no step has run yet");
+    if (!c->last_skeys && n > 0) return fail(c, MPM_ERR_STATE, "no step has run yet");
     std::vector<uint32_t> perm((size_t)std::max<int64_t>(1, n)), skeys((size_t)std::max<int64_t>(1, n));
+    bool unsorted = false;  // a step without the sort: slot keys in storage order
     if (n > 0) {
-        CK(cudaMemcpyAsync(perm.data(), c->last_perm, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
+        if (c->last_perm)
+            CK(cudaMemcpyAsync(perm.data(), c->last_perm, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
+        else
+            unsorted = true;
         CK(cudaMemcpyAsync(skeys.data(), c->last_skeys, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
     }
     CK(cudaStreamSynchronize(c->stream));
+    if (unsorted) {  // the stable order of the slots by key
+        for (int64_t s = 0; s < n; ++s) perm[s] = (uint32_t)s;
+        std::stable_sort(perm.begin(), perm.begin() + n, [&](uint32_t a, uint32_t b) { return skeys[a] < skeys[b]; });
+        std::vector<uint32_t> sk((size_t)n);
+        for (int64_t s = 0; s < n; ++s) sk[s] = skeys[perm[s]];
+        skeys.swap(sk);
+    }
     // the last step's key of slot perm[s] is its sorted key skeys[s]
     if (!c->have_orig) {
         if (keys)
@@ -1677,7 +1737,7 @@ int mpm_autotune(mpm_ctx* c, int32_t steps, double dt, int contact, mpm_tune_res
     CK(cudaEventCreate(&a));
     CK(cudaEventCreate(&b));
     const int blocks[3] = {128, 256, 512};
-    for (int red = 0; red < 3 && rc == MPM_OK; ++red)
+    for (int red = 0; red < 5 && rc == MPM_OK; ++red)
         for (int pb = 0; pb < 3 && rc == MPM_OK; ++pb)
             for (int qb = 0; qb < 3 && rc == MPM_OK; ++qb)
             for (int gb = 0; gb < 2 && rc == MPM_OK; ++gb) {

@@ -276,17 +276,52 @@ __global__ void __launch_bounds__(512) k_p2g(PView<T> P, NView<T> nd, Geom g, co
 // Shared memory: (12 + 13) values per slot plus the keys, particle indices
 // and run starts (p2g_cells_smem).
 // ---------------------------------------------------------------------------
+// Runs of equal cell keys among the block's first nslots slots (keys staged
+// in shared memory, a __syncthreads after the staging): run r covers slots
+// run_start[r] .. run_start[r + 1] - 1.  Returns the run count.  The slots
+// need not be sorted (a cell met twice is two runs) and slots whose key is out
+// of range form runs of their own, which the callers skip.
+__device__ __forceinline__ int block_runs(const unsigned* skey, int nslots, int* run_start, int* wsum) {
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const bool head = t < nslots && (t == 0 || skey[t - 1] != skey[t]);
+    const unsigned bal = __ballot_sync(FULL_MASK, head);
+    if (lane == 0) wsum[w] = __popc(bal);
+    __syncthreads();
+    if (t < 32) {
+        const int nw = blockDim.x >> 5;
+        int v = (t < nw) ? wsum[t] : 0;
+        int incl = v;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            int o = __shfl_up_sync(FULL_MASK, incl, off);
+            if (t >= off) incl += o;
+        }
+        if (t < nw) wsum[t] = incl - v;
+        if (t == 31) wsum[32] = incl;
+    }
+    __syncthreads();
+    if (head) run_start[wsum[w] + __popc(bal & ((1u << lane) - 1u))] = t;
+    const int R = wsum[32];
+    if (t == 0) run_start[R] = nslots;
+    __syncthreads();
+    return R;
+}
+
 template <typename T>
 __host__ __device__ constexpr size_t p2g_cells_smem(int bs) {
     return (size_t)25 * bs * sizeof(T) + (size_t)bs * 8 + (size_t)(bs + 1) * 4 + 64 * 4;
 }
 
-template <typename T>
+// CPT corners per phase-2 thread (1, 2 or 4): the corners sharing the
+// thread's x (CPT 4) or x and y (CPT 2) bases, so a particle's quantities are
+// read from shared memory 8 / CPT times instead of 8.
+template <typename T, int CPT>
 __global__ void __launch_bounds__(512) k_p2g_cells(PView<T> P, NView<T> nd, Geom g, const unsigned* __restrict__ skeys,
                                                    const unsigned* __restrict__ perm, long long n, int with_mg,
                                                    int mark_active) {
+    static_assert(CPT == 1 || CPT == 2 || CPT == 4, "corners per thread");
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int bs = blockDim.x, t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const int bs = blockDim.x, t = threadIdx.x;
     T* sw = reinterpret_cast<T*>(smem_raw);        // 12 x bs: Nx0 Nx1 Ny0 Ny1 Nz0 Nz1 gx0 gx1 gy0 gy1 gz0 gz1
     T* sq = sw + 12 * bs;                          // 13 x bs: m, m v (3), -V sigma (6), f_ext (3)
     unsigned* skey = reinterpret_cast<unsigned*>(sq + 13 * bs);
@@ -298,7 +333,7 @@ __global__ void __launch_bounds__(512) k_p2g_cells(PView<T> P, NView<T> nd, Geom
     const bool valid = key < g.key_max;
     const long long np = P.n, nn = nd.nn;
     if (valid) {
-        const long long p = perm[s];
+        const long long p = perm ? perm[s] : s;
         const Geom& gs = spec_geom(g, P.sid, p);
         int b[3];
         key_to_base(key, gs, b);
@@ -329,74 +364,63 @@ __global__ void __launch_bounds__(512) k_p2g_cells(PView<T> P, NView<T> nd, Geom
     }
     skey[t] = key;
     __syncthreads();
-    // runs: a valid slot whose key differs from its predecessor's starts one
-    // (invalid keys sort last, so the valid slots are a prefix of the block)
-    const bool head = valid && (t == 0 || skey[t - 1] != key);
-    const unsigned bal = __ballot_sync(FULL_MASK, head);
-    if (lane == 0) wsum[w] = __popc(bal);
-    const int nvalid = __syncthreads_count(valid);
-    if (t < 32) {
-        const int nw = bs >> 5;
-        int v = (t < nw) ? wsum[t] : 0;
-        int incl = v;
-#pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-            int o = __shfl_up_sync(FULL_MASK, incl, off);
-            if (t >= off) incl += o;
-        }
-        if (t < nw) wsum[t] = incl - v;
-        if (t == 31) wsum[32] = incl;
-    }
-    __syncthreads();
-    if (head) run_start[wsum[w] + __popc(bal & ((1u << lane) - 1u))] = t;
-    const int R = wsum[32];
-    if (t == 0) run_start[R] = nvalid;
-    __syncthreads();
-    for (int item = t; item < R * 8; item += bs) {
-        const int r = item >> 3, k = item & 7;
-        const int ix = (k >> 2) & 1, iy = (k >> 1) & 1, iz = k & 1;
+    const int R = block_runs(skey, (int)min((long long)bs, n - blockIdx.x * (long long)bs), run_start, wsum);
+    constexpr int TPR = 8 / CPT;  // threads per run
+    for (int item = t; item < R * TPR; item += bs) {
+        const int r = item / TPR, k0 = (item % TPR) * CPT;  // corners k0 .. k0 + CPT - 1
         const int a = run_start[r], e = run_start[r + 1];
-        T am = 0, ap0 = 0, ap1 = 0, ap2 = 0, af0 = 0, af1 = 0, af2 = 0, g0 = 0, g1 = 0, g2 = 0;
+        if (!(skey[a] < g.key_max)) continue;  // slots outside the grid
+        T am[CPT], ap0[CPT], ap1[CPT], ap2[CPT], af0[CPT], af1[CPT], af2[CPT], g0[CPT], g1[CPT], g2[CPT];
+#pragma unroll
+        for (int j = 0; j < CPT; ++j) am[j] = ap0[j] = ap1[j] = ap2[j] = af0[j] = af1[j] = af2[j] = g0[j] = g1[j] = g2[j] = 0;
         for (int i = a; i < e; ++i) {
-            const T nx = sw[ix * bs + i], ny = sw[(2 + iy) * bs + i], nz = sw[(4 + iz) * bs + i];
-            const T N = nx * ny * nz;
-            const T G0 = -(ny * nz) * sw[(6 + ix) * bs + i];
-            const T G1 = -(nx * nz) * sw[(8 + iy) * bs + i];
-            const T G2 = -(nx * ny) * sw[(10 + iz) * bs + i];
-            const T m = sq[i];
-            am += N * m;
-            ap0 += N * sq[1 * bs + i];
-            ap1 += N * sq[2 * bs + i];
-            ap2 += N * sq[3 * bs + i];
+            const T m = sq[i], mv0 = sq[1 * bs + i], mv1 = sq[2 * bs + i], mv2 = sq[3 * bs + i];
             const T v0 = sq[4 * bs + i], v1 = sq[5 * bs + i], v2 = sq[6 * bs + i];
             const T v3 = sq[7 * bs + i], v4 = sq[8 * bs + i], v5 = sq[9 * bs + i];
-            af0 += G0 * v0 + G1 * v3 + G2 * v5 + N * sq[10 * bs + i];
-            af1 += G1 * v1 + G0 * v3 + G2 * v4 + N * sq[11 * bs + i];
-            af2 += G2 * v2 + G0 * v5 + G1 * v4 + N * sq[12 * bs + i];
-            if (with_mg) {
-                g0 += G0 * m;
-                g1 += G1 * m;
-                g2 += G2 * m;
+            const T fe0 = sq[10 * bs + i], fe1 = sq[11 * bs + i], fe2 = sq[12 * bs + i];
+#pragma unroll
+            for (int j = 0; j < CPT; ++j) {
+                const int k = k0 + j;
+                const int ix = (k >> 2) & 1, iy = (k >> 1) & 1, iz = k & 1;
+                const T nx = sw[ix * bs + i], ny = sw[(2 + iy) * bs + i], nz = sw[(4 + iz) * bs + i];
+                const T N = nx * ny * nz;
+                const T G0 = -(ny * nz) * sw[(6 + ix) * bs + i];
+                const T G1 = -(nx * nz) * sw[(8 + iy) * bs + i];
+                const T G2 = -(nx * ny) * sw[(10 + iz) * bs + i];
+                am[j] += N * m;
+                ap0[j] += N * mv0;
+                ap1[j] += N * mv1;
+                ap2[j] += N * mv2;
+                af0[j] += G0 * v0 + G1 * v3 + G2 * v5 + N * fe0;
+                af1[j] += G1 * v1 + G0 * v3 + G2 * v4 + N * fe1;
+                af2[j] += G2 * v2 + G0 * v5 + G1 * v4 + N * fe2;
+                if (with_mg) {
+                    g0[j] += G0 * m;
+                    g1[j] += G1 * m;
+                    g2[j] += G2 * m;
+                }
             }
         }
         const Geom& gs = spec_geom(g, P.sid, sperm[a]);
         int b[3];
         key_to_base(skey[a], gs, b);
-        const long long nid = corner_node(gs, b, k);
-        if (nid >= 0) {
+#pragma unroll
+        for (int j = 0; j < CPT; ++j) {
+            const long long nid = corner_node(gs, b, k0 + j);
+            if (nid < 0) continue;
             // active nodes: the in-range corners of occupied cells (b_Active, …MPLocks.cpp:36)
             if (mark_active && !(nd.state[nid] & 1u)) atomicOr(&nd.state[nid], 1u);
-            atomicAdd(&nd.mass[nid], am);
-            atomicAdd(&nd.mom[nid], ap0);
-            atomicAdd(&nd.mom[nn + nid], ap1);
-            atomicAdd(&nd.mom[2 * nn + nid], ap2);
-            atomicAdd(&nd.force[nid], af0);
-            atomicAdd(&nd.force[nn + nid], af1);
-            atomicAdd(&nd.force[2 * nn + nid], af2);
+            atomicAdd(&nd.mass[nid], am[j]);
+            atomicAdd(&nd.mom[nid], ap0[j]);
+            atomicAdd(&nd.mom[nn + nid], ap1[j]);
+            atomicAdd(&nd.mom[2 * nn + nid], ap2[j]);
+            atomicAdd(&nd.force[nid], af0[j]);
+            atomicAdd(&nd.force[nn + nid], af1[j]);
+            atomicAdd(&nd.force[2 * nn + nid], af2[j]);
             if (with_mg) {
-                atomicAdd(&nd.mg[nid], g0);
-                atomicAdd(&nd.mg[nn + nid], g1);
-                atomicAdd(&nd.mg[2 * nn + nid], g2);
+                atomicAdd(&nd.mg[nid], g0[j]);
+                atomicAdd(&nd.mg[nn + nid], g1[j]);
+                atomicAdd(&nd.mg[2 * nn + nid], g2[j]);
             }
         }
     }
@@ -695,13 +719,13 @@ __host__ __device__ constexpr size_t pass1_cells_smem(int bs) {
     return (size_t)9 * bs * sizeof(T) + (size_t)bs * 8 + (size_t)(bs + 1) * 4 + 64 * 4;
 }
 
-template <typename T>
+template <typename T, int CPT>
 __global__ void __launch_bounds__(512) k_pass1_cells(PView<T> P, NView<T> nd, Geom g,
                                                      const unsigned* __restrict__ skeys,
                                                      const unsigned* __restrict__ perm, long long n, T dt,
                                                      T mass_min, int contact) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int bs = blockDim.x, t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const int bs = blockDim.x, t = threadIdx.x;
     T* sn = reinterpret_cast<T*>(smem_raw);  // 6 x bs: Nx0 Nx1 Ny0 Ny1 Nz0 Nz1
     T* smv = sn + 6 * bs;                    // 3 x bs: m v
     unsigned* skey = reinterpret_cast<unsigned*>(smv + 3 * bs);
@@ -713,7 +737,7 @@ __global__ void __launch_bounds__(512) k_pass1_cells(PView<T> P, NView<T> nd, Ge
     const bool key_ok = key < g.key_max;
     const long long np = P.n, nn = nd.nn;
     if (key_ok) {
-        const long long p = perm[s];
+        const long long p = perm ? perm[s] : s;
         sperm[t] = (unsigned)p;
         const bool valid = !(contact && (P.pflags[p] & 8u));
         T N6[6] = {0, 0, 0, 0, 0, 0}, mv[3] = {0, 0, 0};
@@ -756,46 +780,37 @@ __global__ void __launch_bounds__(512) k_pass1_cells(PView<T> P, NView<T> nd, Ge
     }
     skey[t] = key;
     __syncthreads();
-    const bool head = key_ok && (t == 0 || skey[t - 1] != key);
-    const unsigned bal = __ballot_sync(FULL_MASK, head);
-    if (lane == 0) wsum[w] = __popc(bal);
-    const int nvalid = __syncthreads_count(key_ok);
-    if (t < 32) {
-        const int nw = bs >> 5;
-        int v = (t < nw) ? wsum[t] : 0;
-        int incl = v;
-#pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-            int o = __shfl_up_sync(FULL_MASK, incl, off);
-            if (t >= off) incl += o;
-        }
-        if (t < nw) wsum[t] = incl - v;
-        if (t == 31) wsum[32] = incl;
-    }
-    __syncthreads();
-    if (head) run_start[wsum[w] + __popc(bal & ((1u << lane) - 1u))] = t;
-    const int R = wsum[32];
-    if (t == 0) run_start[R] = nvalid;
-    __syncthreads();
-    for (int item = t; item < R * 8; item += bs) {
-        const int r = item >> 3, k = item & 7;
-        const int ix = (k >> 2) & 1, iy = (k >> 1) & 1, iz = k & 1;
+    const int R = block_runs(skey, (int)min((long long)bs, n - blockIdx.x * (long long)bs), run_start, wsum);
+    constexpr int TPR = 8 / CPT;  // threads per run; each sums CPT corners sharing its x (and y) bases
+    for (int item = t; item < R * TPR; item += bs) {
+        const int r = item / TPR, k0 = (item % TPR) * CPT;
         const int a = run_start[r], e = run_start[r + 1];
-        T q0 = 0, q1 = 0, q2 = 0;
+        if (!(skey[a] < g.key_max)) continue;  // slots outside the grid
+        T q0[CPT], q1[CPT], q2[CPT];
+#pragma unroll
+        for (int j = 0; j < CPT; ++j) q0[j] = q1[j] = q2[j] = 0;
         for (int i = a; i < e; ++i) {
-            const T N = sn[ix * bs + i] * sn[(2 + iy) * bs + i] * sn[(4 + iz) * bs + i];
-            q0 += N * smv[i];
-            q1 += N * smv[bs + i];
-            q2 += N * smv[2 * bs + i];
+            const T mv0 = smv[i], mv1 = smv[bs + i], mv2 = smv[2 * bs + i];
+#pragma unroll
+            for (int j = 0; j < CPT; ++j) {
+                const int k = k0 + j;
+                const int ix = (k >> 2) & 1, iy = (k >> 1) & 1, iz = k & 1;
+                const T N = sn[ix * bs + i] * sn[(2 + iy) * bs + i] * sn[(4 + iz) * bs + i];
+                q0[j] += N * mv0;
+                q1[j] += N * mv1;
+                q2[j] += N * mv2;
+            }
         }
         const Geom& gs = spec_geom(g, P.sid, sperm[a]);
         int b[3];
         key_to_base(skey[a], gs, b);
-        const long long nid = corner_node(gs, b, k);
-        if (nid >= 0) {
-            atomicAdd(&nd.q[nid], q0);
-            atomicAdd(&nd.q[nn + nid], q1);
-            atomicAdd(&nd.q[2 * nn + nid], q2);
+#pragma unroll
+        for (int j = 0; j < CPT; ++j) {
+            const long long nid = corner_node(gs, b, k0 + j);
+            if (nid < 0) continue;
+            atomicAdd(&nd.q[nid], q0[j]);
+            atomicAdd(&nd.q[nn + nid], q1[j]);
+            atomicAdd(&nd.q[2 * nn + nid], q2[j]);
         }
     }
 }
@@ -1239,7 +1254,7 @@ __global__ void __launch_bounds__(512) k_pass2(PView<T> P, NView<T> nd, Geom g, 
     float u[3];
     const unsigned nk = particle_key(gs, xn, u, err);
     keys[p] = nk;
-    keys_next[p] = nk;
+    if (keys_next) keys_next[p] = nk;
     if constexpr (sizeof(T) == 4) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) P.loc[c * np + p] = u[c];

@@ -117,6 +117,7 @@ OPT_PASS_BLOCK = 5
 OPT_GATHER = 6
 OPT_GRAPH = 7
 OPT_REORDER = 8
+OPT_CELL_SORT = 9
 
 
 def library_path() -> str:

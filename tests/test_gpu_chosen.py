@@ -56,7 +56,7 @@ def test_autotune_restores_state_and_picks_valid_options(golden, form):
         before = e.download_state(st)
         res = e.autotune(steps=2, contact=True)
         after = e.download_state(st)
-        assert res["candidates"] == 54 and res["gather_batch"] in (0, 1) and res["p2g_block"] in (128, 256, 512) and res["pass_block"] in (128, 256, 512)
+        assert res["candidates"] == 90 and res["gather_batch"] in (0, 1) and res["p2g_block"] in (128, 256, 512) and res["pass_block"] in (128, 256, 512)
         assert res["best_ms_per_step"] <= res["worst_ms_per_step"]
         for k in ("pos", "vel", "stress", "F", "g_mass", "g_state"):
             assert np.array_equal(before[k], after[k]), k
@@ -66,7 +66,7 @@ def test_autotune_restores_state_and_picks_valid_options(golden, form):
 def test_plain_form_parity_holds_for_every_launch_configuration(golden):
     st = golden("contact_in")
     ref = golden("contact_ref25")
-    for red in (0, 1, 2):
+    for red in (0, 1, 2, 3, 4):
         for blk in (128, 512):
             with engine.Engine.from_state(st) as e:
                 e.set_option(engine.OPT_GATHER, 1 if blk == 512 else 0)
@@ -82,12 +82,13 @@ def test_plain_form_parity_holds_for_every_launch_configuration(golden):
 
 
 def test_chosen_form_p2g_modes_agree():
-    """The three P2G reductions (per-particle atomics, lane runs, shared-memory cell runs) sum the same
-    contributions in different orders; with the contact path they also carry the FP32 mass gradient."""
+    """The P2G reductions (per-particle atomics, lane runs, shared-memory cell runs with 1, 2 or 4 corners per
+    thread) sum the same contributions in different orders; with the contact path they also carry the FP32 mass
+    gradient."""
     st = scenes.contact_small(seed=2)
     outs = []
-    for red in (0, 1, 2):
-        for blk in ((128, 512) if red == 2 else (256,)):
+    for red in (0, 1, 2, 3, 4):
+        for blk in ((128, 512) if red >= 2 else (256,)):
             with engine.Engine.from_state(st, engine.FORM_FP32) as e:
                 e.set_option(engine.OPT_P2G_REDUCE, red)
                 e.set_option(engine.OPT_P2G_BLOCK, blk)

@@ -9,10 +9,13 @@ from code_mpm_gb300 import engine, metrics, scenes
 pytestmark = pytest.mark.gpu
 
 
-def run(st, steps, contact, reorder, floor=0, graph=1):
+def run(st, steps, contact, reorder, floor=0, graph=1, cell_sort=1, p2g=None):
     with engine.Engine.from_state(st, engine.FORM_FP32) as e:
         e.set_option(engine.OPT_REORDER, reorder)
         e.set_option(engine.OPT_GRAPH, graph)
+        e.set_option(engine.OPT_CELL_SORT, cell_sort)
+        if p2g is not None:
+            e.set_option(engine.OPT_P2G_REDUCE, p2g)
         if floor:
             e.set_option(engine.OPT_FLOOR_FRICTION, 1)
         e.advance(steps, st.dt_max, contact)
@@ -77,3 +80,32 @@ def test_lists_uploaded_after_a_reorder():
     for k in ("strain_energy", "plastic_energy"):
         assert abs(mons[0][k] - mons[1][k]) <= 1e-4 * abs(mons[1][k]) + 1e-30, k
     assert mons[0]["count"] == mons[1]["count"]
+
+
+@pytest.mark.parametrize("reorder,p2g", [(0, 2), (7, 3), (-1, 2), (-1, 4)])
+def test_sort_free_run_matches_sorted(reorder, p2g):
+    """Without the per-step sort the cell-run kernels take the slots in storage order: cell order after a
+    reorder, the caller's (unordered) order with reorders off, where nearly every cell splits into many runs."""
+    st = scenes.contact_small(seed=2)
+    a = run(st, 30, 1, reorder, cell_sort=0, p2g=p2g)
+    b = run(st, 30, 1, -1)
+    close(a, b)
+    st = scenes.mixed_small(seed=1)
+    a = run(st, 20, 0, reorder, floor=1, cell_sort=0, p2g=p2g)
+    b = run(st, 20, 0, -1, floor=1)
+    close(a, b)
+
+
+def test_sort_free_cell_order_is_the_sorted_runs():
+    """The cell order reported after steps without the sort: the keys of the positions before the last step and
+    their stable order, the same as with the per-step sort."""
+    st = scenes.mixed_small(seed=1)
+    got = []
+    for cs in (1, 0):
+        with engine.Engine.from_state(st, engine.FORM_FP32) as e:
+            e.set_option(engine.OPT_CELL_SORT, cs)
+            e.advance(3, st.dt_max, False)
+            got.append(e.cell_order())
+    (k1, o1), (k0, o0) = got
+    assert np.mean(k1 == k0) > 0.999
+    assert np.array_equal(o0, np.argsort(k0, kind="stable"))
