@@ -279,6 +279,8 @@ def apply_tune(e, tune):
         e.set_option(engine.OPT_P2G_BLOCK, tune["p2g_block"])
         e.set_option(engine.OPT_PASS_BLOCK, tune["pass_block"])
         e.set_option(engine.OPT_GATHER, tune["gather_batch"])
+        e.set_option(engine.OPT_PASS1_CORNERS, tune["pass1_corners"])
+        e.set_option(engine.OPT_PASS1_BLOCK, tune["pass1_block"])
 
 
 def timed(e, steps, warmup, dt, contact, dist):

@@ -53,6 +53,7 @@ struct mpm_ctx {
     int floor_friction = 0;
     int profile = 0;
     int p2g_reduce = 2, p2g_block = 128, pass_block = 128, gather_batch = 0;
+    int pass1_corners = 1, pass1_block = 128;  // cell-run pass 1 (P2G modes 2-4)
     // simulation scalars
     mpm_sim sim{0.0, 1.0e-3, 0.0, 0.0, 10.0, 0};
     // counts
@@ -677,8 +678,14 @@ void graph_reset(mpm_ctx* c) {
     }
 }
 
+// detect: run the contact detection of the contact path (node mass
+// gradients, particle and node normals, node contact flags,
+// …_Contact.cpp:126-237).  Its results are output only: nothing in the step
+// reads them (GridPoint.h:17-18 marks the flags as graphics debugging) and
+// each step recomputes them from that step's particles, so callers run it on
+// the last step of an advance, whose results are the ones a download sees.
 template <typename T>
-int step_impl(mpm_ctx* c, double dt, int contact, bool graph = false) {
+int step_impl(mpm_ctx* c, double dt, int contact, bool graph, bool detect) {
     const long long n = c->n, nn = c->nn;
     PView<T> P = pview<T>(c);
     NView<T> N = nview<T>(c);
@@ -706,14 +713,16 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph = false) {
         // and P2G marks the active nodes; the FP64 form marks them here and
         // records the per-cell ranges its bit-exact ordered gather reads.
         const int fp32 = c->form == MPM_FORM_FP32 ? 1 : 0;
-        const int mg_in_p2g = (contact && fp32) ? 1 : 0;
+        const bool detecting = contact && detect;
+        const int mg_in_p2g = (detecting && fp32) ? 1 : 0;
         if (!fp32) {
-            if (contact) {
+            if (detecting) {
                 CK(cudaMemsetAsync(c->cstart.p, 0, (size_t)g.key_max * 4, c->stream));
                 CK(cudaMemsetAsync(c->cend.p, 0, (size_t)g.key_max * 4, c->stream));
             }
             LAUNCH("cell_ranges", k_cell_ranges, blocks_for(n), NTHREADS, skeys, n, g, N.state,
-                   contact ? (unsigned*)c->cstart.p : nullptr, contact ? (unsigned*)c->cend.p : nullptr, perm, P.sid);
+                   detecting ? (unsigned*)c->cstart.p : nullptr, detecting ? (unsigned*)c->cend.p : nullptr, perm,
+                   P.sid);
         }
         if (c->p2g_reduce >= 2) {  // shared-memory cell runs, 1 / 2 / 4 corners per thread
             const unsigned gb = blocks_for(n, c->p2g_block);
@@ -742,7 +751,7 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph = false) {
             LAUNCH("dc_claim", k_dc_claim, blocks_for(c->ndc), NTHREADS, (const unsigned*)c->dclist.p, c->ndc, keys,
                    (const uint8_t*)c->pflags.p, g, (unsigned*)c->g_owner.p, nn, contact, P.sid);
         }
-        if (contact) {
+        if (detecting) {
             const unsigned* surf = (const unsigned*)c->surf.p;
             const int ns = c->nsurf;
             const unsigned sb = blocks_for(ns);
@@ -773,17 +782,18 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph = false) {
         LAUNCH("node_phase_a", k_node_phase_a<T>, nodeblocks, NTHREADS, N, (T)dt, c->sim.damping, contact,
                c->floor_friction, (const unsigned*)c->dclist.p, c->ndc, (const T*)c->vel.p, n, mm);
         if (c->p2g_reduce >= 2) {  // the same reduction as P2G: shared-memory cell runs
-            const unsigned gb = blocks_for(n, c->p2g_block);
-            const size_t sm = pass1_cells_smem<T>(c->p2g_block);
-            if (c->p2g_reduce == 2)
-                LAUNCH_SMEM("pass1_remap", (k_pass1_cells<T, 1>), gb, c->p2g_block, sm, P, N, g, skeys, perm, n, (T)dt,
-                            mm, contact);
-            else if (c->p2g_reduce == 3)
-                LAUNCH_SMEM("pass1_remap", (k_pass1_cells<T, 2>), gb, c->p2g_block, sm, P, N, g, skeys, perm, n, (T)dt,
-                            mm, contact);
+            const int b1 = c->pass1_block;
+            const unsigned gb = blocks_for(n, b1);
+            const size_t sm = pass1_cells_smem<T>(b1);
+            if (c->pass1_corners == 1)
+                LAUNCH_SMEM("pass1_remap", (k_pass1_cells<T, 1>), gb, b1, sm, P, N, g, skeys, perm, n, (T)dt, mm,
+                            contact);
+            else if (c->pass1_corners == 2)
+                LAUNCH_SMEM("pass1_remap", (k_pass1_cells<T, 2>), gb, b1, sm, P, N, g, skeys, perm, n, (T)dt, mm,
+                            contact);
             else
-                LAUNCH_SMEM("pass1_remap", (k_pass1_cells<T, 4>), gb, c->p2g_block, sm, P, N, g, skeys, perm, n, (T)dt,
-                            mm, contact);
+                LAUNCH_SMEM("pass1_remap", (k_pass1_cells<T, 4>), gb, b1, sm, P, N, g, skeys, perm, n, (T)dt, mm,
+                            contact);
         }
         else if (c->gather_batch)
             LAUNCH("pass1_remap", (k_pass1_remap<T, 1>), blocks_for(n), NTHREADS, P, N, g, skeys, perm, n, (T)dt, mm,
@@ -860,9 +870,9 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph = false) {
     return MPM_OK;
 }
 
-int step(mpm_ctx* c, double dt, int contact, bool graph = false) {
-    return c->form == MPM_FORM_FP64 ? step_impl<double>(c, dt, contact, graph)
-                                    : step_impl<float>(c, dt, contact, graph);
+int step(mpm_ctx* c, double dt, int contact, bool graph = false, bool detect = true) {
+    return c->form == MPM_FORM_FP64 ? step_impl<double>(c, dt, contact, graph, detect)
+                                    : step_impl<float>(c, dt, contact, graph, detect);
 }
 
 // Steps nsteps with the two-step graph where it applies: the steady state
@@ -881,7 +891,8 @@ int reorder_every(const mpm_ctx* c) {
     return (!c->cell_sort && c->p2g_reduce >= 2) ? SORT_FREE_REORDER : 0;
 }
 
-int advance_graph(mpm_ctx* c, int nsteps, double dt, int contact, bool between_reorders = false) {
+int advance_graph(mpm_ctx* c, int nsteps, double dt, int contact, bool between_reorders = false,
+                  bool detect_last = true) {
     if (!between_reorders) {
         if (c->reorder_pending && c->have_particles) {
             int rc = reorder(c);
@@ -892,7 +903,7 @@ int advance_graph(mpm_ctx* c, int nsteps, double dt, int contact, bool between_r
             while (nsteps > 0) {
                 const long long left = std::max<long long>(1, every - c->steps_since_reorder);
                 const int k = (int)std::min<long long>(nsteps, left);
-                int rc = advance_graph(c, k, dt, contact, true);
+                int rc = advance_graph(c, k, dt, contact, true, detect_last && k == nsteps);
                 if (rc) return rc;
                 nsteps -= k;
                 if (c->steps_since_reorder >= every && (rc = reorder(c))) return rc;
@@ -901,23 +912,26 @@ int advance_graph(mpm_ctx* c, int nsteps, double dt, int contact, bool between_r
         }
     }
     int s = 0;
-    auto plain = [&](int k) -> int {
-        for (int i = 0; i < k; ++i)
-            if (int rc = step(c, dt, contact)) return rc;
+    // launches the remaining steps one by one, the contact detection on the last
+    auto plain = [&]() -> int {
+        for (; s < nsteps; ++s)
+            if (int rc = step(c, dt, contact, false, detect_last && s == nsteps - 1)) return rc;
         return MPM_OK;
     };
     while (s < nsteps && (!c->keys_valid || !c->have_alist)) {
-        if (int rc = plain(1)) return rc;
+        if (int rc = step(c, dt, contact, false, detect_last && s == nsteps - 1)) return rc;
         ++s;
     }
-    const bool can = c->use_graph && !c->profile && c->stream != nullptr && c->n > 0 && nsteps - s >= 2;
-    if (!can) return plain(nsteps - s);
+    // the graph's steps skip the contact detection; the last step then runs plainly with it
+    const int tail = (contact && detect_last) ? 1 : 0;
+    const bool can = c->use_graph && !c->profile && c->stream != nullptr && c->n > 0 && nsteps - tail - s >= 2;
+    if (!can) return plain();
     if (c->gexec && (c->g_dt != dt || c->g_contact != contact)) graph_reset(c);
     int rc;
     if ((rc = ensure(c, c->dsim, sizeof(DevSim)))) return rc;
     if (!c->h_sim && cudaMallocHost(&c->h_sim, sizeof(DevSim)) != cudaSuccess) {
         cudaGetLastError();
-        return plain(nsteps - s);
+        return plain();
     }
     // the device clock from the host's
     CK(cudaStreamSynchronize(c->stream));
@@ -928,8 +942,8 @@ int advance_graph(mpm_ctx* c, int nsteps, double dt, int contact, bool between_r
         const long long l0 = c->launches;
         cudaGraph_t gr = nullptr;
         CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
-        int r1 = step(c, dt, contact, true);
-        int r2 = r1 ? r1 : step(c, dt, contact, true);
+        int r1 = step(c, dt, contact, true, false);
+        int r2 = r1 ? r1 : step(c, dt, contact, true, false);
         cudaError_t ec = cudaStreamEndCapture(c->stream, &gr);
         if (r2 || ec != cudaSuccess) {
             cudaGetLastError();
@@ -949,7 +963,7 @@ int advance_graph(mpm_ctx* c, int nsteps, double dt, int contact, bool between_r
         CK(cudaGraphLaunch(c->gexec, c->stream));  // the two captured steps (host state already advanced)
         s += 2;
     }
-    for (; nsteps - s >= 2; s += 2) {
+    for (; nsteps - tail - s >= 2; s += 2) {
         CK(cudaGraphLaunch(c->gexec, c->stream));
         c->launches += c->g_launches;
         c->steps_since_reorder += 2;
@@ -958,7 +972,7 @@ int advance_graph(mpm_ctx* c, int nsteps, double dt, int contact, bool between_r
         c->sim.time += dt;
         c->sim.step += 1;
     }
-    return plain(nsteps - s);
+    return plain();
 }
 
 int alloc_particles(mpm_ctx* c, long long n) {
@@ -1205,11 +1219,17 @@ int mpm_set_option(mpm_ctx* c, int key, double value) {
             if (value != 0.0 && value != 1.0) return fail(c, MPM_ERR_ARG, "gather mode must be 0 or 1");
             c->gather_batch = (int)value;
             return MPM_OK;
+        case MPM_OPT_PASS1_CORNERS:
+            if (value != 1.0 && value != 2.0 && value != 4.0)
+                return fail(c, MPM_ERR_ARG, "pass-1 corners per thread must be 1, 2 or 4");
+            c->pass1_corners = (int)value;
+            return MPM_OK;
         case MPM_OPT_P2G_BLOCK:
-        case MPM_OPT_PASS_BLOCK: {
+        case MPM_OPT_PASS_BLOCK:
+        case MPM_OPT_PASS1_BLOCK: {
             int b = (int)value;
             if (b != 128 && b != 256 && b != 512) return fail(c, MPM_ERR_ARG, "block size must be 128, 256 or 512");
-            (key == MPM_OPT_P2G_BLOCK ? c->p2g_block : c->pass_block) = b;
+            (key == MPM_OPT_P2G_BLOCK ? c->p2g_block : key == MPM_OPT_PASS_BLOCK ? c->pass_block : c->pass1_block) = b;
             return MPM_OK;
         }
         default: return fail(c, MPM_ERR_ARG, "unknown option %d", key);
@@ -1729,66 +1749,70 @@ int mpm_autotune(mpm_ctx* c, int32_t steps, double dt, int contact, mpm_tune_res
     const mpm_sim sim0 = c->sim;
     const int prof0 = c->profile;
     c->profile = 0;
-    const int old[4] = {c->p2g_reduce, c->p2g_block, c->pass_block, c->gather_batch};
-    int best[4] = {old[0], old[1], old[2], old[3]};
+    // the tuned options: P2G mode, P2G block, pass-1 corners, pass-1 block, pass-2 block, gather mode
+    int* opt[6] = {&c->p2g_reduce, &c->p2g_block, &c->pass1_corners, &c->pass1_block, &c->pass_block, &c->gather_batch};
+    int old[6], best[6];
+    for (int i = 0; i < 6; ++i) old[i] = best[i] = *opt[i];
     double best_ms = 1e300, worst_ms = 0.0;
     int ncand = 0;
     cudaEvent_t a, b;
     CK(cudaEventCreate(&a));
     CK(cudaEventCreate(&b));
-    const int blocks[3] = {128, 256, 512};
-    for (int red = 0; red < 5 && rc == MPM_OK; ++red)
-        for (int pb = 0; pb < 3 && rc == MPM_OK; ++pb)
-            for (int qb = 0; qb < 3 && rc == MPM_OK; ++qb)
-            for (int gb = 0; gb < 2 && rc == MPM_OK; ++gb) {
-                c->p2g_reduce = red;
-                c->p2g_block = blocks[pb];
-                c->pass_block = blocks[qb];
-                c->gather_batch = gb;
-                if ((rc = step(c, dt, contact))) break;  // warm-up for this configuration
-                cudaEventRecord(a, c->stream);
-                for (int s = 0; s < steps && rc == MPM_OK; ++s) rc = step(c, dt, contact);
-                cudaEventRecord(b, c->stream);
-                cudaEventSynchronize(b);
-                float ms = 0.f;
-                cudaEventElapsedTime(&ms, a, b);
-                const double per = ms / steps;
-                ++ncand;
-                if (per < best_ms) {
-                    best_ms = per;
-                    best[0] = red;
-                    best[1] = blocks[pb];
-                    best[2] = blocks[qb];
-                    best[3] = gb;
-                }
-                worst_ms = std::max(worst_ms, per);
-                if (copy_all(false) != MPM_OK) rc = MPM_ERR_CUDA;
-                c->keys_valid = false;  // positions restored: keys are recomputed next step
-                c->have_alist = false;
-                c->sim = sim0;
+    // one trial: the candidate's options over the best so far, a warm-up step, `steps` timed steps, restore
+    auto trial = [&](int i0, int v0, int i1, int v1) -> int {
+        for (int i = 0; i < 6; ++i) *opt[i] = best[i];
+        *opt[i0] = v0;
+        *opt[i1] = v1;
+        int r = step(c, dt, contact, false, false);  // the run's steps: without the output-only detection
+        if (r == MPM_OK) {
+            cudaEventRecord(a, c->stream);
+            for (int s = 0; s < steps && r == MPM_OK; ++s) r = step(c, dt, contact, false, false);
+            cudaEventRecord(b, c->stream);
+        }
+        if (r == MPM_OK) {
+            cudaEventSynchronize(b);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, a, b);
+            const double per = ms / steps;
+            ++ncand;
+            worst_ms = std::max(worst_ms, per);
+            if (per < best_ms) {
+                best_ms = per;
+                for (int i = 0; i < 6; ++i) best[i] = *opt[i];
             }
+        }
+        if (copy_all(false) != MPM_OK && r == MPM_OK) r = MPM_ERR_CUDA;
+        c->keys_valid = false;  // positions restored: keys are recomputed next step
+        c->have_alist = false;
+        c->sim = sim0;
+        return r;
+    };
+    const int blocks[3] = {128, 256, 512}, corners[3] = {1, 2, 4};
+    for (int red = 0; red < 5 && rc == MPM_OK; ++red)
+        for (int pb = 0; pb < 3 && rc == MPM_OK; ++pb) rc = trial(0, red, 1, blocks[pb]);
+    if (best[0] >= 2)
+        for (int k = 0; k < 3 && rc == MPM_OK; ++k)
+            for (int pb = 0; pb < 3 && rc == MPM_OK; ++pb) rc = trial(2, corners[k], 3, blocks[pb]);
+    for (int qb = 0; qb < 3 && rc == MPM_OK; ++qb)
+        for (int gb = 0; gb < 2 && rc == MPM_OK; ++gb) rc = trial(4, blocks[qb], 5, gb);
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     c->steps_since_reorder = since0;
     c->profile = prof0;
     c->sim = sim0;
     if (rc) {
-        c->p2g_reduce = old[0];
-        c->p2g_block = old[1];
-        c->pass_block = old[2];
-        c->gather_batch = old[3];
+        for (int i = 0; i < 6; ++i) *opt[i] = old[i];
         return rc;
     }
     CK(cudaStreamSynchronize(c->stream));
-    c->p2g_reduce = best[0];
-    c->p2g_block = best[1];
-    c->pass_block = best[2];
-    c->gather_batch = best[3];
+    for (int i = 0; i < 6; ++i) *opt[i] = best[i];
     if (out) {
         out->p2g_reduce = best[0];
         out->p2g_block = best[1];
-        out->pass_block = best[2];
-        out->gather_batch = best[3];
+        out->pass1_corners = best[2];
+        out->pass1_block = best[3];
+        out->pass_block = best[4];
+        out->gather_batch = best[5];
         out->candidates = ncand;
         out->best_ms_per_step = best_ms;
         out->worst_ms_per_step = worst_ms;

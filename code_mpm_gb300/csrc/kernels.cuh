@@ -273,8 +273,8 @@ __global__ void __launch_bounds__(512) k_p2g(PView<T> P, NView<T> nd, Geom g, co
 // run's particles in slot order and issues one atomic per field.  Same
 // per-particle arithmetic as k_p2g; the cross-lane shuffles of REDUCE = 1
 // become shared-memory reads, and the atomics are issued by full warps.
-// Shared memory: (12 + 13) values per slot plus the keys, particle indices
-// and run starts (p2g_cells_smem).
+// Shared memory: (12 + 13) values per slot (the 12 base rows padded to an odd
+// stride) plus the keys, particle indices and run starts (p2g_cells_smem).
 // ---------------------------------------------------------------------------
 // Runs of equal cell keys among the block's first nslots slots (keys staged
 // in shared memory, a __syncthreads after the staging): run r covers slots
@@ -309,7 +309,7 @@ __device__ __forceinline__ int block_runs(const unsigned* skey, int nslots, int*
 
 template <typename T>
 __host__ __device__ constexpr size_t p2g_cells_smem(int bs) {
-    return (size_t)25 * bs * sizeof(T) + (size_t)bs * 8 + (size_t)(bs + 1) * 4 + 64 * 4;
+    return ((size_t)12 * (bs + 1) + (size_t)13 * bs) * sizeof(T) + (size_t)bs * 8 + (size_t)(bs + 1) * 4 + 64 * 4;
 }
 
 // CPT corners per phase-2 thread (1, 2 or 4): the corners sharing the
@@ -322,8 +322,11 @@ __global__ void __launch_bounds__(512) k_p2g_cells(PView<T> P, NView<T> nd, Geom
     static_assert(CPT == 1 || CPT == 2 || CPT == 4, "corners per thread");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int bs = blockDim.x, t = threadIdx.x;
-    T* sw = reinterpret_cast<T*>(smem_raw);        // 12 x bs: Nx0 Nx1 Ny0 Ny1 Nz0 Nz1 gx0 gx1 gy0 gy1 gz0 gz1
-    T* sq = sw + 12 * bs;                          // 13 x bs: m, m v (3), -V sigma (6), f_ext (3)
+    // 12 rows of bs + 1 (the odd stride puts the two nodes' values of an axis in different banks):
+    // Nx0 Nx1 Ny0 Ny1 Nz0 Nz1 gx0 gx1 gy0 gy1 gz0 gz1
+    const int S = bs + 1;
+    T* sw = reinterpret_cast<T*>(smem_raw);
+    T* sq = sw + 12 * S;                           // 13 x bs: m, m v (3), -V sigma (6), f_ext (3)
     unsigned* skey = reinterpret_cast<unsigned*>(sq + 13 * bs);
     unsigned* sperm = skey + bs;
     int* run_start = reinterpret_cast<int*>(sperm + bs);  // bs + 1
@@ -339,18 +342,18 @@ __global__ void __launch_bounds__(512) k_p2g_cells(PView<T> P, NView<T> nd, Geom
         key_to_base(key, gs, b);
         Bases<T> B;
         particle_bases<T>(P, gs, p, b, B);
-        sw[0 * bs + t] = B.Nx[0];
-        sw[1 * bs + t] = B.Nx[1];
-        sw[2 * bs + t] = B.Ny[0];
-        sw[3 * bs + t] = B.Ny[1];
-        sw[4 * bs + t] = B.Nz[0];
-        sw[5 * bs + t] = B.Nz[1];
-        sw[6 * bs + t] = B.gx[0];
-        sw[7 * bs + t] = B.gx[1];
-        sw[8 * bs + t] = B.gy[0];
-        sw[9 * bs + t] = B.gy[1];
-        sw[10 * bs + t] = B.gz[0];
-        sw[11 * bs + t] = B.gz[1];
+        sw[0 * S + t] = B.Nx[0];
+        sw[1 * S + t] = B.Nx[1];
+        sw[2 * S + t] = B.Ny[0];
+        sw[3 * S + t] = B.Ny[1];
+        sw[4 * S + t] = B.Nz[0];
+        sw[5 * S + t] = B.Nz[1];
+        sw[6 * S + t] = B.gx[0];
+        sw[7 * S + t] = B.gx[1];
+        sw[8 * S + t] = B.gy[0];
+        sw[9 * S + t] = B.gy[1];
+        sw[10 * S + t] = B.gz[0];
+        sw[11 * S + t] = B.gz[1];
         const T m = P.mass[p], V = P.vol[p];
         sq[t] = m;
 #pragma unroll
@@ -382,11 +385,11 @@ __global__ void __launch_bounds__(512) k_p2g_cells(PView<T> P, NView<T> nd, Geom
             for (int j = 0; j < CPT; ++j) {
                 const int k = k0 + j;
                 const int ix = (k >> 2) & 1, iy = (k >> 1) & 1, iz = k & 1;
-                const T nx = sw[ix * bs + i], ny = sw[(2 + iy) * bs + i], nz = sw[(4 + iz) * bs + i];
+                const T nx = sw[ix * S + i], ny = sw[(2 + iy) * S + i], nz = sw[(4 + iz) * S + i];
                 const T N = nx * ny * nz;
-                const T G0 = -(ny * nz) * sw[(6 + ix) * bs + i];
-                const T G1 = -(nx * nz) * sw[(8 + iy) * bs + i];
-                const T G2 = -(nx * ny) * sw[(10 + iz) * bs + i];
+                const T G0 = -(ny * nz) * sw[(6 + ix) * S + i];
+                const T G1 = -(nx * nz) * sw[(8 + iy) * S + i];
+                const T G2 = -(nx * ny) * sw[(10 + iz) * S + i];
                 am[j] += N * m;
                 ap0[j] += N * mv0;
                 ap1[j] += N * mv1;
@@ -716,7 +719,7 @@ __global__ void __launch_bounds__(256) k_pass1_remap(PView<T> P, NView<T> nd, Ge
 // ---------------------------------------------------------------------------
 template <typename T>
 __host__ __device__ constexpr size_t pass1_cells_smem(int bs) {
-    return (size_t)9 * bs * sizeof(T) + (size_t)bs * 8 + (size_t)(bs + 1) * 4 + 64 * 4;
+    return ((size_t)6 * (bs + 1) + (size_t)3 * bs) * sizeof(T) + (size_t)bs * 8 + (size_t)(bs + 1) * 4 + 64 * 4;
 }
 
 template <typename T, int CPT>
@@ -726,8 +729,9 @@ __global__ void __launch_bounds__(512) k_pass1_cells(PView<T> P, NView<T> nd, Ge
                                                      T mass_min, int contact) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int bs = blockDim.x, t = threadIdx.x;
-    T* sn = reinterpret_cast<T*>(smem_raw);  // 6 x bs: Nx0 Nx1 Ny0 Ny1 Nz0 Nz1
-    T* smv = sn + 6 * bs;                    // 3 x bs: m v
+    const int S = bs + 1;                    // odd row stride: the two nodes' values of an axis in different banks
+    T* sn = reinterpret_cast<T*>(smem_raw);  // 6 x S: Nx0 Nx1 Ny0 Ny1 Nz0 Nz1
+    T* smv = sn + 6 * S;                     // 3 x bs: m v
     unsigned* skey = reinterpret_cast<unsigned*>(smv + 3 * bs);
     unsigned* sperm = skey + bs;
     int* run_start = reinterpret_cast<int*>(sperm + bs);
@@ -774,7 +778,7 @@ __global__ void __launch_bounds__(512) k_pass1_cells(PView<T> P, NView<T> nd, Ge
             N6[5] = B.Nz[1];
         }
 #pragma unroll
-        for (int c = 0; c < 6; ++c) sn[c * bs + t] = N6[c];
+        for (int c = 0; c < 6; ++c) sn[c * S + t] = N6[c];
 #pragma unroll
         for (int c = 0; c < 3; ++c) smv[c * bs + t] = mv[c];
     }
@@ -795,7 +799,7 @@ __global__ void __launch_bounds__(512) k_pass1_cells(PView<T> P, NView<T> nd, Ge
             for (int j = 0; j < CPT; ++j) {
                 const int k = k0 + j;
                 const int ix = (k >> 2) & 1, iy = (k >> 1) & 1, iz = k & 1;
-                const T N = sn[ix * bs + i] * sn[(2 + iy) * bs + i] * sn[(4 + iz) * bs + i];
+                const T N = sn[ix * S + i] * sn[(2 + iy) * S + i] * sn[(4 + iz) * S + i];
                 q0[j] += N * mv0;
                 q1[j] += N * mv1;
                 q2[j] += N * mv2;

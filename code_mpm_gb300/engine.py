@@ -99,7 +99,7 @@ class KernelStat(C.Structure):
 class TuneResult(C.Structure):
     _fields_ = [("p2g_reduce", C.c_int32), ("p2g_block", C.c_int32), ("pass_block", C.c_int32),
                 ("candidates", C.c_int32), ("best_ms_per_step", C.c_double), ("worst_ms_per_step", C.c_double),
-                ("gather_batch", C.c_int32)]
+                ("gather_batch", C.c_int32), ("pass1_corners", C.c_int32), ("pass1_block", C.c_int32)]
 
 
 class Monitors(C.Structure):
@@ -118,6 +118,8 @@ OPT_GATHER = 6
 OPT_GRAPH = 7
 OPT_REORDER = 8
 OPT_CELL_SORT = 9
+OPT_PASS1_CORNERS = 10
+OPT_PASS1_BLOCK = 11
 
 
 def library_path() -> str:
@@ -396,7 +398,7 @@ class Engine:
         r = TuneResult()
         self._check(self._L.mpm_autotune(self._h, int(steps), float(dt), 1 if contact else 0, C.byref(r)))
         return {"p2g_reduce": r.p2g_reduce, "p2g_block": r.p2g_block, "pass_block": r.pass_block,
-                "gather_batch": r.gather_batch,
+                "gather_batch": r.gather_batch, "pass1_corners": r.pass1_corners, "pass1_block": r.pass1_block,
                 "candidates": r.candidates, "best_ms_per_step": r.best_ms_per_step,
                 "worst_ms_per_step": r.worst_ms_per_step}
 

@@ -76,6 +76,8 @@ extern "C" {
 #define MPM_OPT_GATHER 6         /* G2P node gathers: 0 = one corner at a time, 1 = several corners' loads issued together */
 #define MPM_OPT_GRAPH 7          /* 1 (default): mpm_advance replays a captured two-step CUDA graph in the steady state; 0: launch every kernel */
 #define MPM_OPT_REORDER 8        /* FP32 form: store particles in cell order after each particle upload (0, default), also every N steps (N > 0), or never (-1); results stay in the caller's order */
+#define MPM_OPT_PASS1_CORNERS 10 /* cell-run G2P pass 1 (P2G modes 2-4): corners per thread, 1 (default), 2 or 4 */
+#define MPM_OPT_PASS1_BLOCK 11   /* cell-run G2P pass 1: threads per block (128, 256 or 512) */
 #define MPM_OPT_CELL_SORT 9      /* FP32 form, P2G modes 2-4: 1 sorts the particles by cell every step; 0 (default) takes the storage order as it is (a cell whose particles are not adjacent is summed in several runs) and, with MPM_OPT_REORDER 0, restores the cell order every 256 steps */
 
 typedef struct mpm_ctx mpm_ctx;
@@ -196,15 +198,16 @@ int mpm_synchronize(mpm_ctx* ctx);
 int mpm_advance_timed(mpm_ctx* ctx, int32_t nsteps, double dt, int contact, float* ms);
 
 /* Autotuner (no counterpart in the reference, which has one fixed OpenMP
- * loop): times `steps` steps of dt for every candidate launch configuration
- * (P2G reduction mode x P2G block size x pass-2 block size) on the current
- * state, keeps the fastest, and restores the particle and node state and the
- * time exactly as they were.  Results are the chosen options and the best
- * and worst candidate times per step. */
+ * loop): times `steps` steps of dt per candidate launch configuration on the
+ * current state in three stages, each keeping the fastest so far: P2G mode x
+ * P2G block (15), then pass-1 corners per thread x pass-1 block (9, cell-run
+ * modes only), then pass-2 block x gather mode (6).  The particle and node
+ * state and the time are restored exactly as they were.  Results are the
+ * chosen options and the best and worst candidate times per step. */
 typedef struct mpm_tune_result {
     int32_t p2g_reduce, p2g_block, pass_block, candidates;
     double best_ms_per_step, worst_ms_per_step;
-    int32_t gather_batch;
+    int32_t gather_batch, pass1_corners, pass1_block;
 } mpm_tune_result;
 int mpm_autotune(mpm_ctx* ctx, int32_t steps, double dt, int contact, mpm_tune_result* out);
 

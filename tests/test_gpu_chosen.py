@@ -56,7 +56,7 @@ def test_autotune_restores_state_and_picks_valid_options(golden, form):
         before = e.download_state(st)
         res = e.autotune(steps=2, contact=True)
         after = e.download_state(st)
-        assert res["candidates"] == 90 and res["gather_batch"] in (0, 1) and res["p2g_block"] in (128, 256, 512) and res["pass_block"] in (128, 256, 512)
+        assert res["candidates"] in (21, 30) and res["pass1_corners"] in (1, 2, 4) and res["pass1_block"] in (128, 256, 512) and res["gather_batch"] in (0, 1) and res["p2g_block"] in (128, 256, 512) and res["pass_block"] in (128, 256, 512)
         assert res["best_ms_per_step"] <= res["worst_ms_per_step"]
         for k in ("pos", "vel", "stress", "F", "g_mass", "g_state"):
             assert np.array_equal(before[k], after[k]), k
@@ -71,6 +71,8 @@ def test_plain_form_parity_holds_for_every_launch_configuration(golden):
             with engine.Engine.from_state(st) as e:
                 e.set_option(engine.OPT_GATHER, 1 if blk == 512 else 0)
                 e.set_option(engine.OPT_P2G_REDUCE, red)
+                e.set_option(engine.OPT_PASS1_CORNERS, {2: 1, 3: 2, 4: 4}.get(red, 1))
+                e.set_option(engine.OPT_PASS1_BLOCK, blk)
                 e.set_option(engine.OPT_P2G_BLOCK, blk)
                 e.set_option(engine.OPT_PASS_BLOCK, blk)
                 e.advance(25, st.dt_max, True)
@@ -92,6 +94,8 @@ def test_chosen_form_p2g_modes_agree():
             with engine.Engine.from_state(st, engine.FORM_FP32) as e:
                 e.set_option(engine.OPT_P2G_REDUCE, red)
                 e.set_option(engine.OPT_P2G_BLOCK, blk)
+                e.set_option(engine.OPT_PASS1_CORNERS, {2: 1, 3: 2, 4: 4}.get(red, 1))
+                e.set_option(engine.OPT_PASS1_BLOCK, {128: 512, 512: 128}.get(blk, 128))
                 e.advance(10, st.dt_max, True)
                 outs.append(((red, blk), e.download_state(st)))
     (_, a) = outs[0]
