@@ -46,8 +46,8 @@ FALLBACK_HBM_GBS = 6800.0
 # Algorithmic bytes per particle-update per sweep (plain FP64 / FP32 transfers),
 # fields read and written once per sweep, shape weights recomputed.
 ALG_BYTES = {
-    "fp64": {"p2g": 136, "pass1_remap": 80, "pass2": 580},
-    "fp32": {"p2g": 80, "pass1_remap": 52, "pass2": 348},
+    "fp64": {"p2g": 136, "pass1_remap": 80, "pass2": 532},
+    "fp32": {"p2g": 80, "pass1_remap": 52, "pass2": 324},
 }
 # Grid bytes per active node of each sweep: P2G writes mass, momentum and force
 # (7 values), pass 1 + remap reads f and m and writes the remap sum (4 + 3),

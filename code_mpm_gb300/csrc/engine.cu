@@ -65,6 +65,7 @@ struct mpm_ctx {
     std::vector<Geom> geoms;
     DevBuf geom_tab, sid, alist, acount;
     bool have_alist = false;  // alist holds the active nodes of the last step
+    bool grid_dirty = true;   // node values at the last step's active nodes (an output step or an upload)
     bool use_alist = false;
     std::vector<double> tl_t, tl_v;
     bool have_particles = false, have_nodes = false;
@@ -678,14 +679,17 @@ void graph_reset(mpm_ctx* c) {
     }
 }
 
-// detect: run the contact detection of the contact path (node mass
-// gradients, particle and node normals, node contact flags,
-// …_Contact.cpp:126-237).  Its results are output only: nothing in the step
-// reads them (GridPoint.h:17-18 marks the flags as graphics debugging) and
-// each step recomputes them from that step's particles, so callers run it on
-// the last step of an advance, whose results are the ones a download sees.
+// output: the step is an output step, the last of an advance, whose results
+// the caller can see.  Only an output step runs the contact path's contact
+// detection (node mass gradients, particle and node normals, node contact
+// flags, …_Contact.cpp:126-237) and writes the contact path's strain rate
+// (:509): both are output only, as nothing in a step reads them
+// (GridPoint.h:17-18 marks the flags as graphics debugging) and each step
+// recomputes them from that step's particles.  Only an output step keeps its
+// node values: the others zero their active nodes once the records are formed
+// (pass 2 reads only the records), so the next step needs no grid reset.
 template <typename T>
-int step_impl(mpm_ctx* c, double dt, int contact, bool graph, bool detect) {
+int step_impl(mpm_ctx* c, double dt, int contact, bool graph, bool output) {
     const long long n = c->n, nn = c->nn;
     PView<T> P = pview<T>(c);
     NView<T> N = nview<T>(c);
@@ -697,7 +701,10 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph, bool detect) {
     // node kernels sweep the active-node list; the reset uses the previous step's
     const unsigned nodeblocks = (unsigned)std::min<long long>(blocks_for(nn), (long long)c->sm_count * 16);
     N.alist = c->have_alist ? (const unsigned*)c->alist.p : nullptr;
-    LAUNCH("reset_grid", k_reset_grid<T>, c->have_alist ? nodeblocks : blocks_for(nn), NTHREADS, N, contact);
+    if (c->grid_dirty) {  // after a step that left its node values (or an upload); clean steps zero their own
+        LAUNCH("reset_grid", k_reset_grid<T>, c->have_alist ? nodeblocks : blocks_for(nn), NTHREADS, N, contact);
+        c->grid_dirty = false;
+    }
     if (n > 0) {
         // The FP32 form's cell-run kernels accept slots out of cell order (a
         // cell met twice is summed in two runs), so with particles stored in
@@ -713,7 +720,7 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph, bool detect) {
         // and P2G marks the active nodes; the FP64 form marks them here and
         // records the per-cell ranges its bit-exact ordered gather reads.
         const int fp32 = c->form == MPM_FORM_FP32 ? 1 : 0;
-        const bool detecting = contact && detect;
+        const bool detecting = contact && output;
         const int mg_in_p2g = (detecting && fp32) ? 1 : 0;
         if (!fp32) {
             if (detecting) {
@@ -803,7 +810,8 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph, bool detect) {
                    contact);
         // remap, displacement control and BC in the path's order, p/m and v: one pass
         LAUNCH("node_phase_b", k_node_phase_b<T>, nodeblocks, NTHREADS, N, contact, (const unsigned*)c->dclist.p,
-               c->ndc, (const T*)c->vel.p, n, mm);
+               c->ndc, (const T*)c->vel.p, n, mm, output ? 0 : 1);
+        if (output) c->grid_dirty = true;  // the last step of an advance keeps its node values for the caller
         if (c->ndc > 0) c->owner_clean = true;
         StepArgs a;
         a.dt = dt;
@@ -825,6 +833,7 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph, bool detect) {
         a.hv_rows = c->hv_rows;
         a.hv_count = (unsigned*)c->hv_count.p;
         a.hv_cap = c->hv_cap;
+        a.outputs = output ? 1 : 0;
         const bool use_net = sizeof(T) == 4 && c->net && c->sg_mats;
         if (use_net) {
             int rq;
@@ -870,9 +879,9 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph, bool detect) {
     return MPM_OK;
 }
 
-int step(mpm_ctx* c, double dt, int contact, bool graph = false, bool detect = true) {
-    return c->form == MPM_FORM_FP64 ? step_impl<double>(c, dt, contact, graph, detect)
-                                    : step_impl<float>(c, dt, contact, graph, detect);
+int step(mpm_ctx* c, double dt, int contact, bool graph = false, bool output = true) {
+    return c->form == MPM_FORM_FP64 ? step_impl<double>(c, dt, contact, graph, output)
+                                    : step_impl<float>(c, dt, contact, graph, output);
 }
 
 // Steps nsteps with the two-step graph where it applies: the steady state
@@ -892,7 +901,7 @@ int reorder_every(const mpm_ctx* c) {
 }
 
 int advance_graph(mpm_ctx* c, int nsteps, double dt, int contact, bool between_reorders = false,
-                  bool detect_last = true) {
+                  bool output_last = true) {
     if (!between_reorders) {
         if (c->reorder_pending && c->have_particles) {
             int rc = reorder(c);
@@ -903,7 +912,7 @@ int advance_graph(mpm_ctx* c, int nsteps, double dt, int contact, bool between_r
             while (nsteps > 0) {
                 const long long left = std::max<long long>(1, every - c->steps_since_reorder);
                 const int k = (int)std::min<long long>(nsteps, left);
-                int rc = advance_graph(c, k, dt, contact, true, detect_last && k == nsteps);
+                int rc = advance_graph(c, k, dt, contact, true, output_last && k == nsteps);
                 if (rc) return rc;
                 nsteps -= k;
                 if (c->steps_since_reorder >= every && (rc = reorder(c))) return rc;
@@ -912,18 +921,19 @@ int advance_graph(mpm_ctx* c, int nsteps, double dt, int contact, bool between_r
         }
     }
     int s = 0;
-    // launches the remaining steps one by one, the contact detection on the last
+    // launches the remaining steps one by one, the last as the output step
     auto plain = [&]() -> int {
         for (; s < nsteps; ++s)
-            if (int rc = step(c, dt, contact, false, detect_last && s == nsteps - 1)) return rc;
+            if (int rc = step(c, dt, contact, false, output_last && s == nsteps - 1)) return rc;
         return MPM_OK;
     };
-    while (s < nsteps && (!c->keys_valid || !c->have_alist)) {
-        if (int rc = step(c, dt, contact, false, detect_last && s == nsteps - 1)) return rc;
+    while (s < nsteps && (!c->keys_valid || !c->have_alist || c->grid_dirty)) {
+        if (int rc = step(c, dt, contact, false, output_last && s == nsteps - 1)) return rc;
         ++s;
     }
-    // the graph's steps skip the contact detection; the last step then runs plainly with it
-    const int tail = (contact && detect_last) ? 1 : 0;
+    // the graph's steps are not output steps (no contact detection, node values zeroed after use); the last
+    // step then runs plainly as the output step
+    const int tail = output_last ? 1 : 0;
     const bool can = c->use_graph && !c->profile && c->stream != nullptr && c->n > 0 && nsteps - tail - s >= 2;
     if (!can) return plain();
     if (c->gexec && (c->g_dt != dt || c->g_contact != contact)) graph_reset(c);
@@ -1434,6 +1444,7 @@ int mpm_upload_nodes(mpm_ctx* c, const mpm_nodes* nd) {
     CK(cudaStreamSynchronize(c->stream));
     c->have_nodes = true;
     c->have_alist = false;
+    c->grid_dirty = true;
     return MPM_OK;
 }
 
@@ -1763,7 +1774,7 @@ int mpm_autotune(mpm_ctx* c, int32_t steps, double dt, int contact, mpm_tune_res
         for (int i = 0; i < 6; ++i) *opt[i] = best[i];
         *opt[i0] = v0;
         *opt[i1] = v1;
-        int r = step(c, dt, contact, false, false);  // the run's steps: without the output-only detection
+        int r = step(c, dt, contact, false, false);  // the run's steps: not output steps
         if (r == MPM_OK) {
             cudaEventRecord(a, c->stream);
             for (int s = 0; s < steps && r == MPM_OK; ++s) r = step(c, dt, contact, false, false);
@@ -1784,6 +1795,7 @@ int mpm_autotune(mpm_ctx* c, int32_t steps, double dt, int contact, mpm_tune_res
         if (copy_all(false) != MPM_OK && r == MPM_OK) r = MPM_ERR_CUDA;
         c->keys_valid = false;  // positions restored: keys are recomputed next step
         c->have_alist = false;
+        c->grid_dirty = true;
         c->sim = sim0;
         return r;
     };

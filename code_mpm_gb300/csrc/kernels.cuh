@@ -894,10 +894,13 @@ __global__ void k_node_phase_a(NView<T> nd, T dt, double damping, int contact, i
 // The node work between pass 1 and pass 2: the remap v += q/m, displacement
 // control and BC in the path's order, then the record p/m and v.  The claims
 // are cleared after this last use (every claimed node is active: platen
-// particles take part in P2G).
+// particles take part in P2G).  clean: a step whose node values nobody sees
+// (not the last of an advance; pass 2 reads only the records) leaves the node
+// zeroed as the next step's grid reset would (ResetGrid, …MPLocks.cpp:4-22),
+// so that step needs no reset pass.
 template <typename T>
 __global__ void k_node_phase_b(NView<T> nd, int contact, const unsigned* __restrict__ dclist, int ndc,
-                               const T* __restrict__ pvel, long long np, T mass_min) {
+                               const T* __restrict__ pvel, long long np, T mass_min, int clean) {
     NODE_LOOP(nd, i) {
         if (!(nd.state[i] & 1u)) continue;
         node_remap<T>(nd, i, mass_min);
@@ -909,6 +912,19 @@ __global__ void k_node_phase_b(NView<T> nd, int contact, const unsigned* __restr
             if (ndc) node_dc<T>(nd, i, dclist, pvel, np, true);
         }
         node_ratio<T>(nd, i, nd.mom, mass_min, 0, 1);
+        if (clean) {
+            const long long nn = nd.nn;
+            const unsigned st = nd.state[i];
+            nd.mass[i] = (T)0;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                nd.vel[c * nn + i] = (T)0;
+                nd.mom[c * nn + i] = (T)0;
+                nd.force[c * nn + i] = (T)0;
+            }
+            if (nd.fixed[i] & 2u) nd.ftemp[nn + i] = (T)0;  // the only reaction-force entry a step writes
+            nd.state[i] = contact ? 0u : (st & ~1u);
+        }
     }
 }
 
@@ -937,6 +953,10 @@ struct StepArgs {
     float* hv_rows;
     unsigned* hv_count;
     long long hv_cap;
+    // 1: also write the step's output-only particle field (the contact path's
+    // strain rate, …_Contact.cpp:509, which no later step reads), as on the
+    // last step of an advance
+    int outputs;
 };
 
 // Apply a constitutive increment o to particle p (stress, plastic strain,
@@ -1029,7 +1049,7 @@ __device__ __forceinline__ void pass2_prefetch(const PView<T>& P, long long p0, 
         comp = t - 24;
     } else if (t == 30) {
         base = P.vol0;
-    } else if (t == 31) {
+    } else if (t == 31 && !contact) {  // the contact path writes V before reading it
         base = P.vol;
     } else if (t == 32) {
         base = P.backstress;
@@ -1209,8 +1229,10 @@ __global__ void __launch_bounds__(512) k_pass2(PView<T> P, NView<T> nd, Geom g, 
                 for (int k = 0; k < 6; ++k) P.strain[k * np + p] += e[k];
             } else {
                 V = P.vol[p];
+                if (a.outputs) {
 #pragma unroll
-                for (int k = 0; k < 6; ++k) P.strain_rate[k * np + p] = e[k] / dt;
+                    for (int k = 0; k < 6; ++k) P.strain_rate[k * np + p] = e[k] / dt;
+                }
             }
             if (queued) {
                 if constexpr (sizeof(T) == 4) {

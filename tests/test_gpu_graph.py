@@ -28,10 +28,10 @@ def test_graph_replay_keeps_plain_parity(golden, name, contact):
     ref = golden(f"{name}_ref25")
     g, lg = run(st, 25, contact, engine.FORM_FP64, 1)
     p, lp = run(st, 25, contact, engine.FORM_FP64, 0)
-    # the graph also runs the two clock kernels of each replayed step: 24 of the 25 (the first one is plain), 22 on
-    # the contact path, whose last step runs plainly with the contact detection (and so does the one before it,
-    # which the two-step graph cannot take alone)
-    assert lg - lp == 2 * (22 if contact else 24)
+    # the graph also runs the two clock kernels of each replayed step: 22 of the 25 (the first step runs plainly,
+    # and so does the last, the output step with the contact detection and the node values the caller sees, and
+    # the one before it, which the two-step graph cannot take alone)
+    assert lg - lp == 2 * 22
     for out in (g, p):
         for k in ("pos", "vel", "stress", "F", "g_vel", "g_mom"):
             scale = np.abs(ref[k]).max()
