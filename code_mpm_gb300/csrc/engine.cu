@@ -298,6 +298,25 @@ int prof_resolve(mpm_ctx* c) {
         kernel<<<(grid), (block), (smem), c->stream>>>(__VA_ARGS__);       \
     } while (0)
 
+// A cell-run kernel template <T, corners per thread, block size> launched for
+// the runtime choice of both (1, 2 or 4 corners; 128, 256 or 512 threads).
+#define LAUNCH_CELLS(name, K, T, cpt, bs, grid, smem, ...)                                              \
+    do {                                                                                                \
+        if ((bs) == 128) {                                                                              \
+            if ((cpt) == 1) LAUNCH_SMEM(name, (K<T, 1, 128>), grid, 128, smem, __VA_ARGS__);            \
+            else if ((cpt) == 2) LAUNCH_SMEM(name, (K<T, 2, 128>), grid, 128, smem, __VA_ARGS__);       \
+            else LAUNCH_SMEM(name, (K<T, 4, 128>), grid, 128, smem, __VA_ARGS__);                       \
+        } else if ((bs) == 256) {                                                                       \
+            if ((cpt) == 1) LAUNCH_SMEM(name, (K<T, 1, 256>), grid, 256, smem, __VA_ARGS__);            \
+            else if ((cpt) == 2) LAUNCH_SMEM(name, (K<T, 2, 256>), grid, 256, smem, __VA_ARGS__);       \
+            else LAUNCH_SMEM(name, (K<T, 4, 256>), grid, 256, smem, __VA_ARGS__);                       \
+        } else {                                                                                        \
+            if ((cpt) == 1) LAUNCH_SMEM(name, (K<T, 1, 512>), grid, 512, smem, __VA_ARGS__);            \
+            else if ((cpt) == 2) LAUNCH_SMEM(name, (K<T, 2, 512>), grid, 512, smem, __VA_ARGS__);       \
+            else LAUNCH_SMEM(name, (K<T, 4, 512>), grid, 512, smem, __VA_ARGS__);                       \
+        }                                                                                               \
+    } while (0)
+
 // ---- host-side timeline (TimeLine::getVelocity, TimeLine.h:33-46) ----------
 void timeline_velocity(const mpm_ctx* c, double t, double out[3]) {
     out[0] = out[1] = out[2] = 0.0;
@@ -732,14 +751,9 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph, bool output) {
                    P.sid);
         }
         if (c->p2g_reduce >= 2) {  // shared-memory cell runs, 1 / 2 / 4 corners per thread
-            const unsigned gb = blocks_for(n, c->p2g_block);
-            const size_t sm = p2g_cells_smem<T>(c->p2g_block);
-            if (c->p2g_reduce == 2)
-                LAUNCH_SMEM("p2g", (k_p2g_cells<T, 1>), gb, c->p2g_block, sm, P, N, g, skeys, perm, n, mg_in_p2g, fp32);
-            else if (c->p2g_reduce == 3)
-                LAUNCH_SMEM("p2g", (k_p2g_cells<T, 2>), gb, c->p2g_block, sm, P, N, g, skeys, perm, n, mg_in_p2g, fp32);
-            else
-                LAUNCH_SMEM("p2g", (k_p2g_cells<T, 4>), gb, c->p2g_block, sm, P, N, g, skeys, perm, n, mg_in_p2g, fp32);
+            const int bs = c->p2g_block, cpt = 1 << (c->p2g_reduce - 2);
+            LAUNCH_CELLS("p2g", k_p2g_cells, T, cpt, bs, blocks_for(n, bs), p2g_cells_smem<T>(bs), P, N, g, skeys, perm,
+                         n, mg_in_p2g, fp32);
         }
         else if (c->p2g_reduce == 1)
             LAUNCH("p2g", (k_p2g<T, 1>), blocks_for(n, c->p2g_block), c->p2g_block, P, N, g, skeys, perm, n,
@@ -790,17 +804,8 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph, bool output) {
                c->floor_friction, (const unsigned*)c->dclist.p, c->ndc, (const T*)c->vel.p, n, mm);
         if (c->p2g_reduce >= 2) {  // the same reduction as P2G: shared-memory cell runs
             const int b1 = c->pass1_block;
-            const unsigned gb = blocks_for(n, b1);
-            const size_t sm = pass1_cells_smem<T>(b1);
-            if (c->pass1_corners == 1)
-                LAUNCH_SMEM("pass1_remap", (k_pass1_cells<T, 1>), gb, b1, sm, P, N, g, skeys, perm, n, (T)dt, mm,
-                            contact);
-            else if (c->pass1_corners == 2)
-                LAUNCH_SMEM("pass1_remap", (k_pass1_cells<T, 2>), gb, b1, sm, P, N, g, skeys, perm, n, (T)dt, mm,
-                            contact);
-            else
-                LAUNCH_SMEM("pass1_remap", (k_pass1_cells<T, 4>), gb, b1, sm, P, N, g, skeys, perm, n, (T)dt, mm,
-                            contact);
+            LAUNCH_CELLS("pass1_remap", k_pass1_cells, T, c->pass1_corners, b1, blocks_for(n, b1),
+                         pass1_cells_smem<T>(b1), P, N, g, skeys, perm, n, (T)dt, mm, contact);
         }
         else if (c->gather_batch)
             LAUNCH("pass1_remap", (k_pass1_remap<T, 1>), blocks_for(n), NTHREADS, P, N, g, skeys, perm, n, (T)dt, mm,
@@ -1013,6 +1018,20 @@ int alloc_particles(mpm_ctx* c, long long n) {
 // =============================================================================
 // C ABI
 // =============================================================================
+// The cell-run P2G stages up to 512 slots in shared memory (109 KB in FP64):
+// allow each instantiation its dynamic shared memory.
+template <typename T, int CPT, int BS>
+bool p2g_cells_attr() {
+    return cudaFuncSetAttribute(k_p2g_cells<T, CPT, BS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)p2g_cells_smem<T>(BS)) == cudaSuccess;
+}
+template <typename T>
+bool p2g_cells_attrs() {
+    return p2g_cells_attr<T, 1, 128>() && p2g_cells_attr<T, 2, 128>() && p2g_cells_attr<T, 4, 128>() &&
+           p2g_cells_attr<T, 1, 256>() && p2g_cells_attr<T, 2, 256>() && p2g_cells_attr<T, 4, 256>() &&
+           p2g_cells_attr<T, 1, 512>() && p2g_cells_attr<T, 2, 512>() && p2g_cells_attr<T, 4, 512>();
+}
+
 extern "C" {
 
 int mpm_device_info(char* name, int name_len, int* sm_count, int* cc_major, int* cc_minor) {
@@ -1067,15 +1086,7 @@ int mpm_create_batch(const mpm_grid_desc* grids, int32_t nspec, int form, mpm_ct
     cudaGetDevice(&c->device);
     cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
     if (c->sm_count <= 0) c->sm_count = 152;
-    // cell-centric P2G stages up to 512 slots in shared memory (109 KB in FP64)
-    const int smd = (int)p2g_cells_smem<double>(512), smf = (int)p2g_cells_smem<float>(512);
-    const cudaFuncAttribute dyn = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    if (cudaFuncSetAttribute(k_p2g_cells<double, 1>, dyn, smd) != cudaSuccess ||
-        cudaFuncSetAttribute(k_p2g_cells<double, 2>, dyn, smd) != cudaSuccess ||
-        cudaFuncSetAttribute(k_p2g_cells<double, 4>, dyn, smd) != cudaSuccess ||
-        cudaFuncSetAttribute(k_p2g_cells<float, 1>, dyn, smf) != cudaSuccess ||
-        cudaFuncSetAttribute(k_p2g_cells<float, 2>, dyn, smf) != cudaSuccess ||
-        cudaFuncSetAttribute(k_p2g_cells<float, 4>, dyn, smf) != cudaSuccess) {
+    if (!p2g_cells_attrs<double>() || !p2g_cells_attrs<float>()) {
         cudaGetLastError();
         delete c;
         return MPM_ERR_DEVICE;

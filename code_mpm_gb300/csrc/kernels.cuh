@@ -314,17 +314,20 @@ __host__ __device__ constexpr size_t p2g_cells_smem(int bs) {
 
 // CPT corners per phase-2 thread (1, 2 or 4): the corners sharing the
 // thread's x (CPT 4) or x and y (CPT 2) bases, so a particle's quantities are
-// read from shared memory 8 / CPT times instead of 8.
-template <typename T, int CPT>
-__global__ void __launch_bounds__(512) k_p2g_cells(PView<T> P, NView<T> nd, Geom g, const unsigned* __restrict__ skeys,
+// read from shared memory 8 / CPT times instead of 8.  BS, the block size, is
+// a compile-time constant so the shared-memory rows sit at fixed offsets from
+// one address.
+template <typename T, int CPT, int BS>
+__global__ void __launch_bounds__(BS) k_p2g_cells(PView<T> P, NView<T> nd, Geom g, const unsigned* __restrict__ skeys,
                                                    const unsigned* __restrict__ perm, long long n, int with_mg,
                                                    int mark_active) {
     static_assert(CPT == 1 || CPT == 2 || CPT == 4, "corners per thread");
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int bs = blockDim.x, t = threadIdx.x;
+    constexpr int bs = BS;
+    const int t = threadIdx.x;
     // 12 rows of bs + 1 (the odd stride puts the two nodes' values of an axis in different banks):
     // Nx0 Nx1 Ny0 Ny1 Nz0 Nz1 gx0 gx1 gy0 gy1 gz0 gz1
-    const int S = bs + 1;
+    constexpr int S = bs + 1;
     T* sw = reinterpret_cast<T*>(smem_raw);
     T* sq = sw + 12 * S;                           // 13 x bs: m, m v (3), -V sigma (6), f_ext (3)
     unsigned* skey = reinterpret_cast<unsigned*>(sq + 13 * bs);
@@ -722,14 +725,15 @@ __host__ __device__ constexpr size_t pass1_cells_smem(int bs) {
     return ((size_t)6 * (bs + 1) + (size_t)3 * bs) * sizeof(T) + (size_t)bs * 8 + (size_t)(bs + 1) * 4 + 64 * 4;
 }
 
-template <typename T, int CPT>
-__global__ void __launch_bounds__(512) k_pass1_cells(PView<T> P, NView<T> nd, Geom g,
+template <typename T, int CPT, int BS>
+__global__ void __launch_bounds__(BS) k_pass1_cells(PView<T> P, NView<T> nd, Geom g,
                                                      const unsigned* __restrict__ skeys,
                                                      const unsigned* __restrict__ perm, long long n, T dt,
                                                      T mass_min, int contact) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int bs = blockDim.x, t = threadIdx.x;
-    const int S = bs + 1;                    // odd row stride: the two nodes' values of an axis in different banks
+    constexpr int bs = BS;
+    const int t = threadIdx.x;
+    constexpr int S = bs + 1;                // odd row stride: the two nodes' values of an axis in different banks
     T* sn = reinterpret_cast<T*>(smem_raw);  // 6 x S: Nx0 Nx1 Ny0 Ny1 Nz0 Nz1
     T* smv = sn + 6 * S;                     // 3 x bs: m v
     unsigned* skey = reinterpret_cast<unsigned*>(smv + 3 * bs);
