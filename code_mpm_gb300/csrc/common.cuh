@@ -75,6 +75,35 @@ __device__ __forceinline__ long long corner_node(const Geom& g, const int b[3], 
     return g.node_off + (long long)nx + (long long)ny * g.nn[0] + (long long)nz * g.nn[0] * g.nn[1];
 }
 
+// A cell's corner nodes in a form the cell-run kernels stage per slot:
+// corner k = 4 ix + 2 iy + iz is node n0 + ix + iy sy + iz sz, in range when
+// bit k of mask is set (the same nodes corner_node gives).
+struct CellNodes {
+    long long n0, sz;
+    int sy;
+    unsigned mask;
+};
+
+__device__ __forceinline__ CellNodes cell_nodes(const Geom& g, const int b[3]) {
+    CellNodes c;
+    c.sy = g.nn[0];
+    c.sz = (long long)g.nn[0] * g.nn[1];
+    c.n0 = g.node_off + (long long)b[0] + (long long)b[1] * c.sy + (long long)b[2] * c.sz;
+    c.mask = 0u;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int nx = b[0] + ((k >> 2) & 1), ny = b[1] + ((k >> 1) & 1), nz = b[2] + (k & 1);
+        if (nx >= 0 && ny >= 0 && nz >= 0 && nx <= g.nn[0] - 1 && ny <= g.nn[1] - 1 && nz <= g.nn[2] - 1)
+            c.mask |= 1u << k;
+    }
+    return c;
+}
+
+// corner k's node (in range: bit k of c.mask)
+__device__ __forceinline__ long long cell_node(const CellNodes& c, int k) {
+    return c.n0 + ((k >> 2) & 1) + (long long)(((k >> 1) & 1) * c.sy) + ((k & 1) ? c.sz : 0ll);
+}
+
 // Specimen owning global node i (binary search over the node offsets).
 __device__ __forceinline__ const Geom& node_geom(const Geom& g, long long i) {
     if (g.nspec <= 1) return g;

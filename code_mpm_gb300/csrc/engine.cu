@@ -1018,18 +1018,19 @@ int alloc_particles(mpm_ctx* c, long long n) {
 // =============================================================================
 // C ABI
 // =============================================================================
-// The cell-run P2G stages up to 512 slots in shared memory (109 KB in FP64):
-// allow each instantiation its dynamic shared memory.
+// The cell-run kernels stage up to 512 slots in shared memory (P2G: 123 KB
+// in FP64, pass 1: 54 KB): allow each instantiation its dynamic shared memory.
 template <typename T, int CPT, int BS>
-bool p2g_cells_attr() {
-    return cudaFuncSetAttribute(k_p2g_cells<T, CPT, BS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)p2g_cells_smem<T>(BS)) == cudaSuccess;
+bool cells_attr() {
+    const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    return cudaFuncSetAttribute(k_p2g_cells<T, CPT, BS>, a, (int)p2g_cells_smem<T>(BS)) == cudaSuccess &&
+           cudaFuncSetAttribute(k_pass1_cells<T, CPT, BS>, a, (int)pass1_cells_smem<T>(BS)) == cudaSuccess;
 }
 template <typename T>
-bool p2g_cells_attrs() {
-    return p2g_cells_attr<T, 1, 128>() && p2g_cells_attr<T, 2, 128>() && p2g_cells_attr<T, 4, 128>() &&
-           p2g_cells_attr<T, 1, 256>() && p2g_cells_attr<T, 2, 256>() && p2g_cells_attr<T, 4, 256>() &&
-           p2g_cells_attr<T, 1, 512>() && p2g_cells_attr<T, 2, 512>() && p2g_cells_attr<T, 4, 512>();
+bool cells_attrs() {
+    return cells_attr<T, 1, 128>() && cells_attr<T, 2, 128>() && cells_attr<T, 4, 128>() &&
+           cells_attr<T, 1, 256>() && cells_attr<T, 2, 256>() && cells_attr<T, 4, 256>() &&
+           cells_attr<T, 1, 512>() && cells_attr<T, 2, 512>() && cells_attr<T, 4, 512>();
 }
 
 extern "C" {
@@ -1086,7 +1087,7 @@ int mpm_create_batch(const mpm_grid_desc* grids, int32_t nspec, int form, mpm_ct
     cudaGetDevice(&c->device);
     cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
     if (c->sm_count <= 0) c->sm_count = 152;
-    if (!p2g_cells_attrs<double>() || !p2g_cells_attrs<float>()) {
+    if (!cells_attrs<double>() || !cells_attrs<float>()) {
         cudaGetLastError();
         delete c;
         return MPM_ERR_DEVICE;

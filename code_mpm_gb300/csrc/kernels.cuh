@@ -274,7 +274,8 @@ __global__ void __launch_bounds__(512) k_p2g(PView<T> P, NView<T> nd, Geom g, co
 // per-particle arithmetic as k_p2g; the cross-lane shuffles of REDUCE = 1
 // become shared-memory reads, and the atomics are issued by full warps.
 // Shared memory: (12 + 13) values per slot (the 12 base rows padded to an odd
-// stride) plus the keys, particle indices and run starts (p2g_cells_smem).
+// stride) plus each slot's cell nodes and key, and the run starts
+// (p2g_cells_smem); phase 2 takes the run's nodes from its first slot.
 // ---------------------------------------------------------------------------
 // Runs of equal cell keys among the block's first nslots slots (keys staged
 // in shared memory, a __syncthreads after the staging): run r covers slots
@@ -307,10 +308,47 @@ __device__ __forceinline__ int block_runs(const unsigned* skey, int nslots, int*
     return R;
 }
 
+// Per slot, beside the values: the cell's nodes (n0, sz, sy, mask: 24 bytes)
+// and the key; then the run starts (bs + 1) and the warp counts.
+constexpr size_t CELL_SLOT_BYTES = 28;
+
 template <typename T>
 __host__ __device__ constexpr size_t p2g_cells_smem(int bs) {
-    return ((size_t)12 * (bs + 1) + (size_t)13 * bs) * sizeof(T) + (size_t)bs * 8 + (size_t)(bs + 1) * 4 + 64 * 4;
+    return ((size_t)12 * (bs + 1) + (size_t)13 * bs) * sizeof(T) + (size_t)bs * CELL_SLOT_BYTES +
+           (size_t)(bs + 1) * 4 + 64 * 4;
 }
+
+// The slot arrays that follow the values (8-byte aligned: even bs).
+struct CellSlots {
+    long long *n0, *sz;
+    int* sy;
+    unsigned *mask, *key;
+    int *run_start, *wsum;
+    __device__ __forceinline__ CellSlots(unsigned char* at, int bs) {
+        n0 = reinterpret_cast<long long*>(at);
+        sz = n0 + bs;
+        sy = reinterpret_cast<int*>(sz + bs);
+        mask = reinterpret_cast<unsigned*>(sy + bs);
+        key = mask + bs;
+        run_start = reinterpret_cast<int*>(key + bs);  // bs + 1
+        wsum = run_start + bs + 1;                     // 32 warp counts + total
+    }
+    __device__ __forceinline__ void put(int t, const CellNodes& c) {
+        n0[t] = c.n0;
+        sz[t] = c.sz;
+        sy[t] = c.sy;
+        mask[t] = c.mask;
+    }
+    // corner k's node of the cell staged at slot a, or -1 out of range
+    __device__ __forceinline__ long long node(int a, int k) const {
+        if (!((mask[a] >> k) & 1u)) return -1;
+        CellNodes c;
+        c.n0 = n0[a];
+        c.sz = sz[a];
+        c.sy = sy[a];
+        return cell_node(c, k);
+    }
+};
 
 // CPT corners per phase-2 thread (1, 2 or 4): the corners sharing the
 // thread's x (CPT 4) or x and y (CPT 2) bases, so a particle's quantities are
@@ -330,10 +368,8 @@ __global__ void __launch_bounds__(BS) k_p2g_cells(PView<T> P, NView<T> nd, Geom 
     constexpr int S = bs + 1;
     T* sw = reinterpret_cast<T*>(smem_raw);
     T* sq = sw + 12 * S;                           // 13 x bs: m, m v (3), -V sigma (6), f_ext (3)
-    unsigned* skey = reinterpret_cast<unsigned*>(sq + 13 * bs);
-    unsigned* sperm = skey + bs;
-    int* run_start = reinterpret_cast<int*>(sperm + bs);  // bs + 1
-    int* wsum = run_start + bs + 1;                        // 32 warp counts + total
+    CellSlots cs(reinterpret_cast<unsigned char*>(sq + 13 * bs), bs);
+    unsigned* skey = cs.key;
     const long long s = blockIdx.x * (long long)bs + t;
     const unsigned key = (s < n) ? skeys[s] : 0xffffffffu;
     const bool valid = key < g.key_max;
@@ -366,15 +402,15 @@ __global__ void __launch_bounds__(BS) k_p2g_cells(PView<T> P, NView<T> nd, Geom 
         }
 #pragma unroll
         for (int c = 0; c < 6; ++c) sq[(4 + c) * bs + t] = -V * P.stress[c * np + p];
-        sperm[t] = (unsigned)p;
+        cs.put(t, cell_nodes(gs, b));
     }
     skey[t] = key;
     __syncthreads();
-    const int R = block_runs(skey, (int)min((long long)bs, n - blockIdx.x * (long long)bs), run_start, wsum);
+    const int R = block_runs(skey, (int)min((long long)bs, n - blockIdx.x * (long long)bs), cs.run_start, cs.wsum);
     constexpr int TPR = 8 / CPT;  // threads per run
     for (int item = t; item < R * TPR; item += bs) {
         const int r = item / TPR, k0 = (item % TPR) * CPT;  // corners k0 .. k0 + CPT - 1
-        const int a = run_start[r], e = run_start[r + 1];
+        const int a = cs.run_start[r], e = cs.run_start[r + 1];
         if (!(skey[a] < g.key_max)) continue;  // slots outside the grid
         T am[CPT], ap0[CPT], ap1[CPT], ap2[CPT], af0[CPT], af1[CPT], af2[CPT], g0[CPT], g1[CPT], g2[CPT];
 #pragma unroll
@@ -407,12 +443,9 @@ __global__ void __launch_bounds__(BS) k_p2g_cells(PView<T> P, NView<T> nd, Geom 
                 }
             }
         }
-        const Geom& gs = spec_geom(g, P.sid, sperm[a]);
-        int b[3];
-        key_to_base(skey[a], gs, b);
 #pragma unroll
         for (int j = 0; j < CPT; ++j) {
-            const long long nid = corner_node(gs, b, k0 + j);
+            const long long nid = cs.node(a, k0 + j);
             if (nid < 0) continue;
             // active nodes: the in-range corners of occupied cells (b_Active, …MPLocks.cpp:36)
             if (mark_active && !(nd.state[nid] & 1u)) atomicOr(&nd.state[nid], 1u);
@@ -722,7 +755,8 @@ __global__ void __launch_bounds__(256) k_pass1_remap(PView<T> P, NView<T> nd, Ge
 // ---------------------------------------------------------------------------
 template <typename T>
 __host__ __device__ constexpr size_t pass1_cells_smem(int bs) {
-    return ((size_t)6 * (bs + 1) + (size_t)3 * bs) * sizeof(T) + (size_t)bs * 8 + (size_t)(bs + 1) * 4 + 64 * 4;
+    return ((size_t)6 * (bs + 1) + (size_t)3 * bs) * sizeof(T) + (size_t)bs * CELL_SLOT_BYTES + (size_t)(bs + 1) * 4 +
+           64 * 4;
 }
 
 template <typename T, int CPT, int BS>
@@ -736,38 +770,45 @@ __global__ void __launch_bounds__(BS) k_pass1_cells(PView<T> P, NView<T> nd, Geo
     constexpr int S = bs + 1;                // odd row stride: the two nodes' values of an axis in different banks
     T* sn = reinterpret_cast<T*>(smem_raw);  // 6 x S: Nx0 Nx1 Ny0 Ny1 Nz0 Nz1
     T* smv = sn + 6 * S;                     // 3 x bs: m v
-    unsigned* skey = reinterpret_cast<unsigned*>(smv + 3 * bs);
-    unsigned* sperm = skey + bs;
-    int* run_start = reinterpret_cast<int*>(sperm + bs);
-    int* wsum = run_start + bs + 1;
+    CellSlots cs(reinterpret_cast<unsigned char*>(smv + 3 * bs), bs);
+    unsigned* skey = cs.key;
     const long long s = blockIdx.x * (long long)bs + t;
     const unsigned key = (s < n) ? skeys[s] : 0xffffffffu;
     const bool key_ok = key < g.key_max;
     const long long np = P.n, nn = nd.nn;
     if (key_ok) {
         const long long p = perm ? perm[s] : s;
-        sperm[t] = (unsigned)p;
+        const Geom& gs = spec_geom(g, P.sid, p);
+        int b[3];
+        key_to_base(key, gs, b);
+        const CellNodes cn = cell_nodes(gs, b);
+        cs.put(t, cn);
         const bool valid = !(contact && (P.pflags[p] & 8u));
         T N6[6] = {0, 0, 0, 0, 0, 0}, mv[3] = {0, 0, 0};
         if (valid) {
-            const Geom& gs = spec_geom(g, P.sid, p);
-            int b[3];
-            key_to_base(key, gs, b);
             Bases<T> B;
             particle_bases<T>(P, gs, p, b, B);
             const T m = P.mass[p];
             T v[3] = {P.vel[p], P.vel[np + p], P.vel[2 * np + p]};
+            // four corners' records requested before any is used; summed in corner order
 #pragma unroll 1
-            for (int k = 0; k < 8; ++k) {
-                const long long nid = corner_node(gs, b, k);
-                if (nid < 0) continue;
-                const Quad<T> r = ld_quad(nd.rec + 8 * nid);
-                if (!(r.w != (T)0)) continue;
-                T N, G[3];
-                B.corner(k, N, G);
-                v[0] = v[0] + N * r.x * dt;
-                v[1] = v[1] + N * r.y * dt;
-                v[2] = v[2] + N * r.z * dt;
+            for (int h = 0; h < 2; ++h) {
+                Quad<T> rq[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int k = 4 * h + j;
+                    const Quad<T> z{(T)0, (T)0, (T)0, (T)0};
+                    rq[j] = ((cn.mask >> k) & 1u) ? ld_quad(nd.rec + 8 * cell_node(cn, k)) : z;
+                }
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    if (!(rq[j].w != (T)0)) continue;
+                    T N, G[3];
+                    B.corner(4 * h + j, N, G);
+                    v[0] = v[0] + N * rq[j].x * dt;
+                    v[1] = v[1] + N * rq[j].y * dt;
+                    v[2] = v[2] + N * rq[j].z * dt;
+                }
             }
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
@@ -788,11 +829,11 @@ __global__ void __launch_bounds__(BS) k_pass1_cells(PView<T> P, NView<T> nd, Geo
     }
     skey[t] = key;
     __syncthreads();
-    const int R = block_runs(skey, (int)min((long long)bs, n - blockIdx.x * (long long)bs), run_start, wsum);
+    const int R = block_runs(skey, (int)min((long long)bs, n - blockIdx.x * (long long)bs), cs.run_start, cs.wsum);
     constexpr int TPR = 8 / CPT;  // threads per run; each sums CPT corners sharing its x (and y) bases
     for (int item = t; item < R * TPR; item += bs) {
         const int r = item / TPR, k0 = (item % TPR) * CPT;
-        const int a = run_start[r], e = run_start[r + 1];
+        const int a = cs.run_start[r], e = cs.run_start[r + 1];
         if (!(skey[a] < g.key_max)) continue;  // slots outside the grid
         T q0[CPT], q1[CPT], q2[CPT];
 #pragma unroll
@@ -809,12 +850,9 @@ __global__ void __launch_bounds__(BS) k_pass1_cells(PView<T> P, NView<T> nd, Geo
                 q2[j] += N * mv2;
             }
         }
-        const Geom& gs = spec_geom(g, P.sid, sperm[a]);
-        int b[3];
-        key_to_base(skey[a], gs, b);
 #pragma unroll
         for (int j = 0; j < CPT; ++j) {
-            const long long nid = corner_node(gs, b, k0 + j);
+            const long long nid = cs.node(a, k0 + j);
             if (nid < 0) continue;
             atomicAdd(&nd.q[nid], q0[j]);
             atomicAdd(&nd.q[nn + nid], q1[j]);
