@@ -52,8 +52,9 @@ struct mpm_ctx {
     // options
     int floor_friction = 0;
     int profile = 0;
-    int p2g_reduce = 2, p2g_block = 128, pass_block = 128, gather_batch = 0;
-    int pass1_corners = 1, pass1_block = 128;  // cell-run pass 1 (P2G modes 2-4)
+    // defaults: the autotuner's choice on the 256-specimen honeycomb batch
+    int p2g_reduce = 3, p2g_block = 128, pass_block = 256, gather_batch = 0;
+    int pass1_corners = 2, pass1_block = 128;  // cell-run pass 1 (P2G modes 2-4)
     // simulation scalars
     mpm_sim sim{0.0, 1.0e-3, 0.0, 0.0, 10.0, 0};
     // counts

@@ -70,13 +70,13 @@ extern "C" {
 /* Options for mpm_set_option. */
 #define MPM_OPT_FLOOR_FRICTION 1 /* contact path: Coulomb friction on x/y of z-fixed nodes (extension; default 0) */
 #define MPM_OPT_PROFILE 2        /* 1: time every kernel with CUDA events (default 0) */
-#define MPM_OPT_P2G_REDUCE 3     /* P2G: 0 = one atomic per particle, 1 = sum each cell's run across lanes first, 2 = stage the block in shared memory and sum each (cell, corner) in one thread, 3 / 4 = as 2 with each thread summing 2 / 4 corners of a cell */
+#define MPM_OPT_P2G_REDUCE 3     /* P2G: 0 = one atomic per particle, 1 = sum each cell's run across lanes first, 2 = stage the block in shared memory and sum each (cell, corner) in one thread, 3 (default) / 4 = as 2 with each thread summing 2 / 4 corners of a cell */
 #define MPM_OPT_P2G_BLOCK 4      /* P2G threads per block (128, 256 or 512) */
-#define MPM_OPT_PASS_BLOCK 5     /* G2P pass-2 threads per block (128, 256 or 512) */
+#define MPM_OPT_PASS_BLOCK 5     /* G2P pass-2 threads per block (128, 256 (default) or 512) */
 #define MPM_OPT_GATHER 6         /* G2P node gathers: 0 = one corner at a time, 1 = several corners' loads issued together */
 #define MPM_OPT_GRAPH 7          /* 1 (default): mpm_advance replays a captured two-step CUDA graph in the steady state; 0: launch every kernel */
 #define MPM_OPT_REORDER 8        /* FP32 form: store particles in cell order after each particle upload (0, default), also every N steps (N > 0), or never (-1); results stay in the caller's order */
-#define MPM_OPT_PASS1_CORNERS 10 /* cell-run G2P pass 1 (P2G modes 2-4): corners per thread, 1 (default), 2 or 4 */
+#define MPM_OPT_PASS1_CORNERS 10 /* cell-run G2P pass 1 (P2G modes 2-4): corners per thread, 1, 2 (default) or 4 */
 #define MPM_OPT_PASS1_BLOCK 11   /* cell-run G2P pass 1: threads per block (128, 256 or 512) */
 #define MPM_OPT_CELL_SORT 9      /* FP32 form, P2G modes 2-4: 1 sorts the particles by cell every step; 0 (default) takes the storage order as it is (a cell whose particles are not adjacent is summed in several runs) and, with MPM_OPT_REORDER 0, restores the cell order every 256 steps */
 
