@@ -753,8 +753,12 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph, bool output) {
         }
         if (c->p2g_reduce >= 2) {  // shared-memory cell runs, 1 / 2 / 4 corners per thread
             const int bs = c->p2g_block, cpt = 1 << (c->p2g_reduce - 2);
-            LAUNCH_CELLS("p2g", k_p2g_cells, T, cpt, bs, blocks_for(n, bs), p2g_cells_smem<T>(bs), P, N, g, skeys, perm,
-                         n, mg_in_p2g, fp32);
+            if (mg_in_p2g)
+                LAUNCH_CELLS("p2g", k_p2g_cells_mg, T, cpt, bs, blocks_for(n, bs), p2g_cells_smem<T>(bs), P, N, g,
+                             skeys, perm, n, fp32);
+            else
+                LAUNCH_CELLS("p2g", k_p2g_cells, T, cpt, bs, blocks_for(n, bs), p2g_cells_smem<T>(bs), P, N, g, skeys,
+                             perm, n, fp32);
         }
         else if (c->p2g_reduce == 1)
             LAUNCH("p2g", (k_p2g<T, 1>), blocks_for(n, c->p2g_block), c->p2g_block, P, N, g, skeys, perm, n,
@@ -1025,6 +1029,7 @@ template <typename T, int CPT, int BS>
 bool cells_attr() {
     const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
     return cudaFuncSetAttribute(k_p2g_cells<T, CPT, BS>, a, (int)p2g_cells_smem<T>(BS)) == cudaSuccess &&
+           cudaFuncSetAttribute(k_p2g_cells_mg<T, CPT, BS>, a, (int)p2g_cells_smem<T>(BS)) == cudaSuccess &&
            cudaFuncSetAttribute(k_pass1_cells<T, CPT, BS>, a, (int)pass1_cells_smem<T>(BS)) == cudaSuccess;
 }
 template <typename T>

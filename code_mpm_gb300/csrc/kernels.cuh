@@ -355,10 +355,11 @@ struct CellSlots {
 // read from shared memory 8 / CPT times instead of 8.  BS, the block size, is
 // a compile-time constant so the shared-memory rows sit at fixed offsets from
 // one address.
-template <typename T, int CPT, int BS>
-__global__ void __launch_bounds__(BS) k_p2g_cells(PView<T> P, NView<T> nd, Geom g, const unsigned* __restrict__ skeys,
-                                                   const unsigned* __restrict__ perm, long long n, int with_mg,
-                                                   int mark_active) {
+// MG: also the contact path's node mass gradients (output steps only).
+template <typename T, int CPT, int BS, bool MG>
+__device__ __forceinline__ void p2g_cells_run(const PView<T>& P, const NView<T>& nd, const Geom& g,
+                                              const unsigned* __restrict__ skeys, const unsigned* __restrict__ perm,
+                                              long long n, int mark_active) {
     static_assert(CPT == 1 || CPT == 2 || CPT == 4, "corners per thread");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int bs = BS;
@@ -436,7 +437,7 @@ __global__ void __launch_bounds__(BS) k_p2g_cells(PView<T> P, NView<T> nd, Geom 
                 af0[j] += G0 * v0 + G1 * v3 + G2 * v5 + N * fe0;
                 af1[j] += G1 * v1 + G0 * v3 + G2 * v4 + N * fe1;
                 af2[j] += G2 * v2 + G0 * v5 + G1 * v4 + N * fe2;
-                if (with_mg) {
+                if constexpr (MG) {
                     g0[j] += G0 * m;
                     g1[j] += G1 * m;
                     g2[j] += G2 * m;
@@ -456,13 +457,26 @@ __global__ void __launch_bounds__(BS) k_p2g_cells(PView<T> P, NView<T> nd, Geom 
             atomicAdd(&nd.force[nid], af0[j]);
             atomicAdd(&nd.force[nn + nid], af1[j]);
             atomicAdd(&nd.force[2 * nn + nid], af2[j]);
-            if (with_mg) {
+            if constexpr (MG) {
                 atomicAdd(&nd.mg[nid], g0[j]);
                 atomicAdd(&nd.mg[nn + nid], g1[j]);
                 atomicAdd(&nd.mg[2 * nn + nid], g2[j]);
             }
         }
     }
+}
+
+template <typename T, int CPT, int BS>
+__global__ void __launch_bounds__(BS) k_p2g_cells(PView<T> P, NView<T> nd, Geom g, const unsigned* __restrict__ skeys,
+                                                   const unsigned* __restrict__ perm, long long n, int mark_active) {
+    p2g_cells_run<T, CPT, BS, false>(P, nd, g, skeys, perm, n, mark_active);
+}
+
+template <typename T, int CPT, int BS>
+__global__ void __launch_bounds__(BS) k_p2g_cells_mg(PView<T> P, NView<T> nd, Geom g,
+                                                      const unsigned* __restrict__ skeys,
+                                                      const unsigned* __restrict__ perm, long long n, int mark_active) {
+    p2g_cells_run<T, CPT, BS, true>(P, nd, g, skeys, perm, n, mark_active);
 }
 
 // ---------------------------------------------------------------------------
