@@ -224,6 +224,11 @@ __device__ __forceinline__ Quad<T> ld_quad(const T* __restrict__ p) {
 
 // The nodes a node kernel works on, grid-stride: the active-node list when
 // one is given, else every node.  The body may `continue`, not `return`.
+// Node state bits beside the caller's (1 active, 2 contact, 4 / 8 contact
+// flags): a displacement-control claim is set on the node (internal, cleared
+// with the claims in the same step).
+constexpr unsigned NODE_CLAIMED = 16u;
+
 #define NODE_LOOP(nd, i)                                                                        \
     for (long long t_ = blockIdx.x * (long long)blockDim.x + threadIdx.x,                        \
                    n_ = (nd).alist ? (long long)*(nd).acount : (nd).nn;                         \

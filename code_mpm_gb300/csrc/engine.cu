@@ -775,7 +775,7 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph, bool output) {
             if (!c->owner_clean) CK(cudaMemsetAsync(c->g_owner.p, 0, (size_t)3 * nn * 4, c->stream));
             c->owner_clean = false;  // claims in use until phase B clears them
             LAUNCH("dc_claim", k_dc_claim, blocks_for(c->ndc), NTHREADS, (const unsigned*)c->dclist.p, c->ndc, keys,
-                   (const uint8_t*)c->pflags.p, g, (unsigned*)c->g_owner.p, nn, contact, P.sid);
+                   (const uint8_t*)c->pflags.p, g, (unsigned*)c->g_owner.p, nn, contact, P.sid, (unsigned*)N.state);
         }
         if (detecting) {
             const unsigned* surf = (const unsigned*)c->surf.p;

@@ -7,12 +7,12 @@
 //   radix sort          particles ordered by cell key
 //   k_cell_ranges       active-node marking (b_Active, :36) + per-cell particle ranges
 //   k_p2g               M2G (:48-89): warp-segmented reduction, then one atomic per run
-//   k_dc_claim/apply    DisplacementControl (:143-174), last writer in list order
-//   k_grid_update       IntegrateGrid (:90-142; contact :242-277)
-//   k_node_ratio        f/m per node (the divisor of G2P pass 1)
+//   k_dc_claim          DisplacementControl (:143-174), last writer in list order
+//   k_node_phase_a      displacement control, IntegrateGrid (:90-142; contact :242-277),
+//                       f/m per node (the divisor of G2P pass 1)
 //   k_pass1_remap       G2P pass 1 (:489-510) fused with the velocity remap (:539-564)
-//   k_node_remap        v_i += (sum N m_p v_p) / m_i
-//   k_node_bc           BC reapply (:573-599)
+//   k_node_phase_b      v_i += (sum N m_p v_p) / m_i, displacement control, BC reapply
+//                       (:573-599), p/m and v per node
 //   k_pass2             G2P_P2_SmallStrain (:175-280; contact :438-525) fused with the
 //                       constitutive increment and the platen timeline (:766-789)
 //   k_contact_*         contact detection (…_Contact.cpp:152-237), bit-exact
@@ -34,7 +34,7 @@ __global__ void k_reset_grid(NView<T> nd, int contact) {
     NODE_LOOP(nd, i) {
         unsigned st = nd.state[i];
         if (!(st & 1u)) continue;
-        nd.state[i] = contact ? 0u : (st & ~1u);
+        nd.state[i] = contact ? 0u : (st & ~(1u | NODE_CLAIMED));
         nd.mass[i] = (T)0;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
@@ -484,11 +484,13 @@ __global__ void __launch_bounds__(BS) k_p2g_cells_mg(PView<T> P, NView<T> nd, Ge
 // The reference overwrites node velocity/momentum/force from each controlled
 // particle in list order, so a node shared by several keeps the last one's.
 // k_dc_claim records, per node and axis, the largest list position writing
-// it; k_dc_apply lets only that particle write.  contact: all three axes.
+// it, and marks the node (NODE_CLAIMED in its state word) so the node phases
+// read the claims of marked nodes only; node_dc lets only the claiming
+// particle write.  contact: all three axes.
 // ---------------------------------------------------------------------------
 static __global__ void k_dc_claim(const unsigned* __restrict__ dclist, int ndc, const unsigned* __restrict__ keys,
                            const uint8_t* __restrict__ pflags, Geom g, unsigned* __restrict__ owner, long long nn,
-                           int contact, const uint16_t* __restrict__ sid) {
+                           int contact, const uint16_t* __restrict__ sid, unsigned* __restrict__ state) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= ndc) return;
     unsigned p = dclist[k];
@@ -503,32 +505,7 @@ static __global__ void k_dc_claim(const unsigned* __restrict__ dclist, int ndc, 
         if (nid < 0) continue;
         for (int a = 0; a < 3; ++a)
             if (axes & (1u << a)) atomicMax(&owner[a * nn + nid], (unsigned)k + 1u);
-    }
-}
-
-template <typename T>
-__global__ void k_dc_apply(const unsigned* __restrict__ dclist, int ndc, const unsigned* __restrict__ keys,
-                           PView<T> P, NView<T> nd, Geom g, int contact) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= ndc) return;
-    unsigned p = dclist[k];
-    unsigned key = keys[p];
-    if (key >= g.key_max) return;
-    const Geom& gs = spec_geom(g, P.sid, p);
-    const long long nn = nd.nn, np = P.n;
-    unsigned axes = contact ? 7u : (P.pflags[p] & 7u);
-    int b[3];
-    key_to_base(key, gs, b);
-    for (int c8 = 0; c8 < 8; ++c8) {
-        long long nid = corner_node(gs, b, c8);
-        if (nid < 0) continue;
-        for (int a = 0; a < 3; ++a) {
-            if (!(axes & (1u << a)) || nd.owner[a * nn + nid] != (unsigned)k + 1u) continue;
-            T vp = P.vel[a * np + p];
-            nd.vel[a * nn + nid] = vp;
-            nd.mom[a * nn + nid] = nd.mass[nid] * vp;
-            nd.force[a * nn + nid] = (T)0;
-        }
+        if (axes && !(state[nid] & NODE_CLAIMED)) atomicOr(&state[nid], NODE_CLAIMED);
     }
 }
 
@@ -549,18 +526,13 @@ __device__ __forceinline__ void coulomb(T p_t, T& f_t, T fn, T mu, T dt) {
     f_t += ff;
 }
 
+// The update of one node's momentum p and force f in registers; zero[c]: the
+// axis is fixed (its velocity is zeroed too); ft_y: the y reaction force of a
+// y-fixed node.  friction is read only where a friction law applies.
 template <typename T>
-__device__ __forceinline__ void grid_update_node(const NView<T>& nd, long long i, T dt, double damping, int contact,
-                                                 int floor_friction) {
-    if (!(nd.state[i] & 1u)) return;
-    const long long nn = nd.nn;
-    T p[3], f[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        p[c] = nd.mom[c * nn + i];
-        f[c] = nd.force[c * nn + i];
-    }
-    const unsigned fx = nd.fixed[i];
+__device__ __forceinline__ void grid_update_regs(const NView<T>& nd, long long i, unsigned fx, T p[3], T f[3], T dt,
+                                                 double damping, int contact, int floor_friction, bool zero[3],
+                                                 T& ft_y) {
     if (damping != 0.0) {
         T pp = p[0] * p[0] + p[1] * p[1] + p[2] * p[2];
         if (sqrt(pp) > (T)1.0e-24) {
@@ -571,8 +543,8 @@ __device__ __forceinline__ void grid_update_node(const NView<T>& nd, long long i
             for (int c = 0; c < 3; ++c) f[c] = f[c] - sc * nrm[c];
         }
     }
-    bool zero[3] = {false, false, false};
-    T ft_y = 0;
+    zero[0] = zero[1] = zero[2] = false;
+    ft_y = 0;
     if (!contact) {
         if (fx & 1u) {
             T trial_y = p[1] + f[1] * dt;
@@ -615,57 +587,6 @@ __device__ __forceinline__ void grid_update_node(const NView<T>& nd, long long i
             }
         }
     }
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        nd.mom[c * nn + i] = p[c];
-        nd.force[c * nn + i] = f[c];
-        if (zero[c]) nd.vel[c * nn + i] = (T)0;
-    }
-    if (fx & 2u) nd.ftemp[nn + i] += ft_y;
-}
-
-template <typename T>
-__global__ void k_grid_update(NView<T> nd, T dt, double damping, int contact, int floor_friction) {
-    NODE_LOOP(nd, i) grid_update_node<T>(nd, i, dt, damping, contact, floor_friction);
-}
-
-// ratio = src / m for nodes with m > mass_min (else 0).  src = force before
-// pass 1 (the f_i/m_i of …MPLocks.cpp:508), momentum before pass 2 (:198).
-// Also clears the remap accumulator when asked.  mass_min is given in the
-// form's type (the FP32 form's is the threshold rounded down to float, which
-// compares every float mass exactly as the double threshold does).
-// The node's record (r, has, v) is written as one or two aligned vectors so
-// the particle passes gather one 32-byte (FP32) sector per corner.
-template <typename T>
-__device__ __forceinline__ void node_ratio(const NView<T>& nd, long long i, const T* __restrict__ src,
-                                           T mass_min, int clear_q, int with_vel) {
-    const long long nn = nd.nn;
-    if (!(nd.state[i] & 1u)) return;
-    T m = nd.mass[i];
-    bool has = m > mass_min;
-    Quad<T> r;
-    r.x = has ? src[i] / m : (T)0;
-    r.y = has ? src[nn + i] / m : (T)0;
-    r.z = has ? src[2 * nn + i] / m : (T)0;
-    r.w = has ? (T)1 : (T)0;
-    *reinterpret_cast<Quad<T>*>(nd.rec + 8 * i) = r;
-    if (with_vel) {
-        Quad<T> v;
-        v.x = nd.vel[i];
-        v.y = nd.vel[nn + i];
-        v.z = nd.vel[2 * nn + i];
-        v.w = (T)0;
-        *reinterpret_cast<Quad<T>*>(nd.rec + 8 * i + 4) = v;
-    }
-    if (clear_q) {
-#pragma unroll
-        for (int c = 0; c < 3; ++c) nd.q[c * nn + i] = (T)0;
-    }
-}
-
-template <typename T>
-__global__ void k_node_ratio(NView<T> nd, const T* __restrict__ src, T mass_min, int clear_q, int with_vel) {
-    NODE_LOOP(nd, i) node_ratio<T>(nd, i, src, mass_min, clear_q, with_vel);
 }
 
 // ---------------------------------------------------------------------------
@@ -875,102 +796,147 @@ __global__ void __launch_bounds__(BS) k_pass1_cells(PView<T> P, NView<T> nd, Geo
     }
 }
 
-// Remap finish: v_i += q_i / m_i on nodes with m_i > mass_min (:559-560).
+// Displacement control from the node's side: for each axis whose last-writer
+// claim (list position + 1, k_dc_claim) is set, the claiming platen particle's
+// velocity v, momentum m v and zero force.
 template <typename T>
-__device__ __forceinline__ void node_remap(const NView<T>& nd, long long i, T mass_min) {
-    if (!(nd.state[i] & 1u)) return;
-    const long long nn = nd.nn;
-    T m = nd.mass[i];
-    if (!(m > mass_min)) return;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) nd.vel[c * nn + i] += nd.q[c * nn + i] / m;
-}
-
-template <typename T>
-__global__ void k_node_remap(NView<T> nd, T mass_min) {
-    NODE_LOOP(nd, i) node_remap<T>(nd, i, mass_min);
-}
-
-// BC reapply (:573-599): zero the fixed components of v, p and f.
-template <typename T>
-__device__ __forceinline__ void node_bc(const NView<T>& nd, long long i) {
-    if (!(nd.state[i] & 1u)) return;
-    const long long nn = nd.nn;
-    unsigned fx = nd.fixed[i];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        if (fx & (1u << c)) {
-            nd.vel[c * nn + i] = (T)0;
-            nd.mom[c * nn + i] = (T)0;
-            nd.force[c * nn + i] = (T)0;
-        }
-    }
-}
-
-template <typename T>
-__global__ void k_node_bc(NView<T> nd) {
-    NODE_LOOP(nd, i) node_bc<T>(nd, i);
-}
-
-// Displacement control applied from the node's side: for each axis whose
-// last-writer claim (list position + 1, k_dc_claim) is set, the claiming
-// platen particle's velocity, as k_dc_apply writes it.
-template <typename T>
-__device__ __forceinline__ void node_dc(const NView<T>& nd, long long i, const unsigned* __restrict__ dclist,
-                                        const T* __restrict__ pvel, long long np, bool clear = false) {
-    const long long nn = nd.nn;
+__device__ __forceinline__ void node_dc_regs(const unsigned own[3], const unsigned* __restrict__ dclist,
+                                             const T* __restrict__ pvel, long long np, T m, T v[3], bool vset[3],
+                                             T p[3], bool fzero[3]) {
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        const unsigned k1 = nd.owner[a * nn + i];
-        if (!k1) continue;
-        if (clear) nd.owner[a * nn + i] = 0u;  // the claims' last use this step: clean for the next
-        const T vp = pvel[a * np + dclist[k1 - 1]];
-        nd.vel[a * nn + i] = vp;
-        nd.mom[a * nn + i] = nd.mass[i] * vp;
-        nd.force[a * nn + i] = (T)0;
+        if (!own[a]) continue;
+        const T vp = pvel[a * np + dclist[own[a] - 1]];
+        v[a] = vp;
+        vset[a] = true;
+        p[a] = m * vp;
+        fzero[a] = true;
     }
 }
 
-// The node work between P2G and pass 1, one pass over the active nodes:
-// displacement control (non-contact: before the update), the grid update,
-// displacement control (contact: after it), then the record f/m.
+// The node work between P2G and pass 1, one pass over the active nodes with
+// the node's values in registers: displacement control (non-contact: before
+// the update, …MPLocks.cpp:143-174), the grid update (IntegrateGrid, :90-142;
+// contact :242-277), displacement control (contact: after it), then the
+// record (f/m, m > m_min), the divisor of G2P pass 1 (:508).
 template <typename T>
-__global__ void k_node_phase_a(NView<T> nd, T dt, double damping, int contact, int floor_friction,
+__global__ void __launch_bounds__(256, 4) k_node_phase_a(NView<T> nd, T dt, double damping, int contact, int floor_friction,
                                const unsigned* __restrict__ dclist, int ndc, const T* __restrict__ pvel, long long np,
                                T mass_min) {
+    const long long nn = nd.nn;
     NODE_LOOP(nd, i) {
-        if (!(nd.state[i] & 1u)) continue;
-        if (!contact && ndc) node_dc<T>(nd, i, dclist, pvel, np);
-        grid_update_node<T>(nd, i, dt, damping, contact, floor_friction);
-        if (contact && ndc) node_dc<T>(nd, i, dclist, pvel, np);
-        node_ratio<T>(nd, i, nd.force, mass_min, 1, 0);
+        const unsigned st = nd.state[i];
+        if (!(st & 1u)) continue;
+        const T m = nd.mass[i];
+        T p[3], f[3], v[3] = {0, 0, 0};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            p[c] = nd.mom[c * nn + i];
+            f[c] = nd.force[c * nn + i];
+        }
+        const unsigned fx = nd.fixed[i];
+        unsigned own[3] = {0u, 0u, 0u};
+        if (ndc && (st & NODE_CLAIMED)) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) own[a] = nd.owner[a * nn + i];
+        }
+        bool vset[3] = {false, false, false}, fz[3] = {false, false, false};
+        if (!contact) node_dc_regs<T>(own, dclist, pvel, np, m, v, vset, p, fz);
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            if (fz[c]) f[c] = (T)0;
+        bool zero[3];
+        T ft_y;
+        grid_update_regs<T>(nd, i, fx, p, f, dt, damping, contact, floor_friction, zero, ft_y);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            if (zero[c]) {
+                v[c] = (T)0;
+                vset[c] = true;
+            }
+            fz[c] = false;
+        }
+        if (contact) {
+            node_dc_regs<T>(own, dclist, pvel, np, m, v, vset, p, fz);
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                if (fz[c]) f[c] = (T)0;
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            nd.mom[c * nn + i] = p[c];
+            nd.force[c * nn + i] = f[c];
+            if (vset[c]) nd.vel[c * nn + i] = v[c];
+        }
+        if (fx & 2u) nd.ftemp[nn + i] += ft_y;
+        const bool has = m > mass_min;
+        Quad<T> r;
+        r.x = has ? f[0] / m : (T)0;
+        r.y = has ? f[1] / m : (T)0;
+        r.z = has ? f[2] / m : (T)0;
+        r.w = has ? (T)1 : (T)0;
+        *reinterpret_cast<Quad<T>*>(nd.rec + 8 * i) = r;
     }
 }
 
-// The node work between pass 1 and pass 2: the remap v += q/m, displacement
-// control and BC in the path's order, then the record p/m and v.  The claims
-// are cleared after this last use (every claimed node is active: platen
-// particles take part in P2G).  clean: a step whose node values nobody sees
-// (not the last of an advance; pass 2 reads only the records) leaves the node
-// zeroed as the next step's grid reset would (ResetGrid, …MPLocks.cpp:4-22),
-// so that step needs no reset pass.
+// The node work between pass 1 and pass 2, in registers: the remap v += q/m
+// (:559-560; q is cleared here for the next step's pass 1), displacement
+// control and BC (:573-599) in the path's order, then the record (p/m,
+// m > m_min, v).  The claims are cleared after this last use (every claimed
+// node is active: platen particles take part in P2G).  clean: a step whose
+// node values nobody sees (not the last of an advance; pass 2 reads only the
+// records) leaves the node zeroed as the next step's grid reset would
+// (ResetGrid, …MPLocks.cpp:4-22), so that step needs no reset pass.
 template <typename T>
-__global__ void k_node_phase_b(NView<T> nd, int contact, const unsigned* __restrict__ dclist, int ndc,
+__global__ void __launch_bounds__(256, 4) k_node_phase_b(NView<T> nd, int contact, const unsigned* __restrict__ dclist, int ndc,
                                const T* __restrict__ pvel, long long np, T mass_min, int clean) {
+    const long long nn = nd.nn;
     NODE_LOOP(nd, i) {
-        if (!(nd.state[i] & 1u)) continue;
-        node_remap<T>(nd, i, mass_min);
-        if (!contact) {
-            if (ndc) node_dc<T>(nd, i, dclist, pvel, np, true);
-            node_bc<T>(nd, i);
-        } else {
-            node_bc<T>(nd, i);
-            if (ndc) node_dc<T>(nd, i, dclist, pvel, np, true);
+        const unsigned st = nd.state[i];
+        if (!(st & 1u)) continue;
+        const T m = nd.mass[i];
+        const bool has = m > mass_min;
+        T v[3], p[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            v[c] = nd.vel[c * nn + i];
+            p[c] = nd.mom[c * nn + i];
+            const T q = nd.q[c * nn + i];
+            if (has) v[c] = v[c] + q / m;
+            nd.q[c * nn + i] = (T)0;
         }
-        node_ratio<T>(nd, i, nd.mom, mass_min, 0, 1);
+        const unsigned fx = nd.fixed[i];
+        unsigned own[3] = {0u, 0u, 0u};
+        if (ndc && (st & NODE_CLAIMED)) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                own[a] = nd.owner[a * nn + i];
+                if (own[a]) nd.owner[a * nn + i] = 0u;  // the claims' last use this step: clean for the next
+            }
+        }
+        bool vset[3] = {false, false, false}, fz[3] = {false, false, false};
+        if (!contact) node_dc_regs<T>(own, dclist, pvel, np, m, v, vset, p, fz);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            if (fx & (1u << c)) {
+                v[c] = (T)0;
+                p[c] = (T)0;
+                fz[c] = true;
+            }
+        }
+        if (contact) node_dc_regs<T>(own, dclist, pvel, np, m, v, vset, p, fz);
+        Quad<T> r, vq;
+        r.x = has ? p[0] / m : (T)0;
+        r.y = has ? p[1] / m : (T)0;
+        r.z = has ? p[2] / m : (T)0;
+        r.w = has ? (T)1 : (T)0;
+        vq.x = v[0];
+        vq.y = v[1];
+        vq.z = v[2];
+        vq.w = (T)0;
+        *reinterpret_cast<Quad<T>*>(nd.rec + 8 * i) = r;
+        *reinterpret_cast<Quad<T>*>(nd.rec + 8 * i + 4) = vq;
         if (clean) {
-            const long long nn = nd.nn;
-            const unsigned st = nd.state[i];
             nd.mass[i] = (T)0;
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
@@ -978,8 +944,16 @@ __global__ void k_node_phase_b(NView<T> nd, int contact, const unsigned* __restr
                 nd.mom[c * nn + i] = (T)0;
                 nd.force[c * nn + i] = (T)0;
             }
-            if (nd.fixed[i] & 2u) nd.ftemp[nn + i] = (T)0;  // the only reaction-force entry a step writes
-            nd.state[i] = contact ? 0u : (st & ~1u);
+            if (fx & 2u) nd.ftemp[nn + i] = (T)0;  // the only reaction-force entry a step writes
+            nd.state[i] = contact ? 0u : (st & ~(1u | NODE_CLAIMED));
+        } else {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                nd.vel[c * nn + i] = v[c];
+                nd.mom[c * nn + i] = p[c];
+                if (fz[c]) nd.force[c * nn + i] = (T)0;
+            }
+            if (st & NODE_CLAIMED) nd.state[i] = st & ~NODE_CLAIMED;
         }
     }
 }
