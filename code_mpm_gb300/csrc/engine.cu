@@ -432,36 +432,50 @@ __global__ void k_compact_flag(const uint8_t* __restrict__ pflags, long long n, 
     if (take) list[base + __popc(m & ((1u << lane) - 1u))] = (unsigned)i;
 }
 // Active-node list: a block of CS_THREADS compacts a tile of CS_THREADS x
-// CS_ROUNDS consecutive nodes into shared memory in node order, then
-// reserves its range with one atomic (a counter shared by every warp would
-// serialise tens of thousands of atomics at one L2 address).
+// CS_ROUNDS consecutive nodes in node order and reserves its range with one
+// atomic (a counter shared by every warp would serialise tens of thousands of
+// atomics at one L2 address).  Each warp takes 32 x CS_ROUNDS consecutive
+// nodes, loads all its state words before counting (the loads overlap), and
+// writes its entries after the warps before it.
 constexpr int CS_THREADS = 256, CS_ROUNDS = 16;
 __global__ void __launch_bounds__(CS_THREADS) k_compact_state(const unsigned* __restrict__ state, long long n,
                                                               unsigned bit, unsigned* __restrict__ list,
                                                               unsigned* __restrict__ count) {
-    __shared__ unsigned buf[CS_THREADS * CS_ROUNDS];
-    __shared__ unsigned wcnt[CS_THREADS / 32];
-    __shared__ unsigned total, base;
+    __shared__ unsigned woff[CS_THREADS / 32];
+    __shared__ unsigned base;
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-    const long long tile = blockIdx.x * (long long)(CS_THREADS * CS_ROUNDS);
-    if (t == 0) total = 0;
-    __syncthreads();
+    const long long wbase = blockIdx.x * (long long)(CS_THREADS * CS_ROUNDS) + (long long)w * 32 * CS_ROUNDS;
+    unsigned v[CS_ROUNDS], m[CS_ROUNDS];
+#pragma unroll
     for (int r = 0; r < CS_ROUNDS; ++r) {
-        const long long i = tile + (long long)r * CS_THREADS + t;
-        const bool take = i < n && (state[i] & bit);
-        const unsigned m = __ballot_sync(0xffffffffu, take);
-        if (lane == 0) wcnt[w] = __popc(m);
-        __syncthreads();
-        unsigned off = total;
-        for (int k = 0; k < w; ++k) off += wcnt[k];
-        if (take) buf[off + __popc(m & ((1u << lane) - 1u))] = (unsigned)i;
-        __syncthreads();
-        if (t == CS_THREADS - 1) total = off + __popc(m);
-        __syncthreads();
+        const long long i = wbase + (long long)r * 32 + lane;
+        v[r] = i < n ? state[i] : 0u;
     }
-    if (t == 0) base = total ? atomicAdd(count, total) : 0u;
+    unsigned cnt = 0;
+#pragma unroll
+    for (int r = 0; r < CS_ROUNDS; ++r) {
+        m[r] = __ballot_sync(FULL_MASK, (v[r] & bit) != 0u);
+        cnt += __popc(m[r]);
+    }
+    if (lane == 0) woff[w] = cnt;
     __syncthreads();
-    for (unsigned k = t; k < total; k += CS_THREADS) list[base + k] = buf[k];
+    if (t == 0) {
+        unsigned total = 0;
+        for (int k = 0; k < CS_THREADS / 32; ++k) {
+            const unsigned c = woff[k];
+            woff[k] = total;
+            total += c;
+        }
+        base = total ? atomicAdd(count, total) : 0u;
+    }
+    __syncthreads();
+    unsigned off = base + woff[w];
+    const unsigned below = (1u << lane) - 1u;
+#pragma unroll
+    for (int r = 0; r < CS_ROUNDS; ++r) {
+        if (v[r] & bit) list[off + __popc(m[r] & below)] = (unsigned)(wbase + (long long)r * 32 + lane);
+        off += __popc(m[r]);
+    }
 }
 __global__ void k_clear_flag(uint8_t* __restrict__ pflags, long long n, uint8_t bits) {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -859,12 +873,20 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph, bool output) {
                                  (unsigned*)c->q_count.p, n};
             a.sg_acc = (SurrogateAcc*)c->sg_acc.p;
         }
-        if (c->gather_batch)
-            LAUNCH("pass2", (k_pass2<T, 1>), blocks_for(n, c->pass_block), c->pass_block, P, N, g,
-                   (unsigned*)c->keys_copy.p, keys_next, (const MatConst*)c->mats.p, c->nmat, a, err);
-        else
-            LAUNCH("pass2", (k_pass2<T, 0>), blocks_for(n, c->pass_block), c->pass_block, P, N, g,
-                   (unsigned*)c->keys_copy.p, keys_next, (const MatConst*)c->mats.p, c->nmat, a, err);
+        {
+            const unsigned pb = blocks_for(n, c->pass_block);
+            unsigned* kc = (unsigned*)c->keys_copy.p;
+            const MatConst* mats = (const MatConst*)c->mats.p;
+#define PASS2(B, S) LAUNCH("pass2", (k_pass2<T, B, S>), pb, S, P, N, g, kc, keys_next, mats, c->nmat, a, err)
+            if (c->pass_block == 128) {
+                if (c->gather_batch) PASS2(1, 128); else PASS2(0, 128);
+            } else if (c->pass_block == 256) {
+                if (c->gather_batch) PASS2(1, 256); else PASS2(0, 256);
+            } else {
+                if (c->gather_batch) PASS2(1, 512); else PASS2(0, 512);
+            }
+#undef PASS2
+        }
         if constexpr (sizeof(T) == 4) {
             if (use_net) {
                 int rq;

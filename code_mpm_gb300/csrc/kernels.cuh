@@ -1114,8 +1114,11 @@ __device__ __forceinline__ void pass2_prefetch(const PView<T>& P, long long p0, 
 // next step needs no separate key pass: `keys` is read (this step) and
 // rewritten (next step), `keys_next` receives the next step's sort input.
 // ---------------------------------------------------------------------------
-template <typename T, int BATCH>
-__global__ void __launch_bounds__(512) k_pass2(PView<T> P, NView<T> nd, Geom g, unsigned* __restrict__ keys,
+// BS: the block size; the FP32 form asks for 1280 / BS blocks per SM (48
+// registers: a few spill, and the extra resident warps hide more of the
+// gathers' latency).
+template <typename T, int BATCH, int BS>
+__global__ void __launch_bounds__(BS, sizeof(T) == 4 ? 1280 / BS : 1) k_pass2(PView<T> P, NView<T> nd, Geom g, unsigned* __restrict__ keys,
                                                unsigned* __restrict__ keys_next, const MatConst* __restrict__ mats,
                                                int nmat, StepArgs a, unsigned* err) {
     long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
