@@ -735,6 +735,8 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph, bool output) {
     // node kernels sweep the active-node list; the reset uses the previous step's
     const unsigned nodeblocks = (unsigned)std::min<long long>(blocks_for(nn), (long long)c->sm_count * 16);
     N.alist = c->have_alist ? (const unsigned*)c->alist.p : nullptr;
+    // after an upload the reset clears the uploaded active nodes only
+    const int vel_zero = c->have_alist ? 1 : 0;
     if (c->grid_dirty) {  // after a step that left its node values (or an upload); clean steps zero their own
         LAUNCH("reset_grid", k_reset_grid<T>, c->have_alist ? nodeblocks : blocks_for(nn), NTHREADS, N, contact);
         c->grid_dirty = false;
@@ -834,7 +836,7 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph, bool output) {
                    contact);
         // remap, displacement control and BC in the path's order, p/m and v: one pass
         LAUNCH("node_phase_b", k_node_phase_b<T>, nodeblocks, NTHREADS, N, contact, (const unsigned*)c->dclist.p,
-               c->ndc, (const T*)c->vel.p, n, mm, output ? 0 : 1);
+               c->ndc, (const T*)c->vel.p, n, mm, output ? 0 : 1, vel_zero);
         if (output) c->grid_dirty = true;  // the last step of an advance keeps its node values for the caller
         if (c->ndc > 0) c->owner_clean = true;
         StepArgs a;

@@ -889,23 +889,27 @@ __global__ void __launch_bounds__(256, 4) k_node_phase_a(NView<T> nd, T dt, doub
 // (ResetGrid, …MPLocks.cpp:4-22), so that step needs no reset pass.
 template <typename T>
 __global__ void __launch_bounds__(256, 4) k_node_phase_b(NView<T> nd, int contact, const unsigned* __restrict__ dclist, int ndc,
-                               const T* __restrict__ pvel, long long np, T mass_min, int clean) {
+                               const T* __restrict__ pvel, long long np, T mass_min, int clean, int vel_zero) {
     const long long nn = nd.nn;
     NODE_LOOP(nd, i) {
         const unsigned st = nd.state[i];
         if (!(st & 1u)) continue;
         const T m = nd.mass[i];
         const bool has = m > mass_min;
+        const unsigned fx = nd.fixed[i];
+        // vel_zero: the step began from a grid whose every nonzero node was in
+        // the last active list (not an upload), so a node's velocity is zero
+        // here unless phase A set it, which it does on fixed or claimed nodes only
+        const bool vel_set = !vel_zero || fx != 0u || (st & NODE_CLAIMED);
         T v[3], p[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            v[c] = nd.vel[c * nn + i];
+            v[c] = vel_set ? nd.vel[c * nn + i] : (T)0;
             p[c] = nd.mom[c * nn + i];
             const T q = nd.q[c * nn + i];
             if (has) v[c] = v[c] + q / m;
             nd.q[c * nn + i] = (T)0;
         }
-        const unsigned fx = nd.fixed[i];
         unsigned own[3] = {0u, 0u, 0u};
         if (ndc && (st & NODE_CLAIMED)) {
 #pragma unroll
@@ -940,7 +944,7 @@ __global__ void __launch_bounds__(256, 4) k_node_phase_b(NView<T> nd, int contac
             nd.mass[i] = (T)0;
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                nd.vel[c * nn + i] = (T)0;
+                if (vel_set) nd.vel[c * nn + i] = (T)0;
                 nd.mom[c * nn + i] = (T)0;
                 nd.force[c * nn + i] = (T)0;
             }
