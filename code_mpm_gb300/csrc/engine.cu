@@ -822,7 +822,7 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph, bool output) {
         const T mm = sizeof(T) == 4 ? (T)fps_float_threshold(c->sim.mass_min) : (T)c->sim.mass_min;
         // displacement control, grid update, displacement control, f/m: one pass over the active nodes
         LAUNCH("node_phase_a", k_node_phase_a<T>, nodeblocks, NTHREADS, N, (T)dt, c->sim.damping, contact,
-               c->floor_friction, (const unsigned*)c->dclist.p, c->ndc, (const T*)c->vel.p, n, mm);
+               c->floor_friction, (const unsigned*)c->dclist.p, c->ndc, (const T*)c->vel.p, n, mm, output ? 0 : 1);
         if (c->p2g_reduce >= 2) {  // the same reduction as P2G: shared-memory cell runs
             const int b1 = c->pass1_block;
             LAUNCH_CELLS("pass1_remap", k_pass1_cells, T, c->pass1_corners, b1, blocks_for(n, b1),

@@ -818,11 +818,14 @@ __device__ __forceinline__ void node_dc_regs(const unsigned own[3], const unsign
 // the node's values in registers: displacement control (non-contact: before
 // the update, …MPLocks.cpp:143-174), the grid update (IntegrateGrid, :90-142;
 // contact :242-277), displacement control (contact: after it), then the
-// record (f/m, m > m_min), the divisor of G2P pass 1 (:508).
+// record (f/m, m > m_min), the divisor of G2P pass 1 (:508).  The updated
+// momentum and the mass also go to the record's second half for phase B
+// (which overwrites it with p/m and v); clean (not an output step): the
+// node's mass, momentum and force are zeroed here, for the next step's P2G.
 template <typename T>
 __global__ void __launch_bounds__(256, 4) k_node_phase_a(NView<T> nd, T dt, double damping, int contact, int floor_friction,
                                const unsigned* __restrict__ dclist, int ndc, const T* __restrict__ pvel, long long np,
-                               T mass_min) {
+                               T mass_min, int clean) {
     const long long nn = nd.nn;
     NODE_LOOP(nd, i) {
         const unsigned st = nd.state[i];
@@ -862,20 +865,26 @@ __global__ void __launch_bounds__(256, 4) k_node_phase_a(NView<T> nd, T dt, doub
             for (int c = 0; c < 3; ++c)
                 if (fz[c]) f[c] = (T)0;
         }
+        if (clean) nd.mass[i] = (T)0;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            nd.mom[c * nn + i] = p[c];
-            nd.force[c * nn + i] = f[c];
+            nd.mom[c * nn + i] = clean ? (T)0 : p[c];
+            nd.force[c * nn + i] = clean ? (T)0 : f[c];
             if (vset[c]) nd.vel[c * nn + i] = v[c];
         }
         if (fx & 2u) nd.ftemp[nn + i] += ft_y;
         const bool has = m > mass_min;
-        Quad<T> r;
+        Quad<T> r, pm;
         r.x = has ? f[0] / m : (T)0;
         r.y = has ? f[1] / m : (T)0;
         r.z = has ? f[2] / m : (T)0;
         r.w = has ? (T)1 : (T)0;
+        pm.x = p[0];
+        pm.y = p[1];
+        pm.z = p[2];
+        pm.w = m;
         *reinterpret_cast<Quad<T>*>(nd.rec + 8 * i) = r;
+        *reinterpret_cast<Quad<T>*>(nd.rec + 8 * i + 4) = pm;
     }
 }
 
@@ -894,18 +903,18 @@ __global__ void __launch_bounds__(256, 4) k_node_phase_b(NView<T> nd, int contac
     NODE_LOOP(nd, i) {
         const unsigned st = nd.state[i];
         if (!(st & 1u)) continue;
-        const T m = nd.mass[i];
+        const Quad<T> pm = ld_quad(nd.rec + 8 * i + 4);  // phase A's momentum and mass
+        const T m = pm.w;
         const bool has = m > mass_min;
         const unsigned fx = nd.fixed[i];
         // vel_zero: the step began from a grid whose every nonzero node was in
         // the last active list (not an upload), so a node's velocity is zero
         // here unless phase A set it, which it does on fixed or claimed nodes only
         const bool vel_set = !vel_zero || fx != 0u || (st & NODE_CLAIMED);
-        T v[3], p[3];
+        T v[3], p[3] = {pm.x, pm.y, pm.z};
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             v[c] = vel_set ? nd.vel[c * nn + i] : (T)0;
-            p[c] = nd.mom[c * nn + i];
             const T q = nd.q[c * nn + i];
             if (has) v[c] = v[c] + q / m;
             nd.q[c * nn + i] = (T)0;
@@ -940,14 +949,10 @@ __global__ void __launch_bounds__(256, 4) k_node_phase_b(NView<T> nd, int contac
         vq.w = (T)0;
         *reinterpret_cast<Quad<T>*>(nd.rec + 8 * i) = r;
         *reinterpret_cast<Quad<T>*>(nd.rec + 8 * i + 4) = vq;
-        if (clean) {
-            nd.mass[i] = (T)0;
+        if (clean) {  // phase A zeroed mass, momentum and force
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
+            for (int c = 0; c < 3; ++c)
                 if (vel_set) nd.vel[c * nn + i] = (T)0;
-                nd.mom[c * nn + i] = (T)0;
-                nd.force[c * nn + i] = (T)0;
-            }
             if (fx & 2u) nd.ftemp[nn + i] = (T)0;  // the only reaction-force entry a step writes
             nd.state[i] = contact ? 0u : (st & ~(1u | NODE_CLAIMED));
         } else {
