@@ -955,14 +955,15 @@ int advance_graph(mpm_ctx* c, int nsteps, double dt, int contact, bool between_r
         }
     }
     int s = 0;
+    auto one = [&]() -> int { return step(c, dt, contact, false, output_last && s == nsteps - 1); };
     // launches the remaining steps one by one, the last as the output step
     auto plain = [&]() -> int {
         for (; s < nsteps; ++s)
-            if (int rc = step(c, dt, contact, false, output_last && s == nsteps - 1)) return rc;
+            if (int rc = one()) return rc;
         return MPM_OK;
     };
     while (s < nsteps && (!c->keys_valid || !c->have_alist || c->grid_dirty)) {
-        if (int rc = step(c, dt, contact, false, output_last && s == nsteps - 1)) return rc;
+        if (int rc = one()) return rc;
         ++s;
     }
     // the graph's steps are not output steps (no contact detection, node values zeroed after use); the last

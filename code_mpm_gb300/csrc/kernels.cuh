@@ -333,7 +333,7 @@ struct CellSlots {
         run_start = reinterpret_cast<int*>(key + bs);  // bs + 1
         wsum = run_start + bs + 1;                     // 32 warp counts + total
     }
-    __device__ __forceinline__ void put(int t, const CellNodes& c) {
+    __device__ __forceinline__ void put(int t, const CellNodes& c) const {
         n0[t] = c.n0;
         sz[t] = c.sz;
         sy[t] = c.sy;
@@ -355,33 +355,23 @@ struct CellSlots {
 // read from shared memory 8 / CPT times instead of 8.  BS, the block size, is
 // a compile-time constant so the shared-memory rows sit at fixed offsets from
 // one address.
-// MG: also the contact path's node mass gradients (output steps only).
-template <typename T, int CPT, int BS, bool MG>
-__device__ __forceinline__ void p2g_cells_run(const PView<T>& P, const NView<T>& nd, const Geom& g,
-                                              const unsigned* __restrict__ skeys, const unsigned* __restrict__ perm,
-                                              long long n, int mark_active) {
-    static_assert(CPT == 1 || CPT == 2 || CPT == 4, "corners per thread");
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    constexpr int bs = BS;
-    const int t = threadIdx.x;
-    // 12 rows of bs + 1 (the odd stride puts the two nodes' values of an axis in different banks):
-    // Nx0 Nx1 Ny0 Ny1 Nz0 Nz1 gx0 gx1 gy0 gy1 gz0 gz1
-    constexpr int S = bs + 1;
-    T* sw = reinterpret_cast<T*>(smem_raw);
-    T* sq = sw + 12 * S;                           // 13 x bs: m, m v (3), -V sigma (6), f_ext (3)
-    CellSlots cs(reinterpret_cast<unsigned char*>(sq + 13 * bs), bs);
-    unsigned* skey = cs.key;
-    const long long s = blockIdx.x * (long long)bs + t;
-    const unsigned key = (s < n) ? skeys[s] : 0xffffffffu;
-    const bool valid = key < g.key_max;
-    const long long np = P.n, nn = nd.nn;
-    if (valid) {
-        const long long p = perm ? perm[s] : s;
-        const Geom& gs = spec_geom(g, P.sid, p);
-        int b[3];
-        key_to_base(key, gs, b);
-        Bases<T> B;
-        particle_bases<T>(P, gs, p, b, B);
+// A cell-run P2G block of BS slots in shared memory: the per-axis bases (12
+// rows of BS + 1: the odd stride puts the two nodes' values of an axis in
+// different banks; Nx0 Nx1 Ny0 Ny1 Nz0 Nz1 gx0 gx1 gy0 gy1 gz0 gz1), the
+// transfer quantities (13 rows of BS: m, m v (3), -V sigma (6), f_ext (3)) and
+// the slots (cell nodes, key, runs).
+template <typename T, int BS>
+struct P2GBlock {
+    static constexpr int S = BS + 1;
+    T* sw;
+    T* sq;
+    CellSlots cs;
+    __device__ __forceinline__ explicit P2GBlock(unsigned char* raw)
+        : sw(reinterpret_cast<T*>(raw)), sq(sw + 12 * S), cs(reinterpret_cast<unsigned char*>(sq + 13 * BS), BS) {}
+
+    // slot t's particle: bases, mass m, volume V, velocity v, external force fe, stress sig, its cell's nodes
+    __device__ __forceinline__ void stage(int t, const Bases<T>& B, T m, T V, const T v[3], const T fe[3],
+                                          const T sig[6], const CellNodes& cn) const {
         sw[0 * S + t] = B.Nx[0];
         sw[1 * S + t] = B.Nx[1];
         sw[2 * S + t] = B.Ny[0];
@@ -394,76 +384,120 @@ __device__ __forceinline__ void p2g_cells_run(const PView<T>& P, const NView<T>&
         sw[9 * S + t] = B.gy[1];
         sw[10 * S + t] = B.gz[0];
         sw[11 * S + t] = B.gz[1];
-        const T m = P.mass[p], V = P.vol[p];
         sq[t] = m;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            sq[(1 + c) * bs + t] = m * P.vel[c * np + p];
-            sq[(10 + c) * bs + t] = P.fext[c * np + p];
+            sq[(1 + c) * BS + t] = m * v[c];
+            sq[(10 + c) * BS + t] = fe[c];
         }
 #pragma unroll
-        for (int c = 0; c < 6; ++c) sq[(4 + c) * bs + t] = -V * P.stress[c * np + p];
-        cs.put(t, cell_nodes(gs, b));
+        for (int c = 0; c < 6; ++c) sq[(4 + c) * BS + t] = -V * sig[c];
+        cs.put(t, cn);
     }
-    skey[t] = key;
-    __syncthreads();
-    const int R = block_runs(skey, (int)min((long long)bs, n - blockIdx.x * (long long)bs), cs.run_start, cs.wsum);
-    constexpr int TPR = 8 / CPT;  // threads per run
-    for (int item = t; item < R * TPR; item += bs) {
-        const int r = item / TPR, k0 = (item % TPR) * CPT;  // corners k0 .. k0 + CPT - 1
-        const int a = cs.run_start[r], e = cs.run_start[r + 1];
-        if (!(skey[a] < g.key_max)) continue;  // slots outside the grid
-        T am[CPT], ap0[CPT], ap1[CPT], ap2[CPT], af0[CPT], af1[CPT], af2[CPT], g0[CPT], g1[CPT], g2[CPT];
-#pragma unroll
-        for (int j = 0; j < CPT; ++j) am[j] = ap0[j] = ap1[j] = ap2[j] = af0[j] = af1[j] = af2[j] = g0[j] = g1[j] = g2[j] = 0;
-        for (int i = a; i < e; ++i) {
-            const T m = sq[i], mv0 = sq[1 * bs + i], mv1 = sq[2 * bs + i], mv2 = sq[3 * bs + i];
-            const T v0 = sq[4 * bs + i], v1 = sq[5 * bs + i], v2 = sq[6 * bs + i];
-            const T v3 = sq[7 * bs + i], v4 = sq[8 * bs + i], v5 = sq[9 * bs + i];
-            const T fe0 = sq[10 * bs + i], fe1 = sq[11 * bs + i], fe2 = sq[12 * bs + i];
-#pragma unroll
+
+    // After the staging and a __syncthreads (keys in cs.key for the first nslots
+    // slots, out of range where nothing was staged): one thread per (cell run,
+    // CPT corners) sums the run's contributions in slot order and issues one
+    // atomic per field; mark_active also marks the corners active.  MG: also the
+    // node mass gradients.
+    template <int CPT, bool MG>
+    __device__ __forceinline__ void scatter(const NView<T>& nd, const Geom& g, int nslots, int mark_active) const {
+        static_assert(CPT == 1 || CPT == 2 || CPT == 4, "corners per thread");
+        constexpr int bs = BS;
+        const int t = threadIdx.x;
+        const long long nn = nd.nn;
+        const unsigned* skey = cs.key;
+        const int R = block_runs(skey, nslots, cs.run_start, cs.wsum);
+        constexpr int TPR = 8 / CPT;  // threads per run
+        for (int item = t; item < R * TPR; item += bs) {
+            const int r = item / TPR, k0 = (item % TPR) * CPT;  // corners k0 .. k0 + CPT - 1
+            const int a = cs.run_start[r], e = cs.run_start[r + 1];
+            if (!(skey[a] < g.key_max)) continue;  // slots outside the grid
+            T am[CPT], ap0[CPT], ap1[CPT], ap2[CPT], af0[CPT], af1[CPT], af2[CPT], g0[CPT], g1[CPT], g2[CPT];
+    #pragma unroll
+            for (int j = 0; j < CPT; ++j) am[j] = ap0[j] = ap1[j] = ap2[j] = af0[j] = af1[j] = af2[j] = g0[j] = g1[j] = g2[j] = 0;
+            for (int i = a; i < e; ++i) {
+                const T m = sq[i], mv0 = sq[1 * bs + i], mv1 = sq[2 * bs + i], mv2 = sq[3 * bs + i];
+                const T v0 = sq[4 * bs + i], v1 = sq[5 * bs + i], v2 = sq[6 * bs + i];
+                const T v3 = sq[7 * bs + i], v4 = sq[8 * bs + i], v5 = sq[9 * bs + i];
+                const T fe0 = sq[10 * bs + i], fe1 = sq[11 * bs + i], fe2 = sq[12 * bs + i];
+    #pragma unroll
+                for (int j = 0; j < CPT; ++j) {
+                    const int k = k0 + j;
+                    const int ix = (k >> 2) & 1, iy = (k >> 1) & 1, iz = k & 1;
+                    const T nx = sw[ix * S + i], ny = sw[(2 + iy) * S + i], nz = sw[(4 + iz) * S + i];
+                    const T N = nx * ny * nz;
+                    const T G0 = -(ny * nz) * sw[(6 + ix) * S + i];
+                    const T G1 = -(nx * nz) * sw[(8 + iy) * S + i];
+                    const T G2 = -(nx * ny) * sw[(10 + iz) * S + i];
+                    am[j] += N * m;
+                    ap0[j] += N * mv0;
+                    ap1[j] += N * mv1;
+                    ap2[j] += N * mv2;
+                    af0[j] += G0 * v0 + G1 * v3 + G2 * v5 + N * fe0;
+                    af1[j] += G1 * v1 + G0 * v3 + G2 * v4 + N * fe1;
+                    af2[j] += G2 * v2 + G0 * v5 + G1 * v4 + N * fe2;
+                    if constexpr (MG) {
+                        g0[j] += G0 * m;
+                        g1[j] += G1 * m;
+                        g2[j] += G2 * m;
+                    }
+                }
+            }
+    #pragma unroll
             for (int j = 0; j < CPT; ++j) {
-                const int k = k0 + j;
-                const int ix = (k >> 2) & 1, iy = (k >> 1) & 1, iz = k & 1;
-                const T nx = sw[ix * S + i], ny = sw[(2 + iy) * S + i], nz = sw[(4 + iz) * S + i];
-                const T N = nx * ny * nz;
-                const T G0 = -(ny * nz) * sw[(6 + ix) * S + i];
-                const T G1 = -(nx * nz) * sw[(8 + iy) * S + i];
-                const T G2 = -(nx * ny) * sw[(10 + iz) * S + i];
-                am[j] += N * m;
-                ap0[j] += N * mv0;
-                ap1[j] += N * mv1;
-                ap2[j] += N * mv2;
-                af0[j] += G0 * v0 + G1 * v3 + G2 * v5 + N * fe0;
-                af1[j] += G1 * v1 + G0 * v3 + G2 * v4 + N * fe1;
-                af2[j] += G2 * v2 + G0 * v5 + G1 * v4 + N * fe2;
+                const long long nid = cs.node(a, k0 + j);
+                if (nid < 0) continue;
+                // active nodes: the in-range corners of occupied cells (b_Active, …MPLocks.cpp:36)
+                if (mark_active && !(nd.state[nid] & 1u)) atomicOr(&nd.state[nid], 1u);
+                atomicAdd(&nd.mass[nid], am[j]);
+                atomicAdd(&nd.mom[nid], ap0[j]);
+                atomicAdd(&nd.mom[nn + nid], ap1[j]);
+                atomicAdd(&nd.mom[2 * nn + nid], ap2[j]);
+                atomicAdd(&nd.force[nid], af0[j]);
+                atomicAdd(&nd.force[nn + nid], af1[j]);
+                atomicAdd(&nd.force[2 * nn + nid], af2[j]);
                 if constexpr (MG) {
-                    g0[j] += G0 * m;
-                    g1[j] += G1 * m;
-                    g2[j] += G2 * m;
+                    atomicAdd(&nd.mg[nid], g0[j]);
+                    atomicAdd(&nd.mg[nn + nid], g1[j]);
+                    atomicAdd(&nd.mg[2 * nn + nid], g2[j]);
                 }
             }
         }
-#pragma unroll
-        for (int j = 0; j < CPT; ++j) {
-            const long long nid = cs.node(a, k0 + j);
-            if (nid < 0) continue;
-            // active nodes: the in-range corners of occupied cells (b_Active, …MPLocks.cpp:36)
-            if (mark_active && !(nd.state[nid] & 1u)) atomicOr(&nd.state[nid], 1u);
-            atomicAdd(&nd.mass[nid], am[j]);
-            atomicAdd(&nd.mom[nid], ap0[j]);
-            atomicAdd(&nd.mom[nn + nid], ap1[j]);
-            atomicAdd(&nd.mom[2 * nn + nid], ap2[j]);
-            atomicAdd(&nd.force[nid], af0[j]);
-            atomicAdd(&nd.force[nn + nid], af1[j]);
-            atomicAdd(&nd.force[2 * nn + nid], af2[j]);
-            if constexpr (MG) {
-                atomicAdd(&nd.mg[nid], g0[j]);
-                atomicAdd(&nd.mg[nn + nid], g1[j]);
-                atomicAdd(&nd.mg[2 * nn + nid], g2[j]);
-            }
-        }
     }
+};
+
+// MG: also the contact path's node mass gradients (output steps only).
+template <typename T, int CPT, int BS, bool MG>
+__device__ __forceinline__ void p2g_cells_run(const PView<T>& P, const NView<T>& nd, const Geom& g,
+                                              const unsigned* __restrict__ skeys, const unsigned* __restrict__ perm,
+                                              long long n, int mark_active) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const P2GBlock<T, BS> blk(smem_raw);
+    const int t = threadIdx.x;
+    const long long s = blockIdx.x * (long long)BS + t;
+    const unsigned key = (s < n) ? skeys[s] : 0xffffffffu;
+    const long long np = P.n;
+    if (key < g.key_max) {
+        const long long p = perm ? perm[s] : s;
+        const Geom& gs = spec_geom(g, P.sid, p);
+        int b[3];
+        key_to_base(key, gs, b);
+        Bases<T> B;
+        particle_bases<T>(P, gs, p, b, B);
+        T v[3], fe[3], sig[6];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            v[c] = P.vel[c * np + p];
+            fe[c] = P.fext[c * np + p];
+        }
+#pragma unroll
+        for (int c = 0; c < 6; ++c) sig[c] = P.stress[c * np + p];
+        blk.stage(t, B, P.mass[p], P.vol[p], v, fe, sig, cell_nodes(gs, b));
+    }
+    blk.cs.key[t] = key;
+    __syncthreads();
+    blk.template scatter<CPT, MG>(nd, g, (int)min((long long)BS, n - blockIdx.x * (long long)BS), mark_active);
 }
 
 template <typename T, int CPT, int BS>
@@ -1123,17 +1157,15 @@ __device__ __forceinline__ void pass2_prefetch(const PView<T>& P, long long p0, 
 // next step needs no separate key pass: `keys` is read (this step) and
 // rewritten (next step), `keys_next` receives the next step's sort input.
 // ---------------------------------------------------------------------------
-// BS: the block size; the FP32 form asks for 1280 / BS blocks per SM (48
-// registers: a few spill, and the extra resident warps hide more of the
-// gathers' latency).
-template <typename T, int BATCH, int BS>
-__global__ void __launch_bounds__(BS, sizeof(T) == 4 ? 1280 / BS : 1) k_pass2(PView<T> P, NView<T> nd, Geom g, unsigned* __restrict__ keys,
-                                               unsigned* __restrict__ keys_next, const MatConst* __restrict__ mats,
-                                               int nmat, StepArgs a, unsigned* err) {
-    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+// One particle of pass 2; returns the new cell key (u: the new cell-local
+// coordinate; queued: its stress increment waits for the network).
+template <typename T, int BATCH>
+__device__ __forceinline__ unsigned pass2_particle(const PView<T>& P, const NView<T>& nd, const Geom& g,
+                                                   unsigned* __restrict__ keys, unsigned* __restrict__ keys_next,
+                                                   const MatConst* __restrict__ mats, int nmat, const StepArgs& a,
+                                                   unsigned* err, long long p, float u[3], bool& queued) {
     const long long np = P.n, nn = nd.nn;
-    if (threadIdx.x < 64) pass2_prefetch<T>(P, blockIdx.x * (long long)blockDim.x, blockDim.x, a.contact);
-    if (p >= np) return;
+    queued = false;
     const unsigned fl = P.pflags[p];
     const T dt = form_const<T>(a.dt, a.dt_f);
     const T mass_min = form_const<T>(a.mass_min, a.mass_min_f);
@@ -1236,7 +1268,7 @@ __global__ void __launch_bounds__(BS, sizeof(T) == 4 ? 1280 / BS : 1) k_pass2(PV
             CrOut<T> o;
             // the network takes clearly plastic trial states of the materials it
             // was trained for; the band near the surface and elastic states stay exact
-            bool queued = false;
+            queued = false;
             if constexpr (sizeof(T) == 4) {
                 if (a.sg_on && mi < 32 && ((a.sg_mats >> mi) & 1u)) {
                     const float f = vmh_trial<float>(M, R, sig, e);
@@ -1319,7 +1351,6 @@ __global__ void __launch_bounds__(BS, sizeof(T) == 4 ? 1280 / BS : 1) k_pass2(PV
     }
     // the next step's cell key (and FP32 cell-local coordinate) from the new position
     const double xn[3] = {P.pos[p], P.pos[np + p], P.pos[2 * np + p]};
-    float u[3];
     const unsigned nk = particle_key(gs, xn, u, err);
     keys[p] = nk;
     if (keys_next) keys_next[p] = nk;
@@ -1327,6 +1358,22 @@ __global__ void __launch_bounds__(BS, sizeof(T) == 4 ? 1280 / BS : 1) k_pass2(PV
 #pragma unroll
         for (int c = 0; c < 3; ++c) P.loc[c * np + p] = u[c];
     }
+    return nk;
+}
+
+// BS: the block size; the FP32 form asks for 1280 / BS blocks per SM (48
+// registers: a few spill, and the extra resident warps hide more of the
+// gathers' latency).
+template <typename T, int BATCH, int BS>
+__global__ void __launch_bounds__(BS, sizeof(T) == 4 ? 1280 / BS : 1) k_pass2(PView<T> P, NView<T> nd, Geom g, unsigned* __restrict__ keys,
+                                               unsigned* __restrict__ keys_next, const MatConst* __restrict__ mats,
+                                               int nmat, StepArgs a, unsigned* err) {
+    const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (threadIdx.x < 64) pass2_prefetch<T>(P, blockIdx.x * (long long)blockDim.x, blockDim.x, a.contact);
+    if (p >= P.n) return;
+    float u[3];
+    bool queued;
+    pass2_particle<T, BATCH>(P, nd, g, keys, keys_next, mats, nmat, a, err, p, u, queued);
 }
 
 // ---------------------------------------------------------------------------

@@ -109,3 +109,21 @@ def test_sort_free_cell_order_is_the_sorted_runs():
     (k1, o1), (k0, o0) = got
     assert np.mean(k1 == k0) > 0.999
     assert np.array_equal(o0, np.argsort(k0, kind="stable"))
+
+
+@pytest.mark.parametrize("contact,floor", [(1, 0), (0, 1)])
+def test_steps_of_one_advance_match_output_steps(contact, floor):
+    """Inside one advance only the last step is an output step (the others zero their nodes instead of a grid
+    reset and skip the contact detection); one step per call makes every step an output step.  Both agree to
+    FP32 summation order."""
+    st = scenes.contact_small(seed=2) if contact else scenes.mixed_small(seed=1)
+    a = run(st, 30, contact, 0, floor=floor, cell_sort=0)
+    with engine.Engine.from_state(st, engine.FORM_FP32) as e:
+        e.set_option(engine.OPT_CELL_SORT, 0)
+        if floor:
+            e.set_option(engine.OPT_FLOOR_FRICTION, 1)
+        for _ in range(30):
+            e.advance(1, st.dt_max, bool(contact))
+        b = e.download_state(st)
+    close(a, b)
+    assert np.array_equal(a["g_state"] & 1, b["g_state"] & 1)
