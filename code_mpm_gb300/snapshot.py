@@ -71,6 +71,11 @@ FIELDS: Tuple[Tuple[str, str, int, str], ...] = (
     ("g_state", "u1", 1, "n"),
 )
 
+# Header flag: the elastic deformation gradient (MaterialPoint_BC.h:65, state of the large-strain pass 2)
+# follows the fields as one more n x 9 array; without it, it is the identity.
+HAS_FE = 1
+FE_FIELD = "F_elastic"
+
 PARTICLE_FIELDS = tuple(f[0] for f in FIELDS if f[3] == "p")
 NODE_FIELDS = tuple(f[0] for f in FIELDS if f[3] == "n")
 
@@ -142,11 +147,19 @@ def empty_state(length, cells, n_particles: int, dt_max: float, n_materials: int
     return st
 
 
+def identity_f(n: int) -> np.ndarray:
+    a = np.zeros((n, 9))
+    a[:, 0] = a[:, 4] = a[:, 8] = 1.0
+    return a
+
+
 def save(path: str, st: State) -> None:
     nm, nt, nd = (len(st.arrays[k]) for k in ("materials", "tl_time", "dc_list"))
+    fe = st.arrays.get(FE_FIELD)
     hdr = struct.pack(HEADER_FMT, MAGIC, 1, int(st.contact), *map(float, st.length),
                       *map(int, st.cells), 0, float(st.time), float(st.dt_max), float(st.mass_min),
-                      float(st.damping), int(st.step), st.n_particles, st.n_nodes, nm, nt, nd, 0)
+                      float(st.damping), int(st.step), st.n_particles, st.n_nodes, nm, nt, nd,
+                      HAS_FE if fe is not None else 0)
     with open(path, "wb") as f:
         f.write(hdr)
         for name, dt, comp, sel in FIELDS:
@@ -156,6 +169,11 @@ def save(path: str, st: State) -> None:
             a = np.ascontiguousarray(a, dtype=want).reshape(-1)
             if a.size != n * comp:
                 raise ValueError(f"field {name}: {a.size} elements, expected {n * comp}")
+            f.write(a.tobytes())
+        if fe is not None:
+            a = np.ascontiguousarray(fe, dtype="<f8").reshape(-1)
+            if a.size != st.n_particles * 9:
+                raise ValueError(f"field {FE_FIELD}: {a.size} elements, expected {st.n_particles * 9}")
             f.write(a.tobytes())
 
 
@@ -169,7 +187,7 @@ def load(path: str) -> State:
     length = np.array(vals[3:6])
     cells = np.array(vals[6:9], dtype=np.int32)
     time, dt_max, mass_min, damping = vals[10:14]
-    step, npart, nnodes, nm, nt, nd = vals[14:20]
+    step, npart, nnodes, nm, nt, nd, flags = vals[14:21]
     st = State(length=length, cells=cells, time=time, dt_max=dt_max, mass_min=mass_min,
                damping=damping, step=step, contact=contact)
     counts = {"p": npart, "n": nnodes, "m": nm, "t": nt, "d": nd}
@@ -180,6 +198,10 @@ def load(path: str) -> State:
         a = np.frombuffer(raw, dtype=want, count=n, offset=off).copy()
         off += n * want.itemsize
         st.arrays[name] = a if comp == 1 else a.reshape(-1, comp)
+    if flags & HAS_FE:
+        n = npart * 9
+        st.arrays[FE_FIELD] = np.frombuffer(raw, dtype="<f8", count=n, offset=off).copy().reshape(-1, 9)
+        off += n * 8
     if off != len(raw):
         raise ValueError(f"{path}: {len(raw) - off} trailing bytes")
     return st

@@ -23,6 +23,11 @@
 # Variants:
 #   ref_seq   OpenMP pragmas off: one thread, particles visited in index
 #             order.  This is the deterministic golden reference.
+#   ref_seq_ls  as ref_seq with the non-contact loop's pass 2 switched to the
+#             large-strain pass the reference ships disabled: a third
+#             mechanical edit, applied as the source streams in, comments out
+#             the SmallStrain call (…MPLocks.cpp:604) and uncomments the
+#             LargeStrain call (:605).
 #   ref_omp   -fopenmp as shipped (_MAX_N_THREADS = 8, PhysicsEngine.h:27).
 #   ref_ompN  -fopenmp with _MAX_N_THREADS set to N (default: nproc).
 #
@@ -67,7 +72,14 @@ build() {
         if [ "$tu" = ref_driver.cpp ]; then src="$HERE/ref_driver.cpp"; else src="$REF/$tu"; fi
         local filt=(cat "$src")
         if [ "$tu" = PhysicsEngine_runSimulation_Classic_DoublePass_MPLocks.cpp ]; then
-            filt=(sed -e 's|^}$|return 0;}|' "$src")
+            if [ "$name" = ref_seq_ls ]; then
+                filt=(sed -e 's|^}$|return 0;}|' \
+                      -e '604s|^\t\t\tthis->runSimulation_G2P_P2_SmallStrain|\t\t\t//this->runSimulation_G2P_P2_SmallStrain|' \
+                      -e '605s|^\t\t\t//this->runSimulation_G2P_P2_LargeStrain|\t\t\tthis->runSimulation_G2P_P2_LargeStrain|' \
+                      "$src")
+            else
+                filt=(sed -e 's|^}$|return 0;}|' "$src")
+            fi
         fi
         if [ -n "$nth" ]; then
             "${filt[@]}" | "$CXX" "${BASE[@]}" "$@" -include <(patch_gridpoint) -include <(patch_mp) \
@@ -83,6 +95,7 @@ build() {
 }
 
 build ref_seq ""
+build ref_seq_ls "" -DMPM_REF_LARGE_STRAIN
 build ref_omp "" -fopenmp
 build "ref_omp$NTH" "$NTH" -fopenmp
 echo "built: $(ls "$OUT")"

@@ -589,6 +589,102 @@ static void g2p_pass2(mpmsnap* s, work* w, double dt) {
     }
 }
 
+/* The matrix series of the large-strain pass
+ * (ConstitutiveRelation_MatrixAlgebra.cpp:25-53): log A = sum over n = 1..8 of
+ * (-1)^(n+1) (A - I)^n / n, exp A = sum over n = 0..8 of A^n / n!.  Each power
+ * is the previous one times the base (getPower multiplies I by the base n
+ * times), so every term is the reference's. */
+static void mat_log8(const double* A, double* R) {
+    double B[9], P[9], T[9];
+    for (int k = 0; k < 9; ++k) {
+        const double I = (k == 0 || k == 4 || k == 8) ? 1.0 : 0.0;
+        B[k] = A[k] - I;
+        P[k] = I;
+        R[k] = 0.0;
+    }
+    for (int n = 1; n <= 8; ++n) {
+        mat_mul(P, B, T);
+        memcpy(P, T, sizeof(P));
+        const double inv = 1.0 / n, sign = (n & 1) ? 1.0 : -1.0;
+        for (int k = 0; k < 9; ++k) R[k] = R[k] + (P[k] * inv) * sign;
+    }
+}
+static void mat_exp8(const double* A, double* R) {
+    double P[9], T[9], fact = 1.0;
+    for (int k = 0; k < 9; ++k) {
+        P[k] = (k == 0 || k == 4 || k == 8) ? 1.0 : 0.0;
+        R[k] = 0.0 + P[k] / 1.0;
+    }
+    for (int n = 1; n <= 8; ++n) {
+        mat_mul(P, A, T);
+        memcpy(P, T, sizeof(P));
+        fact *= n;
+        for (int k = 0; k < 9; ++k) R[k] = R[k] + P[k] / fact;
+    }
+}
+/* 0.5 log(M M^T) in Voigt order with engineering shear */
+static void half_log_voigt(const double* M, double v[6]) {
+    double Mt[9], MMt[9], lg[9];
+    for (int c = 0; c < 3; ++c)
+        for (int r = 0; r < 3; ++r) Mt[3 * c + r] = M[3 * r + c];
+    mat_mul(M, Mt, MMt);
+    mat_log8(MMt, lg);
+    for (int k = 0; k < 9; ++k) lg[k] = 0.5 * lg[k];
+    v[0] = lg[0];
+    v[1] = lg[4];
+    v[2] = lg[8];
+    v[3] = lg[1] + lg[3];
+    v[4] = lg[5] + lg[7];
+    v[5] = lg[6] + lg[2];
+}
+
+/* G2P_P2_LargeStrain (…MPLocks.cpp:281-437), disabled in the reference's loop
+ * (:605): logarithmic strains of F F^T, of the trial elastic gradient and of
+ * the increment; the constitutive map takes zero stress and the trial elastic
+ * strain and returns the Kirchhoff stress; F_e = exp of the elastic strain. */
+static void g2p_pass2_large_strain(mpmsnap* s, work* w, double dt) {
+#pragma omp for
+    for (long lp = 0; lp < (long)s->h.n_particles; ++lp) {
+        size_t p = (size_t)lp;
+        double L[9], dF[9], et[6], ee[6], einc[6];
+        gather_pass2(s, w, p, dt, L);
+        for (int k = 0; k < 6; ++k) s->stress[6 * p + k] = 0.0;
+        for (int c = 0; c < 3; ++c)
+            for (int r = 0; r < 3; ++r) dF[3 * c + r] = (c == r ? 1.0 : 0.0) + L[3 * c + r] * dt;
+        double* F = &s->F[9 * p];
+        double* Fe = &s->F_elastic[9 * p];
+        half_log_voigt(F, et);
+        double Fet[9];
+        mat_mul(dF, Fe, Fet);
+        half_log_voigt(Fet, ee);
+        half_log_voigt(dF, einc);
+        const mpmsnap_material* mat = material_of(s, p);
+        if (!mat) continue;
+        cr_out o;
+        cr_increment(mat, s->backstress[p], &s->stress[6 * p], ee, &o);
+        double el[6], E[9];
+        for (int k = 0; k < 6; ++k) el[k] = ee[k] - o.deps_p[k];
+        E[0] = el[0];
+        E[4] = el[1];
+        E[8] = el[2];
+        E[3] = E[1] = 0.5 * el[3]; /* [1][0] and [0][1] */
+        E[7] = E[5] = 0.5 * el[4]; /* [2][1] and [1][2] */
+        E[2] = E[6] = 0.5 * el[5]; /* [0][2] and [2][0] */
+        mat_exp8(E, Fe);
+        double Fn[9];
+        mat_mul(F, dF, Fn);
+        memcpy(F, Fn, sizeof(Fn));
+        const double det = mat_det(F);
+        s->vol[p] = det * s->vol0[p];
+        for (int k = 0; k < 6; ++k) s->strain[6 * p + k] = et[k];
+        for (int k = 0; k < 6; ++k) s->stress[6 * p + k] = (1.0 / det) * o.dsig[k];
+        for (int k = 0; k < 6; ++k) s->eps_p[6 * p + k] += o.deps_p[k];
+        for (int k = 0; k < 6; ++k) s->e_strain[p] += s->stress[6 * p + k] * einc[k] * s->vol[p];
+        for (int k = 0; k < 6; ++k) s->e_plastic[p] += s->stress[6 * p + k] * o.deps_p[k] * s->vol[p];
+        s->backstress[p] += o.dR;
+    }
+}
+
 /* Contact pass 2 (…_Contact.cpp:438-525) */
 static void g2p_pass2_contact(mpmsnap* s, work* w, double dt) {
 #pragma omp for
@@ -644,7 +740,9 @@ static void displacement_control_contact(mpmsnap* s, work* w) {
 static void step(mpmsnap* s, work* w, double dt, const oracle_opts* o) {
     double tv[3];
     timeline_velocity(s, s->h.time, tv);
-    const int contact = o->contact;
+    /* contact 2: the non-contact loop with the large-strain pass 2 */
+    const int large = o->contact == 2;
+    const int contact = o->contact == 1;
 #pragma omp parallel
     {
         reset_grid(s, contact);
@@ -659,7 +757,10 @@ static void step(mpmsnap* s, work* w, double dt, const oracle_opts* o) {
             remap(s, w, 0);
             displacement_control(s, w);
             reapply_bc(s);
-            g2p_pass2(s, w, dt);
+            if (large)
+                g2p_pass2_large_strain(s, w, dt);
+            else
+                g2p_pass2(s, w, dt);
 #pragma omp for
             for (long k = 0; k < (long)s->h.n_dc; ++k) {
                 size_t p = s->dc_list[k];

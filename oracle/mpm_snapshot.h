@@ -22,7 +22,10 @@
  * the order of the MPMSNAP_FIELDS table below.  Per-particle vectors are
  * stored n x k row-major (the k components of particle 0 first).  The 3x3
  * deformation gradient is stored in glm's column-major element order
- * (F[c][r] at offset 3*c + r).
+ * (F[c][r] at offset 3*c + r).  With MPMSNAP_HAS_FE in the header flags, the
+ * elastic deformation gradient (MaterialPoint_BC.h:65, the state of the
+ * large-strain pass 2) follows as one more [n][9] array; without it, it is
+ * the identity.
  */
 #ifndef MPM_SNAPSHOT_H
 #define MPM_SNAPSHOT_H
@@ -34,6 +37,7 @@
 #include <string.h>
 
 #define MPMSNAP_MAGIC "MPMSNAP1"
+#define MPMSNAP_HAS_FE 1u /* header flags: the elastic deformation gradient block follows */
 
 /* particle flag bits */
 #define MPM_PF_DC_X 1u     /* b3_DisplacementControl.x */
@@ -72,7 +76,7 @@ typedef struct mpmsnap_header {
     uint32_t n_materials;
     uint32_t n_timeline;
     uint32_t n_dc;
-    uint32_t pad1;
+    uint32_t flags; /* MPMSNAP_HAS_FE */
 } mpmsnap_header;
 
 typedef struct mpmsnap {
@@ -98,6 +102,7 @@ typedef struct mpmsnap {
     double* g_mass;     /* [nn] */
     double *g_mom, *g_vel, *g_force, *g_force_temp, *g_mass_gradient; /* [nn][3] */
     uint8_t* g_state;   /* [nn] */
+    double* F_elastic;  /* [n][9], identity unless the file holds it (not in MPMSNAP_FIELDS) */
 } mpmsnap;
 
 /* (pointer member offset, element size, components, count selector: 0 particles, 1 nodes, 2 materials, 3 timeline, 4 dc) */
@@ -166,6 +171,10 @@ static int mpmsnap_alloc(mpmsnap* s) {
         if (!p) return -1;
         *mpmsnap_slot(s, i) = p;
     }
+    const size_t n = (size_t)s->h.n_particles;
+    s->F_elastic = (double*)calloc(n ? n * 9 : 1, sizeof(double));
+    if (!s->F_elastic) return -1;
+    for (size_t p = 0; p < n; ++p) s->F_elastic[9 * p] = s->F_elastic[9 * p + 4] = s->F_elastic[9 * p + 8] = 1.0;
     return 0;
 }
 
@@ -174,6 +183,8 @@ static void mpmsnap_free(mpmsnap* s) {
         free(*mpmsnap_slot(s, i));
         *mpmsnap_slot(s, i) = NULL;
     }
+    free(s->F_elastic);
+    s->F_elastic = NULL;
 }
 
 static int mpmsnap_read(const char* path, mpmsnap* s) {
@@ -195,6 +206,11 @@ static int mpmsnap_read(const char* path, mpmsnap* s) {
             return -4;
         }
     }
+    const size_t nfe = (size_t)s->h.n_particles * 9;
+    if ((s->h.flags & MPMSNAP_HAS_FE) && nfe && fread(s->F_elastic, 8, nfe, f) != nfe) {
+        fclose(f);
+        return -4;
+    }
     fclose(f);
     return 0;
 }
@@ -213,6 +229,11 @@ static int mpmsnap_write(const char* path, const mpmsnap* s) {
             fclose(f);
             return -3;
         }
+    }
+    const size_t nfe = (size_t)s->h.n_particles * 9;
+    if ((s->h.flags & MPMSNAP_HAS_FE) && nfe && fwrite(s->F_elastic, 8, nfe, f) != nfe) {
+        fclose(f);
+        return -3;
     }
     fclose(f);
     return 0;

@@ -6,7 +6,9 @@ it.
 
 ``advance(state, steps, contact)`` runs the one-thread build (particle index
 order, the order the golden states were produced in) in place on a
-``code_mpm_gb300.snapshot.State``; ``advance(..., threads=N, omp=True)`` runs
+``code_mpm_gb300.snapshot.State`` (contact 2: the non-contact loop with the
+large-strain pass 2, which keeps the elastic deformation gradient in
+``state["F_elastic"]``); ``advance(..., threads=N, omp=True)`` runs
 the OpenMP build that mirrors the reference's per-node-lock parallel loop,
 which is only ever timed.
 """
@@ -51,7 +53,7 @@ class _Header(C.Structure):
                 ("time", C.c_double), ("dt_max", C.c_double), ("mass_min", C.c_double),
                 ("damping", C.c_double), ("step", C.c_int64), ("n_particles", C.c_uint64),
                 ("n_nodes", C.c_uint64), ("n_materials", C.c_uint32), ("n_timeline", C.c_uint32),
-                ("n_dc", C.c_uint32), ("pad1", C.c_uint32)]
+                ("n_dc", C.c_uint32), ("flags", C.c_uint32)]
 
 
 _PTRS = ("materials", "tl_time", "tl_vel", "pos", "vel", "fext", "mass", "vol", "vol0", "F", "stress", "strain",
@@ -61,7 +63,7 @@ _PTRS = ("materials", "tl_time", "tl_vel", "pos", "vel", "fext", "mass", "vol", 
 
 
 class _Snap(C.Structure):
-    _fields_ = [("h", _Header)] + [(n, C.c_void_p) for n in _PTRS]
+    _fields_ = [("h", _Header)] + [(n, C.c_void_p) for n in _PTRS] + [("F_elastic", C.c_void_p)]
 
 
 def _make_snap(st):
@@ -86,6 +88,13 @@ def _make_snap(st):
     h.n_dc = len(st.arrays["dc_list"])
     for k in _PTRS:
         setattr(s, k, st.arrays[k].ctypes.data)
+    if "F_elastic" not in st.arrays:
+        from code_mpm_gb300 import snapshot
+
+        st.arrays["F_elastic"] = snapshot.identity_f(st.n_particles)
+    st.arrays["F_elastic"] = np.ascontiguousarray(st.arrays["F_elastic"], dtype=np.float64)
+    s.F_elastic = st.arrays["F_elastic"].ctypes.data
+    h.flags = 1
     return s
 
 

@@ -9,6 +9,10 @@
 //  PhysicsEngine_runSimulation_Classic_DoublePass_MPLocks_Contact.cpp:4-566),
 // one call per step, and writes the resulting state back out.
 //
+// Built with -DMPM_REF_LARGE_STRAIN (ref_seq_ls), the non-contact loop runs
+// the reference's large-strain pass 2; the output state records contact = 2.
+// The elastic deformation gradient is always written out.
+//
 // usage: ref_driver <in.snap> <out.snap> <steps> <contact 0|1> [timing 0|1]
 #include "PhysicsEngine.h"
 
@@ -91,7 +95,10 @@ class HeadlessEngine : public PhysicsEngine {
             mp->d_Volume = s.vol[p];
             mp->d_Volume_Initial = s.vol0[p];
             for (int c = 0; c < 3; ++c)
-                for (int r = 0; r < 3; ++r) mp->d33_DeformationGradient[c][r] = s.F[9 * p + 3 * c + r];
+                for (int r = 0; r < 3; ++r) {
+                    mp->d33_DeformationGradient[c][r] = s.F[9 * p + 3 * c + r];
+                    mp->d33_DeformationGradient_Elastic[c][r] = s.F_elastic[9 * p + 3 * c + r];
+                }
             for (int k = 0; k < 6; ++k) {
                 mp->d6_Stress[k] = s.stress[6 * p + k];
                 mp->d6_Strain[k] = s.strain[6 * p + k];
@@ -154,7 +161,10 @@ class HeadlessEngine : public PhysicsEngine {
             s.vol[p] = mp->d_Volume;
             s.vol0[p] = mp->d_Volume_Initial;
             for (int c = 0; c < 3; ++c)
-                for (int r = 0; r < 3; ++r) s.F[9 * p + 3 * c + r] = mp->d33_DeformationGradient[c][r];
+                for (int r = 0; r < 3; ++r) {
+                    s.F[9 * p + 3 * c + r] = mp->d33_DeformationGradient[c][r];
+                    s.F_elastic[9 * p + 3 * c + r] = mp->d33_DeformationGradient_Elastic[c][r];
+                }
             for (int k = 0; k < 6; ++k) {
                 s.stress[6 * p + k] = mp->d6_Stress[k];
                 s.strain[6 * p + k] = mp->d6_Strain[k];
@@ -200,6 +210,10 @@ int main(int argc, char** argv) {
         fprintf(stderr, "TIMING steps=%d particles=%llu seconds=%.6f updates_per_s=%.6e\n", steps,
                 (unsigned long long)s.h.n_particles, sec, (double)steps * (double)s.h.n_particles / sec);
     s.h.contact = (uint32_t)contact;
+#ifdef MPM_REF_LARGE_STRAIN
+    if (!contact) s.h.contact = 2u;
+#endif
+    s.h.flags |= MPMSNAP_HAS_FE;
     eng.store(s);
     rc = mpmsnap_write(argv[2], &s);
     mpmsnap_free(&s);

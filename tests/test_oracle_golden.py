@@ -11,8 +11,9 @@ import pytest
 import pyoracle
 from code_mpm_gb300 import snapshot
 
+# contact 2: the non-contact loop with the large-strain pass 2 (the reference's build with that pass switched on)
 CASES = [("mixed", 0, 1), ("mixed", 0, 25), ("mixed_contactpath", 1, 3), ("contact", 1, 1), ("contact", 1, 25),
-         ("bar", 0, 60)]
+         ("bar", 0, 60), ("largestrain", 2, 1), ("largestrain", 2, 25)]
 
 
 @pytest.mark.parametrize("name,contact,steps", CASES)
@@ -21,10 +22,24 @@ def test_oracle_bit_exact_vs_reference(golden, name, contact, steps):
     ref = golden(f"{name}_ref{steps}")
     pyoracle.advance(st, steps, contact)
     assert st.time == ref.time and st.step == ref.step
-    for k in snapshot.PARTICLE_FIELDS + snapshot.NODE_FIELDS:
+    fields = snapshot.PARTICLE_FIELDS + snapshot.NODE_FIELDS + ((snapshot.FE_FIELD,) if contact == 2 else ())
+    for k in fields:
         a, b = st[k], ref[k]
         assert a.dtype == b.dtype and a.shape == b.shape, k
         assert np.array_equal(a.view(np.uint8), b.view(np.uint8)), f"field {k} differs"
+
+
+def test_large_strain_golden_is_large_strain(golden):
+    """The large-strain fixture moved the elastic deformation gradient off the identity, yielded, and its strain is
+    the logarithmic strain of F (not the accumulated small-strain increments)."""
+    st = golden("largestrain_ref25")
+    assert st.contact == 2
+    fe = st[snapshot.FE_FIELD]
+    assert np.abs(fe - snapshot.identity_f(st.n_particles)).max() > 1e-3
+    assert (np.abs(st["eps_p"]).sum(1) > 0).any()
+    small = golden("largestrain_in")
+    pyoracle.advance(small, 25, 0)
+    assert np.abs(small["strain"] - st["strain"]).max() > 1e-6
 
 
 def test_golden_cases_exercise_every_branch(golden):
