@@ -186,6 +186,7 @@ struct PView {
     float* loc;  // FP32 form: cell-local coordinate (x - X_b)/h of the current base cell, 3 x n
     const uint16_t* sid;  // specimen of each particle (null with one specimen)
     const unsigned* orig; // FP32 form in cell order: the caller's index of each slot (null: slot = index)
+    double* Fe;           // FP64 form: elastic deformation gradient, 9 x n (large-strain pass 2)
     long long n;
 };
 

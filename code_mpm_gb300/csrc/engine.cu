@@ -75,7 +75,8 @@ struct mpm_ctx {
     DevBuf xtab, err_word;
     // particles
     DevBuf pos, vel, fext, mass, vol, vol0, F, stress, strain, eps_p, e_strain, e_strain_max, e_strain_ti, e_plastic,
-        backstress, mp_mg, strain_rate, material, pflags, dc_mult;
+        backstress, mp_mg, strain_rate, material, pflags, dc_mult,
+        Fe;  // FP64 form: elastic deformation gradient (large-strain pass 2)
     // nodes
     DevBuf g_mass, g_mom, g_vel, g_force, g_ftemp, g_mg, g_state, g_fixed, g_friction, g_ratio, g_q, g_owner,
         g_nowner, g_need, g_list, g_count, rs_chunk;
@@ -126,6 +127,7 @@ struct mpm_ctx {
     bool have_orig = false, reorder_pending = false;
     int reorder_interval = 0;  // -1: never; 0: after each particle upload; N: also every N steps
     bool cell_sort = false;    // FP32 form, P2G modes 2-4: false = take the storage order as the cell order
+    bool large_strain = false; // FP64 form, non-contact loop: the large-strain pass 2
     long long steps_since_reorder = 0;
     bool owner_clean = false;  // displacement-control claims all zero (phase B clears them after use)
 
@@ -136,7 +138,7 @@ struct mpm_ctx {
                           &g_state, &g_fixed, &g_friction, &g_ratio, &g_q, &g_owner, &g_nowner, &g_need, &g_list, &g_count, &rs_chunk, &cstart,
                           &cend, &keys0, &vals0, &keys1, &vals1, &keys_copy, &counts, &dclist, &mats, &staging, &tune_backup, &surf, &mon_mask, &mon_acc, &loc, &geom_tab, &sid, &alist, &acount,
                           &q_in, &q_out, &q_vol, &q_pidx, &q_count, &sg_acc, &hv_count,
-                          &dsim, &tl_dev, &orig, &ptmp};
+                          &dsim, &tl_dev, &orig, &ptmp, &Fe};
         all.assign(std::begin(list), std::end(list));
     }
 };
@@ -200,6 +202,7 @@ PView<T> pview(mpm_ctx* c) {
     v.loc = (float*)c->loc.p;
     v.sid = c->nspec > 1 ? (const uint16_t*)c->sid.p : nullptr;
     v.orig = c->have_orig ? (const unsigned*)c->orig.p : nullptr;
+    v.Fe = (double*)c->Fe.p;
     v.n = c->n;
     return v;
 }
@@ -880,7 +883,16 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph, bool output) {
             unsigned* kc = (unsigned*)c->keys_copy.p;
             const MatConst* mats = (const MatConst*)c->mats.p;
 #define PASS2(B, S) LAUNCH("pass2", (k_pass2<T, B, S>), pb, S, P, N, g, kc, keys_next, mats, c->nmat, a, err)
-            if (c->pass_block == 128) {
+            bool large = false;
+            if constexpr (sizeof(T) == 8) {
+                if (c->large_strain && !contact) {  // non-contact loop only, as in the reference
+                    LAUNCH("pass2", k_pass2_ls<128>, blocks_for(n, 128), 128, P, N, g, kc, keys_next, mats, c->nmat,
+                           a, err);
+                    large = true;
+                }
+            }
+            if (large) {
+            } else if (c->pass_block == 128) {
                 if (c->gather_batch) PASS2(1, 128); else PASS2(0, 128);
             } else if (c->pass_block == 256) {
                 if (c->gather_batch) PASS2(1, 256); else PASS2(0, 256);
@@ -1030,6 +1042,7 @@ int alloc_particles(mpm_ctx* c, long long n) {
                 {&c->strain, 6 * t},  {&c->eps_p, 6 * t},      {&c->e_strain, 8},        {&c->e_strain_max, 8},
                 {&c->e_strain_ti, 8}, {&c->e_plastic, 8},      {&c->backstress, t},      {&c->mp_mg, 3 * t},
                 {&c->strain_rate, 6 * t}, {&c->material, 4},   {&c->pflags, 1},          {&c->dc_mult, 4},
+                {&c->Fe, c->form == MPM_FORM_FP64 ? 72u : 0u},
                 {&c->keys0, 4},       {&c->vals0, 4},          {&c->keys1, 4},           {&c->vals1, 4},
                 {&c->keys_copy, 4},   {&c->loc, c->form == MPM_FORM_FP32 ? 12u : 0u}};
     for (auto& e : plan) {
@@ -1258,6 +1271,12 @@ int mpm_set_option(mpm_ctx* c, int key, double value) {
         case MPM_OPT_GRAPH:
             c->use_graph = value != 0.0;
             return MPM_OK;
+        case MPM_OPT_LARGE_STRAIN:
+            if (value != 0.0 && value != 1.0) return fail(c, MPM_ERR_ARG, "large strain must be 0 or 1");
+            if (value != 0.0 && c->form != MPM_FORM_FP64)
+                return fail(c, MPM_ERR_ARG, "the large-strain pass 2 is built for the FP64 form");
+            c->large_strain = value != 0.0;
+            return MPM_OK;
         case MPM_OPT_CELL_SORT:
             if (value != 0.0 && value != 1.0) return fail(c, MPM_ERR_ARG, "cell sort must be 0 or 1");
             c->cell_sort = value != 0.0;
@@ -1385,6 +1404,13 @@ int mpm_upload_particles(mpm_ctx* c, const mpm_particles* p, int64_t n) {
             LAUNCH("fill", k_identity9, blocks_for(9 * n), NTHREADS, c->F.p, (long long)n, 1);
         else
             CK(cudaMemsetAsync(c->F.p, 0, (size_t)n * 9 * sizeof(float), c->stream));  // H = F - I = 0
+    }
+    if (f64) {  // the elastic deformation gradient, identity unless given
+        if (p->F_elastic) {
+            if ((rc = upload_field(c, c->Fe, p->F_elastic, n, 9, true, 0.0))) return rc;
+        } else if (n > 0) {
+            LAUNCH("fill", k_identity9, blocks_for(9 * n), NTHREADS, c->Fe.p, (long long)n, 1);
+        }
     }
     if (n > 0) {
         if (p->material)
@@ -1545,13 +1571,17 @@ int mpm_download_particles(mpm_ctx* c, mpm_particles* p) {
                   {&c->e_plastic, p->e_plastic, 1, true},
                   {&c->backstress, p->backstress, 1, f64},
                   {&c->mp_mg, p->mp_mass_gradient, 3, f64},
-                  {&c->strain_rate, p->strain_rate, 6, f64}};
+                  {&c->strain_rate, p->strain_rate, 6, f64},
+                  {&c->Fe, f64 ? p->F_elastic : nullptr, 9, true}};
     for (auto& f : fields) {
         if (!f.h) continue;
         const int shift = (f.b == &c->F && !f64) ? 1 : 0;
         if ((rc = download_field(c, *f.b, f.h, n, f.k, f.fp64, shift, true))) return rc;
         CK(cudaStreamSynchronize(c->stream));  // staging is reused by the next field
     }
+    if (!f64 && p->F_elastic)  // the FP32 form has no large-strain pass: the identity
+        for (long long i = 0; i < n; ++i)
+            for (int k = 0; k < 9; ++k) p->F_elastic[9 * i + k] = (k == 0 || k == 4 || k == 8) ? 1.0 : 0.0;
     if (n > 0) {
         // in the caller's order: through the staging buffer when the slots are in cell order
         auto get = [&](void* host, const DevBuf& b, int es) -> int {

@@ -1157,9 +1157,83 @@ __device__ __forceinline__ void pass2_prefetch(const PView<T>& P, long long p0, 
 // next step needs no separate key pass: `keys` is read (this step) and
 // rewritten (next step), `keys_next` receives the next step's sort input.
 // ---------------------------------------------------------------------------
+// The large-strain pass 2's update of one particle after its gather
+// (G2P_P2_LargeStrain, …MPLocks.cpp:311-435; FP64 form): the stress is reset,
+// the logarithmic strains of F F^T (total, from the old F), of the trial
+// elastic gradient dF F_e and of the increment dF are formed, the
+// constitutive map takes zero stress and the trial elastic strain and returns
+// the Kirchhoff stress, F_e becomes the exponential of the elastic strain,
+// F = F dF, and stress = Kirchhoff / det F.  Energies add stress x increment x
+// V component by component, as the reference does.
+template <typename T>
+__device__ __forceinline__ void large_strain_update(const PView<T>& P, long long p, const T Lt[9], double dt,
+                                                    const MatConst* __restrict__ mats, int nmat, unsigned* err) {
+    if constexpr (sizeof(T) == 8) {
+        const long long np = P.n;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) P.stress[k * np + p] = 0.0;
+        double dF[9], F[9], Fe[9];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+            for (int r = 0; r < 3; ++r) dF[3 * c + r] = (c == r ? 1.0 : 0.0) + (double)Lt[3 * c + r] * dt;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            F[k] = P.F[k * np + p];
+            Fe[k] = P.Fe[k * np + p];
+        }
+        double et[6], ee[6], einc[6], Fet[9];
+        half_log_voigt(F, et);
+        mat3_mul(dF, Fe, Fet);
+        half_log_voigt(Fet, ee);
+        half_log_voigt(dF, einc);
+        const int mi = P.material[p];
+        if (!(mi >= 0 && mi < nmat)) {
+            atomicOr(err, ERR_BAD_MATERIAL);
+            return;
+        }
+        const double zero[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        CrOut<double> o;
+        cr_increment<double>(mats[mi], (double)P.backstress[p], zero, ee, o);
+        double el[6], E[9], Fen[9], Fn[9];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) el[k] = ee[k] - o.deps_p[k];
+        E[0] = el[0];
+        E[4] = el[1];
+        E[8] = el[2];
+        E[1] = E[3] = 0.5 * el[3];
+        E[5] = E[7] = 0.5 * el[4];
+        E[2] = E[6] = 0.5 * el[5];
+        mat3_exp8(E, Fen);
+        mat3_mul(F, dF, Fn);
+        const double det = Kinematics<double>::det(Fn);
+        const double V = det * (double)P.vol0[p];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            P.Fe[k * np + p] = Fen[k];
+            P.F[k * np + p] = Fn[k];
+        }
+        P.vol[p] = V;
+        double es = P.e_strain[p], ep = P.e_plastic[p];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const double sn = (1.0 / det) * o.dsig[k];
+            P.strain[k * np + p] = et[k];
+            P.stress[k * np + p] = sn;
+            P.eps_p[k * np + p] += o.deps_p[k];
+            es += sn * einc[k] * V;
+        }
+#pragma unroll
+        for (int k = 0; k < 6; ++k) ep += (1.0 / det) * o.dsig[k] * o.deps_p[k] * V;
+        P.e_strain[p] = es;
+        P.e_plastic[p] = ep;
+        P.backstress[p] += o.dR;
+    }
+}
+
 // One particle of pass 2; returns the new cell key (u: the new cell-local
 // coordinate; queued: its stress increment waits for the network).
-template <typename T, int BATCH>
+template <typename T, int BATCH, bool LS = false>
 __device__ __forceinline__ unsigned pass2_particle(const PView<T>& P, const NView<T>& nd, const Geom& g,
                                                    unsigned* __restrict__ keys, unsigned* __restrict__ keys_next,
                                                    const MatConst* __restrict__ mats, int nmat, const StepArgs& a,
@@ -1233,6 +1307,9 @@ __device__ __forceinline__ unsigned pass2_particle(const PView<T>& P, const NVie
 #pragma unroll
             for (int c = 0; c < 3; ++c) P.pos[c * np + p] = x[c];
         }
+        if constexpr (LS) {
+            large_strain_update(P, p, L, (double)dt, mats, nmat, err);
+        } else {
         // strain increment: diagonal from dF = I + L dt (form-specific, see
         // Kinematics), off-diagonal (L_ij + L_ji) dt in Voigt engineering shear
         T Ldt[9];
@@ -1329,6 +1406,7 @@ __device__ __forceinline__ unsigned pass2_particle(const PView<T>& P, const NVie
         } else if (!a.contact) {
             atomicOr(err, ERR_BAD_MATERIAL);
         }
+        }
     }
     // platen timeline (…MPLocks.cpp:766-789; contact :531-540)
     if (fl & PF_IN_DC) {
@@ -1374,6 +1452,19 @@ __global__ void __launch_bounds__(BS, sizeof(T) == 4 ? 1280 / BS : 1) k_pass2(PV
     float u[3];
     bool queued;
     pass2_particle<T, BATCH>(P, nd, g, keys, keys_next, mats, nmat, a, err, p, u, queued);
+}
+
+// The large-strain pass 2 (non-contact loop, FP64 form; the reference ships
+// it disabled, …MPLocks.cpp:605, and MPM_OPT_LARGE_STRAIN switches it on).
+template <int BS>
+__global__ void __launch_bounds__(BS) k_pass2_ls(PView<double> P, NView<double> nd, Geom g, unsigned* __restrict__ keys,
+                                                 unsigned* __restrict__ keys_next, const MatConst* __restrict__ mats,
+                                                 int nmat, StepArgs a, unsigned* err) {
+    const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (p >= P.n) return;
+    float u[3];
+    bool queued;
+    pass2_particle<double, 0, true>(P, nd, g, keys, keys_next, mats, nmat, a, err, p, u, queued);
 }
 
 // ---------------------------------------------------------------------------

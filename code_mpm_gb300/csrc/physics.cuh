@@ -333,4 +333,81 @@ __device__ __forceinline__ void cr_increment(const MatConst& m, T R, const T sig
     o.dR = (sat > (T)0) ? form_const<T>(m.C0, m.fC0) * sat * ep : (T)0;
 }
 
+
+// ---------------------------------------------------------------------------
+// Large-strain pass 2 helpers (FP64 form; G2P_P2_LargeStrain,
+// PhysicsEngine_runSimulation_Classic_DoublePass_MPLocks.cpp:281-437).  glm
+// column-major 3x3 (element [c][r] at 3c + r); the products associate as
+// glm's operator*: (A B)[c][r] = A[0][r] B[c][0] + A[1][r] B[c][1] + A[2][r] B[c][2].
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void mat3_mul(const double A[9], const double B[9], double R[9]) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int r = 0; r < 3; ++r) R[3 * c + r] = A[r] * B[3 * c] + A[3 + r] * B[3 * c + 1] + A[6 + r] * B[3 * c + 2];
+}
+
+// log A = sum over n = 1..8 of (-1)^(n+1) (A - I)^n / n and exp A = sum over
+// n = 0..8 of A^n / n!, the truncated series of getLog / getExp
+// (ConstitutiveRelation_MatrixAlgebra.cpp:25-53); each power is the previous
+// one times the base, as getPower forms it.
+__device__ __forceinline__ void mat3_log8(const double A[9], double R[9]) {
+    double B[9], P[9], T[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        const double I = (k == 0 || k == 4 || k == 8) ? 1.0 : 0.0;
+        B[k] = A[k] - I;
+        P[k] = I;
+        R[k] = 0.0;
+    }
+#pragma unroll 1
+    for (int n = 1; n <= 8; ++n) {
+        mat3_mul(P, B, T);
+        const double inv = 1.0 / n, sign = (n & 1) ? 1.0 : -1.0;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            P[k] = T[k];
+            R[k] = R[k] + (P[k] * inv) * sign;
+        }
+    }
+}
+
+__device__ __forceinline__ void mat3_exp8(const double A[9], double R[9]) {
+    double P[9], T[9], fact = 1.0;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        P[k] = (k == 0 || k == 4 || k == 8) ? 1.0 : 0.0;
+        R[k] = P[k];
+    }
+#pragma unroll 1
+    for (int n = 1; n <= 8; ++n) {
+        mat3_mul(P, A, T);
+        fact *= n;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            P[k] = T[k];
+            R[k] = R[k] + P[k] / fact;
+        }
+    }
+}
+
+// 0.5 log(M M^T) in Voigt order with engineering shear
+__device__ __forceinline__ void half_log_voigt(const double M[9], double v[6]) {
+    double Mt[9], MMt[9], lg[9];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int r = 0; r < 3; ++r) Mt[3 * c + r] = M[3 * r + c];
+    mat3_mul(M, Mt, MMt);
+    mat3_log8(MMt, lg);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) lg[k] = 0.5 * lg[k];
+    v[0] = lg[0];
+    v[1] = lg[4];
+    v[2] = lg[8];
+    v[3] = lg[1] + lg[3];
+    v[4] = lg[5] + lg[7];
+    v[5] = lg[6] + lg[2];
+}
+
 }  // namespace mpm

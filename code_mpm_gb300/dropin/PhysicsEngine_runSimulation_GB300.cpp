@@ -27,23 +27,24 @@
 namespace {
 
 struct Packed {
-    std::vector<double> pos, vel, fext, mass, vol, vol0, F, stress, strain, eps_p, e_s, e_smax, e_sti, e_p, R, mg, rate;
+    std::vector<double> pos, vel, fext, mass, vol, vol0, F, Fe, stress, strain, eps_p, e_s, e_smax, e_sti, e_p, R, mg,
+        rate;
     std::vector<int32_t> material;
     std::vector<uint8_t> flags;
     std::vector<float> mult;
     void resize(size_t n) {
         pos.resize(3 * n); vel.resize(3 * n); fext.resize(3 * n); mass.resize(n); vol.resize(n); vol0.resize(n);
-        F.resize(9 * n); stress.resize(6 * n); strain.resize(6 * n); eps_p.resize(6 * n); e_s.resize(n);
+        F.resize(9 * n); Fe.resize(9 * n); stress.resize(6 * n); strain.resize(6 * n); eps_p.resize(6 * n); e_s.resize(n);
         e_smax.resize(n); e_sti.resize(n); e_p.resize(n); R.resize(n); mg.resize(3 * n); rate.resize(6 * n);
         material.resize(n); flags.resize(n); mult.resize(n);
     }
     mpm_particles view() {
-        mpm_particles v;
+        mpm_particles v = {};
         v.pos = pos.data(); v.vel = vel.data(); v.fext = fext.data(); v.mass = mass.data(); v.vol = vol.data();
         v.vol0 = vol0.data(); v.F = F.data(); v.stress = stress.data(); v.strain = strain.data();
         v.eps_p = eps_p.data(); v.e_strain = e_s.data(); v.e_strain_max = e_smax.data(); v.e_strain_ti = e_sti.data();
         v.e_plastic = e_p.data(); v.backstress = R.data(); v.mp_mass_gradient = mg.data(); v.strain_rate = rate.data();
-        v.material = material.data(); v.pflags = flags.data(); v.dc_mult = mult.data();
+        v.material = material.data(); v.pflags = flags.data(); v.dc_mult = mult.data(); v.F_elastic = Fe.data();
         return v;
     }
 };
@@ -56,7 +57,7 @@ struct PackedNodes {
         force.resize(3 * n); ftemp.resize(3 * n); mg.resize(3 * n);
     }
     mpm_nodes view() {
-        mpm_nodes v;
+        mpm_nodes v = {};
         v.fixed = fixed.data(); v.friction = friction.data(); v.mass = mass.data(); v.mom = mom.data();
         v.vel = vel.data(); v.force = force.data(); v.force_temp = ftemp.data(); v.mass_gradient = mg.data();
         v.state = state.data();
@@ -75,7 +76,10 @@ void pack_particle(const MaterialPoint_BC* mp, size_t p, const std::map<const Ma
     P.vol[p] = mp->d_Volume;
     P.vol0[p] = mp->d_Volume_Initial;
     for (int c = 0; c < 3; ++c)
-        for (int r = 0; r < 3; ++r) P.F[9 * p + 3 * c + r] = mp->d33_DeformationGradient[c][r];
+        for (int r = 0; r < 3; ++r) {
+            P.F[9 * p + 3 * c + r] = mp->d33_DeformationGradient[c][r];
+            P.Fe[9 * p + 3 * c + r] = mp->d33_DeformationGradient_Elastic[c][r];
+        }
     for (int k = 0; k < 6; ++k) {
         P.stress[6 * p + k] = mp->d6_Stress[k];
         P.strain[6 * p + k] = mp->d6_Strain[k];
@@ -104,7 +108,10 @@ void unpack_particle(MaterialPoint_BC* mp, size_t p, const Packed& P) {
     }
     mp->d_Volume = P.vol[p];
     for (int c = 0; c < 3; ++c)
-        for (int r = 0; r < 3; ++r) mp->d33_DeformationGradient[c][r] = P.F[9 * p + 3 * c + r];
+        for (int r = 0; r < 3; ++r) {
+            mp->d33_DeformationGradient[c][r] = P.F[9 * p + 3 * c + r];
+            mp->d33_DeformationGradient_Elastic[c][r] = P.Fe[9 * p + 3 * c + r];
+        }
     for (int k = 0; k < 6; ++k) {
         mp->d6_Stress[k] = P.stress[6 * p + k];
         mp->d6_Strain[k] = P.strain[6 * p + k];

@@ -61,7 +61,8 @@ _PFIELDS = ("pos", "vel", "fext", "mass", "vol", "vol0", "F", "stress", "strain"
 
 class Particles(C.Structure):
     _fields_ = [(k, C.c_void_p) for k in _PFIELDS] + [("material", C.c_void_p), ("pflags", C.c_void_p),
-                                                      ("dc_mult", C.c_void_p), ("specimen", C.c_void_p)]
+                                                      ("dc_mult", C.c_void_p), ("specimen", C.c_void_p),
+                                                      ("F_elastic", C.c_void_p)]
 
 
 _NMAP = (("fixed", "fixed"), ("friction", "friction"), ("mass", "g_mass"), ("mom", "g_mom"), ("vel", "g_vel"),
@@ -120,6 +121,7 @@ OPT_REORDER = 8
 OPT_CELL_SORT = 9
 OPT_PASS1_CORNERS = 10
 OPT_PASS1_BLOCK = 11
+OPT_LARGE_STRAIN = 12
 
 
 def library_path() -> str:
@@ -318,6 +320,8 @@ class Engine:
         arrs["dc_mult"] = np.ascontiguousarray(st["dc_mult"], dtype=np.float32)
         if "specimen" in st.arrays:
             arrs["specimen"] = np.ascontiguousarray(st["specimen"], dtype=np.int32)
+        if "F_elastic" in st.arrays:
+            arrs["F_elastic"] = np.ascontiguousarray(st["F_elastic"], dtype=np.float64)
         p = Particles(**{k: _ptr(v) for k, v in arrs.items()})
         self._check(self._L.mpm_upload_particles(self._h, C.byref(p), st.n_particles))
         self.n_particles = st.n_particles
@@ -340,6 +344,9 @@ class Engine:
         arrs["material"] = st["material"]
         arrs["pflags"] = st["pflags"]
         arrs["dc_mult"] = st["dc_mult"]
+        if "F_elastic" not in st.arrays:
+            st.arrays["F_elastic"] = np.zeros((st.n_particles, 9))
+        arrs["F_elastic"] = st["F_elastic"]
         p = Particles(**{k: _ptr(v) for k, v in arrs.items()})
         self._check(self._L.mpm_download_particles(self._h, C.byref(p)))
         nd = Nodes(**{k: _ptr(st[src]) for k, src in _NMAP if len(st[src]) > 0})

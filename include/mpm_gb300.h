@@ -78,6 +78,7 @@ extern "C" {
 #define MPM_OPT_REORDER 8        /* FP32 form: store particles in cell order after each particle upload (0, default), also every N steps (N > 0), or never (-1); results stay in the caller's order */
 #define MPM_OPT_PASS1_CORNERS 10 /* cell-run G2P pass 1 (P2G modes 2-4): corners per thread, 1, 2 (default) or 4 */
 #define MPM_OPT_PASS1_BLOCK 11   /* cell-run G2P pass 1: threads per block (128, 256 or 512) */
+#define MPM_OPT_LARGE_STRAIN 12  /* FP64 form, non-contact loop: 1 runs the large-strain pass 2 (G2P_P2_LargeStrain, PhysicsEngine_runSimulation_Classic_DoublePass_MPLocks.cpp:281-437), which the reference ships disabled (:605); 0 (default) the small-strain pass */
 #define MPM_OPT_CELL_SORT 9      /* FP32 form, P2G modes 2-4: 1 sorts the particles by cell every step; 0 (default) takes the storage order as it is (a cell whose particles are not adjacent is summed in several runs) and, with MPM_OPT_REORDER 0, restores the cell order every 256 steps */
 
 typedef struct mpm_ctx mpm_ctx;
@@ -122,6 +123,9 @@ typedef struct mpm_particles {
     uint8_t* pflags;                 /* n, MPM_PF_* */
     float* dc_mult;                  /* n, f_DisplacementControl_Multiplier */
     int32_t* specimen;               /* n, specimen of each particle (batches only; upload only) */
+    double* F_elastic;               /* n x 9, column-major: d33_DeformationGradient_Elastic (MaterialPoint_BC.h:65),
+                                        the large-strain pass 2's state; FP64 form (identity when NULL; the FP32
+                                        form downloads the identity) */
 } mpm_particles;
 
 /* Host views of the node state (GridPoint.h:6-45), n_nodes entries each. */

@@ -67,6 +67,28 @@ def test_gpu_matches_reference_golden(golden, name, contact, steps):
     assert_parity(gpu, ref)
 
 
+@pytest.mark.parametrize("steps", [1, 25])
+def test_gpu_large_strain_matches_reference_golden(golden, steps):
+    """The large-strain pass 2 (MPM_OPT_LARGE_STRAIN) against the reference built with that pass switched on."""
+    st = golden("largestrain_in")
+    ref = golden(f"largestrain_ref{steps}")
+    with engine.Engine.from_state(st, engine.FORM_FP64) as e:
+        e.set_option(engine.OPT_LARGE_STRAIN, 1)
+        e.advance(steps, st.dt_max, False)
+        e.synchronize()
+        gpu = e.download_state(st)
+    fields = tuple(k for k in REAL_PARTICLE + REAL_NODE if k not in ("e_strain_ti", "e_strain_max", "strain_rate",
+                                                                      "mp_mass_gradient", "g_mass_gradient"))
+    assert_parity(gpu, ref, fields=fields + (snapshot.FE_FIELD,))
+
+
+def test_large_strain_option_is_fp64_only():
+    st = scenes.mixed_small(seed=5)
+    with engine.Engine.from_state(st, engine.FORM_FP32) as e:
+        with pytest.raises(engine.MPMError):
+            e.set_option(engine.OPT_LARGE_STRAIN, 1)
+
+
 def test_cell_keys_and_order_bit_exact(golden):
     st = golden("mixed_in")
     with engine.Engine.from_state(st) as e:
