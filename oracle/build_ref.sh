@@ -96,6 +96,8 @@ build() {
 
 build ref_seq ""
 build ref_seq_ls "" -DMPM_REF_LARGE_STRAIN
+# the reference's 2D voxel canvas (Canvas2D_CC.cpp, as shipped) with its driver
+"$CXX" "${BASE[@]}" "$REF/Canvas2D_CC.cpp" "$HERE/canvas_driver.cpp" -o "$OUT/ref_canvas"
 build ref_omp "" -fopenmp
 build "ref_omp$NTH" "$NTH" -fopenmp
 echo "built: $(ls "$OUT")"

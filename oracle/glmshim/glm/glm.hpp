@@ -32,6 +32,9 @@ template <typename T> struct vec<2, T> {
     template <typename A, typename B>
     vec(A a, B b) : x(static_cast<T>(a)), y(static_cast<T>(b)) {}
     template <typename U> vec(const vec<2, U>& o) : x(static_cast<T>(o.x)), y(static_cast<T>(o.y)) {}
+    // the first two components of a longer vector (glm's explicit truncation)
+    template <int L, typename U, typename = typename std::enable_if<(L > 2)>::type>
+    explicit vec(const vec<L, U>& o) : x(static_cast<T>(o[0])), y(static_cast<T>(o[1])) {}
     T& operator[](int i) { return (&x)[i]; }
     const T& operator[](int i) const { return (&x)[i]; }
     static constexpr int length() { return 2; }
@@ -53,6 +56,8 @@ template <typename T> struct vec<3, T> {
     static constexpr int length() { return 3; }
 };
 
+template <typename T> struct vec<4, T>;
+
 template <typename T> struct vec<4, T> {
     T x, y, z, w;
     vec() : x(0), y(0), z(0), w(0) {}
@@ -63,6 +68,9 @@ template <typename T> struct vec<4, T> {
         : x(static_cast<T>(a)), y(static_cast<T>(b)), z(static_cast<T>(c)), w(static_cast<T>(d)) {}
     template <typename U, typename D>
     vec(const vec<3, U>& v, D d) : x(static_cast<T>(v.x)), y(static_cast<T>(v.y)), z(static_cast<T>(v.z)), w(static_cast<T>(d)) {}
+    template <typename U, typename C, typename D>
+    vec(const vec<2, U>& v, C c, D d)
+        : x(static_cast<T>(v.x)), y(static_cast<T>(v.y)), z(static_cast<T>(c)), w(static_cast<T>(d)) {}
     template <typename U>
     vec(const vec<4, U>& o) : x(static_cast<T>(o.x)), y(static_cast<T>(o.y)), z(static_cast<T>(o.z)), w(static_cast<T>(o.w)) {}
     T& operator[](int i) { return (&x)[i]; }
@@ -272,6 +280,58 @@ template <typename T> mat3x3<T> outerProduct(const vec<3, T>& c, const vec<3, T>
     mat3x3<T> m(T(0));
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j) m[i][j] = c[j] * r[i];
+    return m;
+}
+
+// ---- 4x4 matrix (column-major), for the canvas transforms ------------------
+template <typename T> struct mat4x4 {
+    vec<4, T> c[4];
+    mat4x4() { *this = mat4x4(T(1)); }
+    template <typename S, typename = typename std::enable_if<std::is_arithmetic<S>::value>::type>
+    explicit mat4x4(S s) {
+        for (int i = 0; i < 4; ++i)
+            for (int j = 0; j < 4; ++j) c[i][j] = (i == j) ? static_cast<T>(s) : T(0);
+    }
+    vec<4, T>& operator[](int i) { return c[i]; }
+    const vec<4, T>& operator[](int i) const { return c[i]; }
+    mat4x4& operator*=(const mat4x4& o);
+};
+typedef mat4x4<double> dmat4;
+typedef mat4x4<float> mat4;
+
+// (A*B)[c][r] = ((A[0][r]*B[c][0] + A[1][r]*B[c][1]) + A[2][r]*B[c][2]) + A[3][r]*B[c][3]
+template <typename T> mat4x4<T> operator*(const mat4x4<T>& a, const mat4x4<T>& b) {
+    mat4x4<T> r(T(0));
+    for (int col = 0; col < 4; ++col)
+        for (int row = 0; row < 4; ++row)
+            r[col][row] = a[0][row] * b[col][0] + a[1][row] * b[col][1] + a[2][row] * b[col][2] + a[3][row] * b[col][3];
+    return r;
+}
+template <typename T> mat4x4<T>& mat4x4<T>::operator*=(const mat4x4<T>& o) { return (*this = *this * o); }
+// (M*v)[r] = ((M[0][r]*v.x + M[1][r]*v.y) + M[2][r]*v.z) + M[3][r]*v.w
+template <typename T> vec<4, T> operator*(const mat4x4<T>& m, const vec<4, T>& v) {
+    vec<4, T> r;
+    for (int row = 0; row < 4; ++row) r[row] = m[0][row] * v.x + m[1][row] * v.y + m[2][row] * v.z + m[3][row] * v.w;
+    return r;
+}
+// translation by v: the identity with v in the last column
+template <typename T> mat4x4<T> translate(const vec<3, T>& v) {
+    mat4x4<T> m(T(1));
+    m[3][0] = v.x;
+    m[3][1] = v.y;
+    m[3][2] = v.z;
+    return m;
+}
+// rotation by `angle` (radians) about the unit vector along `axis`:
+// R = cos(a) I + (1 - cos(a)) n n^T + sin(a) [n]x (Rodrigues' formula)
+template <typename T> mat4x4<T> rotate(T angle, const vec<3, T>& axis) {
+    const T cs = std::cos(angle), sn = std::sin(angle);
+    const vec<3, T> n = normalize(axis);
+    mat4x4<T> m(T(1));
+    const T k[3][3] = {{T(0), -n.z, n.y}, {n.z, T(0), -n.x}, {-n.y, n.x, T(0)}};  // [n]x by row
+    for (int col = 0; col < 3; ++col)
+        for (int row = 0; row < 3; ++row)
+            m[col][row] = (col == row ? cs : T(0)) + (T(1) - cs) * n[row] * n[col] + sn * k[row][col];
     return m;
 }
 

@@ -1,2 +1,3 @@
-// The reference includes <glm/gtx/transform.hpp>; nothing from it is used on the solver path.
+// The reference includes <glm/gtx/transform.hpp>; translate and rotate (used
+// by its Canvas2D voxeliser, not by the solver path) are in ../glm.hpp.
 #include "../glm.hpp"
