@@ -42,7 +42,7 @@ def test_library_exports_every_declared_symbol(so):
 def test_python_bindings_cover_the_header(so):
     engine.lib()  # loads and sets every signature
     names = declared_functions()
-    src = open(os.path.join(ROOT, "code_mpm_gb300", "engine.py")).read()
+    src = "".join(open(os.path.join(ROOT, "code_mpm_gb300", f)).read() for f in ("engine.py", "canvas.py"))
     unbound = [n for n in names if f'"{n}"' not in src]
     assert not unbound, unbound
 
