@@ -33,6 +33,7 @@ struct CanvasOp {
     double m00, m10, m30, m01, m11, m31;  // rows 0 and 1 of M (rectangle, prism)
     double hx, hy;                        // half sizes 0.5*sx, 0.5*sy
     double sx, half_extra;                // prism: sx and 0.5*extra
+    double reach;  // circle and ring: no voxel with |dx| or |dy| above it is changed by the operation
 };
 
 constexpr int CV_THREADS = 256, CV_PER_THREAD = 16, CV_TILE = CV_THREADS * CV_PER_THREAD;
@@ -52,6 +53,7 @@ __global__ void k_canvas_apply(uint8_t* __restrict__ flags, unsigned nx, long lo
             const CanvasOp& o = ops[k];
             if (o.kind == CV_CIRCLE || o.kind == CV_CUT_CIRCLE || o.kind == CV_RING) {
                 const double dx = __dadd_rn(x, -o.cx), dy = __dadd_rn(y, -o.cy);
+                if (fabs(dx) > o.reach || fabs(dy) > o.reach) continue;
                 const double d = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
                 if (o.kind == CV_CIRCLE) {
                     if (!(d > o.r0)) f |= MPM_VOXEL_ACTIVE;
@@ -277,6 +279,7 @@ int mpm_canvas_draw_circle(mpm_canvas* c, double cx, double cy, double radius) {
     o.cx = cx;
     o.cy = cy;
     o.r0 = radius;
+    o.reach = std::fabs(radius) * (1.0 + 1.0e-9);  // d >= |dx| up to rounding: a margin far above it
     return queue(c, o);
 }
 
@@ -286,6 +289,7 @@ int mpm_canvas_cut_circle(mpm_canvas* c, double cx, double cy, double radius) {
     o.cx = cx;
     o.cy = cy;
     o.r0 = radius;
+    o.reach = std::fabs(radius) * (1.0 + 1.0e-9);
     return queue(c, o);
 }
 
@@ -299,6 +303,7 @@ int mpm_canvas_draw_ring(mpm_canvas* c, double cx, double cy, double radius_oute
     o.ri = radius_inner;
     o.r0 = radius_inner + 0.5 * c->offset;
     o.r1 = radius_outer - 0.5 * c->offset;
+    o.reach = std::fabs(radius_outer);  // the ring takes d <= r_outer - offset/2
     return queue(c, o);
 }
 
