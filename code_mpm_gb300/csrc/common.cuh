@@ -193,10 +193,9 @@ struct PView {
 // Node arrays: structure of arrays, component a of node i at [a*nn + i].
 template <typename T>
 struct NView {
-    T* mass;
-    T* mom;
+    T* acc;            // per node 8 values {m, p[3], f[3], 0}: the accumulated mass, momentum and force
+                       // interleaved, so one node's are one or two aligned vectors (P2G adds them as such)
     T* vel;
-    T* force;
     T* ftemp;
     T* mg;             // mass gradient (contact path), the form's type
     unsigned* state;   // MPM_NS_* bits
@@ -217,6 +216,25 @@ template <typename T>
 struct alignas(4 * sizeof(T)) Quad {
     T x, y, z, w;
 };
+
+// Adds a contribution to node i's accumulator record: two vector atomics in
+// FP32 (one sector), seven scalar ones in FP64.
+template <typename T>
+__device__ __forceinline__ void acc_add(T* acc, long long i, T m, T p0, T p1, T p2, T f0, T f1, T f2) {
+    T* a = acc + 8 * i;
+    if constexpr (sizeof(T) == 4) {
+        atomicAdd(reinterpret_cast<float4*>(a), make_float4(m, p0, p1, p2));
+        atomicAdd(reinterpret_cast<float4*>(a + 4), make_float4(f0, f1, f2, 0.0f));
+    } else {
+        atomicAdd(a, m);
+        atomicAdd(a + 1, p0);
+        atomicAdd(a + 2, p1);
+        atomicAdd(a + 3, p2);
+        atomicAdd(a + 4, f0);
+        atomicAdd(a + 5, f1);
+        atomicAdd(a + 6, f2);
+    }
+}
 
 template <typename T>
 __device__ __forceinline__ Quad<T> ld_quad(const T* __restrict__ p) {

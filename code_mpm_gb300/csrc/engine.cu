@@ -78,7 +78,7 @@ struct mpm_ctx {
         backstress, mp_mg, strain_rate, material, pflags, dc_mult,
         Fe;  // FP64 form: elastic deformation gradient (large-strain pass 2)
     // nodes
-    DevBuf g_mass, g_mom, g_vel, g_force, g_ftemp, g_mg, g_state, g_fixed, g_friction, g_ratio, g_q, g_owner,
+    DevBuf g_acc, g_vel, g_ftemp, g_mg, g_state, g_fixed, g_friction, g_ratio, g_q, g_owner,
         g_nowner, g_need, g_list, g_count, rs_chunk;
     int sm_count = 152;
     DevBuf cstart, cend;
@@ -134,7 +134,7 @@ struct mpm_ctx {
     mpm_ctx() {
         DevBuf* list[] = {&xtab, &err_word, &pos, &vel, &fext, &mass, &vol, &vol0, &F, &stress, &strain, &eps_p,
                           &e_strain, &e_strain_max, &e_strain_ti, &e_plastic, &backstress, &mp_mg, &strain_rate,
-                          &material, &pflags, &dc_mult, &g_mass, &g_mom, &g_vel, &g_force, &g_ftemp, &g_mg,
+                          &material, &pflags, &dc_mult, &g_acc, &g_vel, &g_ftemp, &g_mg,
                           &g_state, &g_fixed, &g_friction, &g_ratio, &g_q, &g_owner, &g_nowner, &g_need, &g_list, &g_count, &rs_chunk, &cstart,
                           &cend, &keys0, &vals0, &keys1, &vals1, &keys_copy, &counts, &dclist, &mats, &staging, &tune_backup, &surf, &mon_mask, &mon_acc, &loc, &geom_tab, &sid, &alist, &acount,
                           &q_in, &q_out, &q_vol, &q_pidx, &q_count, &sg_acc, &hv_count,
@@ -210,10 +210,8 @@ PView<T> pview(mpm_ctx* c) {
 template <typename T>
 NView<T> nview(mpm_ctx* c) {
     NView<T> v;
-    v.mass = (T*)c->g_mass.p;
-    v.mom = (T*)c->g_mom.p;
+    v.acc = (T*)c->g_acc.p;
     v.vel = (T*)c->g_vel.p;
-    v.force = (T*)c->g_force.p;
     v.ftemp = (T*)c->g_ftemp.p;
     v.mg = (T*)c->g_mg.p;
     v.state = (unsigned*)c->g_state.p;
@@ -340,25 +338,28 @@ void timeline_velocity(const mpm_ctx* c, double t, double out[3]) {
 // ---- unpack / pack between host n x k row-major doubles and device SoA -----
 // shift_identity: the FP32 form stores a 3x3 F as H = F - I (diagonal
 // components 0, 4, 8 shifted by one, in FP64 before the conversion).
+// Device layout: component c of item p at c * cs + p * ps (structure of arrays:
+// cs = n, ps = 1; a node's interleaved accumulator record: cs = 1, ps = 8).
 template <typename T>
-__global__ void k_unpack(const double* __restrict__ src, T* __restrict__ dst, long long n, int k, int shift_identity) {
+__global__ void k_unpack(const double* __restrict__ src, T* __restrict__ dst, long long n, int k, int shift_identity,
+                         long long cs, long long ps) {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= n * k) return;
     long long p = i / k;
     int c = (int)(i - p * k);
     double v = src[i];
     if (shift_identity && (c == 0 || c == 4 || c == 8)) v -= 1.0;
-    dst[(long long)c * n + p] = (T)v;
+    dst[(long long)c * cs + p * ps] = (T)v;
 }
 // device SoA (slot order) -> host rows; with orig, slot s goes to the caller's row orig[s]
 template <typename T>
 __global__ void k_pack(const T* __restrict__ src, double* __restrict__ dst, long long n, int k, int shift_identity,
-                       const unsigned* __restrict__ orig) {
+                       const unsigned* __restrict__ orig, long long cs, long long ps) {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= n * k) return;
     long long s = i / k;
     int c = (int)(i - s * k);
-    double v = (double)src[(long long)c * n + s];
+    double v = (double)src[(long long)c * cs + s * ps];
     if (shift_identity && (c == 0 || c == 4 || c == 8)) v += 1.0;
     dst[(orig ? (long long)orig[s] : s) * k + c] = v;
 }
@@ -486,22 +487,28 @@ __global__ void k_clear_flag(uint8_t* __restrict__ pflags, long long n, uint8_t 
 }
 
 // Upload one field: host n x k doubles (or NULL -> default) into a device SoA array of the field's real type.
+// Upload one field from host rows into a structure-of-arrays buffer, or with
+// acc_comp >= 0 into components acc_comp .. acc_comp + k - 1 of the nodes'
+// interleaved accumulator records (dst = g_acc, already allocated).
 int upload_field(mpm_ctx* c, DevBuf& dst, const double* host, long long n, int k, bool fp64, double def,
-                 int shift_identity = 0) {
+                 int shift_identity = 0, int acc_comp = -1) {
     size_t esz = fp64 ? 8 : 4;
-    int rc = ensure(c, dst, (size_t)n * k * esz);
+    const bool acc = acc_comp >= 0;
+    const long long off = acc ? acc_comp : 0, cs = acc ? 1 : n, ps = acc ? 8 : 1;
+    int rc = acc ? MPM_OK : ensure(c, dst, (size_t)n * k * esz);
     if (rc) return rc;
     if (n == 0) return MPM_OK;
+    if (acc && !host) return MPM_OK;  // accumulator components are only written from host rows
     if (host) {
         rc = ensure(c, c->staging, (size_t)n * k * 8);
         if (rc) return rc;
         CK(cudaMemcpyAsync(c->staging.p, host, (size_t)n * k * 8, cudaMemcpyHostToDevice, c->stream));
         if (fp64)
             LAUNCH("unpack", k_unpack<double>, blocks_for(n * k), NTHREADS, (const double*)c->staging.p,
-                   (double*)dst.p, n, k, shift_identity);
+                   (double*)dst.p + off, n, k, shift_identity, cs, ps);
         else
             LAUNCH("unpack", k_unpack<float>, blocks_for(n * k), NTHREADS, (const double*)c->staging.p,
-                   (float*)dst.p, n, k, shift_identity);
+                   (float*)dst.p + off, n, k, shift_identity, cs, ps);
     } else if (def == 0.0) {
         CK(cudaMemsetAsync(dst.p, 0, (size_t)n * k * esz, c->stream));
     } else if (fp64) {
@@ -516,17 +523,19 @@ int upload_field(mpm_ctx* c, DevBuf& dst, const double* host, long long n, int k
 // through the slot -> caller-index map when the slots are in cell order;
 // node fields never do.
 int download_field(mpm_ctx* c, const DevBuf& src, double* host, long long n, int k, bool fp64,
-                   int shift_identity = 0, bool particles = false) {
+                   int shift_identity = 0, bool particles = false, int acc_comp = -1) {
     if (!host || n == 0) return MPM_OK;
     int rc = ensure(c, c->staging, (size_t)n * k * 8);
     if (rc) return rc;
     const unsigned* orig = (particles && c->have_orig) ? (const unsigned*)c->orig.p : nullptr;
+    const bool acc = acc_comp >= 0;
+    const long long off = acc ? acc_comp : 0, cs = acc ? 1 : n, ps = acc ? 8 : 1;
     if (fp64)
-        LAUNCH("pack", k_pack<double>, blocks_for(n * k), NTHREADS, (const double*)src.p, (double*)c->staging.p, n,
-               k, shift_identity, orig);
+        LAUNCH("pack", k_pack<double>, blocks_for(n * k), NTHREADS, (const double*)src.p + off, (double*)c->staging.p,
+               n, k, shift_identity, orig, cs, ps);
     else
-        LAUNCH("pack", k_pack<float>, blocks_for(n * k), NTHREADS, (const float*)src.p, (double*)c->staging.p, n, k,
-               shift_identity, orig);
+        LAUNCH("pack", k_pack<float>, blocks_for(n * k), NTHREADS, (const float*)src.p + off, (double*)c->staging.p,
+               n, k, shift_identity, orig, cs, ps);
     CK(cudaMemcpyAsync(host, c->staging.p, (size_t)n * k * 8, cudaMemcpyDeviceToHost, c->stream));
     return MPM_OK;
 }
@@ -1201,8 +1210,8 @@ int mpm_create_batch(const mpm_grid_desc* grids, int32_t nspec, int form, mpm_ct
     struct {
         DevBuf* b;
         size_t bytes;
-    } plan[] = {{&c->g_mass, nn * t},      {&c->g_mom, 3 * nn * t},  {&c->g_vel, 3 * nn * t},
-                {&c->g_force, 3 * nn * t}, {&c->g_ftemp, 3 * nn * t}, {&c->g_mg, 3 * nn * t},
+    } plan[] = {{&c->g_acc, 8 * nn * t},   {&c->g_vel, 3 * nn * t},
+                {&c->g_ftemp, 3 * nn * t}, {&c->g_mg, 3 * nn * t},
                 {&c->g_state, nn * 4},     {&c->g_fixed, nn},        {&c->g_friction, nn * 8},
                 {&c->g_ratio, 8 * nn * t}, {&c->g_q, 3 * nn * t},    {&c->g_owner, 3 * nn * 4},
                 {&c->g_nowner, nn * 4},    {&c->g_need, nn * 4},     {&c->g_list, nn * 4},
@@ -1496,12 +1505,12 @@ int mpm_upload_nodes(mpm_ctx* c, const mpm_nodes* nd) {
         DevBuf* b;
         const double* h;
         int k;
-        bool fp64;
-    } fields[] = {{&c->g_mass, nd->mass, 1, f64},  {&c->g_mom, nd->mom, 3, f64},
-                  {&c->g_vel, nd->vel, 3, f64},    {&c->g_force, nd->force, 3, f64},
-                  {&c->g_ftemp, nd->force_temp, 3, f64}, {&c->g_mg, nd->mass_gradient, 3, f64}};
+        int acc;  // component of the accumulator record, or -1
+    } fields[] = {{&c->g_acc, nd->mass, 1, 0},   {&c->g_acc, nd->mom, 3, 1},
+                  {&c->g_vel, nd->vel, 3, -1},   {&c->g_acc, nd->force, 3, 4},
+                  {&c->g_ftemp, nd->force_temp, 3, -1}, {&c->g_mg, nd->mass_gradient, 3, -1}};
     for (auto& f : fields)
-        if (f.h && (rc = upload_field(c, *f.b, f.h, nn, f.k, f.fp64, 0.0))) return rc;
+        if (f.h && (rc = upload_field(c, *f.b, f.h, nn, f.k, f64, 0.0, 0, f.acc))) return rc;
     if (nd->state) {
         int rc2 = ensure(c, c->staging, (size_t)nn);
         if (rc2) return rc2;
@@ -1619,13 +1628,13 @@ int mpm_download_nodes(mpm_ctx* c, mpm_nodes* nd) {
         DevBuf* b;
         double* h;
         int k;
-        bool fp64;
-    } fields[] = {{&c->g_mass, nd->mass, 1, f64},  {&c->g_mom, nd->mom, 3, f64},
-                  {&c->g_vel, nd->vel, 3, f64},    {&c->g_force, nd->force, 3, f64},
-                  {&c->g_ftemp, nd->force_temp, 3, f64}, {&c->g_mg, nd->mass_gradient, 3, f64}};
+        int acc;  // component of the accumulator record, or -1
+    } fields[] = {{&c->g_acc, nd->mass, 1, 0},   {&c->g_acc, nd->mom, 3, 1},
+                  {&c->g_vel, nd->vel, 3, -1},   {&c->g_acc, nd->force, 3, 4},
+                  {&c->g_ftemp, nd->force_temp, 3, -1}, {&c->g_mg, nd->mass_gradient, 3, -1}};
     for (auto& f : fields) {
         if (!f.h) continue;
-        if ((rc = download_field(c, *f.b, f.h, nn, f.k, f.fp64))) return rc;
+        if ((rc = download_field(c, *f.b, f.h, nn, f.k, f64, 0, false, f.acc))) return rc;
         CK(cudaStreamSynchronize(c->stream));
     }
     if (nd->fixed) CK(cudaMemcpyAsync(nd->fixed, c->g_fixed.p, (size_t)nn, cudaMemcpyDeviceToHost, c->stream));
@@ -1812,8 +1821,8 @@ int mpm_autotune(mpm_ctx* c, int32_t steps, double dt, int contact, mpm_tune_res
     // everything a step writes that outlives the step
     DevBuf* state[] = {&c->pos,        &c->vel,      &c->F,          &c->stress,  &c->strain,  &c->eps_p,
                        &c->vol,        &c->e_strain, &c->e_strain_max, &c->e_strain_ti, &c->e_plastic,
-                       &c->backstress, &c->mp_mg,    &c->strain_rate, &c->g_mass, &c->g_mom,   &c->g_vel,
-                       &c->g_force,    &c->g_ftemp,  &c->g_mg,       &c->g_state};
+                       &c->backstress, &c->mp_mg,    &c->strain_rate, &c->g_acc,   &c->g_vel,
+                       &c->g_ftemp,  &c->g_mg,       &c->g_state};
     size_t total = 0;
     for (DevBuf* b : state) total += b->bytes;
     int rc = ensure(c, c->tune_backup, total);

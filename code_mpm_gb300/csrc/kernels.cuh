@@ -35,13 +35,13 @@ __global__ void k_reset_grid(NView<T> nd, int contact) {
         unsigned st = nd.state[i];
         if (!(st & 1u)) continue;
         nd.state[i] = contact ? 0u : (st & ~(1u | NODE_CLAIMED));
-        nd.mass[i] = (T)0;
+        const Quad<T> z{(T)0, (T)0, (T)0, (T)0};
+        *reinterpret_cast<Quad<T>*>(nd.acc + 8 * i) = z;
+        *reinterpret_cast<Quad<T>*>(nd.acc + 8 * i + 4) = z;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             if (contact) nd.mg[c * nn + i] = 0.0;
             nd.vel[c * nn + i] = (T)0;
-            nd.mom[c * nn + i] = (T)0;
-            nd.force[c * nn + i] = (T)0;
             nd.ftemp[c * nn + i] = (T)0;
         }
     }
@@ -247,13 +247,7 @@ __global__ void __launch_bounds__(512) k_p2g(PView<T> P, NView<T> nd, Geom g, co
             long long nid = corner_node(*gsp, b, k);
             if (nid >= 0) {
                 if (mark_active && !(nd.state[nid] & 1u)) atomicOr(&nd.state[nid], 1u);
-                atomicAdd(&nd.mass[nid], c[0]);
-                atomicAdd(&nd.mom[nid], c[1]);
-                atomicAdd(&nd.mom[nn + nid], c[2]);
-                atomicAdd(&nd.mom[2 * nn + nid], c[3]);
-                atomicAdd(&nd.force[nid], c[4]);
-                atomicAdd(&nd.force[nn + nid], c[5]);
-                atomicAdd(&nd.force[2 * nn + nid], c[6]);
+                acc_add<T>(nd.acc, nid, c[0], c[1], c[2], c[3], c[4], c[5], c[6]);
                 if (nf == 10) {
                     atomicAdd(&nd.mg[nid], c[7]);
                     atomicAdd(&nd.mg[nn + nid], c[8]);
@@ -444,19 +438,13 @@ struct P2GBlock {
                     }
                 }
             }
-    #pragma unroll
+#pragma unroll
             for (int j = 0; j < CPT; ++j) {
                 const long long nid = cs.node(a, k0 + j);
                 if (nid < 0) continue;
                 // active nodes: the in-range corners of occupied cells (b_Active, …MPLocks.cpp:36)
                 if (mark_active && !(nd.state[nid] & 1u)) atomicOr(&nd.state[nid], 1u);
-                atomicAdd(&nd.mass[nid], am[j]);
-                atomicAdd(&nd.mom[nid], ap0[j]);
-                atomicAdd(&nd.mom[nn + nid], ap1[j]);
-                atomicAdd(&nd.mom[2 * nn + nid], ap2[j]);
-                atomicAdd(&nd.force[nid], af0[j]);
-                atomicAdd(&nd.force[nn + nid], af1[j]);
-                atomicAdd(&nd.force[2 * nn + nid], af2[j]);
+                acc_add<T>(nd.acc, nid, am[j], ap0[j], ap1[j], ap2[j], af0[j], af1[j], af2[j]);
                 if constexpr (MG) {
                     atomicAdd(&nd.mg[nid], g0[j]);
                     atomicAdd(&nd.mg[nn + nid], g1[j]);
@@ -864,13 +852,9 @@ __global__ void __launch_bounds__(256, 4) k_node_phase_a(NView<T> nd, T dt, doub
     NODE_LOOP(nd, i) {
         const unsigned st = nd.state[i];
         if (!(st & 1u)) continue;
-        const T m = nd.mass[i];
-        T p[3], f[3], v[3] = {0, 0, 0};
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            p[c] = nd.mom[c * nn + i];
-            f[c] = nd.force[c * nn + i];
-        }
+        const Quad<T> a0 = ld_quad(nd.acc + 8 * i), a1 = ld_quad(nd.acc + 8 * i + 4);
+        const T m = a0.x;
+        T p[3] = {a0.y, a0.z, a0.w}, f[3] = {a1.x, a1.y, a1.z}, v[3] = {0, 0, 0};
         const unsigned fx = nd.fixed[i];
         unsigned own[3] = {0u, 0u, 0u};
         if (ndc && (st & NODE_CLAIMED)) {
@@ -899,13 +883,15 @@ __global__ void __launch_bounds__(256, 4) k_node_phase_a(NView<T> nd, T dt, doub
             for (int c = 0; c < 3; ++c)
                 if (fz[c]) f[c] = (T)0;
         }
-        if (clean) nd.mass[i] = (T)0;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            nd.mom[c * nn + i] = clean ? (T)0 : p[c];
-            nd.force[c * nn + i] = clean ? (T)0 : f[c];
-            if (vset[c]) nd.vel[c * nn + i] = v[c];
+        {
+            const Quad<T> w0{clean ? (T)0 : m, clean ? (T)0 : p[0], clean ? (T)0 : p[1], clean ? (T)0 : p[2]};
+            const Quad<T> w1{clean ? (T)0 : f[0], clean ? (T)0 : f[1], clean ? (T)0 : f[2], (T)0};
+            *reinterpret_cast<Quad<T>*>(nd.acc + 8 * i) = w0;
+            *reinterpret_cast<Quad<T>*>(nd.acc + 8 * i + 4) = w1;
         }
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            if (vset[c]) nd.vel[c * nn + i] = v[c];
         if (fx & 2u) nd.ftemp[nn + i] += ft_y;
         const bool has = m > mass_min;
         Quad<T> r, pm;
@@ -993,8 +979,8 @@ __global__ void __launch_bounds__(256, 4) k_node_phase_b(NView<T> nd, int contac
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 nd.vel[c * nn + i] = v[c];
-                nd.mom[c * nn + i] = p[c];
-                if (fz[c]) nd.force[c * nn + i] = (T)0;
+                nd.acc[8 * i + 1 + c] = p[c];
+                if (fz[c]) nd.acc[8 * i + 4 + c] = (T)0;
             }
             if (st & NODE_CLAIMED) nd.state[i] = st & ~NODE_CLAIMED;
         }
