@@ -203,7 +203,7 @@ struct NView {
     double* friction;
     T* rec;            // scratch: per node 8 values {r, has, v, 0}: r = f/m before pass 1, p/m before
                        // pass 2; has = 1 when m > mass_min; v = node velocity (pass 2 only)
-    T* q;              // scratch: remap accumulator sum N m_p v_p
+    T* q;              // scratch: remap accumulator sum N m_p v_p, 4 values per node {q[3], 0}
     unsigned* owner;   // scratch: displacement-control last-writer claims, 3 x nn
     unsigned* nowner;  // scratch: contact-normal last-writer claims, nn
     const unsigned* alist;   // active nodes of this step (null: sweep every node)
@@ -216,6 +216,19 @@ template <typename T>
 struct alignas(4 * sizeof(T)) Quad {
     T x, y, z, w;
 };
+
+// Adds to node i's remap accumulator {q[3], 0}: one vector atomic in FP32.
+template <typename T>
+__device__ __forceinline__ void q_add(T* q, long long i, T q0, T q1, T q2) {
+    T* a = q + 4 * i;
+    if constexpr (sizeof(T) == 4) {
+        atomicAdd(reinterpret_cast<float4*>(a), make_float4(q0, q1, q2, 0.0f));
+    } else {
+        atomicAdd(a, q0);
+        atomicAdd(a + 1, q1);
+        atomicAdd(a + 2, q2);
+    }
+}
 
 // Adds a contribution to node i's accumulator record: two vector atomics in
 // FP32 (one sector), seven scalar ones in FP64.

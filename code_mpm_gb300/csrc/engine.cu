@@ -1213,7 +1213,7 @@ int mpm_create_batch(const mpm_grid_desc* grids, int32_t nspec, int form, mpm_ct
     } plan[] = {{&c->g_acc, 8 * nn * t},   {&c->g_vel, 3 * nn * t},
                 {&c->g_ftemp, 3 * nn * t}, {&c->g_mg, 3 * nn * t},
                 {&c->g_state, nn * 4},     {&c->g_fixed, nn},        {&c->g_friction, nn * 8},
-                {&c->g_ratio, 8 * nn * t}, {&c->g_q, 3 * nn * t},    {&c->g_owner, 3 * nn * 4},
+                {&c->g_ratio, 8 * nn * t}, {&c->g_q, 4 * nn * t},    {&c->g_owner, 3 * nn * 4},
                 {&c->g_nowner, nn * 4},    {&c->g_need, nn * 4},     {&c->g_list, nn * 4},
                 {&c->g_count, 4},          {&c->alist, nn * 4},       {&c->acount, 4},
                 // per-cell particle ranges: the FP64 form's exact contact gather only

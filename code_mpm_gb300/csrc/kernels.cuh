@@ -694,9 +694,7 @@ __global__ void __launch_bounds__(256) k_pass1_remap(PView<T> P, NView<T> nd, Ge
         if (key_ok && run.tail) {
             long long nid = corner_node(*gsp, b, k);
             if (nid >= 0) {
-                atomicAdd(&nd.q[nid], q0);
-                atomicAdd(&nd.q[nn + nid], q1);
-                atomicAdd(&nd.q[2 * nn + nid], q2);
+                q_add<T>(nd.q, nid, q0, q1, q2);
             }
         }
     }
@@ -811,9 +809,7 @@ __global__ void __launch_bounds__(BS) k_pass1_cells(PView<T> P, NView<T> nd, Geo
         for (int j = 0; j < CPT; ++j) {
             const long long nid = cs.node(a, k0 + j);
             if (nid < 0) continue;
-            atomicAdd(&nd.q[nid], q0[j]);
-            atomicAdd(&nd.q[nn + nid], q1[j]);
-            atomicAdd(&nd.q[2 * nn + nid], q2[j]);
+            q_add<T>(nd.q, nid, q0[j], q1[j], q2[j]);
         }
     }
 }
@@ -905,11 +901,12 @@ __global__ void __launch_bounds__(256, 4) k_node_phase_a(NView<T> nd, T dt, doub
         pm.w = m;
         *reinterpret_cast<Quad<T>*>(nd.rec + 8 * i) = r;
         *reinterpret_cast<Quad<T>*>(nd.rec + 8 * i + 4) = pm;
+        *reinterpret_cast<Quad<T>*>(nd.q + 4 * i) = Quad<T>{(T)0, (T)0, (T)0, (T)0};  // for pass 1's remap sums
     }
 }
 
 // The node work between pass 1 and pass 2, in registers: the remap v += q/m
-// (:559-560; q is cleared here for the next step's pass 1), displacement
+// (:559-560; phase A cleared q before pass 1 summed it), displacement
 // control and BC (:573-599) in the path's order, then the record (p/m,
 // m > m_min, v).  The claims are cleared after this last use (every claimed
 // node is active: platen particles take part in P2G).  clean: a step whose
@@ -932,12 +929,12 @@ __global__ void __launch_bounds__(256, 4) k_node_phase_b(NView<T> nd, int contac
         // here unless phase A set it, which it does on fixed or claimed nodes only
         const bool vel_set = !vel_zero || fx != 0u || (st & NODE_CLAIMED);
         T v[3], p[3] = {pm.x, pm.y, pm.z};
+        const Quad<T> q4 = ld_quad(nd.q + 4 * i);  // cleared by phase A, summed by pass 1
+        const T q[3] = {q4.x, q4.y, q4.z};
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             v[c] = vel_set ? nd.vel[c * nn + i] : (T)0;
-            const T q = nd.q[c * nn + i];
-            if (has) v[c] = v[c] + q / m;
-            nd.q[c * nn + i] = (T)0;
+            if (has) v[c] = v[c] + q[c] / m;
         }
         unsigned own[3] = {0u, 0u, 0u};
         if (ndc && (st & NODE_CLAIMED)) {
