@@ -845,9 +845,9 @@ __global__ void __launch_bounds__(256, 4) k_node_phase_a(NView<T> nd, T dt, doub
                                const unsigned* __restrict__ dclist, int ndc, const T* __restrict__ pvel, long long np,
                                T mass_min, int clean) {
     const long long nn = nd.nn;
-    NODE_LOOP(nd, i) {
+    NODE_LOOP_AHEAD(nd, i) {
         const unsigned st = nd.state[i];
-        if (!(st & 1u)) continue;
+        if (!nd.alist && !(st & 1u)) continue;  // the list holds active nodes only
         const Quad<T> a0 = ld_quad(nd.acc + 8 * i), a1 = ld_quad(nd.acc + 8 * i + 4);
         const T m = a0.x;
         T p[3] = {a0.y, a0.z, a0.w}, f[3] = {a1.x, a1.y, a1.z}, v[3] = {0, 0, 0};
@@ -917,9 +917,9 @@ template <typename T>
 __global__ void __launch_bounds__(256, 4) k_node_phase_b(NView<T> nd, int contact, const unsigned* __restrict__ dclist, int ndc,
                                const T* __restrict__ pvel, long long np, T mass_min, int clean, int vel_zero) {
     const long long nn = nd.nn;
-    NODE_LOOP(nd, i) {
+    NODE_LOOP_AHEAD(nd, i) {
         const unsigned st = nd.state[i];
-        if (!(st & 1u)) continue;
+        if (!nd.alist && !(st & 1u)) continue;  // the list holds active nodes only
         const Quad<T> pm = ld_quad(nd.rec + 8 * i + 4);  // phase A's momentum and mass
         const T m = pm.w;
         const bool has = m > mass_min;
