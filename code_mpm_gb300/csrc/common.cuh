@@ -13,6 +13,7 @@ constexpr unsigned FULL_MASK = 0xffffffffu;
 // Bits of the sticky device error word.
 constexpr unsigned ERR_NONFINITE_POSITION = 1u;
 constexpr unsigned ERR_BAD_MATERIAL = 2u;
+constexpr unsigned ERR_WAIT_TIMEOUT = 4u;  // a kernel's bounded wait on an mbarrier ran out
 
 // Internal particle flag: member of the displacement-control list.
 constexpr unsigned PF_IN_DC = 32u;

@@ -549,6 +549,7 @@ int check_device_error(mpm_ctx* c) {
         std::string what;
         if (e & ERR_NONFINITE_POSITION) what += " non-finite particle position;";
         if (e & ERR_BAD_MATERIAL) what += " particle without a valid material;";
+        if (e & ERR_WAIT_TIMEOUT) what += " a kernel's wait for its bulk copies or tensor-core work timed out;";
         return fail(c, MPM_ERR_DEVICE, "device reported:%s", what.c_str());
     }
     return MPM_OK;
@@ -901,12 +902,24 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph, bool output) {
                 }
             }
             if (large) {
+            } else if (c->gather_batch == 2 && sizeof(T) == 4) {
+                if constexpr (sizeof(T) == 4) {
+                    if (c->pass_block == 128)
+                        LAUNCH_SMEM("pass2", k_pass2_staged<128>, pb, 128, Pass2Stage<128>::SMEM, P, N, g, kc,
+                                    keys_next, mats, c->nmat, a, err);
+                    else if (c->pass_block == 256)
+                        LAUNCH_SMEM("pass2", k_pass2_staged<256>, pb, 256, Pass2Stage<256>::SMEM, P, N, g, kc,
+                                    keys_next, mats, c->nmat, a, err);
+                    else
+                        LAUNCH_SMEM("pass2", k_pass2_staged<512>, pb, 512, Pass2Stage<512>::SMEM, P, N, g, kc,
+                                    keys_next, mats, c->nmat, a, err);
+                }
             } else if (c->pass_block == 128) {
-                if (c->gather_batch) PASS2(1, 128); else PASS2(0, 128);
+                if (c->gather_batch == 1) PASS2(1, 128); else PASS2(0, 128);
             } else if (c->pass_block == 256) {
-                if (c->gather_batch) PASS2(1, 256); else PASS2(0, 256);
+                if (c->gather_batch == 1) PASS2(1, 256); else PASS2(0, 256);
             } else {
-                if (c->gather_batch) PASS2(1, 512); else PASS2(0, 512);
+                if (c->gather_batch == 1) PASS2(1, 512); else PASS2(0, 512);
             }
 #undef PASS2
         }
@@ -1079,6 +1092,12 @@ bool cells_attr() {
            cudaFuncSetAttribute(k_p2g_cells_mg<T, CPT, BS>, a, (int)p2g_cells_smem<T>(BS)) == cudaSuccess &&
            cudaFuncSetAttribute(k_pass1_cells<T, CPT, BS>, a, (int)pass1_cells_smem<T>(BS)) == cudaSuccess;
 }
+bool pass2_staged_attrs() {
+    const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    return cudaFuncSetAttribute(k_pass2_staged<128>, a, Pass2Stage<128>::SMEM) == cudaSuccess &&
+           cudaFuncSetAttribute(k_pass2_staged<256>, a, Pass2Stage<256>::SMEM) == cudaSuccess &&
+           cudaFuncSetAttribute(k_pass2_staged<512>, a, Pass2Stage<512>::SMEM) == cudaSuccess;
+}
 template <typename T>
 bool cells_attrs() {
     return cells_attr<T, 1, 128>() && cells_attr<T, 2, 128>() && cells_attr<T, 4, 128>() &&
@@ -1140,7 +1159,7 @@ int mpm_create_batch(const mpm_grid_desc* grids, int32_t nspec, int form, mpm_ct
     cudaGetDevice(&c->device);
     cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
     if (c->sm_count <= 0) c->sm_count = 152;
-    if (!cells_attrs<double>() || !cells_attrs<float>()) {
+    if (!cells_attrs<double>() || !cells_attrs<float>() || !pass2_staged_attrs()) {
         cudaGetLastError();
         delete c;
         return MPM_ERR_DEVICE;
@@ -1297,7 +1316,10 @@ int mpm_set_option(mpm_ctx* c, int key, double value) {
             if (c->reorder_interval < 0) c->reorder_pending = false;
             return MPM_OK;
         case MPM_OPT_GATHER:
-            if (value != 0.0 && value != 1.0) return fail(c, MPM_ERR_ARG, "gather mode must be 0 or 1");
+            if (value != 0.0 && value != 1.0 && value != 2.0)
+                return fail(c, MPM_ERR_ARG, "pass-2 mode must be 0, 1 or 2");
+            if (value == 2.0 && c->form != MPM_FORM_FP32)
+                return fail(c, MPM_ERR_ARG, "the staged pass 2 is built for the FP32 form");
             c->gather_batch = (int)value;
             return MPM_OK;
         case MPM_OPT_PASS1_CORNERS:
@@ -1887,8 +1909,9 @@ int mpm_autotune(mpm_ctx* c, int32_t steps, double dt, int contact, mpm_tune_res
     if (best[0] >= 2)
         for (int k = 0; k < 3 && rc == MPM_OK; ++k)
             for (int pb = 0; pb < 3 && rc == MPM_OK; ++pb) rc = trial(2, corners[k], 3, blocks[pb]);
+    const int gmodes = c->form == MPM_FORM_FP32 ? 3 : 2;
     for (int qb = 0; qb < 3 && rc == MPM_OK; ++qb)
-        for (int gb = 0; gb < 2 && rc == MPM_OK; ++gb) rc = trial(4, blocks[qb], 5, gb);
+        for (int gb = 0; gb < gmodes && rc == MPM_OK; ++gb) rc = trial(4, blocks[qb], 5, gb);
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     c->steps_since_reorder = since0;

@@ -1015,20 +1015,171 @@ struct StepArgs {
     int outputs;
 };
 
+// Where pass 2 reads a particle's fields from: its arrays in global memory
+// (DirectSrc), or the block's copies in shared memory (StagedSrc below).
+// Values written by the same step are always read back from global memory.
+template <typename T>
+struct DirectSrc {
+    __device__ __forceinline__ unsigned pflags(const PView<T>& P, long long p) const { return P.pflags[p]; }
+    __device__ __forceinline__ unsigned sid(const PView<T>& P, long long p) const { return P.sid[p]; }
+    __device__ __forceinline__ unsigned key(const unsigned* keys, long long p) const { return keys[p]; }
+    __device__ __forceinline__ int material(const PView<T>& P, long long p) const { return P.material[p]; }
+    __device__ __forceinline__ T vol0(const PView<T>& P, long long p) const { return P.vol0[p]; }
+    __device__ __forceinline__ T backstress(const PView<T>& P, long long p) const { return P.backstress[p]; }
+    __device__ __forceinline__ float loc(const PView<T>& P, int k, long long p) const { return P.loc[k * P.n + p]; }
+    __device__ __forceinline__ T F(const PView<T>& P, int k, long long p) const { return P.F[k * P.n + p]; }
+    __device__ __forceinline__ T stress(const PView<T>& P, int k, long long p) const { return P.stress[k * P.n + p]; }
+    __device__ __forceinline__ T strain(const PView<T>& P, int k, long long p) const { return P.strain[k * P.n + p]; }
+    __device__ __forceinline__ T eps_p(const PView<T>& P, int k, long long p) const { return P.eps_p[k * P.n + p]; }
+    __device__ __forceinline__ double pos(const PView<T>& P, int k, long long p) const { return P.pos[k * P.n + p]; }
+    __device__ __forceinline__ double e_strain(const PView<T>& P, long long p) const { return P.e_strain[p]; }
+    __device__ __forceinline__ double e_plastic(const PView<T>& P, long long p) const { return P.e_plastic[p]; }
+};
+
+__device__ __forceinline__ uint32_t shared_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Bounded wait for an mbarrier phase: false, with the error bit set, when it
+// does not complete within 2^22 polls.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned* err) {
+    for (int it = 0; it < (1 << 22); ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    atomicOr(err, ERR_WAIT_TIMEOUT);
+    return false;
+}
+
+// The FP32 pass 2's particle fields for one block of BS particles [p0, p0 + BS)
+// in shared memory, brought in by bulk copies (cp.async.bulk) that all start
+// at once and complete on one mbarrier, so the block's particle reads wait
+// for one memory round trip instead of one per dependent load.  One segment
+// per (field, component): BS elements plus 16 bytes, copied from the 16-byte
+// boundary at or below the block's first element (component k of an n-element
+// array starts (k n es) mod 16 bytes into its segment).  A block may stage
+// only if p0 + BS + 16 <= n (every copy then stays inside its array) and
+// every array starts on a 16-byte boundary.
+template <int BS>
+struct Pass2Stage {
+    static constexpr int SEG1 = BS + 16, SEG2 = 2 * BS + 16, SEG4 = 4 * BS + 16, SEG8 = 8 * BS + 16;
+    static constexpr int O_FLAGS = 0, O_SID = O_FLAGS + SEG1, O_KEYS = O_SID + SEG2, O_MAT = O_KEYS + SEG4;
+    static constexpr int O_VOL0 = O_MAT + SEG4, O_BACK = O_VOL0 + SEG4, O_LOC = O_BACK + SEG4;
+    static constexpr int O_F = O_LOC + 3 * SEG4, O_STRESS = O_F + 9 * SEG4, O_STRAIN = O_STRESS + 6 * SEG4;
+    static constexpr int O_EPSP = O_STRAIN + 6 * SEG4, O_POS = O_EPSP + 6 * SEG4, O_ES = O_POS + 3 * SEG8;
+    static constexpr int O_EP = O_ES + SEG8, BYTES = O_EP + SEG8;
+    static constexpr int NSEG = 41;  // flags, sid, keys, material, vol0, back stress, 3 loc, 9 F, 3 x 6 tensors, 3 pos, 2 energies
+    static constexpr int SMEM = BYTES + 16;  // and the mbarrier
+
+    static __device__ __forceinline__ bool usable(const PView<float>& P, const unsigned* keys, long long p0) {
+        const unsigned long long a = (unsigned long long)P.pflags | (unsigned long long)P.sid |
+                                     (unsigned long long)keys | (unsigned long long)P.material |
+                                     (unsigned long long)P.vol0 | (unsigned long long)P.backstress |
+                                     (unsigned long long)P.loc | (unsigned long long)P.F |
+                                     (unsigned long long)P.stress | (unsigned long long)P.strain |
+                                     (unsigned long long)P.eps_p | (unsigned long long)P.pos |
+                                     (unsigned long long)P.e_strain | (unsigned long long)P.e_plastic;
+        const bool all = P.pflags && keys && P.material && P.vol0 && P.backstress && P.loc && P.F && P.stress &&
+                         P.strain && P.eps_p && P.pos && P.e_strain && P.e_plastic;
+        return all && (a & 15ull) == 0 && p0 + BS + 16 <= P.n;
+    }
+    // segment i: its array, element size, component and shared offset
+    static __device__ __forceinline__ void segment(int i, const PView<float>& P, const unsigned* keys, const void*& base,
+                                                   int& es, int& k, int& off) {
+        k = 0;
+        if (i == 0) { base = P.pflags; es = 1; off = O_FLAGS; }
+        else if (i == 1) { base = P.sid; es = 2; off = O_SID; }
+        else if (i == 2) { base = keys; es = 4; off = O_KEYS; }
+        else if (i == 3) { base = P.material; es = 4; off = O_MAT; }
+        else if (i == 4) { base = P.vol0; es = 4; off = O_VOL0; }
+        else if (i == 5) { base = P.backstress; es = 4; off = O_BACK; }
+        else if (i < 9) { base = P.loc; es = 4; k = i - 6; off = O_LOC; }
+        else if (i < 18) { base = P.F; es = 4; k = i - 9; off = O_F; }
+        else if (i < 24) { base = P.stress; es = 4; k = i - 18; off = O_STRESS; }
+        else if (i < 30) { base = P.strain; es = 4; k = i - 24; off = O_STRAIN; }
+        else if (i < 36) { base = P.eps_p; es = 4; k = i - 30; off = O_EPSP; }
+        else if (i < 39) { base = P.pos; es = 8; k = i - 36; off = O_POS; }
+        else if (i == 39) { base = P.e_strain; es = 8; off = O_ES; }
+        else { base = P.e_plastic; es = 8; off = O_EP; }
+        off += k * (BS * es + 16);
+    }
+    // bytes the block's copies deliver (no specimen ids with one specimen)
+    static __device__ __forceinline__ unsigned tx_bytes(const PView<float>& P) {
+        return (unsigned)(BYTES - (P.sid ? 0 : SEG2));
+    }
+    // issue segment i's copy (called by the lanes of one warp)
+    static __device__ __forceinline__ void copy(int i, const PView<float>& P, const unsigned* keys, long long p0,
+                                                unsigned char* sm, uint32_t bar) {
+        const void* base;
+        int es, k, off;
+        segment(i, P, keys, base, es, k, off);
+        if (!base) return;
+        const unsigned long long src = ((unsigned long long)base + (unsigned long long)(k * P.n + p0) * es) & ~15ull;
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                shared_addr(sm + off)),
+            "l"(src), "r"((unsigned)(BS * es + 16)), "r"(bar)
+            : "memory");
+    }
+};
+
+// Reads from a Pass2Stage: thread t's element of component k sits (k n es) mod
+// 16 bytes plus t es into the component's segment.
+template <int BS>
+struct StagedSrc {
+    using S = Pass2Stage<BS>;
+    const unsigned char* sm;
+    template <typename E, int OFF, int ES>
+    __device__ __forceinline__ E at(const PView<float>& P, int k) const {
+        const unsigned mis = ((unsigned)k * (unsigned)(P.n * ES)) & 15u;
+        return *reinterpret_cast<const E*>(sm + OFF + k * (BS * ES + 16) + mis + threadIdx.x * ES);
+    }
+    __device__ __forceinline__ unsigned pflags(const PView<float>&, long long) const { return sm[S::O_FLAGS + threadIdx.x]; }
+    __device__ __forceinline__ unsigned sid(const PView<float>& P, long long) const { return at<uint16_t, S::O_SID, 2>(P, 0); }
+    __device__ __forceinline__ unsigned key(const unsigned*, long long) const {
+        return *reinterpret_cast<const unsigned*>(sm + S::O_KEYS + 4 * threadIdx.x);
+    }
+    __device__ __forceinline__ int material(const PView<float>& P, long long) const { return at<int, S::O_MAT, 4>(P, 0); }
+    __device__ __forceinline__ float vol0(const PView<float>& P, long long) const { return at<float, S::O_VOL0, 4>(P, 0); }
+    __device__ __forceinline__ float backstress(const PView<float>& P, long long) const {
+        return at<float, S::O_BACK, 4>(P, 0);
+    }
+    __device__ __forceinline__ float loc(const PView<float>& P, int k, long long) const { return at<float, S::O_LOC, 4>(P, k); }
+    __device__ __forceinline__ float F(const PView<float>& P, int k, long long) const { return at<float, S::O_F, 4>(P, k); }
+    __device__ __forceinline__ float stress(const PView<float>& P, int k, long long) const {
+        return at<float, S::O_STRESS, 4>(P, k);
+    }
+    __device__ __forceinline__ float strain(const PView<float>& P, int k, long long) const {
+        return at<float, S::O_STRAIN, 4>(P, k);
+    }
+    __device__ __forceinline__ float eps_p(const PView<float>& P, int k, long long) const {
+        return at<float, S::O_EPSP, 4>(P, k);
+    }
+    __device__ __forceinline__ double pos(const PView<float>& P, int k, long long) const {
+        return at<double, S::O_POS, 8>(P, k);
+    }
+    __device__ __forceinline__ double e_strain(const PView<float>& P, long long) const { return at<double, S::O_ES, 8>(P, 0); }
+    __device__ __forceinline__ double e_plastic(const PView<float>& P, long long) const { return at<double, S::O_EP, 8>(P, 0); }
+};
+
 // Apply a constitutive increment o to particle p (stress, plastic strain,
 // back stress, energies; …MPLocks.cpp:246-270, contact …_Contact.cpp:486-525).
 // The step's energy increments are summed in the form's type and added once
 // to the FP64 energy accumulators.
-template <typename T>
+template <typename T, class SRC = DirectSrc<T>>
 __device__ __forceinline__ void apply_increment(const PView<T>& P, long long p, const T sig[6], const T e[6],
-                                                const CrOut<T>& o, T V, T R, int contact, double dt) {
+                                                const CrOut<T>& o, T V, T R, int contact, double dt,
+                                                const SRC& src = SRC{}) {
     const long long np = P.n;
     T dEs = 0, dEp = 0;
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
         T sn = sig[k] + o.dsig[k];
         P.stress[k * np + p] = sn;
-        P.eps_p[k * np + p] += o.deps_p[k];
+        P.eps_p[k * np + p] = src.eps_p(P, k, p) + o.deps_p[k];
         if (!contact) {
             T mid = sn - (T)0.5 * o.dsig[k];
             dEs += mid * e[k] * V;
@@ -1038,13 +1189,13 @@ __device__ __forceinline__ void apply_increment(const PView<T>& P, long long p, 
             dEp += sn * o.deps_p[k] * V;
         }
     }
-    double es = P.e_strain[p] + fps_f2d_form(dEs);
+    double es = src.e_strain(P, p) + fps_f2d_form(dEs);
     P.e_strain[p] = es;
     if (!contact) {
         P.e_strain_ti[p] += es * dt;
         if (es > P.e_strain_max[p]) P.e_strain_max[p] = es;
     }
-    P.e_plastic[p] += fps_f2d_form(dEp);
+    P.e_plastic[p] = src.e_plastic(P, p) + fps_f2d_form(dEp);
     P.backstress[p] = R + o.dR;
 }
 
@@ -1216,21 +1367,22 @@ __device__ __forceinline__ void large_strain_update(const PView<T>& P, long long
 
 // One particle of pass 2; returns the new cell key (u: the new cell-local
 // coordinate; queued: its stress increment waits for the network).
-template <typename T, int BATCH, bool LS = false>
+template <typename T, int BATCH, bool LS = false, class SRC = DirectSrc<T>>
 __device__ __forceinline__ unsigned pass2_particle(const PView<T>& P, const NView<T>& nd, const Geom& g,
                                                    unsigned* __restrict__ keys, unsigned* __restrict__ keys_next,
                                                    const MatConst* __restrict__ mats, int nmat, const StepArgs& a,
-                                                   unsigned* err, long long p, float u[3], bool& queued) {
+                                                   unsigned* err, long long p, float u[3], bool& queued,
+                                                   const SRC& src = SRC{}) {
     const long long np = P.n, nn = nd.nn;
     queued = false;
-    const unsigned fl = P.pflags[p];
+    const unsigned fl = src.pflags(P, p);
     const T dt = form_const<T>(a.dt, a.dt_f);
     const T mass_min = form_const<T>(a.mass_min, a.mass_min_f);
     const bool skip = a.contact && (fl & 8u);
-    const Geom& gs = spec_geom(g, P.sid, p);
+    const Geom& gs = (g.nspec > 1) ? g.tab[src.sid(P, p)] : g;
     if (!skip) {
-        unsigned key = keys[p];
-        double x[3] = {P.pos[p], P.pos[np + p], P.pos[2 * np + p]};
+        unsigned key = src.key(keys, p);
+        double x[3] = {src.pos(P, 0, p), src.pos(P, 1, p), src.pos(P, 2, p)};
         T L[9];
 #pragma unroll
         for (int k = 0; k < 9; ++k) L[k] = 0;
@@ -1238,7 +1390,12 @@ __device__ __forceinline__ unsigned pass2_particle(const PView<T>& P, const NVie
             int b[3];
             key_to_base(key, gs, b);
             Bases<T> B;
-            particle_bases<T>(P, gs, p, b, B);
+            if constexpr (sizeof(T) == 4) {
+                const float ul[3] = {src.loc(P, 0, p), src.loc(P, 1, p), src.loc(P, 2, p)};
+                B.init_local(gs, ul);
+            } else {
+                particle_bases<T>(P, gs, p, b, B);
+            }
             const double ddt = a.dt;
             // FP32 form: the displacement sum N (p/m) is formed in FP32 and
             // added to the FP64 position once; FP64 form: added per corner
@@ -1305,26 +1462,26 @@ __device__ __forceinline__ unsigned pass2_particle(const PView<T>& P, const NVie
         e[3] = Ldt[1] + Ldt[3];
         e[4] = Ldt[5] + Ldt[7];
         e[5] = Ldt[6] + Ldt[2];
-        int mi = P.material[p];
+        int mi = src.material(P, p);
         T F[9];
 #pragma unroll
-        for (int k = 0; k < 9; ++k) F[k] = P.F[k * np + p];
+        for (int k = 0; k < 9; ++k) F[k] = src.F(P, k, p);
         T Fn[9];
         Kinematics<T>::update(a.contact != 0, F, L, Ldt, dt, Fn);
         if (a.contact) {
             // contact: strain, F and V are updated before the material check (…_Contact.cpp:464-484)
 #pragma unroll
-            for (int k = 0; k < 6; ++k) P.strain[k * np + p] += e[k];
+            for (int k = 0; k < 6; ++k) P.strain[k * np + p] = src.strain(P, k, p) + e[k];
 #pragma unroll
             for (int k = 0; k < 9; ++k) P.F[k * np + p] = Fn[k];
-            P.vol[p] = Kinematics<T>::det(Fn) * P.vol0[p];
+            P.vol[p] = Kinematics<T>::det(Fn) * src.vol0(P, p);
         }
         if (mi >= 0 && mi < nmat) {
             const MatConst& M = mats[mi];
             T sig[6];
 #pragma unroll
-            for (int k = 0; k < 6; ++k) sig[k] = P.stress[k * np + p];
-            T R = P.backstress[p];
+            for (int k = 0; k < 6; ++k) sig[k] = src.stress(P, k, p);
+            T R = src.backstress(P, p);
             CrOut<T> o;
             // the network takes clearly plastic trial states of the materials it
             // was trained for; the band near the surface and elastic states stay exact
@@ -1357,10 +1514,10 @@ __device__ __forceinline__ unsigned pass2_particle(const PView<T>& P, const NVie
             if (!a.contact) {
 #pragma unroll
                 for (int k = 0; k < 9; ++k) P.F[k * np + p] = Fn[k];
-                V = Kinematics<T>::det(Fn) * P.vol0[p];
+                V = Kinematics<T>::det(Fn) * src.vol0(P, p);
                 P.vol[p] = V;
 #pragma unroll
-                for (int k = 0; k < 6; ++k) P.strain[k * np + p] += e[k];
+                for (int k = 0; k < 6; ++k) P.strain[k * np + p] = src.strain(P, k, p) + e[k];
             } else {
                 V = P.vol[p];
                 if (a.outputs) {
@@ -1384,7 +1541,7 @@ __device__ __forceinline__ unsigned pass2_particle(const PView<T>& P, const NVie
                     }
                 }
             } else {
-                apply_increment<T>(P, p, sig, e, o, V, R, a.contact, a.dt);
+                apply_increment<T>(P, p, sig, e, o, V, R, a.contact, a.dt, src);
             }
         } else if (!a.contact) {
             atomicOr(err, ERR_BAD_MATERIAL);
@@ -1435,6 +1592,50 @@ __global__ void __launch_bounds__(BS, sizeof(T) == 4 ? 1280 / BS : 1) k_pass2(PV
     float u[3];
     bool queued;
     pass2_particle<T, BATCH>(P, nd, g, keys, keys_next, mats, nmat, a, err, p, u, queued);
+}
+
+// FP32 pass 2 with the block's particle fields staged in shared memory
+// (Pass2Stage): warp 0 issues the bulk copies, every thread waits once on the
+// mbarrier, then runs pass2_particle reading from shared memory.  Blocks that
+// cannot stage (the last ones, or unaligned arrays) read global memory.
+template <int BS>
+__global__ void __launch_bounds__(BS, 1280 / BS) k_pass2_staged(PView<float> P, NView<float> nd, Geom g,
+                                                               unsigned* __restrict__ keys,
+                                                               unsigned* __restrict__ keys_next,
+                                                               const MatConst* __restrict__ mats, int nmat,
+                                                               StepArgs a, unsigned* err) {
+    using S = Pass2Stage<BS>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int t = threadIdx.x;
+    const long long p0 = blockIdx.x * (long long)BS, p = p0 + t;
+    float u[3];
+    bool queued;
+    if (!S::usable(P, keys, p0)) {
+        if (t < 64) pass2_prefetch<float>(P, p0, BS, a.contact);
+        if (p < P.n) pass2_particle<float, 0>(P, nd, g, keys, keys_next, mats, nmat, a, err, p, u, queued);
+        return;
+    }
+    const uint32_t bar = shared_addr(smem_raw + S::BYTES);
+    if (t == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    if (t < 32) {
+        if (t == 0)
+            asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}\n" ::"r"(bar),
+                         "r"(S::tx_bytes(P))
+                         : "memory");
+        __syncwarp();
+        for (int i = t; i < S::NSEG; i += 32) S::copy(i, P, keys, p0, smem_raw, bar);
+    }
+    if (!mbar_wait(bar, 0, err)) {
+        mbar_wait(bar, 0, err);  // once more (bounded) for copies still in flight, then leave
+        return;
+    }
+    pass2_particle<float, 0, false, StagedSrc<BS>>(P, nd, g, keys, keys_next, mats, nmat, a, err, p, u, queued,
+                                                   StagedSrc<BS>{smem_raw});
 }
 
 // The large-strain pass 2 (non-contact loop, FP64 form; the reference ships

@@ -498,7 +498,7 @@ __device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity, unsigned
             : "memory");
         if (ok) return true;
     }
-    atomicOr(err, 4u);
+    atomicOr(err, ERR_WAIT_TIMEOUT);
     return false;
 }
 

@@ -73,7 +73,9 @@ extern "C" {
 #define MPM_OPT_P2G_REDUCE 3     /* P2G: 0 = one atomic per particle, 1 = sum each cell's run across lanes first, 2 = stage the block in shared memory and sum each (cell, corner) in one thread, 3 (default) / 4 = as 2 with each thread summing 2 / 4 corners of a cell */
 #define MPM_OPT_P2G_BLOCK 4      /* P2G threads per block (128, 256 or 512) */
 #define MPM_OPT_PASS_BLOCK 5     /* G2P pass-2 threads per block (128, 256 (default) or 512) */
-#define MPM_OPT_GATHER 6         /* G2P node gathers: 0 = one corner at a time, 1 = several corners' loads issued together */
+#define MPM_OPT_GATHER 6         /* pass-2 (G2P) mode: 0 = node gathers one corner at a time, 1 = several corners'
+                                    loads issued together, 2 = (FP32 form) as 0 with the block's particle fields
+                                    brought into shared memory by bulk copies first */
 #define MPM_OPT_GRAPH 7          /* 1 (default): mpm_advance replays a captured two-step CUDA graph in the steady state; 0: launch every kernel */
 #define MPM_OPT_REORDER 8        /* FP32 form: store particles in cell order after each particle upload (0, default), also every N steps (N > 0), or never (-1); results stay in the caller's order */
 #define MPM_OPT_PASS1_CORNERS 10 /* cell-run G2P pass 1 (P2G modes 2-4): corners per thread, 1, 2 (default) or 4 */
@@ -205,7 +207,7 @@ int mpm_advance_timed(mpm_ctx* ctx, int32_t nsteps, double dt, int contact, floa
  * loop): times `steps` steps of dt per candidate launch configuration on the
  * current state in three stages, each keeping the fastest so far: P2G mode x
  * P2G block (15), then pass-1 corners per thread x pass-1 block (9, cell-run
- * modes only), then pass-2 block x gather mode (6).  The particle and node
+ * modes only), then pass-2 block x pass-2 mode (6; 9 in the FP32 form).  The particle and node
  * state and the time are restored exactly as they were.  Results are the
  * chosen options and the best and worst candidate times per step. */
 typedef struct mpm_tune_result {

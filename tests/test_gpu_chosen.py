@@ -56,7 +56,10 @@ def test_autotune_restores_state_and_picks_valid_options(golden, form):
         before = e.download_state(st)
         res = e.autotune(steps=2, contact=True)
         after = e.download_state(st)
-        assert res["candidates"] in (21, 30) and res["pass1_corners"] in (1, 2, 4) and res["pass1_block"] in (128, 256, 512) and res["gather_batch"] in (0, 1) and res["p2g_block"] in (128, 256, 512) and res["pass_block"] in (128, 256, 512)
+        # P2G stage 15, pass-1 stage 9 (cell-run P2G only), pass-2 stage 6 (FP64) or 9 (FP32: also the staged mode)
+        ncand = (21, 30) if form == engine.FORM_FP64 else (24, 33)
+        modes = (0, 1) if form == engine.FORM_FP64 else (0, 1, 2)
+        assert res["candidates"] in ncand and res["pass1_corners"] in (1, 2, 4) and res["pass1_block"] in (128, 256, 512) and res["gather_batch"] in modes and res["p2g_block"] in (128, 256, 512) and res["pass_block"] in (128, 256, 512)
         assert res["best_ms_per_step"] <= res["worst_ms_per_step"]
         for k in ("pos", "vel", "stress", "F", "g_mass", "g_state"):
             assert np.array_equal(before[k], after[k]), k
@@ -104,3 +107,50 @@ def test_chosen_form_p2g_modes_agree():
             scale = np.abs(a[k]).max()
             assert np.abs(b[k] - a[k]).max() <= 1e-4 * scale, (cfg, k)
         assert np.array_equal(a["g_state"] & 1, b["g_state"] & 1), cfg
+
+
+PASS2_FIELDS = ("pos", "vel", "stress", "strain", "eps_p", "F", "vol", "backstress", "e_strain", "e_plastic")
+
+
+@pytest.mark.parametrize("scene", ["mixed", "batch"])
+def test_staged_pass2_reads_the_same_fields(scene):
+    """Pass-2 mode 2 brings each block's particle fields into shared memory with bulk copies before the particle
+    update; mode 0 reads them from global memory.  From the same state, one step of each agrees in every particle
+    field to FP32 rounding (the only difference between two runs is the order of P2G's FP32 atomics), at each
+    pass-2 block size; a misplaced component or particle would show as an O(1) difference.  "batch" covers the
+    specimen ids (several specimens) and the contact path, "mixed" the non-contact path."""
+    if scene == "mixed":
+        sts, contact = [scenes.mixed_small(seed=1, ncell=(16, 14, 8))], False
+    else:
+        sts = [scenes.honeycomb(0.8e-3, 3e-3, 2, 3000, 8.0, h=0.5e-3),
+               scenes.honeycomb(0.6e-3, 2.5e-3, 3, 5000, 4.0, h=0.5e-3)]
+        contact = True
+    assert sum(s.n_particles for s in sts) > 2 * (512 + 16)  # blocks of every size stage
+
+    def one(mode, blk):
+        make = (lambda: engine.Engine.from_state(sts[0], engine.FORM_FP32)) if len(sts) == 1 else \
+            (lambda: engine.Engine.from_batch(sts, engine.FORM_FP32))
+        with make() as e:
+            e.set_option(engine.OPT_GATHER, mode)
+            e.set_option(engine.OPT_PASS_BLOCK, blk)
+            e.advance(1, sts[0].dt_max, contact)
+            return e.download_state(sts[0]) if len(sts) == 1 else e.download_batch(sts)
+
+    for blk in (128, 256, 512):
+        a = one(0, blk)
+        a = a if isinstance(a, list) else [a]
+        for mode in (2,):
+            b = one(mode, blk)
+            b = b if isinstance(b, list) else [b]
+            for x, y in zip(a, b):
+                for k in PASS2_FIELDS:
+                    d = x[k] - y[k] if k != "pos" else (x[k] - y[k]) / float((sts[0].length / sts[0].cells).min())
+                    scale = max(np.abs(x[k]).max(), 1e-300) if k != "pos" else 1.0
+                    assert np.abs(d).max() <= 1e-5 * scale, (mode, blk, k)
+
+
+def test_staged_pass2_only_in_the_fp32_form():
+    st = scenes.mixed_small(seed=1)
+    with engine.Engine.from_state(st) as e:
+        with pytest.raises(engine.MPMError):
+            e.set_option(engine.OPT_GATHER, 2)
