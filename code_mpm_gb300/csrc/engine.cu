@@ -1155,6 +1155,10 @@ int mpm_create_batch(const mpm_grid_desc* grids, int32_t nspec, int form, mpm_ct
     mpm_ctx* c = new mpm_ctx();
     c->form = form;
     c->tsize = form == MPM_FORM_FP64 ? 8 : 4;
+    if (form == MPM_FORM_FP32) {  // the autotuner's choice on the honeycomb batch
+        c->gather_batch = 2;
+        c->pass_block = 128;
+    }
     c->nspec = nspec;
     cudaGetDevice(&c->device);
     cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);

@@ -1403,16 +1403,18 @@ __device__ __forceinline__ unsigned pass2_particle(const PView<T>& P, const NVie
             T disp[3] = {0, 0, 0};
             // BATCH: four corners' records are requested before any is used
             // (two round trips to memory instead of eight, at more registers);
-            // sums run in corner order either way
-#pragma unroll(BATCH ? 2 : 1)
+            // sums run in corner order either way.  The FP32 form unrolls the
+            // corners (fewer instructions per corner)
+            const CellNodes cn = cell_nodes(gs, b);
+#pragma unroll(BATCH ? 2 : (sizeof(T) == 4 ? 8 : 1))
             for (int h = 0; h < (BATCH ? 2 : 8); ++h) {
                 constexpr int W = BATCH ? 4 : 1;
                 Quad<T> rq[W], vq[W];
                 bool in[W];
 #pragma unroll
                 for (int j = 0; j < W; ++j) {
-                    const long long nid = corner_node(gs, b, W * h + j);
-                    in[j] = nid >= 0;
+                    const long long nid = cell_node(cn, W * h + j);
+                    in[j] = (cn.mask >> (W * h + j)) & 1u;
                     const Quad<T> z{(T)0, (T)0, (T)0, (T)0};
                     rq[j] = in[j] ? ld_quad(nd.rec + 8 * nid) : z;
                     vq[j] = in[j] ? ld_quad(nd.rec + 8 * nid + 4) : z;
@@ -1598,8 +1600,15 @@ __global__ void __launch_bounds__(BS, sizeof(T) == 4 ? 1280 / BS : 1) k_pass2(PV
 // (Pass2Stage): warp 0 issues the bulk copies, every thread waits once on the
 // mbarrier, then runs pass2_particle reading from shared memory.  Blocks that
 // cannot stage (the last ones, or unaligned arrays) read global memory.
+// Blocks per SM: as many as the staging buffers fit (228 KB of shared memory,
+// 1 KB reserved per block), which sets the register budget.
 template <int BS>
-__global__ void __launch_bounds__(BS, 1280 / BS) k_pass2_staged(PView<float> P, NView<float> nd, Geom g,
+constexpr int pass2_staged_blocks() {
+    return (228 * 1024) / (Pass2Stage<BS>::SMEM + 1024);
+}
+
+template <int BS>
+__global__ void __launch_bounds__(BS, pass2_staged_blocks<BS>()) k_pass2_staged(PView<float> P, NView<float> nd, Geom g,
                                                                unsigned* __restrict__ keys,
                                                                unsigned* __restrict__ keys_next,
                                                                const MatConst* __restrict__ mats, int nmat,
