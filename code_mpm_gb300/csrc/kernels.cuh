@@ -308,8 +308,8 @@ constexpr size_t CELL_SLOT_BYTES = 28;
 
 template <typename T>
 __host__ __device__ constexpr size_t p2g_cells_smem(int bs) {
-    return ((size_t)12 * (bs + 1) + (size_t)13 * bs) * sizeof(T) + (size_t)bs * CELL_SLOT_BYTES +
-           (size_t)(bs + 1) * 4 + 64 * 4;
+    return (sizeof(T) == 4 ? (size_t)25 * bs * 4 : ((size_t)12 * (bs + 1) + (size_t)13 * bs) * sizeof(T)) +
+           (size_t)bs * CELL_SLOT_BYTES + (size_t)(bs + 1) * 4 + 64 * 4;
 }
 
 // The slot arrays that follow the values (8-byte aligned: even bs).
@@ -349,11 +349,14 @@ struct CellSlots {
 // read from shared memory 8 / CPT times instead of 8.  BS, the block size, is
 // a compile-time constant so the shared-memory rows sit at fixed offsets from
 // one address.
-// A cell-run P2G block of BS slots in shared memory: the per-axis bases (12
-// rows of BS + 1: the odd stride puts the two nodes' values of an axis in
-// different banks; Nx0 Nx1 Ny0 Ny1 Nz0 Nz1 gx0 gx1 gy0 gy1 gz0 gz1), the
-// transfer quantities (13 rows of BS: m, m v (3), -V sigma (6), f_ext (3)) and
-// the slots (cell nodes, key, runs).
+// A cell-run P2G block of BS slots in shared memory: the per-axis bases, the
+// transfer quantities (m, m v (3), -V sigma (6), f_ext (3)) and the slots
+// (cell nodes, key, runs).  FP64: 12 rows of BS + 1 bases (the odd stride puts
+// the two nodes' values of an axis in different banks; Nx0 Nx1 Ny0 Ny1 Nz0
+// Nz1 gx0 gx1 gy0 gy1 gz0 gz1) and 13 rows of BS quantities.  FP32: six rows
+// of BS float4 ({Nx0 Nx1 gx0 gx1}, y, z, {m, m v}, {-V sigma 0..3},
+// {-V sigma 4..5, f_ext 0..1}) and a row of f_ext 2, so a scatter thread reads
+// a particle with seven shared loads.
 template <typename T, int BS>
 struct P2GBlock {
     static constexpr int S = BS + 1;
@@ -361,11 +364,24 @@ struct P2GBlock {
     T* sq;
     CellSlots cs;
     __device__ __forceinline__ explicit P2GBlock(unsigned char* raw)
-        : sw(reinterpret_cast<T*>(raw)), sq(sw + 12 * S), cs(reinterpret_cast<unsigned char*>(sq + 13 * BS), BS) {}
+        : sw(reinterpret_cast<T*>(raw)), sq(sw + (sizeof(T) == 4 ? 24 * BS : 12 * S)),
+          cs(reinterpret_cast<unsigned char*>(sq + (sizeof(T) == 4 ? BS : 13 * BS)), BS) {}
 
     // slot t's particle: bases, mass m, volume V, velocity v, external force fe, stress sig, its cell's nodes
     __device__ __forceinline__ void stage(int t, const Bases<T>& B, T m, T V, const T v[3], const T fe[3],
                                           const T sig[6], const CellNodes& cn) const {
+        if constexpr (sizeof(T) == 4) {
+            float4* sv = reinterpret_cast<float4*>(sw);
+            sv[t] = make_float4(B.Nx[0], B.Nx[1], B.gx[0], B.gx[1]);
+            sv[BS + t] = make_float4(B.Ny[0], B.Ny[1], B.gy[0], B.gy[1]);
+            sv[2 * BS + t] = make_float4(B.Nz[0], B.Nz[1], B.gz[0], B.gz[1]);
+            sv[3 * BS + t] = make_float4(m, m * v[0], m * v[1], m * v[2]);
+            sv[4 * BS + t] = make_float4(-V * sig[0], -V * sig[1], -V * sig[2], -V * sig[3]);
+            sv[5 * BS + t] = make_float4(-V * sig[4], -V * sig[5], fe[0], fe[1]);
+            sq[t] = fe[2];
+            cs.put(t, cn);
+            return;
+        }
         sw[0 * S + t] = B.Nx[0];
         sw[1 * S + t] = B.Nx[1];
         sw[2 * S + t] = B.Ny[0];
@@ -411,19 +427,41 @@ struct P2GBlock {
     #pragma unroll
             for (int j = 0; j < CPT; ++j) am[j] = ap0[j] = ap1[j] = ap2[j] = af0[j] = af1[j] = af2[j] = g0[j] = g1[j] = g2[j] = 0;
             for (int i = a; i < e; ++i) {
-                const T m = sq[i], mv0 = sq[1 * bs + i], mv1 = sq[2 * bs + i], mv2 = sq[3 * bs + i];
-                const T v0 = sq[4 * bs + i], v1 = sq[5 * bs + i], v2 = sq[6 * bs + i];
-                const T v3 = sq[7 * bs + i], v4 = sq[8 * bs + i], v5 = sq[9 * bs + i];
-                const T fe0 = sq[10 * bs + i], fe1 = sq[11 * bs + i], fe2 = sq[12 * bs + i];
+                T m, mv0, mv1, mv2, v0, v1, v2, v3, v4, v5, fe0, fe1, fe2;
+                float4 X, Y, Z;
+                if constexpr (sizeof(T) == 4) {
+                    const float4* sv = reinterpret_cast<const float4*>(sw);
+                    X = sv[i];
+                    Y = sv[BS + i];
+                    Z = sv[2 * BS + i];
+                    const float4 q0 = sv[3 * BS + i], q1 = sv[4 * BS + i], q2 = sv[5 * BS + i];
+                    m = q0.x, mv0 = q0.y, mv1 = q0.z, mv2 = q0.w;
+                    v0 = q1.x, v1 = q1.y, v2 = q1.z, v3 = q1.w;
+                    v4 = q2.x, v5 = q2.y, fe0 = q2.z, fe1 = q2.w;
+                    fe2 = sq[i];
+                } else {
+                    m = sq[i], mv0 = sq[1 * bs + i], mv1 = sq[2 * bs + i], mv2 = sq[3 * bs + i];
+                    v0 = sq[4 * bs + i], v1 = sq[5 * bs + i], v2 = sq[6 * bs + i];
+                    v3 = sq[7 * bs + i], v4 = sq[8 * bs + i], v5 = sq[9 * bs + i];
+                    fe0 = sq[10 * bs + i], fe1 = sq[11 * bs + i], fe2 = sq[12 * bs + i];
+                }
     #pragma unroll
                 for (int j = 0; j < CPT; ++j) {
                     const int k = k0 + j;
                     const int ix = (k >> 2) & 1, iy = (k >> 1) & 1, iz = k & 1;
-                    const T nx = sw[ix * S + i], ny = sw[(2 + iy) * S + i], nz = sw[(4 + iz) * S + i];
+                    T nx, ny, nz, gxv, gyv, gzv;
+                    if constexpr (sizeof(T) == 4) {
+                        nx = ix ? X.y : X.x, gxv = ix ? X.w : X.z;
+                        ny = iy ? Y.y : Y.x, gyv = iy ? Y.w : Y.z;
+                        nz = iz ? Z.y : Z.x, gzv = iz ? Z.w : Z.z;
+                    } else {
+                        nx = sw[ix * S + i], ny = sw[(2 + iy) * S + i], nz = sw[(4 + iz) * S + i];
+                        gxv = sw[(6 + ix) * S + i], gyv = sw[(8 + iy) * S + i], gzv = sw[(10 + iz) * S + i];
+                    }
                     const T N = nx * ny * nz;
-                    const T G0 = -(ny * nz) * sw[(6 + ix) * S + i];
-                    const T G1 = -(nx * nz) * sw[(8 + iy) * S + i];
-                    const T G2 = -(nx * ny) * sw[(10 + iz) * S + i];
+                    const T G0 = -(ny * nz) * gxv;
+                    const T G1 = -(nx * nz) * gyv;
+                    const T G2 = -(nx * ny) * gzv;
                     am[j] += N * m;
                     ap0[j] += N * mv0;
                     ap1[j] += N * mv1;
