@@ -748,8 +748,8 @@ __global__ void __launch_bounds__(256) k_pass1_remap(PView<T> P, NView<T> nd, Ge
 // ---------------------------------------------------------------------------
 template <typename T>
 __host__ __device__ constexpr size_t pass1_cells_smem(int bs) {
-    return ((size_t)6 * (bs + 1) + (size_t)3 * bs) * sizeof(T) + (size_t)bs * CELL_SLOT_BYTES + (size_t)(bs + 1) * 4 +
-           64 * 4;
+    return (sizeof(T) == 4 ? (size_t)9 * bs * 4 : ((size_t)6 * (bs + 1) + (size_t)3 * bs) * sizeof(T)) +
+           (size_t)bs * CELL_SLOT_BYTES + (size_t)(bs + 1) * 4 + 64 * 4;
 }
 
 template <typename T, int CPT, int BS>
@@ -760,10 +760,14 @@ __global__ void __launch_bounds__(BS) k_pass1_cells(PView<T> P, NView<T> nd, Geo
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int bs = BS;
     const int t = threadIdx.x;
-    constexpr int S = bs + 1;                // odd row stride: the two nodes' values of an axis in different banks
-    T* sn = reinterpret_cast<T*>(smem_raw);  // 6 x S: Nx0 Nx1 Ny0 Ny1 Nz0 Nz1
-    T* smv = sn + 6 * S;                     // 3 x bs: m v
-    CellSlots cs(reinterpret_cast<unsigned char*>(smv + 3 * bs), bs);
+    // FP64: 6 rows of S = bs + 1 (odd stride: the two nodes' values of an axis
+    // in different banks) Nx0 Nx1 Ny0 Ny1 Nz0 Nz1, then 3 rows of bs m v.
+    // FP32: two rows of bs float4 {Nx0 Nx1 Ny0 Ny1} {Nz0 Nz1 mv0 mv1} and a row of mv2.
+    constexpr int S = bs + 1;
+    constexpr bool F32 = sizeof(T) == 4;
+    T* sn = reinterpret_cast<T*>(smem_raw);
+    T* smv = sn + (F32 ? 8 * bs : 6 * S);
+    CellSlots cs(reinterpret_cast<unsigned char*>(smv + (F32 ? bs : 3 * bs)), bs);
     unsigned* skey = cs.key;
     const long long s = blockIdx.x * (long long)bs + t;
     const unsigned key = (s < n) ? skeys[s] : 0xffffffffu;
@@ -784,7 +788,7 @@ __global__ void __launch_bounds__(BS) k_pass1_cells(PView<T> P, NView<T> nd, Geo
             const T m = P.mass[p];
             T v[3] = {P.vel[p], P.vel[np + p], P.vel[2 * np + p]};
             // four corners' records requested before any is used; summed in corner order
-#pragma unroll 1
+#pragma unroll(F32 ? 2 : 1)
             for (int h = 0; h < 2; ++h) {
                 Quad<T> rq[4];
 #pragma unroll
@@ -815,10 +819,17 @@ __global__ void __launch_bounds__(BS) k_pass1_cells(PView<T> P, NView<T> nd, Geo
             N6[4] = B.Nz[0];
             N6[5] = B.Nz[1];
         }
+        if constexpr (F32) {
+            float4* sv = reinterpret_cast<float4*>(sn);
+            sv[t] = make_float4(N6[0], N6[1], N6[2], N6[3]);
+            sv[bs + t] = make_float4(N6[4], N6[5], mv[0], mv[1]);
+            smv[t] = mv[2];
+        } else {
 #pragma unroll
-        for (int c = 0; c < 6; ++c) sn[c * S + t] = N6[c];
+            for (int c = 0; c < 6; ++c) sn[c * S + t] = N6[c];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) smv[c * bs + t] = mv[c];
+            for (int c = 0; c < 3; ++c) smv[c * bs + t] = mv[c];
+        }
     }
     skey[t] = key;
     __syncthreads();
@@ -832,12 +843,25 @@ __global__ void __launch_bounds__(BS) k_pass1_cells(PView<T> P, NView<T> nd, Geo
 #pragma unroll
         for (int j = 0; j < CPT; ++j) q0[j] = q1[j] = q2[j] = 0;
         for (int i = a; i < e; ++i) {
-            const T mv0 = smv[i], mv1 = smv[bs + i], mv2 = smv[2 * bs + i];
+            T mv0, mv1, mv2;
+            float4 A, B;
+            if constexpr (F32) {
+                const float4* sv = reinterpret_cast<const float4*>(sn);
+                A = sv[i];
+                B = sv[bs + i];
+                mv0 = B.z, mv1 = B.w, mv2 = smv[i];
+            } else {
+                mv0 = smv[i], mv1 = smv[bs + i], mv2 = smv[2 * bs + i];
+            }
 #pragma unroll
             for (int j = 0; j < CPT; ++j) {
                 const int k = k0 + j;
                 const int ix = (k >> 2) & 1, iy = (k >> 1) & 1, iz = k & 1;
-                const T N = sn[ix * S + i] * sn[(2 + iy) * S + i] * sn[(4 + iz) * S + i];
+                T N;
+                if constexpr (F32)
+                    N = (ix ? A.y : A.x) * (iy ? A.w : A.z) * (iz ? B.y : B.x);
+                else
+                    N = sn[ix * S + i] * sn[(2 + iy) * S + i] * sn[(4 + iz) * S + i];
                 q0[j] += N * mv0;
                 q1[j] += N * mv1;
                 q2[j] += N * mv2;
