@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(512) k_p2g(PView<T> P, NView<T> nd, Geom g, co
         if (valid && (!REDUCE || run.tail)) {
             long long nid = corner_node(*gsp, b, k);
             if (nid >= 0) {
-                if (mark_active && !(nd.state[nid] & 1u)) atomicOr(&nd.state[nid], 1u);
+                if (mark_active) atomicOr(&nd.state[nid], 1u);  // a reduction: no load to wait for
                 acc_add<T>(nd.acc, nid, c[0], c[1], c[2], c[3], c[4], c[5], c[6]);
                 if (nf == 10) {
                     atomicAdd(&nd.mg[nid], c[7]);
@@ -481,7 +481,7 @@ struct P2GBlock {
                 const long long nid = cs.node(a, k0 + j);
                 if (nid < 0) continue;
                 // active nodes: the in-range corners of occupied cells (b_Active, …MPLocks.cpp:36)
-                if (mark_active && !(nd.state[nid] & 1u)) atomicOr(&nd.state[nid], 1u);
+                if (mark_active) atomicOr(&nd.state[nid], 1u);  // a reduction: no load to wait for
                 acc_add<T>(nd.acc, nid, am[j], ap0[j], ap1[j], ap2[j], af0[j], af1[j], af2[j]);
                 if constexpr (MG) {
                     atomicAdd(&nd.mg[nid], g0[j]);
@@ -565,7 +565,7 @@ static __global__ void k_dc_claim(const unsigned* __restrict__ dclist, int ndc, 
         if (nid < 0) continue;
         for (int a = 0; a < 3; ++a)
             if (axes & (1u << a)) atomicMax(&owner[a * nn + nid], (unsigned)k + 1u);
-        if (axes && !(state[nid] & NODE_CLAIMED)) atomicOr(&state[nid], NODE_CLAIMED);
+        if (axes) atomicOr(&state[nid], NODE_CLAIMED);
     }
 }
 
