@@ -278,7 +278,10 @@ def apply_tune(e, tune):
         e.set_option(engine.OPT_P2G_REDUCE, tune["p2g_reduce"])
         e.set_option(engine.OPT_P2G_BLOCK, tune["p2g_block"])
         e.set_option(engine.OPT_PASS_BLOCK, tune["pass_block"])
-        e.set_option(engine.OPT_GATHER, tune["gather_batch"])
+        # the staged pass 2 (mode 2) exists in the FP32 form only; an FP64 engine given an FP32 tuning gathers
+        # one corner at a time
+        gather = tune["gather_batch"]
+        e.set_option(engine.OPT_GATHER, 0 if gather == 2 and e.form == engine.FORM_FP64 else gather)
         e.set_option(engine.OPT_PASS1_CORNERS, tune["pass1_corners"])
         e.set_option(engine.OPT_PASS1_BLOCK, tune["pass1_block"])
 
