@@ -546,7 +546,8 @@ __global__ void __launch_bounds__(BS) k_p2g_cells_mg(PView<T> P, NView<T> nd, Ge
 // k_dc_claim records, per node and axis, the largest list position writing
 // it, and marks the node (NODE_CLAIMED in its state word) so the node phases
 // read the claims of marked nodes only; node_dc lets only the claiming
-// particle write.  contact: all three axes.
+// particle write.  contact: every particle claims all three axes, so the axis-0
+// claim word stands for the three (one atomic per corner instead of three).
 // ---------------------------------------------------------------------------
 static __global__ void k_dc_claim(const unsigned* __restrict__ dclist, int ndc, const unsigned* __restrict__ keys,
                            const uint8_t* __restrict__ pflags, Geom g, unsigned* __restrict__ owner, long long nn,
@@ -564,7 +565,7 @@ static __global__ void k_dc_claim(const unsigned* __restrict__ dclist, int ndc, 
         long long nid = corner_node(gs, b, c8);
         if (nid < 0) continue;
         for (int a = 0; a < 3; ++a)
-            if (axes & (1u << a)) atomicMax(&owner[a * nn + nid], (unsigned)k + 1u);
+            if ((axes & (1u << a)) && !(contact && a > 0)) atomicMax(&owner[a * nn + nid], (unsigned)k + 1u);
         if (axes) atomicOr(&state[nid], NODE_CLAIMED);
     }
 }
@@ -916,8 +917,9 @@ __global__ void __launch_bounds__(256, 4) k_node_phase_a(NView<T> nd, T dt, doub
         const unsigned fx = nd.fixed[i];
         unsigned own[3] = {0u, 0u, 0u};
         if (ndc && (st & NODE_CLAIMED)) {
+            // contact: every controlled particle claims all three axes, so one claim word serves them
 #pragma unroll
-            for (int a = 0; a < 3; ++a) own[a] = nd.owner[a * nn + i];
+            for (int a = 0; a < 3; ++a) own[a] = (contact && a > 0) ? own[0] : nd.owner[a * nn + i];
         }
         bool vset[3] = {false, false, false}, fz[3] = {false, false, false};
         if (!contact) node_dc_regs<T>(own, dclist, pvel, np, m, v, vset, p, fz);
@@ -1002,6 +1004,10 @@ __global__ void __launch_bounds__(256, 4) k_node_phase_b(NView<T> nd, int contac
         if (ndc && (st & NODE_CLAIMED)) {
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
+                if (contact && a > 0) {  // one claim word for the three axes (k_dc_claim)
+                    own[a] = own[0];
+                    continue;
+                }
                 own[a] = nd.owner[a * nn + i];
                 if (own[a]) nd.owner[a * nn + i] = 0u;  // the claims' last use this step: clean for the next
             }
