@@ -481,6 +481,20 @@ __global__ void __launch_bounds__(CS_THREADS) k_compact_state(const unsigned* __
         off += __popc(m[r]);
     }
 }
+// Specimen ids of an upload (int32 from the caller) to the 16-bit device
+// array; the smallest index of an id outside [0, nspec) goes to *bad.
+__global__ void k_specimen_ids(const int32_t* __restrict__ in, long long n, int nspec, uint16_t* __restrict__ out,
+                               unsigned* __restrict__ bad) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int32_t s = in[i];
+    if (s < 0 || s >= nspec) {
+        atomicMin(bad, (unsigned)i);
+        return;
+    }
+    out[i] = (uint16_t)s;
+}
+
 __global__ void k_clear_flag(uint8_t* __restrict__ pflags, long long n, uint8_t bits) {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i < n) pflags[i] &= (uint8_t)~bits;
@@ -1391,23 +1405,34 @@ int mpm_upload_particles(mpm_ctx* c, const mpm_particles* p, int64_t n) {
     if (!c) return MPM_ERR_ARG;
     if (!p || n < 0 || n >= 0x7fffffffLL) return fail(c, MPM_ERR_ARG, "bad particle upload (n=%lld)", (long long)n);
     const bool f64 = c->form == MPM_FORM_FP64;
-    std::vector<uint16_t> sid16;
+    int rc;
     if (c->nspec > 1) {
+        // specimen ids checked and narrowed on the device (into the staging
+        // buffer, then into place once all are valid: a bad upload changes nothing)
         if (!p->specimen && n > 0) return fail(c, MPM_ERR_ARG, "a batch of specimens needs the specimen of each particle");
-        sid16.resize((size_t)std::max<int64_t>(1, n));
-        for (int64_t i = 0; i < n; ++i) {
-            if (p->specimen[i] < 0 || p->specimen[i] >= c->nspec)
-                return fail(c, MPM_ERR_ARG, "particle %lld: specimen %d out of range", (long long)i, p->specimen[i]);
-            sid16[i] = (uint16_t)p->specimen[i];
+        const size_t in_bytes = ((size_t)std::max<int64_t>(1, n) * 4 + 15) / 16 * 16;
+        if ((rc = ensure(c, c->staging, in_bytes + (size_t)std::max<int64_t>(1, n) * 2 + 4))) return rc;
+        unsigned char* stg = (unsigned char*)c->staging.p;
+        unsigned* bad = (unsigned*)(stg + in_bytes + (size_t)std::max<int64_t>(1, n) * 2);
+        CK(cudaMemsetAsync(bad, 0xff, 4, c->stream));
+        if (n > 0) {
+            CK(cudaMemcpyAsync(stg, p->specimen, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
+            LAUNCH("fill", k_specimen_ids, blocks_for(n), NTHREADS, (const int32_t*)stg, (long long)n, c->nspec,
+                   (uint16_t*)(stg + in_bytes), bad);
         }
+        CK(cudaMemcpyAsync(c->h_err, bad, 4, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        if (*c->h_err != 0xffffffffu) {
+            const long long i = *c->h_err;
+            return fail(c, MPM_ERR_ARG, "particle %lld: specimen %d out of range", i, p->specimen[i]);
+        }
+        if ((rc = ensure(c, c->sid, (size_t)std::max<int64_t>(1, n) * 2))) return rc;
+        if (n > 0)
+            CK(cudaMemcpyAsync(c->sid.p, stg + in_bytes, (size_t)n * 2, cudaMemcpyDeviceToDevice, c->stream));
     }
-    int rc = alloc_particles(c, n);
+    rc = alloc_particles(c, n);
     if (rc) return rc;
     c->n = n;
-    if (c->nspec > 1) {
-        if ((rc = ensure(c, c->sid, sid16.size() * 2))) return rc;
-        CK(cudaMemcpy(c->sid.p, sid16.data(), sid16.size() * 2, cudaMemcpyHostToDevice));
-    }
     struct {
         DevBuf* b;
         const double* h;

@@ -71,3 +71,23 @@ def test_platen_sharing_cells_with_the_body():
     for k in ("pos", "vel", "stress", "g_vel", "g_mom"):
         assert relerr(out[k], ref[k]) <= 1e-9, k
     assert np.array_equal(out["g_state"], ref["g_state"])
+
+
+def test_upload_rejects_a_specimen_id_out_of_range_and_changes_nothing():
+    """Specimen ids are checked on the device during the upload: an id outside the batch fails the upload with
+    the first offending particle named, before any particle array is touched."""
+    from code_mpm_gb300 import batch
+
+    sts = specimens()[:2]
+    with engine.Engine.from_batch(sts, engine.FORM_FP32) as e:
+        e.advance(2, sts[0].dt_max, True)
+        before = e.download_batch(sts)
+        bad = batch.pack(sts).state
+        bad["specimen"][[7, 11]] = [2, -1]
+        with pytest.raises(engine.MPMError, match="particle 7: specimen 2 out of range"):
+            e.upload_state(bad)
+        e.packed = batch.pack(sts)
+        after = e.download_batch(sts)
+    for b, a in zip(before, after):
+        for k in ("pos", "vel", "stress"):
+            assert np.array_equal(b[k], a[k]), k
