@@ -306,6 +306,14 @@ __device__ __forceinline__ int block_runs(const unsigned* skey, int nslots, int*
 // and the key; then the run starts (bs + 1) and the warp counts.
 constexpr size_t CELL_SLOT_BYTES = 28;
 
+// FP32 cell-run value rows: slot s is stored at row position s ^ ((s >> 3) & 7),
+// a permutation inside each aligned group of 8 slots (block sizes are multiples
+// of 8).  The cell runs one warp sums start 8 slots apart when cells hold 8
+// particles, so in slot order their 16-byte values fall in the same four banks
+// and a quarter-warp's two runs conflict; swizzled, eight consecutive runs read
+// eight distinct bank groups.  Sums still run in slot order.
+__device__ __forceinline__ int slot_swz(int s) { return s ^ ((s >> 3) & 7); }
+
 template <typename T>
 __host__ __device__ constexpr size_t p2g_cells_smem(int bs) {
     return (sizeof(T) == 4 ? (size_t)25 * bs * 4 : ((size_t)12 * (bs + 1) + (size_t)13 * bs) * sizeof(T)) +
@@ -371,14 +379,16 @@ struct P2GBlock {
     __device__ __forceinline__ void stage(int t, const Bases<T>& B, T m, T V, const T v[3], const T fe[3],
                                           const T sig[6], const CellNodes& cn) const {
         if constexpr (sizeof(T) == 4) {
+            static_assert(BS % 8 == 0, "slot swizzle groups");
             float4* sv = reinterpret_cast<float4*>(sw);
-            sv[t] = make_float4(B.Nx[0], B.Nx[1], B.gx[0], B.gx[1]);
-            sv[BS + t] = make_float4(B.Ny[0], B.Ny[1], B.gy[0], B.gy[1]);
-            sv[2 * BS + t] = make_float4(B.Nz[0], B.Nz[1], B.gz[0], B.gz[1]);
-            sv[3 * BS + t] = make_float4(m, m * v[0], m * v[1], m * v[2]);
-            sv[4 * BS + t] = make_float4(-V * sig[0], -V * sig[1], -V * sig[2], -V * sig[3]);
-            sv[5 * BS + t] = make_float4(-V * sig[4], -V * sig[5], fe[0], fe[1]);
-            sq[t] = fe[2];
+            const int u = slot_swz(t);
+            sv[u] = make_float4(B.Nx[0], B.Nx[1], B.gx[0], B.gx[1]);
+            sv[BS + u] = make_float4(B.Ny[0], B.Ny[1], B.gy[0], B.gy[1]);
+            sv[2 * BS + u] = make_float4(B.Nz[0], B.Nz[1], B.gz[0], B.gz[1]);
+            sv[3 * BS + u] = make_float4(m, m * v[0], m * v[1], m * v[2]);
+            sv[4 * BS + u] = make_float4(-V * sig[0], -V * sig[1], -V * sig[2], -V * sig[3]);
+            sv[5 * BS + u] = make_float4(-V * sig[4], -V * sig[5], fe[0], fe[1]);
+            sq[u] = fe[2];
             cs.put(t, cn);
             return;
         }
@@ -431,14 +441,15 @@ struct P2GBlock {
                 float4 X, Y, Z;
                 if constexpr (sizeof(T) == 4) {
                     const float4* sv = reinterpret_cast<const float4*>(sw);
-                    X = sv[i];
-                    Y = sv[BS + i];
-                    Z = sv[2 * BS + i];
-                    const float4 q0 = sv[3 * BS + i], q1 = sv[4 * BS + i], q2 = sv[5 * BS + i];
+                    const int u = slot_swz(i);
+                    X = sv[u];
+                    Y = sv[BS + u];
+                    Z = sv[2 * BS + u];
+                    const float4 q0 = sv[3 * BS + u], q1 = sv[4 * BS + u], q2 = sv[5 * BS + u];
                     m = q0.x, mv0 = q0.y, mv1 = q0.z, mv2 = q0.w;
                     v0 = q1.x, v1 = q1.y, v2 = q1.z, v3 = q1.w;
                     v4 = q2.x, v5 = q2.y, fe0 = q2.z, fe1 = q2.w;
-                    fe2 = sq[i];
+                    fe2 = sq[u];
                 } else {
                     m = sq[i], mv0 = sq[1 * bs + i], mv1 = sq[2 * bs + i], mv2 = sq[3 * bs + i];
                     v0 = sq[4 * bs + i], v1 = sq[5 * bs + i], v2 = sq[6 * bs + i];
@@ -821,10 +832,12 @@ __global__ void __launch_bounds__(BS) k_pass1_cells(PView<T> P, NView<T> nd, Geo
             N6[5] = B.Nz[1];
         }
         if constexpr (F32) {
+            static_assert(BS % 8 == 0, "slot swizzle groups");
             float4* sv = reinterpret_cast<float4*>(sn);
-            sv[t] = make_float4(N6[0], N6[1], N6[2], N6[3]);
-            sv[bs + t] = make_float4(N6[4], N6[5], mv[0], mv[1]);
-            smv[t] = mv[2];
+            const int u = slot_swz(t);
+            sv[u] = make_float4(N6[0], N6[1], N6[2], N6[3]);
+            sv[bs + u] = make_float4(N6[4], N6[5], mv[0], mv[1]);
+            smv[u] = mv[2];
         } else {
 #pragma unroll
             for (int c = 0; c < 6; ++c) sn[c * S + t] = N6[c];
@@ -848,9 +861,10 @@ __global__ void __launch_bounds__(BS) k_pass1_cells(PView<T> P, NView<T> nd, Geo
             float4 A, B;
             if constexpr (F32) {
                 const float4* sv = reinterpret_cast<const float4*>(sn);
-                A = sv[i];
-                B = sv[bs + i];
-                mv0 = B.z, mv1 = B.w, mv2 = smv[i];
+                const int u = slot_swz(i);
+                A = sv[u];
+                B = sv[bs + u];
+                mv0 = B.z, mv1 = B.w, mv2 = smv[u];
             } else {
                 mv0 = smv[i], mv1 = smv[bs + i], mv2 = smv[2 * bs + i];
             }
