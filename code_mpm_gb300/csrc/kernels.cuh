@@ -456,6 +456,44 @@ struct P2GBlock {
                     v3 = sq[7 * bs + i], v4 = sq[8 * bs + i], v5 = sq[9 * bs + i];
                     fe0 = sq[10 * bs + i], fe1 = sq[11 * bs + i], fe2 = sq[12 * bs + i];
                 }
+                if constexpr (sizeof(T) == 4 && CPT >= 2) {
+                    // FP32, corners sharing x (and y) bases: the products are
+                    // regrouped around the z factor.  With A = Nx Ny, Bx = Ny gx,
+                    // By = Nx gy a corner's N = A Nz, G = -(Bx Nz, By Nz, A gz),
+                    // so its seven sums are N m, N m v and Nz c + gz d, with
+                    // c and d formed once per slot and (x, y) pair.
+                    const int ix = (k0 >> 2) & 1;
+                    const float nx = ix ? X.y : X.x, gxv = ix ? X.w : X.z;
+#pragma unroll
+                    for (int jy = 0; jy < CPT / 2; ++jy) {
+                        const int iy = CPT == 4 ? jy : ((k0 >> 1) & 1);
+                        const float ny = iy ? Y.y : Y.x, gyv = iy ? Y.w : Y.z;
+                        const float A = nx * ny, Bx = ny * gxv, By = nx * gyv;
+                        const float Am = A * m, Am0 = A * mv0, Am1 = A * mv1, Am2 = A * mv2;
+                        const float c0 = A * fe0 - Bx * v0 - By * v3;
+                        const float c1 = A * fe1 - By * v1 - Bx * v3;
+                        const float c2 = A * fe2 - Bx * v5 - By * v4;
+                        const float d0 = -A * v5, d1 = -A * v4, d2 = -A * v2;
+#pragma unroll
+                        for (int iz = 0; iz < 2; ++iz) {
+                            const int j = 2 * jy + iz;
+                            const float nz = iz ? Z.y : Z.x, gzv = iz ? Z.w : Z.z;
+                            am[j] += nz * Am;
+                            ap0[j] += nz * Am0;
+                            ap1[j] += nz * Am1;
+                            ap2[j] += nz * Am2;
+                            af0[j] = fmaf(gzv, d0, fmaf(nz, c0, af0[j]));
+                            af1[j] = fmaf(gzv, d1, fmaf(nz, c1, af1[j]));
+                            af2[j] = fmaf(gzv, d2, fmaf(nz, c2, af2[j]));
+                            if constexpr (MG) {
+                                g0[j] -= nz * (Bx * m);
+                                g1[j] -= nz * (By * m);
+                                g2[j] -= gzv * Am;
+                            }
+                        }
+                    }
+                    continue;
+                }
     #pragma unroll
                 for (int j = 0; j < CPT; ++j) {
                     const int k = k0 + j;
