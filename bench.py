@@ -66,7 +66,11 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--form", default="fp32", choices=["fp64", "fp32"],
                     help="fp32: the chosen form, timed beside the plain FP64 form; fp64: the plain form alone")
-    ap.add_argument("--workload", default="batch", choices=["batch", "block", "foam"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "block", "foam", "bar"])
+    ap.add_argument("--accuracy-steps", type=int, default=-1,
+                    help="steps of the accuracy leg (chosen form against the plain FP64 form), independent of "
+                         "--steps; default: the workload's configured horizon (batch 3000, block 5000, "
+                         "foam 10000, bar 2000); 0 skips the leg")
     ap.add_argument("--specimens", type=int, default=256, help="batch workload: specimen count")
     ap.add_argument("--total", type=float, default=40.0e6, help="batch workload: target particle count")
     ap.add_argument("--block", default="0.08,0.08,0.04", help="block workload: block size in m")
@@ -189,6 +193,15 @@ def workload(args):
                "material": "von Mises hardening aluminium E=70GPa nu=0.33 rho=2700 yield=120MPa H=700MPa",
                "l2_policy": "inputs larger than L2 (~6 GB particle state)"}
         return [st], cfg
+    if args.workload == "bar":
+        st = scenes.bar()  # 50 x 10 x 10 cells of 1 mm plus one padding cell per side, 8 particles per cell
+        cfg = {"workload": "elastic cuboid bar, first-mode vibration, fixed end, non-contact path, single instance",
+               "bar_m": [0.05, 0.01, 0.01], "h_m": 1.0e-3, "grid_cells": [int(c) for c in st.cells],
+               "particles_per_cell": 8, "n_particles": st.n_particles, "n_nodes": st.n_nodes, "dt_s": st.dt_max,
+               "material": "linear elastic E=70GPa nu=0.3 rho=2700", "initial_velocity": "v_x = sin(pi x / 2L) m/s",
+               "l2_policy": "inputs smaller than L2 (40,000 particles, ~20 MB): the rate is launch- and "
+                            "latency-bound, not a bandwidth figure"}
+        return [st], cfg
     if args.workload == "block":
         size = [float(v) for v in args.block.split(",")]
         st = scenes.platen_block(size=size)  # h = 1 mm, 8 ppc, platen -5 m/s, friction 0.1
@@ -248,6 +261,8 @@ def cpu_sample(args, sts):
 
         st = scenes.graded_foam(ncell=2, block=(0.02, 0.02, 0.012), seed=5)
         return [st], [0], f"a reduced foam of the same generator (2 x 2 cells, {st.n_particles} particles)"
+    if len(sts) == 1:
+        return sts, [0], f"the whole workload ({sts[0].n_particles} particles)"
     idx = subset(sts, 16)
     n = sum(sts[i].n_particles for i in idx)
     return sts, idx, f"{len(idx)} of the {len(sts)} specimens ({n} particles, spread over the size range)"
@@ -333,6 +348,7 @@ def plain_per_specimen(sts, args, dist, contact, floor, steps):
 
 
 ACC_FIELDS = {"pos": 3, "vel": 3, "stress": 6, "e_strain": 1, "e_plastic": 1}
+ACC_STEPS = {"batch": 3000, "block": 5000, "foam": 10000, "bar": 2000}
 
 
 def download_fields(e, n, names=ACC_FIELDS):
@@ -353,36 +369,119 @@ def perturbed(st, rel, seed=1):
     return s
 
 
-def accuracy_vs_plain(sts, pk, idx, chosen, steps, contact, floor, tune_plain):
-    """Chosen-form errors against the plain FP64 form run alone on specimens idx for the same steps, and the
-    conditioning floor: the plain FP64 form against itself with positions perturbed by 1e-7 relative (the size
-    of an FP32 rounding)."""
-    from code_mpm_gb300 import engine, metrics
+def energy_mask(st, contact):
+    """The particles whose energy is counted: all but the displacement-controlled platen."""
+    import numpy as np
 
-    def plain_run(st):
-        with engine.Engine.from_state(st, engine.FORM_FP64) as e:
-            e.set_option(engine.OPT_FLOOR_FRICTION, floor)
-            apply_tune(e, tune_plain)
-            e.advance(steps, st.dt_max, contact)
-            return download_fields(e, st.n_particles)
+    from code_mpm_gb300 import snapshot
+
+    if contact:
+        return (st["pflags"] & snapshot.PF_DC_SKIP) == 0
+    m = np.ones(st.n_particles, dtype=bool)
+    m[st["dc_list"].astype(np.int64)] = False
+    return m
+
+
+def accuracy_leg(states, what, steps, contact, floor, tune, net, cell_sort=-1):
+    """The chosen form (launch shapes, FP64 fallback and network as timed) against the plain FP64 form on the same
+    specimens for `steps` steps: von Mises stress errors per specimen in two norms, and the FP64 energy balance
+    (kinetic + strain energy against the boundary work) at six checkpoints.  conditioning floor: the plain FP64
+    form against itself with positions perturbed by 1e-7 relative (the size of an FP32 rounding)."""
+    import numpy as np
+
+    from code_mpm_gb300 import batch, engine, metrics
+
+    pk = batch.pack(states) if len(states) > 1 else None
+    src = pk.state if pk is not None else states[0]
+    grids = pk.grids if pk is not None else [(src.length, src.cells)]
+    poff = pk.particle_offsets if pk is not None else np.array([0, src.n_particles], dtype=np.int64)
+    n, dt = src.n_particles, src.dt_max
+    mask = energy_mask(src, contact)
+    e0 = float(0.5 * np.sum(src["mass"][mask] * np.sum(src["vel"][mask] ** 2, axis=1)) +
+               np.sum(src["e_strain"][mask]))
+    checkpoints = sorted({max(1, round(steps * k / 6)) for k in range(1, 7)})
+
+    def run(form, state, with_net):
+        e = engine.Engine(None, None, form, grids=grids)
+        e.upload_state(state)
+        e.set_option(engine.OPT_FLOOR_FRICTION, floor)
+        apply_tune(e, tune)
+        if form == engine.FORM_FP32 and cell_sort >= 0:
+            e.set_option(engine.OPT_CELL_SORT, cell_sort)
+        if form == engine.FORM_FP32 and with_net and net is not None:
+            e.attach_surrogate(net, band=0.02, recheck=0.01)
+        e.upload_monitor_mask(mask.astype(np.uint8) * engine.MON_ENERGY)
+        series, done = [], 0
+        for c in checkpoints:
+            e.advance(c - done, dt, contact)
+            done = c
+            m = e.monitors()
+            en = m["kinetic"] + m["strain_energy"]
+            series.append({"step": c, "kinetic": m["kinetic"], "strain_energy": m["strain_energy"],
+                           "plastic_energy": m["plastic_energy"], "platen_work": m["platen_work"],
+                           "friction_work": m["friction_work"],
+                           "residual": en - e0 - m["platen_work"] - m["friction_work"]})
+        out = download_fields(e, n)
+        sg = e.surrogate_stats() if (form == engine.FORM_FP32 and with_net and net is not None) else None
+        e.close()
+        return out, series, sg
+
+    t0 = time.perf_counter()
+    chosen, ser_c, sg = run(engine.FORM_FP32, src, True)
+    plain, ser_p, _ = run(engine.FORM_FP64, src, False)
+    pert, ser_f, _ = run(engine.FORM_FP64, perturbed(src, 1e-7), False)
+    nonet = run(engine.FORM_FP32, src, False) if net is not None else None
+    secs = time.perf_counter() - t0
+
+    def cut(d, i):
+        return {k: v[poff[i]:poff[i + 1]] for k, v in d.items()}
 
     per, floor_per = [], []
-    for i in idx:
-        st = sts[i]
-        ref = plain_run(st)
-        lo, hi = (0, st.n_particles) if pk is None else (int(pk.particle_offsets[i]), int(pk.particle_offsets[i + 1]))
-        err = metrics.form_errors({k: v[lo:hi] for k, v in chosen.items()}, ref)
-        per.append(dict(err, specimen=int(i), n_particles=int(st.n_particles)))
-        floor_per.append(dict(metrics.form_errors(plain_run(perturbed(st, 1e-7)), ref), specimen=int(i)))
+    for i in range(len(poff) - 1):
+        per.append(dict(metrics.form_errors(cut(chosen, i), cut(plain, i)), specimen=i,
+                        n_particles=int(poff[i + 1] - poff[i])))
+        floor_per.append(metrics.form_errors(cut(pert, i), cut(plain, i)))
     keys = ("vm_stress_rel_l2", "vm_stress_rel", "strain_energy_rel", "plastic_energy_rel", "pos_abs_max",
             "vel_rel")
     worst = {k: max(p[k] for p in per) for k in keys}
-    bars = {"vm_stress_rel_l2": 1e-2, "strain_energy_rel": 5e-3}
-    return dict(worst, steps=steps, specimens=per, bars=bars, within_bars=all(worst[k] <= v for k, v in bars.items()),
+
+    def total(r):
+        return r["kinetic"] + r["strain_energy"]
+
+    def drift(a, b):
+        return abs(total(a) - total(b)) / abs(total(b)) if total(b) != 0 else abs(total(a))
+
+    scale = max(abs(ser_p[-1]["platen_work"]) + abs(ser_p[-1]["friction_work"]), abs(e0), 1e-300)
+    energy = {
+        "energy_drift_rel": drift(ser_c[-1], ser_p[-1]),
+        "energy_drift_rel_series": [drift(a, b) for a, b in zip(ser_c, ser_p)],
+        "work_rel": (abs(ser_c[-1]["platen_work"] - ser_p[-1]["platen_work"]) / abs(ser_p[-1]["platen_work"])
+                     if ser_p[-1]["platen_work"] != 0 else None),
+        "balance_residual_rel": {"chosen": ser_c[-1]["residual"] / scale, "plain_fp64": ser_p[-1]["residual"] / scale},
+        "conditioning_floor_energy_drift_rel": drift(ser_f[-1], ser_p[-1]),
+        "initial_energy": e0,
+        "series": {"chosen": ser_c, "plain_fp64": ser_p},
+        "definition": "E = kinetic + strain energy of the specimen particles (the platen excluded); the strain "
+                      "energy is the stress work, plastic dissipation included.  energy_drift_rel = "
+                      "|E_chosen - E_plain| / |E_plain| at the last checkpoint; balance residual = E - E_0 - "
+                      "platen work - friction work (FP64 sums on the device), over the boundary work",
+    }
+    without_network = None
+    if nonet is not None:  # the FP32 form alone: how much of the error is the network's
+        errs = [metrics.form_errors(cut(nonet[0], i), cut(plain, i)) for i in range(len(poff) - 1)]
+        without_network = {k: max(e[k] for e in errs) for k in keys}
+        without_network["energy_drift_rel"] = drift(nonet[1][-1], ser_p[-1])
+    bars = {"vm_stress_rel_l2": 1e-2, "energy_drift_rel": 5e-3}
+    got = {"vm_stress_rel_l2": worst["vm_stress_rel_l2"], "energy_drift_rel": energy["energy_drift_rel"]}
+    return dict(worst, steps=steps, specimens=per, energy=energy, bars=bars,
+                bar_norms="the stress bar is the relative L2 norm of the von Mises stress over each specimen's "
+                          "particles (worst specimen); the max-norm (vm_stress_rel) is reported beside the "
+                          "conditioning floor, the same FP64 run perturbed by 1e-7",
+                within_bars=all(got[k] <= v for k, v in bars.items()),
                 conditioning_floor={k: max(p[k] for p in floor_per) for k in keys},
-                versus="plain FP64 GPU form (itself within 1e-9 of the FP64 oracle) run alone on each listed "
-                       "specimen for the same steps; worst over the listed specimens.  conditioning_floor: the "
-                       "plain FP64 form against itself with positions perturbed by 1e-7 relative")
+                network_in_run=sg, without_network=without_network, seconds=secs,
+                versus=f"plain FP64 GPU form (itself within 1e-9 of the FP64 oracle) on {what}, same steps; "
+                       "worst over the specimens")
 
 
 def peaks_bf16():
@@ -396,6 +495,39 @@ def peaks_bf16():
 
 # algorithmic FLOPs of one sample through 13 -> 128 -> 128 -> 128 -> 7
 NET_FLOPS = 2 * (13 * 128 + 128 * 128 + 128 * 128 + 128 * 7)
+
+
+def harvest_run(e, rows, cap, steps, dt, contact, every=4):
+    """Advance engine e by `steps` steps, recording the return-map inputs of every plastic von Mises hardening
+    particle in one step out of `every` into the device rows (n x 13), up to cap rows; returns the rows written.
+    Sampling the whole run keeps its late states in the training set."""
+    n, done = 0, 0
+    while done < steps:
+        k = min(every - 1, steps - done)
+        if k:
+            e.advance(k, dt, contact)
+            done += k
+        if done >= steps:
+            break
+        if n < cap:
+            e.harvest_begin(rows.data_ptr() + 4 * 13 * n, cap - n, mat_mask=1, band=0.0)
+            e.advance(1, dt, contact)
+            n += min(e.harvest_end(), cap - n)
+        else:
+            e.advance(1, dt, contact)
+        done += 1
+    return n
+
+
+def deps_scale(rows, n):
+    """Input scale of the strain increments: the standard deviation, raised so that the largest increments
+    (the 99.9th percentile of |de| over a sample of the rows) sit within three scales."""
+    import torch
+
+    d = rows[:n, 7:]
+    std = float(d.std().item())
+    sample = d[torch.randint(0, n, (min(n, 200_000),), device=d.device)].abs().flatten()
+    return max(std, float(torch.quantile(sample, 0.999).item()) / 3.0)
 
 
 def network_for_batch(args, contact, floor, steps):
@@ -413,19 +545,18 @@ def network_for_batch(args, contact, floor, steps):
     e = engine.Engine(None, None, engine.FORM_FP64, grids=ppk.grids)
     e.upload_state(ppk.state)
     e.set_option(engine.OPT_FLOOR_FRICTION, floor)
-    e.harvest_begin(rows.data_ptr(), cap, mat_mask=1, band=0.0)
-    e.advance(steps, pilot[0].dt_max, contact)
-    n = min(e.harvest_end(), cap)
+    n = harvest_run(e, rows, cap, steps, pilot[0].dt_max, contact)
     e.close()
     t1 = time.perf_counter()
-    dsig = float(rows[:n, 7:].std().item())
+    dsig = deps_scale(rows, n)
     bsz = 8192
     epochs = int(max(20, math.ceil(5000 * bsz / max(n, 1))))  # about 5000 Adam steps
     net = engine.Net(E=200.0e9, nu=0.3, yield_=250.0e6, C0=2.0e-3, C1=1.0e12, n_samples=1000, epochs=epochs,
                      batch=bsz, deps_sigma=dsig, lr=2.0e-3)
     rep = net.train_rows(rows.data_ptr(), n)
     del rows
-    info = {"pilot": f"16 honeycomb specimens (seed 99, {ppk.state.n_particles} particles), plain FP64, {steps} steps",
+    info = {"pilot": f"16 honeycomb specimens (seed 99, {ppk.state.n_particles} particles), plain FP64, {steps} steps "
+                     "(inputs of one step in four)",
             "harvested_rows": n, "seconds_pilot": t1 - t0, "training": rep}
     return net, info
 
@@ -443,42 +574,16 @@ def network_for_foam(args, contact, floor, steps):
     t0 = time.perf_counter()
     with engine.Engine.from_state(pilot, engine.FORM_FP64) as e:
         e.set_option(engine.OPT_FLOOR_FRICTION, floor)
-        e.harvest_begin(rows.data_ptr(), cap, mat_mask=1, band=0.0)
-        e.advance(steps, pilot.dt_max, contact)
-        n = min(e.harvest_end(), cap)
+        n = harvest_run(e, rows, cap, steps, pilot.dt_max, contact)
     t1 = time.perf_counter()
-    dsig = float(rows[:n, 7:].std().item())
+    dsig = deps_scale(rows, n)
     bsz = 8192
     epochs = int(max(20, math.ceil(5000 * bsz / max(n, 1))))
     net = engine.Net(E=70.0e9, nu=0.33, yield_=120.0e6, C0=700.0e6 / 1.0e12, C1=1.0e12, n_samples=1000,
                      epochs=epochs, batch=bsz, deps_sigma=dsig, lr=2.0e-3)
     rep = net.train_rows(rows.data_ptr(), n)
     return net, {"pilot": f"reduced foam 2 x 2 cells (seed 9, {pilot.n_particles} particles), plain FP64, "
-                          f"{steps} steps", "harvested_rows": n, "seconds_pilot": t1 - t0, "training": rep}
-
-
-def accuracy_reduced_foam(steps, contact, floor, tune, net, cell_sort=-1):
-    """Foam accuracy: the chosen form (same launch shapes and network) against the plain FP64 form on a reduced
-    foam of the same generator (2 x 2 cells) for the same steps."""
-    from code_mpm_gb300 import engine, metrics, scenes
-
-    st = scenes.graded_foam(ncell=2, block=(0.02, 0.02, 0.012), seed=5)
-    outs = {}
-    for form in (engine.FORM_FP32, engine.FORM_FP64):
-        with engine.Engine.from_state(st, form) as e:
-            e.set_option(engine.OPT_FLOOR_FRICTION, floor)
-            apply_tune(e, tune)
-            if form == engine.FORM_FP32 and cell_sort >= 0:
-                e.set_option(engine.OPT_CELL_SORT, cell_sort)
-            if form == engine.FORM_FP32 and net is not None:
-                e.attach_surrogate(net, band=0.02, recheck=0.01)
-            e.advance(steps, st.dt_max, contact)
-            outs[form] = download_fields(e, st.n_particles)
-    err = metrics.form_errors(outs[engine.FORM_FP32], outs[engine.FORM_FP64])
-    bars = {"vm_stress_rel_l2": 1e-2, "strain_energy_rel": 5e-3}
-    return dict(err, steps=steps, bars=bars, within_bars=all(err[k] <= v for k, v in bars.items()),
-                versus=f"plain FP64 form on a reduced foam of the same generator ({st.n_particles} particles), "
-                       "same steps")
+                          f"{steps} steps (inputs of one step in four)", "harvested_rows": n, "seconds_pilot": t1 - t0, "training": rep}
 
 
 def network_isolated(contact_unused=None):
@@ -630,7 +735,8 @@ def run_gb300(args, dist: Dist):
     dist.barrier()
     sts, cfg = workload(args)
     pk = batch.pack(sts) if len(sts) > 1 else None
-    contact, floor = 1, 1
+    # the bar vibrates freely on the non-contact path; the other workloads are platen crushes on the contact path
+    contact, floor = (0, 0) if args.workload == "bar" else (1, 1)
     n = sum(st.n_particles for st in sts)
     n_nodes = sum(st.n_nodes for st in sts)
     dt = sts[0].dt_max
@@ -654,8 +760,10 @@ def run_gb300(args, dist: Dist):
     # the learned return map (chosen form, batch workload): trained on a pilot batch's plain-method samples
     net, net_info = None, None
     use_net = compare and not args.no_network and args.workload in ("batch", "foam")
+    acc_steps = ACC_STEPS[args.workload] if args.accuracy_steps < 0 else args.accuracy_steps
     if use_net:
-        pilot_steps = min(args.warmup + args.steps, 1000)
+        # the pilot covers every state the network will serve: the timed steps and the accuracy horizon
+        pilot_steps = max(args.warmup + args.steps, acc_steps)
         if args.workload == "foam":
             net, net_info = network_for_foam(args, contact, floor, steps=pilot_steps)
         else:
@@ -677,17 +785,24 @@ def run_gb300(args, dist: Dist):
 
     accuracy = None
     if compare:
-        if args.workload == "foam":
-            accuracy = accuracy_reduced_foam(args.warmup + args.steps, contact, floor, tune, net, args.cell_sort)
-        else:
-            chosen_out = download_fields(e, n)
-            idx = subset(sts, 8)
-            tune_plain = plain["autotune"] if plain else None
-            accuracy = accuracy_vs_plain(sts, pk, idx, chosen_out, args.warmup + args.steps, contact, floor,
-                                         tune_plain)
-            del chosen_out
+        if acc_steps > 0:
+            if args.workload == "foam":
+                from code_mpm_gb300 import scenes
+
+                red = scenes.graded_foam(ncell=2, block=(0.02, 0.02, 0.012), seed=5)
+                acc_states = [red]
+                what = f"a reduced foam of the same generator (2 x 2 cells, {red.n_particles} particles)"
+            elif pk is not None:
+                idx = subset(sts, 8)
+                acc_states = [sts[i] for i in idx]
+                what = (f"{len(idx)} of the {len(sts)} specimens spread over the size range "
+                        f"({sum(s.n_particles for s in acc_states)} particles), batched in both forms")
+            else:
+                acc_states = sts
+                what = f"the workload itself ({n} particles)"
+            accuracy = accuracy_leg(acc_states, what, acc_steps, contact, floor, tune, net, args.cell_sort)
         if pk is None:  # single instance: the plain form timed on the same state (fewer steps for the foam)
-            kp = args.steps if args.workload == "block" else max(1, min(args.steps, 20))
+            kp = args.steps if args.workload in ("block", "bar") else max(1, min(args.steps, 20))
             with make_engine(sts, pk, engine.FORM_FP64) as ep:
                 ep.set_option(engine.OPT_FLOOR_FRICTION, floor)
                 tune_p = None if args.no_autotune else ep.autotune(steps=2, dt=dt, contact=bool(contact))
@@ -696,7 +811,15 @@ def run_gb300(args, dist: Dist):
                      "steps": kp, "dtype": "f64", "gpu_launches": launches_p, "clocks": clocks_p,
                      "autotune": tune_p}
 
-    prof, kernels = kernel_table(e, min(args.steps, 30), dt, contact)
+    prof_steps = min(args.steps, 30)
+    prof, kernels = kernel_table(e, prof_steps, dt, contact)
+    # launch gaps: the kernels' own time (each launch bracketed by events, graph off) against the graph-replayed step
+    kernel_ms = sum(v["ms"] for v in prof.values()) / prof_steps
+    launch_gaps = {"kernel_ms_per_step": kernel_ms, "step_ms": ms / args.steps,
+                   "busy_fraction": kernel_ms / (ms / args.steps),
+                   "launches_per_step": sum(v["launches"] for v in prof.values()) / prof_steps,
+                   "how": f"sum of per-kernel CUDA-event times over {prof_steps} profiled steps (graph off) per step, "
+                          "over the timed step (graph replay)"}
     n_active = active_nodes(e, n_nodes)
     roofline = roofline_of(prof, formkey, n, n_active, args.workload)
     without_net = None
@@ -730,7 +853,7 @@ def run_gb300(args, dist: Dist):
                                       else "")),
                           parallelism=f"replicas x{dist.world}"),
            "clocks": clocks_rec, "gpu_launches": launches, "autotune": tune, "roofline": roofline,
-           "kernels": kernels, "e2e": e2e}
+           "kernels": kernels, "launch_gaps": launch_gaps, "e2e": e2e}
     if plain is not None:
         out["plain_fp64"] = plain
         out["chosen_over_plain"] = value / plain["value"]
@@ -764,20 +887,23 @@ def run_reference(args, dist: Dist):
     threads = os.cpu_count() or 1
     work = [sts_[i].copy() for i in idx]
     n = sum(s.n_particles for s in work)
+    contact, floor = (0, 0) if args.workload == "bar" else (1, 1)
 
     def step():
-        return sum(pyoracle.advance(s, 1, 1, floor_friction=1, threads=threads, omp=True) for s in work)
+        return sum(pyoracle.advance(s, 1, contact, floor_friction=floor, threads=threads, omp=True) for s in work)
 
-    w = max(1, min(args.warmup, 1))
+    # warm-up as asked (each step is a bounded sample); timed steps as asked unless they would pass two minutes
+    w = max(1, args.warmup)
+    t0 = time.perf_counter()
     for _ in range(w):
         step()
-    one = step()
+    one = (time.perf_counter() - t0) / w
     k = max(1, min(args.steps, int(120.0 / max(one, 1e-3))))
     secs = sum(step() for _ in range(k))
     rate = n * k / secs
-    sample = (f"{k} timed steps (+{w + 1} warm-up) of {what}; CPU restatement of the reference path, OpenMP with "
+    sample = (f"{k} timed steps (+{w} warm-up) of {what}; CPU restatement of the reference path, OpenMP with "
               f"per-node locks, {threads} threads")
-    return {"metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": dist.world, "steps": k, "warmup": w + 1,
+    return {"metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": dist.world, "steps": k, "warmup": w,
             "ms_per_step": 1e3 * secs / k, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (seeded scene generators)", "config": dict(cfg, form="reference-cpu"),
             "impl": "reference",

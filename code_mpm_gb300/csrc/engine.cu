@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "kernels.cuh"
+#include "run_pairs.cuh"
 #include "mpm_gb300.h"
 #include "mpm_surrogate.h"
 #include "radix_sort.cuh"
@@ -85,6 +86,7 @@ struct mpm_ctx {
     // sort
     DevBuf keys0, vals0, keys1, vals1, keys_copy, counts;
     DevBuf dclist, mats, staging, tune_backup, surf, mon_mask, mon_acc;
+    DevBuf work_acc;  // boundary work since the last particle upload (FP64): displacement control, friction
     int nsurf = 0;
     bool have_mon = false;
     // host pinned staging for the error word
@@ -103,16 +105,22 @@ struct mpm_ctx {
     DevBuf loc;
     // return-map network (FP32 form)
     mpm_net* net = nullptr;
-    float sg_band = 0.02f, sg_recheck = 0.01f;
+    float sg_band = 0.02f, sg_recheck = 0.01f;  // the fallback band also bounds the FP64 fallback without a network
+    float sg_guard = 0.01f;  // tolerance of the guard on the network's results, a fraction of k0 (0: off)
+    int fp64_fallback = 1;  // FP32 form: the exact map in FP64 for von Mises hardening particles near or past the surface
     unsigned sg_mats = 0;
     std::vector<MatConst> mats_host;
     DevBuf q_in, q_out, q_vol, q_pidx, q_count, sg_acc;
     // CUDA graph of two steps, replayed while nothing it captured changes
     int use_graph = 1;
-    cudaGraphExec_t gexec = nullptr;
-    double g_dt = 0.0;
-    int g_contact = -1;
-    long long g_launches = 0;
+    // One graph per key-buffer parity: a captured step reads the cell keys from
+    // the buffer key_buf named at capture and leaves the next keys in the other,
+    // so a graph is valid only while key_buf has the value it was captured with;
+    // advances of odd length change the parity between replays.
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    double g_dt[2] = {0.0, 0.0};
+    int g_contact[2] = {-1, -1};
+    long long g_launches[2] = {0, 0};
     DevBuf dsim, tl_dev;
     double* h_sim = nullptr;  // pinned: time, dt, step (as double bits), tv[3]
     // harvesting of return-map inputs
@@ -138,7 +146,7 @@ struct mpm_ctx {
                           &g_state, &g_fixed, &g_friction, &g_ratio, &g_q, &g_owner, &g_nowner, &g_need, &g_list, &g_count, &rs_chunk, &cstart,
                           &cend, &keys0, &vals0, &keys1, &vals1, &keys_copy, &counts, &dclist, &mats, &staging, &tune_backup, &surf, &mon_mask, &mon_acc, &loc, &geom_tab, &sid, &alist, &acount,
                           &q_in, &q_out, &q_vol, &q_pidx, &q_count, &sg_acc, &hv_count,
-                          &dsim, &tl_dev, &orig, &ptmp, &Fe};
+                          &dsim, &tl_dev, &orig, &ptmp, &Fe, &work_acc};
         all.assign(std::begin(list), std::end(list));
     }
 };
@@ -734,9 +742,10 @@ __global__ void k_step_end(DevSim* d) {
 }
 
 void graph_reset(mpm_ctx* c) {
-    if (c && c->gexec) {
-        cudaGraphExecDestroy(c->gexec);
-        c->gexec = nullptr;
+    for (int k = 0; c && k < 2; ++k) {
+        if (!c->gexec[k]) continue;
+        cudaGraphExecDestroy(c->gexec[k]);
+        c->gexec[k] = nullptr;
     }
 }
 
@@ -794,8 +803,35 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph, bool output) {
                    detecting ? (unsigned*)c->cstart.p : nullptr, detecting ? (unsigned*)c->cend.p : nullptr, perm,
                    P.sid);
         }
-        if (c->p2g_reduce >= 2) {  // shared-memory cell runs, 1 / 2 / 4 corners per thread
-            const int bs = c->p2g_block, cpt = 1 << (c->p2g_reduce - 2);
+        bool pairs_done = false;
+        if constexpr (sizeof(T) == 4) {
+            if (c->p2g_reduce >= 5) {  // runs reduced in registers and by a pair shuffle (mode 6: tile staged)
+                const int bs = c->p2g_block;
+                const unsigned pg = (unsigned)((n + 4LL * bs - 1) / (4LL * bs));
+                const bool st = c->p2g_reduce == 6;
+#define PAIRS(B, MGV, STV)                                                                                       \
+    LAUNCH_SMEM("p2g", (k_p2g_pairs<B, MGV, STV>), pg, B, p2g_pairs_smem<B>(STV), P, N, g, skeys, perm, n, 1, err)
+#define PAIRS_BS(B)                            \
+    do {                                       \
+        if (mg_in_p2g) {                       \
+            if (st) PAIRS(B, true, true);      \
+            else PAIRS(B, true, false);        \
+        } else {                               \
+            if (st) PAIRS(B, false, true);     \
+            else PAIRS(B, false, false);       \
+        }                                      \
+    } while (0)
+                if (bs == 128) PAIRS_BS(128);
+                else if (bs == 256) PAIRS_BS(256);
+                else PAIRS_BS(512);
+#undef PAIRS_BS
+#undef PAIRS
+                pairs_done = true;
+            }
+        }
+        if (pairs_done) {
+        } else if (c->p2g_reduce >= 2) {  // shared-memory cell runs, 1 / 2 / 4 corners per thread
+            const int bs = c->p2g_block, cpt = 1 << std::min(2, c->p2g_reduce - 2);
             if (mg_in_p2g)
                 LAUNCH_CELLS("p2g", k_p2g_cells_mg, T, cpt, bs, blocks_for(n, bs), p2g_cells_smem<T>(bs), P, N, g,
                              skeys, perm, n, fp32);
@@ -849,8 +885,20 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph, bool output) {
         const T mm = sizeof(T) == 4 ? (T)fps_float_threshold(c->sim.mass_min) : (T)c->sim.mass_min;
         // displacement control, grid update, displacement control, f/m: one pass over the active nodes
         LAUNCH("node_phase_a", k_node_phase_a<T>, nodeblocks, NTHREADS, N, (T)dt, c->sim.damping, contact,
-               c->floor_friction, (const unsigned*)c->dclist.p, c->ndc, (const T*)c->vel.p, n, mm, output ? 0 : 1);
-        if (c->p2g_reduce >= 2) {  // the same reduction as P2G: shared-memory cell runs
+               c->floor_friction, (const unsigned*)c->dclist.p, c->ndc, (const T*)c->vel.p, n, mm, output ? 0 : 1,
+               (double*)c->work_acc.p, dt);
+        if (sizeof(T) == 4 && c->p2g_reduce >= 5) {  // the same runs as P2G, reduced by lane pairs
+            if constexpr (sizeof(T) == 4) {
+                const int b1 = c->pass1_block;
+                const unsigned pg = (unsigned)((n + 4LL * b1 - 1) / (4LL * b1));
+                if (b1 == 128)
+                    LAUNCH("pass1_remap", k_pass1_pairs<128>, pg, 128, P, N, g, skeys, perm, n, (float)dt, contact);
+                else if (b1 == 256)
+                    LAUNCH("pass1_remap", k_pass1_pairs<256>, pg, 256, P, N, g, skeys, perm, n, (float)dt, contact);
+                else
+                    LAUNCH("pass1_remap", k_pass1_pairs<512>, pg, 512, P, N, g, skeys, perm, n, (float)dt, contact);
+            }
+        } else if (c->p2g_reduce >= 2) {  // the same reduction as P2G: shared-memory cell runs
             const int b1 = c->pass1_block;
             LAUNCH_CELLS("pass1_remap", k_pass1_cells, T, c->pass1_corners, b1, blocks_for(n, b1),
                          pass1_cells_smem<T>(b1), P, N, g, skeys, perm, n, (T)dt, mm, contact);
@@ -880,6 +928,8 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph, bool output) {
         a.sg_band = 0.0f;
         a.q = SurrogateQueue{};
         a.sg_acc = nullptr;
+        a.fb_wide = (sizeof(T) == 4 && c->fp64_fallback) ? 1 : 0;
+        a.fb_band = c->sg_band;
         a.hv_on = c->hv_on;
         a.hv_mats = c->hv_mats;
         a.hv_band = c->hv_band;
@@ -946,8 +996,9 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph, bool output) {
                 }
                 if (rq) return rq;
                 LAUNCH("net_finish", k_sg_finish, (unsigned)c->sm_count * 8, 256, P, a.q, net_material(c->net),
-                       contact, dt, 1.0f / net_yield(c->net), c->sg_recheck, (unsigned long long)c->sim.step,
-                       graph ? &dsim->step : (const unsigned long long*)nullptr, a.sg_acc);
+                       contact, dt, 1.0 / (double)net_yield(c->net), c->sg_recheck, (unsigned long long)c->sim.step,
+                       graph ? &dsim->step : (const unsigned long long*)nullptr, a.sg_acc,
+                       net_guard(c->net, c->sg_guard));
             }
         }
         c->keys_valid = true;
@@ -1019,7 +1070,8 @@ int advance_graph(mpm_ctx* c, int nsteps, double dt, int contact, bool between_r
     const int tail = output_last ? 1 : 0;
     const bool can = c->use_graph && !c->profile && c->stream != nullptr && c->n > 0 && nsteps - tail - s >= 2;
     if (!can) return plain();
-    if (c->gexec && (c->g_dt != dt || c->g_contact != contact)) graph_reset(c);
+    const int par = c->key_buf;  // the capture's two steps flip it twice: the same on return
+    if (c->gexec[par] && (c->g_dt[par] != dt || c->g_contact[par] != contact)) graph_reset(c);
     int rc;
     if ((rc = ensure(c, c->dsim, sizeof(DevSim)))) return rc;
     if (!c->h_sim && cudaMallocHost(&c->h_sim, sizeof(DevSim)) != cudaSuccess) {
@@ -1031,7 +1083,7 @@ int advance_graph(mpm_ctx* c, int nsteps, double dt, int contact, bool between_r
     DevSim hs{c->sim.time, dt, (unsigned long long)c->sim.step, {0.0, 0.0, 0.0}};
     memcpy(c->h_sim, &hs, sizeof(hs));
     CK(cudaMemcpyAsync(c->dsim.p, c->h_sim, sizeof(DevSim), cudaMemcpyHostToDevice, c->stream));
-    if (!c->gexec) {
+    if (!c->gexec[par]) {
         const long long l0 = c->launches;
         cudaGraph_t gr = nullptr;
         CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
@@ -1043,22 +1095,23 @@ int advance_graph(mpm_ctx* c, int nsteps, double dt, int contact, bool between_r
             if (gr) cudaGraphDestroy(gr);
             return r2 ? r2 : fail(c, MPM_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(ec));
         }
-        ec = cudaGraphInstantiate(&c->gexec, gr, 0);
+        ec = cudaGraphInstantiate(&c->gexec[par], gr, 0);
         cudaGraphDestroy(gr);
         if (ec != cudaSuccess) {
             cudaGetLastError();
-            c->gexec = nullptr;
+            c->gexec[par] = nullptr;
             return fail(c, MPM_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(ec));
         }
-        c->g_dt = dt;
-        c->g_contact = contact;
-        c->g_launches = c->launches - l0;
-        CK(cudaGraphLaunch(c->gexec, c->stream));  // the two captured steps (host state already advanced)
+        if (c->key_buf != par) return fail(c, MPM_ERR_STATE, "captured steps left the key buffers out of phase");
+        c->g_dt[par] = dt;
+        c->g_contact[par] = contact;
+        c->g_launches[par] = c->launches - l0;
+        CK(cudaGraphLaunch(c->gexec[par], c->stream));  // the two captured steps (host state already advanced)
         s += 2;
     }
     for (; nsteps - tail - s >= 2; s += 2) {
-        CK(cudaGraphLaunch(c->gexec, c->stream));
-        c->launches += c->g_launches;
+        CK(cudaGraphLaunch(c->gexec[par], c->stream));
+        c->launches += c->g_launches[par];
         c->steps_since_reorder += 2;
         c->sim.time += dt;
         c->sim.step += 1;
@@ -1105,6 +1158,14 @@ bool cells_attr() {
     return cudaFuncSetAttribute(k_p2g_cells<T, CPT, BS>, a, (int)p2g_cells_smem<T>(BS)) == cudaSuccess &&
            cudaFuncSetAttribute(k_p2g_cells_mg<T, CPT, BS>, a, (int)p2g_cells_smem<T>(BS)) == cudaSuccess &&
            cudaFuncSetAttribute(k_pass1_cells<T, CPT, BS>, a, (int)pass1_cells_smem<T>(BS)) == cudaSuccess;
+}
+template <int BS>
+bool pairs_attr() {
+    const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    return cudaFuncSetAttribute(k_p2g_pairs<BS, false, false>, a, (int)p2g_pairs_smem<BS>(false)) == cudaSuccess &&
+           cudaFuncSetAttribute(k_p2g_pairs<BS, true, false>, a, (int)p2g_pairs_smem<BS>(false)) == cudaSuccess &&
+           cudaFuncSetAttribute(k_p2g_pairs<BS, false, true>, a, (int)p2g_pairs_smem<BS>(true)) == cudaSuccess &&
+           cudaFuncSetAttribute(k_p2g_pairs<BS, true, true>, a, (int)p2g_pairs_smem<BS>(true)) == cudaSuccess;
 }
 bool pass2_staged_attrs() {
     const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
@@ -1177,7 +1238,8 @@ int mpm_create_batch(const mpm_grid_desc* grids, int32_t nspec, int form, mpm_ct
     cudaGetDevice(&c->device);
     cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
     if (c->sm_count <= 0) c->sm_count = 152;
-    if (!cells_attrs<double>() || !cells_attrs<float>() || !pass2_staged_attrs()) {
+    if (!cells_attrs<double>() || !cells_attrs<float>() || !pass2_staged_attrs() || !pairs_attr<128>() ||
+        !pairs_attr<256>() || !pairs_attr<512>()) {
         cudaGetLastError();
         delete c;
         return MPM_ERR_DEVICE;
@@ -1286,7 +1348,7 @@ void mpm_destroy(mpm_ctx* c) {
         if (b->p) cudaFree(b->p);
     if (c->h_err) cudaFreeHost(c->h_err);
     if (c->h_sim) cudaFreeHost(c->h_sim);
-    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    graph_reset(c);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -1310,8 +1372,10 @@ int mpm_set_option(mpm_ctx* c, int key, double value) {
         case MPM_OPT_FLOOR_FRICTION: c->floor_friction = value != 0.0; return MPM_OK;
         case MPM_OPT_PROFILE: c->profile = value != 0.0; return MPM_OK;
         case MPM_OPT_P2G_REDUCE:
-            if (!(value >= 0.0 && value <= 4.0) || value != (double)(int)value)
-                return fail(c, MPM_ERR_ARG, "P2G mode must be 0 to 4");
+            if (!(value >= 0.0 && value <= 6.0) || value != (double)(int)value)
+                return fail(c, MPM_ERR_ARG, "P2G mode must be 0 to 6");
+            if (value >= 5.0 && c->form != MPM_FORM_FP32)
+                return fail(c, MPM_ERR_ARG, "P2G modes 5 and 6 are built for the FP32 form");
             c->p2g_reduce = (int)value;
             return MPM_OK;
         case MPM_OPT_GRAPH:
@@ -1322,6 +1386,14 @@ int mpm_set_option(mpm_ctx* c, int key, double value) {
             if (value != 0.0 && c->form != MPM_FORM_FP64)
                 return fail(c, MPM_ERR_ARG, "the large-strain pass 2 is built for the FP64 form");
             c->large_strain = value != 0.0;
+            return MPM_OK;
+        case MPM_OPT_SURROGATE_GUARD:
+            if (!(value >= 0.0 && value < 1.0)) return fail(c, MPM_ERR_ARG, "guard tolerance must be in [0, 1)");
+            c->sg_guard = (float)value;
+            return MPM_OK;
+        case MPM_OPT_FP64_FALLBACK:
+            if (value != 0.0 && value != 1.0) return fail(c, MPM_ERR_ARG, "FP64 fallback must be 0 or 1");
+            c->fp64_fallback = value != 0.0;
             return MPM_OK;
         case MPM_OPT_CELL_SORT:
             if (value != 0.0 && value != 1.0) return fail(c, MPM_ERR_ARG, "cell sort must be 0 or 1");
@@ -1492,6 +1564,9 @@ int mpm_upload_particles(mpm_ctx* c, const mpm_particles* p, int64_t n) {
             LAUNCH("fill", k_mark_dc, blocks_for(c->ndc), NTHREADS, (const unsigned*)c->dclist.p, c->ndc,
                    (uint8_t*)c->pflags.p);
     }
+    // the boundary work counts from this upload on
+    if ((rc = ensure(c, c->work_acc, 2 * sizeof(double)))) return rc;
+    CK(cudaMemsetAsync(c->work_acc.p, 0, 2 * sizeof(double), c->stream));
     // the surface particles (b_Surface) as a list, for the contact kernels
     if ((rc = ensure(c, c->surf, (size_t)std::max<long long>(1, n) * 4))) return rc;
     CK(cudaMemsetAsync(c->g_count.p, 0, 4, c->stream));
@@ -1593,8 +1668,10 @@ int mpm_set_timeline(mpm_ctx* c, const double* t, const double* v3, int32_t n) {
 }
 
 int mpm_set_sim(mpm_ctx* c, const mpm_sim* s) {
-    graph_reset(c);
     if (!c || !s) return MPM_ERR_ARG;
+    // the step graph bakes in the mass threshold and the damping; time and
+    // step count reach it through the device clock, set at every replay
+    if (s->mass_min != c->sim.mass_min || s->damping != c->sim.damping) graph_reset(c);
     c->sim = *s;
     return MPM_OK;
 }
@@ -1856,6 +1933,13 @@ int mpm_monitors_read(mpm_ctx* c, mpm_monitors* out) {
     out->kinetic = a[14];
     out->strain_energy = a[15];
     out->plastic_energy = a[16];
+    double w[2] = {0.0, 0.0};
+    if (c->work_acc.p) {
+        CK(cudaMemcpyAsync(w, c->work_acc.p, sizeof(w), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    out->platen_work = w[0];
+    out->friction_work = w[1];
     return check_device_error(c);
 }
 
@@ -1873,7 +1957,7 @@ int mpm_autotune(mpm_ctx* c, int32_t steps, double dt, int contact, mpm_tune_res
     DevBuf* state[] = {&c->pos,        &c->vel,      &c->F,          &c->stress,  &c->strain,  &c->eps_p,
                        &c->vol,        &c->e_strain, &c->e_strain_max, &c->e_strain_ti, &c->e_plastic,
                        &c->backstress, &c->mp_mg,    &c->strain_rate, &c->g_acc,   &c->g_vel,
-                       &c->g_ftemp,  &c->g_mg,       &c->g_state};
+                       &c->g_ftemp,  &c->g_mg,       &c->g_state,     &c->work_acc};
     size_t total = 0;
     for (DevBuf* b : state) total += b->bytes;
     int rc = ensure(c, c->tune_backup, total);
@@ -1933,7 +2017,8 @@ int mpm_autotune(mpm_ctx* c, int32_t steps, double dt, int contact, mpm_tune_res
         return r;
     };
     const int blocks[3] = {128, 256, 512}, corners[3] = {1, 2, 4};
-    for (int red = 0; red < 5 && rc == MPM_OK; ++red)
+    const int p2g_modes = c->form == MPM_FORM_FP32 ? 7 : 5;
+    for (int red = 0; red < p2g_modes && rc == MPM_OK; ++red)
         for (int pb = 0; pb < 3 && rc == MPM_OK; ++pb) rc = trial(0, red, 1, blocks[pb]);
     if (best[0] >= 2)
         for (int k = 0; k < 3 && rc == MPM_OK; ++k)
@@ -2057,6 +2142,7 @@ int mpm_surrogate_stats_read(mpm_ctx* c, mpm_surrogate_stats* out, int reset) {
     out->rechecked = (int64_t)h.rechecked;
     out->recheck_rms = h.rechecked ? std::sqrt(h.sq_err / (double)h.rechecked) : 0.0;
     out->recheck_max = h.max_err;
+    out->rejected = (int64_t)h.rejected;
     if (reset) {
         CK(cudaMemsetAsync(c->sg_acc.p, 0, sizeof(SurrogateAcc), c->stream));
         CK(cudaStreamSynchronize(c->stream));

@@ -642,7 +642,8 @@ __device__ __forceinline__ void coulomb(T p_t, T& f_t, T fn, T mu, T dt) {
 template <typename T>
 __device__ __forceinline__ void grid_update_regs(const NView<T>& nd, long long i, unsigned fx, T p[3], T f[3], T dt,
                                                  double damping, int contact, int floor_friction, bool zero[3],
-                                                 T& ft_y) {
+                                                 T& ft_y, T dfr[3]) {
+    dfr[0] = dfr[1] = dfr[2] = (T)0;  // the force each friction law added (for the friction work)
     if (damping != 0.0) {
         T pp = p[0] * p[0] + p[1] * p[1] + p[2] * p[2];
         if (sqrt(pp) > (T)1.0e-24) {
@@ -658,7 +659,11 @@ __device__ __forceinline__ void grid_update_regs(const NView<T>& nd, long long i
     if (!contact) {
         if (fx & 1u) {
             T trial_y = p[1] + f[1] * dt;
-            if (fabs(trial_y * dt) > (T)1.0e-24 && f[0] > (T)0) coulomb<T>(p[1], f[1], f[0], (T)nd.friction[i], dt);
+            if (fabs(trial_y * dt) > (T)1.0e-24 && f[0] > (T)0) {
+                const T f0 = f[1];
+                coulomb<T>(p[1], f[1], f[0], (T)nd.friction[i], dt);
+                dfr[1] = f[1] - f0;
+            }
             zero[0] = true;
             p[0] = 0;
             f[0] = 0;
@@ -682,7 +687,11 @@ __device__ __forceinline__ void grid_update_regs(const NView<T>& nd, long long i
 #pragma unroll
             for (int t = 0; t < 2; ++t) {
                 T trial = p[t] + f[t] * dt;
-                if (fabs(trial * dt) > (T)1.0e-24) coulomb<T>(p[t], f[t], fz, mu, dt);
+                if (fabs(trial * dt) > (T)1.0e-24) {
+                    const T f0 = f[t];
+                    coulomb<T>(p[t], f[t], fz, mu, dt);
+                    dfr[t] = f[t] - f0;
+                }
             }
         }
 #pragma unroll
@@ -955,11 +964,46 @@ __device__ __forceinline__ void node_dc_regs(const unsigned own[3], const unsign
 // momentum and the mass also go to the record's second half for phase B
 // (which overwrites it with p/m and v); clean (not an output step): the
 // node's mass, momentum and force are zeroed here, for the next step's P2G.
+//
+// work (when given): the step's boundary work in FP64, added to work[0]
+// (displacement control) and work[1] (friction).  No counterpart in the
+// reference, whose energy report has no external-work term
+// (PhysicsEngine.cpp:140-156).  A displacement-controlled node axis takes the
+// platen's velocity v and its force f is zeroed (…MPLocks.cpp:143-174;
+// contact …_Contact.cpp:283-297), so the platen supplies -f there; the
+// velocity field pass 2 strains the particles with is v at that node, so the
+// platen's work is -f v dt.  A friction law adds df to a tangent force, whose
+// work is df (p/m) dt at the updated momentum.  Summed per node in the
+// form's type, per thread in double, then over the warp and added once.
+template <typename T>
+__device__ __forceinline__ void work_add(double* work, double w_dc, double w_fr, double dt) {
+    if (!work || !__any_sync(FULL_MASK, w_dc != 0.0 || w_fr != 0.0)) return;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        w_dc += __shfl_down_sync(FULL_MASK, w_dc, off);
+        w_fr += __shfl_down_sync(FULL_MASK, w_fr, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (w_dc != 0.0) atomicAdd(work, w_dc * dt);
+        if (w_fr != 0.0) atomicAdd(work + 1, w_fr * dt);
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ double dc_power(const T f[3], const T v[3], const bool fz[3]) {
+    T s = (T)0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+        if (fz[c]) s -= f[c] * v[c];
+    return fps_f2d_form(s);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256, 4) k_node_phase_a(NView<T> nd, T dt, double damping, int contact, int floor_friction,
                                const unsigned* __restrict__ dclist, int ndc, const T* __restrict__ pvel, long long np,
-                               T mass_min, int clean) {
+                               T mass_min, int clean, double* work, double dtd) {
     const long long nn = nd.nn;
+    double w_dc = 0.0, w_fr = 0.0;
     NODE_LOOP_AHEAD(nd, i) {
         const unsigned st = nd.state[i];
         if (!nd.alist && !(st & 1u)) continue;  // the list holds active nodes only
@@ -974,13 +1018,18 @@ __global__ void __launch_bounds__(256, 4) k_node_phase_a(NView<T> nd, T dt, doub
             for (int a = 0; a < 3; ++a) own[a] = (contact && a > 0) ? own[0] : nd.owner[a * nn + i];
         }
         bool vset[3] = {false, false, false}, fz[3] = {false, false, false};
-        if (!contact) node_dc_regs<T>(own, dclist, pvel, np, m, v, vset, p, fz);
+        if (!contact) {
+            node_dc_regs<T>(own, dclist, pvel, np, m, v, vset, p, fz);
+            if (work && (fz[0] | fz[1] | fz[2])) w_dc += dc_power<T>(f, v, fz);
+        }
 #pragma unroll
         for (int c = 0; c < 3; ++c)
             if (fz[c]) f[c] = (T)0;
         bool zero[3];
-        T ft_y;
-        grid_update_regs<T>(nd, i, fx, p, f, dt, damping, contact, floor_friction, zero, ft_y);
+        T ft_y, dfr[3];
+        grid_update_regs<T>(nd, i, fx, p, f, dt, damping, contact, floor_friction, zero, ft_y, dfr);
+        if (work && (dfr[0] != (T)0 || dfr[1] != (T)0) && m > mass_min)
+            w_fr += fps_f2d_form((dfr[0] * p[0] + dfr[1] * p[1]) / m);
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             if (zero[c]) {
@@ -991,6 +1040,7 @@ __global__ void __launch_bounds__(256, 4) k_node_phase_a(NView<T> nd, T dt, doub
         }
         if (contact) {
             node_dc_regs<T>(own, dclist, pvel, np, m, v, vset, p, fz);
+            if (work && (fz[0] | fz[1] | fz[2])) w_dc += dc_power<T>(f, v, fz);
 #pragma unroll
             for (int c = 0; c < 3; ++c)
                 if (fz[c]) f[c] = (T)0;
@@ -1019,6 +1069,7 @@ __global__ void __launch_bounds__(256, 4) k_node_phase_a(NView<T> nd, T dt, doub
         *reinterpret_cast<Quad<T>*>(nd.rec + 8 * i + 4) = pm;
         *reinterpret_cast<Quad<T>*>(nd.q + 4 * i) = Quad<T>{(T)0, (T)0, (T)0, (T)0};  // for pass 1's remap sums
     }
+    work_add<T>(work, w_dc, w_fr, dtd);
 }
 
 // The node work between pass 1 and pass 2, in registers: the remap v += q/m
@@ -1122,6 +1173,11 @@ struct StepArgs {
     float sg_band;
     SurrogateQueue q;
     SurrogateAcc* sg_acc;
+    // FP32 form: von Mises hardening particles whose trial yield function is
+    // above -fb_band x k0 (the fallback band and the plastic states the network
+    // does not take) run the exact map in FP64 (cr_increment_wide)
+    int fb_wide;
+    float fb_band;
     // harvesting of return-map inputs (either form)
     int hv_on;
     unsigned hv_mats;
@@ -1606,16 +1662,24 @@ __device__ __forceinline__ unsigned pass2_particle(const PView<T>& P, const NVie
             T R = src.backstress(P, p);
             CrOut<T> o;
             // the network takes clearly plastic trial states of the materials it
-            // was trained for; the band near the surface and elastic states stay exact
+            // was trained for; the band near the surface and elastic states stay
+            // exact, the band (and every plastic state the network does not take)
+            // in FP64
             queued = false;
+            CrTrial<T> tr;
+            cr_trial<T>(M, R, sig, e, tr);
+            bool wide = false;
             if constexpr (sizeof(T) == 4) {
-                if (a.sg_on && mi < 32 && ((a.sg_mats >> mi) & 1u)) {
-                    const float f = vmh_trial<float>(M, R, sig, e);
-                    queued = f >= a.sg_band * M.fk0;
-                    if (!queued && f > 0.0f) {
-                        const unsigned m = __activemask();
-                        if ((threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(&a.sg_acc->band, (unsigned long long)__popc(m));
+                if (M.type == 4) {
+                    const float f = sqrtf(tr.J2) - tr.rad;  // the trial yield function (…_VonMisesHardening.cpp:35-46)
+                    if (a.sg_on && mi < 32 && ((a.sg_mats >> mi) & 1u)) {
+                        queued = f >= a.sg_band * M.fk0;
+                        if (!queued && f > 0.0f) {
+                            const unsigned m = __activemask();
+                            if ((threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(&a.sg_acc->band, (unsigned long long)__popc(m));
+                        }
                     }
+                    wide = a.fb_wide && !queued && f > -a.fb_band * M.fk0;
                 }
             }
             if (a.hv_on && mi < 32 && ((a.hv_mats >> mi) & 1u) && M.type == 4 &&
@@ -1631,7 +1695,19 @@ __device__ __forceinline__ unsigned pass2_particle(const PView<T>& P, const NVie
                     hr[6] = (float)R;
                 }
             }
-            if (!queued) cr_increment<T>(M, R, sig, e, o);
+            if (!queued) {
+                if constexpr (sizeof(T) == 4) {
+                    if (wide) {
+                        CrOut<double> w;
+                        cr_increment_wide(M, R, sig, e, w);
+                        cr_narrow(w, o);
+                    } else {
+                        cr_return<T>(M, R, sig, e, tr, o);
+                    }
+                } else {
+                    cr_return<T>(M, R, sig, e, tr, o);
+                }
+            }
             T V;
             if (!a.contact) {
 #pragma unroll
@@ -2241,12 +2317,14 @@ __global__ void __launch_bounds__(256) k_monitor_force(NView<T> nd, double* acc)
 // and dR to each queued particle (dR kept non-negative, as the hardening law
 // gives), with the plastic strain increment recovered as de - C^-1 dsigma
 // (the compliance of …_VonMisesHardening.cpp:64-71), and re-check a hashed
-// fraction of the particles against the exact map (the error is recorded;
+// fraction of the particles against the exact map computed in FP64 on the
+// same inputs (cr_increment_wide; the network's error is recorded; then a
+// guard replaces implausible results by that exact map, see below;
 // the network's result is kept).
 // ---------------------------------------------------------------------------
-static __global__ void k_sg_finish(PView<float> P, SurrogateQueue q, MatConst M, int contact, double dt, float inv_yield,
+static __global__ void k_sg_finish(PView<float> P, SurrogateQueue q, MatConst M, int contact, double dt, double inv_yield,
                             float recheck, unsigned long long step, const unsigned long long* step_dev,
-                            SurrogateAcc* acc) {
+                            SurrogateAcc* acc, SurrogateGuard gd) {
     if (step_dev) step = *step_dev;
     const unsigned cnt = (unsigned)min((unsigned long long)*q.count, (unsigned long long)q.cap);
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&acc->queued, (unsigned long long)cnt);
@@ -2277,18 +2355,47 @@ static __global__ void k_sg_finish(PView<float> P, SurrogateQueue q, MatConst M,
         unsigned long long h = (step + 1) * 0x9e3779b97f4a7c15ULL ^ ((unsigned long long)p * 0xbf58476d1ce4e5b9ULL);
         h = (h ^ (h >> 31)) * 0x94d049bb133111ebULL;
         if ((unsigned)(h >> 32) < thr) {
-            CrOut<float> x;
-            cr_increment<float>(M, R, sig, e, x);
-            float sq = 0.0f, mx = 0.0f;
+            // the judge: the exact map in FP64 on the same inputs
+            CrOut<double> x;
+            cr_increment_wide(M, R, sig, e, x);
+            double sq = 0.0, mx = 0.0;
 #pragma unroll
             for (int k = 0; k < 6; ++k) {
-                const float d = fabsf(o.dsig[k] - x.dsig[k]) * inv_yield;
+                const double d = fabs(fps_f2d(o.dsig[k]) - x.dsig[k]) * inv_yield;
                 sq += d * d;
-                mx = fmaxf(mx, d);
+                mx = fmax(mx, d);
             }
             atomicAdd(&acc->rechecked, 1ULL);
-            atomicAdd(&acc->sq_err, (double)sq / 6.0);
-            atomicMax(reinterpret_cast<unsigned long long*>(&acc->max_err), (unsigned long long)__double_as_longlong((double)mx));
+            atomicAdd(&acc->sq_err, sq / 6.0);
+            atomicMax(reinterpret_cast<unsigned long long*>(&acc->max_err), (unsigned long long)__double_as_longlong(mx));
+        }
+        // the guard: an input outside the training box, or a result that is not a radial return (the new stress
+        // off the yield surface k0 + R/sqrt 2, or a correction dsigma - D de with a hydrostatic part; both by more
+        // than tol k0), takes the exact map in FP64 instead
+        if (gd.tol > 0.0f) {
+            bool ok = true;
+#pragma unroll
+            for (int c = 0; c < 13; ++c) {
+                const float xn = qi[c] * gd.in_inv_scale[c];
+                ok = ok && xn >= gd.lo[c] && xn <= gd.hi[c];
+            }
+            float d[6], sn[6];
+            trial_increment<float>(M, e, d);
+#pragma unroll
+            for (int k = 0; k < 6; ++k) sn[k] = sig[k] + o.dsig[k];
+            const float a01 = sn[0] - sn[1], a12 = sn[1] - sn[2], a20 = sn[2] - sn[0];
+            const float J2 = (a01 * a01 + a12 * a12 + a20 * a20) * (1.0f / 6.0f) + sn[3] * sn[3] + sn[4] * sn[4] +
+                             sn[5] * sn[5];
+            const float rad = M.fk0 + R * 0.70710678118654752440f;
+            const float hyd = ((o.dsig[0] - d[0]) + (o.dsig[1] - d[1]) + (o.dsig[2] - d[2])) * (1.0f / 3.0f);
+            const float lim = gd.tol * M.fk0;
+            ok = ok && fabsf(sqrtf(J2) - rad) <= lim && fabsf(hyd) <= lim;
+            if (!ok) {
+                CrOut<double> w;
+                cr_increment_wide(M, R, sig, e, w);
+                cr_narrow(w, o);
+                atomicAdd(&acc->rejected, 1ULL);
+            }
         }
         apply_increment<float>(P, p, sig, e, o, q.vol[s], R, contact, dt);
     }

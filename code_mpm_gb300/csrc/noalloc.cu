@@ -30,7 +30,9 @@ namespace {
 constexpr long long NA_MAX = MPM_NOALLOC_MAX_PARTICLES;
 constexpr long long NA_TILES = (NA_MAX + RS_TILE - 1) / RS_TILE;
 // layout (32-bit words): keysA, valsA, keysB, valsB (NA_MAX each), digit counts
-// (256 per tile), then one error word, padded to 64 words.
+// (256 per tile), then one word k_cell_keys may flag a non-finite position in
+// (a write-only sink: such a particle already gets the out-of-grid key, and
+// the word is never read), padded to 64 words.
 constexpr long long NA_WORDS = 4 * NA_MAX + 256 * NA_TILES + 64;
 
 // The scratch: file scope, static storage on every device that loads the library.
@@ -72,16 +74,19 @@ extern "C" int mpm_cell_order_noalloc(const mpm_grid_desc* grid, const double* d
     Geom g{};
     long long keyspace = 1;
     for (int a = 0; a < 3; ++a) {
-        if (!(grid->length[a] > 0.0) || grid->cells[a] < 1) return MPM_ERR_ARG;
+        // cells + 2 must fit an int, and the key count a 32-bit key: check each factor before multiplying
+        if (!(grid->length[a] > 0.0) || grid->cells[a] < 1 || grid->cells[a] > (1 << 30)) return MPM_ERR_ARG;
         g.h[a] = grid->length[a] / (double)grid->cells[a];
         g.inv_h[a] = 1.0 / g.h[a];
         set_float_geometry(g, a);
         g.nn[a] = grid->cells[a] + 1;
         g.kd[a] = grid->cells[a] + 2;
-        keyspace *= (long long)g.kd[a];
+        keyspace *= (long long)g.kd[a];  // < 2^32 * (2^30 + 2): no overflow
+        if (keyspace >= 0xffffffffLL) return MPM_ERR_ARG;
     }
-    if (keyspace >= 0xffffffffLL) return MPM_ERR_ARG;
     g.key_max = (unsigned)keyspace;
+    // an error left pending by the caller's own work is not this call's to report or to clear
+    if (cudaPeekAtLastError() != cudaSuccess) return MPM_ERR_CUDA;
     unsigned* s = nullptr;
     int rc = scratch_for_current_device(&s);
     if (rc) return rc;
@@ -92,18 +97,22 @@ extern "C" int mpm_cell_order_noalloc(const mpm_grid_desc* grid, const double* d
     unsigned* counts = s + 4 * NA_MAX;
     unsigned* err = counts + 256 * NA_TILES;
     cudaStream_t st = (cudaStream_t)stream;
-    // the scratch keeps the previous call's contents: clear the error word
-    if (cudaMemsetAsync(err, 0, sizeof(unsigned), st) != cudaSuccess) return MPM_ERR_CUDA;
+    // every scratch word the sort reads is written first by this call (keys and values by k_cell_keys,
+    // digit counts by each pass's histogram), so the previous call's contents need no clearing
     const unsigned nb = (unsigned)((n + 255) / 256);
     k_cell_keys<<<nb, 256, 0, st>>>(d_pos, n, g, keysA, valsA, d_keys, err, nullptr, nullptr);
+    if (cudaGetLastError() != cudaSuccess) return MPM_ERR_CUDA;
     int bits = 1;
     while (bits < 32 && ((unsigned long long)1 << bits) <= (unsigned long long)g.key_max) ++bits;
     const int nblocks = (int)((n + RS_TILE - 1) / RS_TILE);
     unsigned *kin = keysA, *vin = valsA, *kout = keysB, *vout = valsB;
     for (int shift = 0; shift < bits; shift += 8) {
         k_rs_hist<<<nblocks, RS_THREADS, 0, st>>>(kin, n, shift, counts, nblocks);
+        if (cudaGetLastError() != cudaSuccess) return MPM_ERR_CUDA;
         k_rs_scan<<<1, 1024, 0, st>>>(counts, 256 * nblocks);
+        if (cudaGetLastError() != cudaSuccess) return MPM_ERR_CUDA;
         k_rs_scatter<<<nblocks, RS_THREADS, 0, st>>>(kin, vin, kout, vout, n, shift, counts, nblocks, nullptr);
+        if (cudaGetLastError() != cudaSuccess) return MPM_ERR_CUDA;
         unsigned* t = kin;
         kin = kout;
         kout = t;
@@ -113,6 +122,5 @@ extern "C" int mpm_cell_order_noalloc(const mpm_grid_desc* grid, const double* d
     }
     if (cudaMemcpyAsync(d_order, vin, (size_t)n * sizeof(unsigned), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
         return MPM_ERR_CUDA;
-    if (cudaGetLastError() != cudaSuccess) return MPM_ERR_CUDA;
     return MPM_OK;
 }

@@ -266,45 +266,55 @@ __device__ __forceinline__ void trial_increment(const MatConst& m, const T e[6],
     d[5] = C * (hb * e[5]);
 }
 
-// Elastic (…_Elastic.cpp:4-18); PerfectlyPlastic radial return
-// (…_PerfectlyPlastic.cpp:4-76, radius k0); von Mises with explicit
-// isotropic hardening (…_VonMisesHardening.cpp:4-92, radius k0 + R/sqrt 2,
-// dR = C0 (sqrt(2/3) C1 - R) sqrt(2/3 sum deps_p^2) when positive).
+// The trial state of a constitutive increment: the elastic predictor
+// dtr = D de and, for the plastic laws, the trial stress tr = sig + dtr, its
+// J2 and the yield radius rad (k0, plus R/sqrt 2 with hardening).
 template <typename T>
-__device__ __forceinline__ void cr_increment(const MatConst& m, T R, const T sig[6], const T e[6], CrOut<T>& o) {
-    T dtr[6];
-    trial_increment<T>(m, e, dtr);
-    o.dR = (T)0;
+struct CrTrial {
+    T dtr[6], tr[6];
+    T J2, rad;
+};
+
+template <typename T>
+__device__ __forceinline__ void cr_trial(const MatConst& m, T R, const T sig[6], const T e[6], CrTrial<T>& t) {
+    trial_increment<T>(m, e, t.dtr);
+    if (m.type == 0) return;
 #pragma unroll
-    for (int i = 0; i < 6; ++i) o.deps_p[i] = (T)0;
-    if (m.type == 0) {
-#pragma unroll
-        for (int i = 0; i < 6; ++i) o.dsig[i] = dtr[i];
-        return;
-    }
-    const bool hard = (m.type == 4);
-    T tr[6];
-#pragma unroll
-    for (int i = 0; i < 6; ++i) tr[i] = sig[i] + dtr[i];
-    const T hyd = (T)(1.0 / 3.0) * (tr[0] + tr[1] + tr[2]);
-    const T a01 = tr[0] - tr[1], a12 = tr[1] - tr[2], a20 = tr[2] - tr[0];
+    for (int i = 0; i < 6; ++i) t.tr[i] = sig[i] + t.dtr[i];
+    const T a01 = t.tr[0] - t.tr[1], a12 = t.tr[1] - t.tr[2], a20 = t.tr[2] - t.tr[0];
     T J2 = (T)(1.0 / 6.0) * a01 * a01;
     J2 += (T)(1.0 / 6.0) * a12 * a12;
     J2 += (T)(1.0 / 6.0) * a20 * a20;
-    J2 += tr[3] * tr[3];
-    J2 += tr[4] * tr[4];
-    J2 += tr[5] * tr[5];
+    J2 += t.tr[3] * t.tr[3];
+    J2 += t.tr[4] * t.tr[4];
+    J2 += t.tr[5] * t.tr[5];
+    t.J2 = J2;
     T rad = form_const<T>(m.k0, m.fk0);
-    if (hard) rad = rad + R * (T)0.70710678118654752440;  // R / sqrt(2)
-    if (J2 <= rad * rad) {
+    if (m.type == 4) rad = rad + R * (T)0.70710678118654752440;  // R / sqrt(2)
+    t.rad = rad;
+}
+
+// Elastic (…_Elastic.cpp:4-18); PerfectlyPlastic radial return
+// (…_PerfectlyPlastic.cpp:4-76, radius k0); von Mises with explicit
+// isotropic hardening (…_VonMisesHardening.cpp:4-92, radius k0 + R/sqrt 2,
+// dR = C0 (sqrt(2/3) C1 - R) sqrt(2/3 sum deps_p^2) when positive), from
+// the trial state.
+template <typename T>
+__device__ __forceinline__ void cr_return(const MatConst& m, T R, const T sig[6], const T e[6], const CrTrial<T>& t,
+                                          CrOut<T>& o) {
+    o.dR = (T)0;
 #pragma unroll
-        for (int i = 0; i < 6; ++i) o.dsig[i] = dtr[i];
+    for (int i = 0; i < 6; ++i) o.deps_p[i] = (T)0;
+    if (m.type == 0 || t.J2 <= t.rad * t.rad) {
+#pragma unroll
+        for (int i = 0; i < 6; ++i) o.dsig[i] = t.dtr[i];
         return;
     }
-    const T sc = rad / sqrt(J2);
+    const T hyd = (T)(1.0 / 3.0) * (t.tr[0] + t.tr[1] + t.tr[2]);
+    const T sc = t.rad / sqrt(t.J2);
     T dev[6];
 #pragma unroll
-    for (int i = 0; i < 6; ++i) dev[i] = tr[i];
+    for (int i = 0; i < 6; ++i) dev[i] = t.tr[i];
     dev[0] -= hyd;
     dev[1] -= hyd;
     dev[2] -= hyd;
@@ -324,7 +334,7 @@ __device__ __forceinline__ void cr_increment(const MatConst& m, T R, const T sig
     ee[5] = o.dsig[5] * iG;
 #pragma unroll
     for (int i = 0; i < 6; ++i) o.deps_p[i] = e[i] - ee[i];
-    if (!hard) return;
+    if (m.type != 4) return;
     T ep = (T)0;
 #pragma unroll
     for (int i = 0; i < 6; ++i) ep += o.deps_p[i] * o.deps_p[i];
@@ -333,6 +343,36 @@ __device__ __forceinline__ void cr_increment(const MatConst& m, T R, const T sig
     o.dR = (sat > (T)0) ? form_const<T>(m.C0, m.fC0) * sat * ep : (T)0;
 }
 
+template <typename T>
+__device__ __forceinline__ void cr_increment(const MatConst& m, T R, const T sig[6], const T e[6], CrOut<T>& o) {
+    CrTrial<T> t;
+    cr_trial<T>(m, R, sig, e, t);
+    cr_return<T>(m, R, sig, e, t, o);
+}
+
+// The exact map in FP64 on FP32 state (the chosen form's fallback path and
+// the judge of the learned map): the float inputs widened exactly, the
+// increment computed in double (cr_increment<double>, the plain form's
+// arithmetic), each output rounded once to float.
+__device__ __forceinline__ void cr_increment_wide(const MatConst& m, float R, const float sig[6], const float e[6],
+                                                  CrOut<double>& w) {
+    double s64[6], e64[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        s64[i] = fps_f2d(sig[i]);
+        e64[i] = fps_f2d(e[i]);
+    }
+    cr_increment<double>(m, fps_f2d(R), s64, e64, w);
+}
+
+__device__ __forceinline__ void cr_narrow(const CrOut<double>& w, CrOut<float>& o) {
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        o.dsig[i] = __double2float_rn(w.dsig[i]);
+        o.deps_p[i] = __double2float_rn(w.deps_p[i]);
+    }
+    o.dR = __double2float_rn(w.dR);
+}
 
 // ---------------------------------------------------------------------------
 // Large-strain pass 2 helpers (FP64 form; G2P_P2_LargeStrain,

@@ -142,6 +142,41 @@ __device__ void label_sample(long long i, const double sig[6], double R, const d
     ti[7] = (float)(f / M.k0);
 }
 
+// Per-column min and max of the normalised inputs x (n x 16, first NIN
+// columns) as order-preserving unsigned keys: box[c] min, box[NIN + c] max.
+__device__ __forceinline__ unsigned f2ord(float f) {
+    const unsigned u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__global__ void k_box(long long n, const float* __restrict__ x, unsigned* __restrict__ box) {
+    unsigned lo[NIN], hi[NIN];
+    for (int c = 0; c < NIN; ++c) {
+        lo[c] = 0xffffffffu;
+        hi[c] = 0u;
+    }
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        for (int c = 0; c < NIN; ++c) {
+            const unsigned k = f2ord(x[i * IN + c]);
+            lo[c] = min(lo[c], k);
+            hi[c] = max(hi[c], k);
+        }
+    for (int c = 0; c < NIN; ++c) {
+        const unsigned a = __reduce_min_sync(0xffffffffu, lo[c]), b = __reduce_max_sync(0xffffffffu, hi[c]);
+        if ((threadIdx.x & 31) == 0) {
+            atomicMin(&box[c], a);
+            atomicMax(&box[NIN + c], b);
+        }
+    }
+}
+
+static float ord2f(unsigned k) {
+    const unsigned u = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+}
+
 // per-output sums of the targets (mean and standard deviation)
 __global__ void k_moments(long long n, const float* __restrict__ t, double* __restrict__ acc) {
     __shared__ double s[2 * NOUT];
@@ -422,6 +457,24 @@ __global__ void k_exact_fp32(long long n, const float* __restrict__ in, MatConst
     }
     CrOut<float> o;
     cr_increment<float>(M, in[i * NIN + 6], sig, e, o);
+    for (int c = 0; c < 6; ++c) out[i * NOUT + c] = o.dsig[c];
+    out[i * NOUT + 6] = o.dR;
+}
+
+// the exact return map in FP64 on physical rows, outputs rounded once to
+// float: the arithmetic of the FP32 form's fallback path (cr_increment_wide)
+__global__ void k_exact_wide(long long n, const float* __restrict__ in, MatConst M, float* __restrict__ out) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float sig[6], e[6];
+    for (int c = 0; c < 6; ++c) {
+        sig[c] = in[i * NIN + c];
+        e[c] = in[i * NIN + 7 + c];
+    }
+    CrOut<double> w;
+    cr_increment_wide(M, in[i * NIN + 6], sig, e, w);
+    CrOut<float> o;
+    cr_narrow(w, o);
     for (int c = 0; c < 6; ++c) out[i * NOUT + c] = o.dsig[c];
     out[i * NOUT + 6] = o.dR;
 }
@@ -708,6 +761,8 @@ struct mpm_net {
     float in_inv_scale[NIN];
     float out_scale[NOUT], out_shift[NOUT];
     bool packed = false;
+    // box of the normalised training inputs (the guard's first check); unbounded until trained
+    float box_lo[NIN], box_hi[NIN];
 };
 
 static MatConst make_mat(const mpm_net_config& c) {
@@ -878,6 +933,10 @@ int mpm_net_create(const mpm_net_config* cfg, mpm_net** out) {
         net->in_inv_scale[7 + c] = (float)(1.0 / cfg->deps_sigma);
     }
     net->in_inv_scale[6] = (float)(1.0 / cfg->yield);
+    for (int c = 0; c < NIN; ++c) {
+        net->box_lo[c] = -INFINITY;
+        net->box_hi[c] = INFINITY;
+    }
     for (int c = 0; c < NOUT; ++c) {
         net->out_scale[c] = 1.0f;
         net->out_shift[c] = 0.0f;
@@ -987,6 +1046,21 @@ static int train_impl(mpm_net* net, const float* d_rows, long long n_rows, mpm_n
         cudaGetLastError();
         freeall();
         return MPM_ERR_NOMEM;
+    }
+    {  // the box of the training inputs, for the guard
+        unsigned hb[2 * NIN];
+        for (int c = 0; c < NIN; ++c) {
+            hb[c] = 0xffffffffu;
+            hb[NIN + c] = 0u;
+        }
+        unsigned* db = reinterpret_cast<unsigned*>(dvec);
+        cudaMemcpy(db, hb, sizeof(hb), cudaMemcpyHostToDevice);
+        k_box<<<net->sm_count * 4, 256>>>(n, x, db);
+        cudaMemcpy(hb, db, sizeof(hb), cudaMemcpyDeviceToHost);
+        for (int c = 0; c < NIN; ++c) {
+            net->box_lo[c] = ord2f(hb[c]);
+            net->box_hi[c] = ord2f(hb[NIN + c]);
+        }
     }
     cudaMemset(acc, 0, 64 * 8);
     k_moments<<<net->sm_count * 4, 256>>>(n, t, acc);
@@ -1132,12 +1206,17 @@ int mpm_net_train_rows(mpm_net* net, const float* d_rows, int64_t n, mpm_net_rep
 }
 
 int mpm_net_infer(mpm_net* net, const float* d_in, float* d_out, int64_t n, int kernel, void* stream) {
-    if (!net || n < 0 || kernel < 0 || kernel > 2) return MPM_ERR_ARG;
+    if (!net || n < 0 || kernel < 0 || kernel > 3) return MPM_ERR_ARG;
     if (n == 0) return MPM_OK;
     if (!d_in || !d_out) return MPM_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
     if (kernel == 2) {
         k_exact_fp32<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, d_in, net->mat, d_out);
+        NCK(cudaGetLastError());
+        return MPM_OK;
+    }
+    if (kernel == 3) {
+        k_exact_wide<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, d_in, net->mat, d_out);
         NCK(cudaGetLastError());
         return MPM_OK;
     }
@@ -1225,5 +1304,15 @@ int net_run_queue(mpm_net* net, const SurrogateQueue& q, cudaStream_t s, unsigne
 }
 
 float net_yield(const mpm_net* net) { return (float)net->cfg.yield; }
+SurrogateGuard net_guard(const mpm_net* net, float tol) {
+    SurrogateGuard g;
+    for (int c = 0; c < NIN; ++c) {
+        g.in_inv_scale[c] = net->in_inv_scale[c];
+        g.lo[c] = net->box_lo[c];
+        g.hi[c] = net->box_hi[c];
+    }
+    g.tol = tol;
+    return g;
+}
 const MatConst& net_material(const mpm_net* net) { return net->mat; }
 }  // namespace mpm

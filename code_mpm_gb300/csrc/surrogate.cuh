@@ -25,8 +25,18 @@ struct SurrogateQueue {
 
 // Counters of the in-loop use (device, doubles/u64 as laid out here).
 struct SurrogateAcc {
-    unsigned long long queued, band, rechecked, pad;
+    unsigned long long queued, band, rechecked, rejected;
     double sq_err, max_err;  // over rechecks, |dsigma error| / yield
+};
+
+// The guard on the network's results: the box of normalised inputs the
+// network was trained on, the input scaling, and the tolerance (a fraction
+// of k0) of the plasticity checks.  A result outside the guard is replaced by
+// the exact map in FP64.
+struct SurrogateGuard {
+    float in_inv_scale[13];
+    float lo[13], hi[13];
+    float tol;
 };
 
 // Run the network over the queue (device-side count; no host sync).
@@ -34,5 +44,7 @@ int net_run_queue(mpm_net* net, const SurrogateQueue& q, cudaStream_t s, unsigne
 // The material the network was trained for, and its yield stress.
 const MatConst& net_material(const mpm_net* net);
 float net_yield(const mpm_net* net);
+// The guard of the network's results at tolerance tol (tol <= 0: no guard).
+SurrogateGuard net_guard(const mpm_net* net, float tol);
 
 }  // namespace mpm

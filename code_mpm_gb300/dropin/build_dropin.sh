@@ -10,10 +10,11 @@
 # streamed through sed, no copy written), and glm comes from oracle/glmshim.
 #
 # usage: code_mpm_gb300/dropin/build_dropin.sh [reference_dir]
+#   reference_dir: default $MPM_REFERENCE_DIR, else a checkout named `reference` beside this repository
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 ROOT="$(cd "$HERE/../.." && pwd)"
-REF="${1:-/root/reference}"
+REF="${1:-${MPM_REFERENCE_DIR:-$ROOT/../reference}}"
 OUT="$ROOT/oracle/_ref"
 LIBDIR="$ROOT/code_mpm_gb300/_lib"
 if [ ! -f "$REF/PhysicsEngine.h" ]; then
@@ -23,7 +24,7 @@ fi
 [ -f "$LIBDIR/libmpm_gb300.so" ] || python -m code_mpm_gb300.build
 mkdir -p "$OUT/obj_gb300"
 CXX="${CXX:-g++}"
-BASE=(-std=c++17 -O2 -ffp-contract=off -w -I "$ROOT/oracle/glmshim" -I "$REF" -I "$ROOT/oracle" -I "$ROOT/include"
+BASE=(-std=c++17 -O2 -ffp-contract=off -w -I "$ROOT/oracle/glmshim" -I "$REF" -I "$ROOT/oracle" -I "$ROOT/include" -I "$HERE"
       -include vector -include iostream)
 patch_gridpoint() { sed -e '26s|^//||' "$REF/GridPoint.h"; }
 patch_mp() { sed -e '33s|^//||' -e '51s|^//||' -e '71s|^//||' "$REF/MaterialPoint_BC.h"; }

@@ -90,7 +90,7 @@ class NetReport(C.Structure):
 
 class SurrogateStats(C.Structure):
     _fields_ = [("queued", C.c_int64), ("band", C.c_int64), ("rechecked", C.c_int64), ("recheck_rms", C.c_double),
-                ("recheck_max", C.c_double)]
+                ("recheck_max", C.c_double), ("rejected", C.c_int64)]
 
 
 class KernelStat(C.Structure):
@@ -107,7 +107,8 @@ class Monitors(C.Structure):
     _fields_ = [("time", C.c_double), ("position_mean", C.c_double * 3), ("force_sum", C.c_double * 3),
                 ("momentum", C.c_double * 3), ("strain_p_max", C.c_double), ("stress_p_max", C.c_double),
                 ("stress_mean", C.c_double * 3), ("strain_mean", C.c_double * 3), ("kinetic", C.c_double),
-                ("strain_energy", C.c_double), ("plastic_energy", C.c_double), ("count", C.c_int64 * 5)]
+                ("strain_energy", C.c_double), ("plastic_energy", C.c_double), ("count", C.c_int64 * 5),
+                ("platen_work", C.c_double), ("friction_work", C.c_double)]
 
 
 MON_DISPLACEMENT, MON_MOMENTUM, MON_PRINCIPAL, MON_STRESS, MON_ENERGY = 1, 2, 4, 8, 16
@@ -122,6 +123,8 @@ OPT_CELL_SORT = 9
 OPT_PASS1_CORNERS = 10
 OPT_PASS1_BLOCK = 11
 OPT_LARGE_STRAIN = 12
+OPT_FP64_FALLBACK = 13
+OPT_SURROGATE_GUARD = 14
 
 
 def library_path() -> str:
@@ -445,7 +448,8 @@ class Engine:
         return {"time": r.time, "position_mean": list(r.position_mean), "force_sum": list(r.force_sum),
                 "momentum": list(r.momentum), "strain_p_max": r.strain_p_max, "stress_p_max": r.stress_p_max,
                 "stress_mean": list(r.stress_mean), "strain_mean": list(r.strain_mean), "kinetic": r.kinetic,
-                "strain_energy": r.strain_energy, "plastic_energy": r.plastic_energy, "count": list(r.count)}
+                "strain_energy": r.strain_energy, "plastic_energy": r.plastic_energy, "count": list(r.count),
+                "platen_work": r.platen_work, "friction_work": r.friction_work}
 
     def cell_order(self):
         """(cell key per particle, particle order sorted by key) of the last step."""
@@ -489,10 +493,10 @@ class Engine:
         r = SurrogateStats()
         self._check(self._L.mpm_surrogate_stats_read(self._h, C.byref(r), 1 if reset else 0))
         return {"queued": r.queued, "band": r.band, "rechecked": r.rechecked, "recheck_rms": r.recheck_rms,
-                "recheck_max": r.recheck_max}
+                "recheck_max": r.recheck_max, "rejected": r.rejected}
 
 
-INFER_TC, INFER_FP32, INFER_EXACT = 0, 1, 2
+INFER_TC, INFER_FP32, INFER_EXACT, INFER_EXACT_FP64 = 0, 1, 2, 3
 
 
 class Net:

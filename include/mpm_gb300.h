@@ -81,6 +81,14 @@ extern "C" {
 #define MPM_OPT_PASS1_CORNERS 10 /* cell-run G2P pass 1 (P2G modes 2-4): corners per thread, 1, 2 (default) or 4 */
 #define MPM_OPT_PASS1_BLOCK 11   /* cell-run G2P pass 1: threads per block (128, 256 or 512) */
 #define MPM_OPT_LARGE_STRAIN 12  /* FP64 form, non-contact loop: 1 runs the large-strain pass 2 (G2P_P2_LargeStrain, PhysicsEngine_runSimulation_Classic_DoublePass_MPLocks.cpp:281-437), which the reference ships disabled (:605); 0 (default) the small-strain pass */
+#define MPM_OPT_FP64_FALLBACK 13 /* FP32 form: 1 (default) computes the von Mises hardening return map
+                                    (…_VonMisesHardening.cpp:4-92) in FP64 for particles whose FP32 trial yield
+                                    function is above -band x k0 (band: the fallback band of mpm_attach_surrogate,
+                                    0.02 by default) and that the network does not take: the fallback band and
+                                    every plastic state without a network; 0: FP32 throughout */
+#define MPM_OPT_SURROGATE_GUARD 14 /* FP32 form with the learned return map: tolerance of the guard on the network's
+                                      results as a fraction of k0 (default 0.01; 0 turns the guard off), see
+                                      mpm_attach_surrogate */
 #define MPM_OPT_CELL_SORT 9      /* FP32 form, P2G modes 2-4: 1 sorts the particles by cell every step; 0 (default) takes the storage order as it is (a cell whose particles are not adjacent is summed in several runs) and, with MPM_OPT_REORDER 0, restores the cell order every 256 steps */
 
 typedef struct mpm_ctx mpm_ctx;
@@ -278,6 +286,19 @@ typedef struct mpm_monitors {
     double strain_energy;     /* energy list: sum of d_Energy_Strain */
     double plastic_energy;    /* energy list: sum of d_Energy_Plastic */
     int64_t count[5];         /* members of each list, in the order of the MPM_MON_* bits */
+    /* Boundary work since the last mpm_upload_particles, accumulated in FP64
+     * every step (no counterpart in the reference, whose report has no
+     * external-work term).  platen_work: the work of displacement control,
+     * sum over controlled node axes of -f v dt (f: the node's force the
+     * control zeroes, v: the velocity it imposes, …MPLocks.cpp:143-174,
+     * …_Contact.cpp:283-297).  friction_work: the work of the friction laws,
+     * sum of df (p/m) dt (df: the force a friction law adds to a tangent,
+     * p/m: the node's updated velocity; dissipation, so <= 0).  The strain
+     * energy is the stress work, plastic dissipation included, so
+     * kinetic + strain_energy - (initial values) - platen_work - friction_work
+     * is the discrete energy balance's residual. */
+    double platen_work;
+    double friction_work;
 } mpm_monitors;
 int mpm_upload_monitor_mask(mpm_ctx* ctx, const uint8_t* mask, int64_t n);
 int mpm_monitors_read(mpm_ctx* ctx, mpm_monitors* out);

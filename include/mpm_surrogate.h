@@ -17,8 +17,13 @@
  * particles whose trial yield function lies within `band` x k0 of the
  * surface (k0 = yield/sqrt 3) and for elastic trial states, queues the
  * clearly plastic ones for the network, and re-checks a random fraction of
- * the queued particles against the exact map every step (the recheck keeps
- * the network's result and records the error).
+ * the queued particles against the exact map (in FP64) every step: the judge
+ * of the network's error, recorded in mpm_surrogate_stats.  A guard then
+ * checks every network result: its inputs must lie in the box of inputs the
+ * network was trained on, and the result must be a radial return (the new
+ * stress on the yield surface k0 + R/sqrt 2 and the correction dsigma - D de
+ * deviatoric, both to MPM_OPT_SURROGATE_GUARD x k0, default 0.01); a result
+ * that fails takes the exact map in FP64 instead (counted as rejected).
  *
  * All functions return MPM_OK (0) or a negative MPM_ERR_* code.  Samples
  * are rows of floats in physical units: inputs n x 13, outputs n x 7.
@@ -81,7 +86,9 @@ int mpm_net_set_params(mpm_net* net, const float* host, int64_t n);
 int mpm_net_loss_grad(mpm_net* net, const float* x, const float* t, int64_t n, float* grad, double* loss);
 /* Inference on device rows (inputs n x 13, outputs n x 7, physical units).
  * kernel: 0 = BF16 tcgen05, 1 = FP32 CUDA cores (reference), 2 = the exact
- * FP32 return map (the method without the network). */
+ * FP32 return map (the method without the network), 3 = the exact return map
+ * in FP64 on the float inputs, outputs rounded once to float (the FP32 form's
+ * fallback path and the judge of the network, MPM_OPT_FP64_FALLBACK). */
 int mpm_net_infer(mpm_net* net, const float* d_in, float* d_out, int64_t n, int kernel, void* stream);
 /* Normalisation in use: physical input = normalised x in_scale; physical
  * output = normalised x out_scale + out_shift (+ D de for the stress). */
@@ -93,6 +100,7 @@ typedef struct mpm_surrogate_stats {
     int64_t rechecked;       /* queued particles re-checked against the exact map */
     double recheck_rms;      /* RMS of |dsigma_net - dsigma_exact| / yield over the rechecks */
     double recheck_max;      /* max of the same */
+    int64_t rejected;        /* queued particles whose network result the guard replaced by the exact FP64 map */
 } mpm_surrogate_stats;
 
 /* Use the network in the engine's FP32 form for von Mises hardening

@@ -32,9 +32,10 @@
 #   ref_ompN  -fopenmp with _MAX_N_THREADS set to N (default: nproc).
 #
 # usage: oracle/build_ref.sh [reference_dir] [N]
+#   reference_dir: default $MPM_REFERENCE_DIR, else a checkout named `reference` beside this repository
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${1:-/root/reference}"
+REF="${1:-${MPM_REFERENCE_DIR:-$HERE/../../reference}}"
 NTH="${2:-$(nproc)}"
 OUT="$HERE/_ref"
 if [ ! -f "$REF/PhysicsEngine_runSimulation_Classic_DoublePass_MPLocks.cpp" ]; then

@@ -64,6 +64,12 @@ typedef struct work {
     double h[3];
     int nn[3];
     double* xnode; /* [nn][3] */
+    /* boundary work (an extension; NULL bw: off): the step's sums and the
+     * scratch of the displacement-control term */
+    double* bw;       /* [2] accumulated work: displacement control, friction */
+    double bw_dc, bw_fr;
+    double* fsave;    /* [nn][3] force of a controlled node before the control zeroes it */
+    uint8_t* dcax;    /* [nn] axes the list controls on the node */
 #ifdef _OPENMP
     omp_lock_t* locks;
 #endif
@@ -218,6 +224,52 @@ static void work_free(work* w, const mpmsnap* s) {
     free(w->agps);
     free(w->nagp);
     free(w->xnode);
+    free(w->fsave);
+    free(w->dcax);
+}
+
+/* ---- boundary work (an extension, off unless requested) ----------------------
+ * Not in the reference, whose energy report has no external-work term
+ * (PhysicsEngine.cpp:140-156).  A displacement-controlled node axis takes the
+ * platen particle's velocity v and its force f is zeroed, so the platen
+ * supplies -f there and works -f v dt; a friction law that adds df to a
+ * tangent force works df (p/m) dt at the node's updated momentum p.  The
+ * displacement-control term is counted at the first control pass of a step
+ * (the one before G2P pass 1), with the force each controlled node had just
+ * before that pass and the velocity the list's last writer imposed. */
+static void dc_work_begin(mpmsnap* s, work* w, int contact) {
+    if (!w->bw) return;
+    for (long k = 0; k < (long)s->h.n_dc; ++k) {
+        size_t p = s->dc_list[k];
+        uint8_t axes = contact ? 7u : (uint8_t)(s->pflags[p] & 7u);
+        for (int j = 0; j < w->nagp[p]; ++j) {
+            uint32_t i = w->agps[8 * p + j].idx;
+            for (int c = 0; c < 3; ++c) w->fsave[3 * (size_t)i + c] = s->g_force[3 * (size_t)i + c];
+            w->dcax[i] |= axes;
+        }
+    }
+}
+
+static void dc_work_end(mpmsnap* s, work* w) {
+    if (!w->bw) return;
+    for (long k = 0; k < (long)s->h.n_dc; ++k) {
+        size_t p = s->dc_list[k];
+        for (int j = 0; j < w->nagp[p]; ++j) {
+            size_t i = w->agps[8 * p + j].idx;
+            if (!w->dcax[i]) continue;
+            double sum = 0.0;
+            for (int c = 0; c < 3; ++c)
+                if (w->dcax[i] & (1u << c)) sum -= w->fsave[3 * i + c] * s->g_vel[3 * i + c];
+            w->bw_dc += sum;
+            w->dcax[i] = 0;
+        }
+    }
+}
+
+/* friction work of node i after its update; dfr: the force the friction law added per axis */
+static void friction_work(mpmsnap* s, work* w, size_t i, const double dfr[3]) {
+    if (!w->bw || (dfr[0] == 0.0 && dfr[1] == 0.0) || !(s->g_mass[i] > s->h.mass_min)) return;
+    w->bw_fr += (dfr[0] * s->g_mom[3 * i] + dfr[1] * s->g_mom[3 * i + 1]) / s->g_mass[i];
 }
 
 #ifdef _OPENMP
@@ -323,7 +375,7 @@ static void damping(mpmsnap* s, size_t i) {
 }
 
 /* IntegrateGrid, non-contact (…MPLocks.cpp:90-142) */
-static void integrate_grid(mpmsnap* s, double dt) {
+static void integrate_grid(mpmsnap* s, work* w, double dt) {
 #pragma omp for
     for (long li = 0; li < (long)s->h.n_nodes; ++li) {
         size_t i = (size_t)li;
@@ -331,9 +383,14 @@ static void integrate_grid(mpmsnap* s, double dt) {
         double* p = &s->g_mom[3 * i];
         double* f = &s->g_force[3 * i];
         damping(s, i);
+        double dfr[3] = {0.0, 0.0, 0.0};
         if (s->fixed[i] & MPM_NF_FIX_X) {
             double trial_y = p[1] + f[1] * dt;
-            if (gabs(trial_y * dt) > 1.0e-24 && f[0] > 0.0) coulomb(s, i, 1, f[0], dt);
+            if (gabs(trial_y * dt) > 1.0e-24 && f[0] > 0.0) {
+                double f0 = f[1];
+                coulomb(s, i, 1, f[0], dt);
+                dfr[1] = f[1] - f0;
+            }
             zero_fixed(s, i, 0);
         }
         if (s->fixed[i] & MPM_NF_FIX_Y) {
@@ -344,11 +401,12 @@ static void integrate_grid(mpmsnap* s, double dt) {
         }
         if (s->fixed[i] & MPM_NF_FIX_Z) zero_fixed(s, i, 2);
         for (int c = 0; c < 3; ++c) p[c] = p[c] + f[c] * dt;
+        friction_work(s, w, i, dfr);
     }
 }
 
 /* IntegrateGrid, contact form (…_Contact.cpp:242-277), with the optional floor friction. */
-static void integrate_grid_contact(mpmsnap* s, double dt, int floor_friction) {
+static void integrate_grid_contact(mpmsnap* s, work* w, double dt, int floor_friction) {
 #pragma omp for
     for (long li = 0; li < (long)s->h.n_nodes; ++li) {
         size_t i = (size_t)li;
@@ -356,11 +414,16 @@ static void integrate_grid_contact(mpmsnap* s, double dt, int floor_friction) {
         double* p = &s->g_mom[3 * i];
         double* f = &s->g_force[3 * i];
         damping(s, i);
+        double dfr[3] = {0.0, 0.0, 0.0};
         if (floor_friction && (s->fixed[i] & MPM_NF_FIX_Z) && s->friction[i] > 0.0 && f[2] < 0.0) {
             double fz = f[2];
             for (int t = 0; t < 2; ++t) {
                 double trial_t = p[t] + f[t] * dt;
-                if (gabs(trial_t * dt) > 1.0e-24) coulomb(s, i, t, fz, dt);
+                if (gabs(trial_t * dt) > 1.0e-24) {
+                    double f0 = f[t];
+                    coulomb(s, i, t, fz, dt);
+                    dfr[t] = f[t] - f0;
+                }
             }
         }
         for (int c = 0; c < 3; ++c) p[c] = p[c] + f[c] * dt;
@@ -372,6 +435,7 @@ static void integrate_grid_contact(mpmsnap* s, double dt, int floor_friction) {
             f[1] = 0.0;
         }
         if (s->fixed[i] & MPM_NF_FIX_Z) zero_fixed(s, i, 2);
+        friction_work(s, w, i, dfr);
     }
 }
 
@@ -751,8 +815,10 @@ static void step(mpmsnap* s, work* w, double dt, const oracle_opts* o) {
         for (long lp = 0; lp < (long)s->h.n_particles; ++lp) find_agps(s, w, (size_t)lp);
         p2g(s, w, contact);
         if (!contact) {
+            dc_work_begin(s, w, 0);
             displacement_control(s, w);
-            integrate_grid(s, dt);
+            dc_work_end(s, w);
+            integrate_grid(s, w, dt);
             g2p_pass1(s, w, dt, 0);
             remap(s, w, 0);
             displacement_control(s, w);
@@ -770,8 +836,10 @@ static void step(mpmsnap* s, work* w, double dt, const oracle_opts* o) {
             }
         } else {
             contact_phases(s, w);
-            integrate_grid_contact(s, dt, o->floor_friction);
+            integrate_grid_contact(s, w, dt, o->floor_friction);
+            dc_work_begin(s, w, 1);
             displacement_control_contact(s, w);
+            dc_work_end(s, w);
             g2p_pass1(s, w, dt, 1);
             remap(s, w, 1);
             reapply_bc(s);
@@ -785,6 +853,11 @@ static void step(mpmsnap* s, work* w, double dt, const oracle_opts* o) {
                 for (int c = 0; c < 3; ++c) s->pos[3 * p + c] += s->vel[3 * p + c] * dt;
             }
         }
+    }
+    if (w->bw) {
+        w->bw[0] += w->bw_dc * dt;
+        w->bw[1] += w->bw_fr * dt;
+        w->bw_dc = w->bw_fr = 0.0;
     }
     s->h.time += dt;
     s->h.step += 1;
@@ -820,6 +893,31 @@ int oracle_advance(mpmsnap* s, int steps, int contact, int floor_friction, int t
     s->h.contact = (uint32_t)contact;
     work_free(&w, s);
     return 0;
+}
+
+/* As oracle_advance in the one-thread build, also adding the steps' boundary
+ * work to bwork[0] (displacement control) and bwork[1] (friction). */
+int oracle_advance_work(mpmsnap* s, int steps, int contact, int floor_friction, double* bwork) {
+#ifdef _OPENMP
+    (void)s, (void)steps, (void)contact, (void)floor_friction, (void)bwork;
+    return -2; /* the work sums are restated in index order: one-thread build only */
+#else
+    oracle_opts o = {contact, floor_friction, 0};
+    work w;
+    if (work_init(&w, s) != 0) return -1;
+    size_t nn = (size_t)s->h.n_nodes;
+    w.bw = bwork;
+    w.fsave = (double*)malloc(sizeof(double) * 3 * (nn ? nn : 1));
+    w.dcax = (uint8_t*)calloc(nn ? nn : 1, 1);
+    if (!w.fsave || !w.dcax) {
+        work_free(&w, s);
+        return -1;
+    }
+    for (int k = 0; k < steps; ++k) step(s, &w, s->h.dt_max, &o);
+    s->h.contact = (uint32_t)contact;
+    work_free(&w, s);
+    return 0;
+#endif
 }
 
 /* File form: read in_path, advance, write out_path. */

@@ -10,7 +10,8 @@ order, the order the golden states were produced in) in place on a
 large-strain pass 2, which keeps the elastic deformation gradient in
 ``state["F_elastic"]``); ``advance(..., threads=N, omp=True)`` runs
 the OpenMP build that mirrors the reference's per-node-lock parallel loop,
-which is only ever timed.
+which is only ever timed.  ``advance_work`` is ``advance`` that also sums the
+boundary work (displacement control, friction) the engine's monitors report.
 """
 from __future__ import annotations
 
@@ -43,6 +44,8 @@ def _lib(omp: bool):
             lib.oracle_advance.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]
             lib.oracle_advance.restype = C.c_int
             lib.oracle_threads_available.restype = C.c_int
+            lib.oracle_advance_work.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]
+            lib.oracle_advance_work.restype = C.c_int
             _libs[name] = lib
         return _libs[name]
 
@@ -112,6 +115,23 @@ def advance(st, steps: int, contact: int, floor_friction: int = 0, threads: int 
     st.step = s.h.step
     st.contact = s.h.contact
     return sec.value
+
+
+def advance_work(st, steps: int, contact: int, floor_friction: int = 0, work=None):
+    """As advance() (one-thread build), also summing the boundary work of the steps: returns
+    [displacement-control work, friction work] added to `work` (a 2-list, zeros if None)."""
+    lib = _lib(False)
+    if len(st.arrays["g_mass"]) != st.n_nodes:
+        raise ValueError("the oracle needs every node array (this State holds only the nodes' boundary conditions)")
+    s = _make_snap(st)
+    w = (C.c_double * 2)(*(work or (0.0, 0.0)))
+    rc = lib.oracle_advance_work(C.byref(s), int(steps), int(contact), int(floor_friction), w)
+    if rc != 0:
+        raise RuntimeError(f"oracle_advance_work failed ({rc})")
+    st.time = s.h.time
+    st.step = s.h.step
+    st.contact = s.h.contact
+    return [w[0], w[1]]
 
 
 def threads_available() -> int:

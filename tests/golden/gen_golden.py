@@ -1,7 +1,7 @@
 """Regenerates the golden MPM states under tests/golden/ from the reference itself.
 
-Needs the reference checkout (default /root/reference; override with
-MPM_REFERENCE_DIR): it builds the reference's own physics sources headless
+Needs the reference checkout ($MPM_REFERENCE_DIR, else a checkout named
+`reference` beside this repository): it builds the reference's own physics sources headless
 (oracle/build_ref.sh) and advances each seeded input scene with the
 one-thread build (oracle/_ref/ref_seq), whose scatter-add and overwrite order
 is particle index order; the large-strain case uses the same build with the
@@ -81,7 +81,7 @@ def _gz(src: str, dst: str) -> None:
 
 
 def main() -> None:
-    ref = os.environ.get("MPM_REFERENCE_DIR", "/root/reference")
+    ref = os.environ.get("MPM_REFERENCE_DIR") or os.path.normpath(os.path.join(ROOT, os.pardir, "reference"))
     subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh"), ref])
     wanted = sys.argv[1:] or list(CASES) + list(_canvas_cases())
     with tempfile.TemporaryDirectory() as td:

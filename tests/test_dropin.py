@@ -11,7 +11,7 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("MPM_REFERENCE_DIR", "/root/reference")
+REF = os.environ.get("MPM_REFERENCE_DIR") or os.path.normpath(os.path.join(ROOT, os.pardir, "reference"))
 
 
 @pytest.mark.skipif(not os.path.exists(os.path.join(REF, "PhysicsEngine.h")), reason="reference checkout absent")

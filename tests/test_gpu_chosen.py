@@ -57,7 +57,7 @@ def test_autotune_restores_state_and_picks_valid_options(golden, form):
         res = e.autotune(steps=2, contact=True)
         after = e.download_state(st)
         # P2G stage 15, pass-1 stage 9 (cell-run P2G only), pass-2 stage 6 (FP64) or 9 (FP32: also the staged mode)
-        ncand = (21, 30) if form == engine.FORM_FP64 else (24, 33)
+        ncand = (21, 30) if form == engine.FORM_FP64 else (30, 39)
         modes = (0, 1) if form == engine.FORM_FP64 else (0, 1, 2)
         assert res["candidates"] in ncand and res["pass1_corners"] in (1, 2, 4) and res["pass1_block"] in (128, 256, 512) and res["gather_batch"] in modes and res["p2g_block"] in (128, 256, 512) and res["pass_block"] in (128, 256, 512)
         assert res["best_ms_per_step"] <= res["worst_ms_per_step"]
@@ -88,11 +88,13 @@ def test_plain_form_parity_holds_for_every_launch_configuration(golden):
 
 def test_chosen_form_p2g_modes_agree():
     """The P2G reductions (per-particle atomics, lane runs, shared-memory cell runs with 1, 2 or 4 corners per
-    thread) sum the same contributions in different orders; with the contact path they also carry the FP32 mass
-    gradient."""
+    thread, runs reduced in registers by lane pairs with the tile read from global memory or staged by bulk
+    copies) sum the same contributions in different orders; with the contact path they also carry the FP32 mass
+    gradient.  At 128 threads the pair kernel's tiles are 512 slots: the first two of this scene stage, the last
+    (partial) one reads global memory."""
     st = scenes.contact_small(seed=2)
     outs = []
-    for red in (0, 1, 2, 3, 4):
+    for red in (0, 1, 2, 3, 4, 5, 6):
         for blk in ((128, 512) if red >= 2 else (256,)):
             with engine.Engine.from_state(st, engine.FORM_FP32) as e:
                 e.set_option(engine.OPT_P2G_REDUCE, red)
@@ -107,6 +109,26 @@ def test_chosen_form_p2g_modes_agree():
             scale = np.abs(a[k]).max()
             assert np.abs(b[k] - a[k]).max() <= 1e-4 * scale, (cfg, k)
         assert np.array_equal(a["g_state"] & 1, b["g_state"] & 1), cfg
+
+
+def test_pair_modes_through_the_sort_permutation():
+    """P2G modes 5 and 6 (and their pass 1) read particles through the per-step sort's permutation when the
+    particles are sorted every step (MPM_OPT_CELL_SORT 1); mode 6 then reads global memory."""
+    st = scenes.mixed_small(seed=3)
+    outs = {}
+    for red in (3, 5, 6):
+        with engine.Engine.from_state(st, engine.FORM_FP32) as e:
+            e.set_option(engine.OPT_CELL_SORT, 1)
+            e.set_option(engine.OPT_REORDER, -1)
+            e.set_option(engine.OPT_P2G_REDUCE, red)
+            e.set_option(engine.OPT_FLOOR_FRICTION, 1)
+            e.advance(12, st.dt_max, False)
+            outs[red] = e.download_state(st)
+    for red in (5, 6):
+        for k in ("g_mass", "g_mom", "stress", "vel", "pos"):
+            scale = np.abs(outs[3][k]).max()
+            assert np.abs(outs[red][k] - outs[3][k]).max() <= 1e-4 * scale, (red, k)
+        assert np.array_equal(outs[3]["g_state"] & 1, outs[red]["g_state"] & 1), red
 
 
 PASS2_FIELDS = ("pos", "vel", "stress", "strain", "eps_p", "F", "vol", "backstress", "e_strain", "e_plastic")

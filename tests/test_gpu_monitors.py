@@ -63,3 +63,27 @@ def test_monitors_match_report_console(contact):
     np.testing.assert_allclose(mon["kinetic"], ke, rtol=1e-9)
     np.testing.assert_allclose(mon["strain_energy"], ref["e_strain"][ee].sum(), rtol=1e-9)
     np.testing.assert_allclose(mon["plastic_energy"], ref["e_plastic"][ee].sum(), rtol=1e-9, atol=1e-20)
+
+
+@pytest.mark.parametrize("contact", [0, 1])
+def test_boundary_work_matches_restatement(contact):
+    """Platen (displacement-control) and friction work against the oracle's restatement of the same sums
+    (oracle/mpm_oracle.c, dc_work_* and friction_work): FP64 form to summation order, FP32 form to 1e-4."""
+    if contact:
+        st = scenes.platen_block(size=(0.01, 0.01, 0.006), speed=20.0)  # floor friction 0.1, platen at 20 m/s
+    else:
+        st = scenes.mixed_small(seed=6)  # platen particles on the list, x-wall friction
+    steps = 40
+    ref = st.copy()
+    w = pyoracle.advance_work(ref, steps, contact, floor_friction=1)
+    assert w[0] != 0.0
+    for form, rtol in ((engine.FORM_FP64, 1e-9), (engine.FORM_FP32, 1e-4)):
+        with engine.Engine.from_state(st, form) as e:
+            e.set_option(engine.OPT_FLOOR_FRICTION, 1)
+            e.upload_monitor_mask(np.full(st.n_particles, 31, dtype=np.uint8))
+            e.advance(steps, st.dt_max, bool(contact))
+            mon = e.monitors()
+        np.testing.assert_allclose(mon["platen_work"], w[0], rtol=rtol)
+        np.testing.assert_allclose(mon["friction_work"], w[1], rtol=rtol, atol=rtol * abs(w[0]))
+    if contact:
+        assert w[1] < 0.0  # the floor friction dissipates

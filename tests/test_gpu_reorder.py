@@ -82,7 +82,7 @@ def test_lists_uploaded_after_a_reorder():
     assert mons[0]["count"] == mons[1]["count"]
 
 
-@pytest.mark.parametrize("reorder,p2g", [(0, 2), (7, 3), (-1, 2), (-1, 4)])
+@pytest.mark.parametrize("reorder,p2g", [(0, 2), (7, 3), (-1, 2), (-1, 4), (0, 5), (7, 6), (-1, 6)])
 def test_sort_free_run_matches_sorted(reorder, p2g):
     """Without the per-step sort the cell-run kernels take the slots in storage order: cell order after a
     reorder, the caller's (unordered) order with reorders off, where nearly every cell splits into many runs."""

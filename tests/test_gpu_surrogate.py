@@ -233,3 +233,33 @@ def test_network_in_the_step():
     assert err_exact["vm_stress_rel_l2"] <= 1e-3
     # the chosen form's bars hold with the network in the loop
     assert err_net["vm_stress_rel_l2"] <= 1e-2 and err_net["strain_energy_rel"] <= 5e-3, err_net
+
+
+def test_guard_replaces_implausible_network_results():
+    """A network with random weights (its results are not radial returns) in the step: the guard rejects every
+    result and the exact FP64 map takes its place, so the run equals the run without the network (the same
+    FP64 map, applied by the finishing kernel instead of pass 2: equal to float rounding); with the guard off
+    (MPM_OPT_SURROGATE_GUARD 0) the same network leaves the queued particles off the yield surface."""
+    st = scenes.platen_block(size=(0.012, 0.012, 0.008), speed=20.0)
+    net = engine.Net(**MAT, n_samples=1000)
+    net.set_params(random_params(11))
+    steps = 40
+    outs = {}
+    for mode in ("none", "guard", "off"):
+        with engine.Engine.from_state(st, engine.FORM_FP32) as e:
+            e.set_option(engine.OPT_FLOOR_FRICTION, 1)
+            if mode != "none":
+                e.attach_surrogate(net, band=0.02, recheck=0.01)
+            if mode == "off":
+                e.set_option(engine.OPT_SURROGATE_GUARD, 0.0)
+            e.advance(steps, st.dt_max, True)
+            outs[mode] = e.download_state(st)
+            if mode == "guard":
+                stats = e.surrogate_stats()
+    assert stats["queued"] > 0 and stats["rejected"] == stats["queued"], stats
+    for k in ("pos", "vel", "stress", "backstress", "e_strain", "e_plastic"):
+        scale = np.abs(outs["none"][k]).max()
+        assert np.abs(outs["guard"][k] - outs["none"][k]).max() <= 1e-6 * scale, k
+    scale = np.abs(outs["none"]["stress"]).max()
+    assert np.abs(outs["off"]["stress"] - outs["none"]["stress"]).max() > 1e-3 * scale
+    net.close()

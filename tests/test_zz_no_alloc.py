@@ -53,6 +53,19 @@ def test_noalloc_cell_order_matches_allocating_path_twice():
         assert np.array_equal(order, want_order)
 
 
+def test_noalloc_cell_order_at_exactly_its_capacity():
+    """n = MPM_NOALLOC_MAX_PARTICLES: the whole scratch layout is in use, the digit counts of the last tiles
+    included; twice in a row, against the allocating path."""
+    torch = pytest.importorskip("torch")
+    st = scenes.bar(cells_len=128, cells_w=32)  # 128 x 32 x 32 cells at 8 particles per cell
+    assert st.n_particles == engine.NOALLOC_MAX_PARTICLES
+    want_keys, want_order = _reference_order(st)
+    for _ in range(2):
+        keys, order = _noalloc_order(torch, st)
+        assert np.array_equal(keys, want_keys)
+        assert np.array_equal(order, want_order)
+
+
 def test_noalloc_rejects_more_than_its_capacity():
     torch = pytest.importorskip("torch")
     st = scenes.mixed_small(seed=22)
