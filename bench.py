@@ -183,8 +183,10 @@ def workload(args):
     """(specimen states, config record).  One state for the block workload."""
     from code_mpm_gb300 import scenes
 
+    # the GPU arm builds the cellular bodies on the device (same bits); the reference arm stays on the host
+    device = getattr(args, "impl", "gb300") != "reference"
     if args.workload == "foam":
-        st = scenes.graded_foam()  # 800 x 800 x 400 cells, 8 x 8 graded cells of 5 mm, platen -20 m/s
+        st = scenes.graded_foam(device=device)  # 800 x 800 x 400 cells, 8 x 8 graded cells of 5 mm, platen -20 m/s
         cfg = {"workload": "density-graded square-cell foam crushed by a rigid platen, contact path, single instance",
                "block_m": [0.2, 0.2, 0.1], "h_m": 0.25e-3, "grid_cells": [800, 800, 400],
                "cells_per_side": 8, "pitch_m": 5.0e-3, "wall_m": [0.3e-3, 1.0e-3], "wall_perturbation": 0.1,
@@ -211,7 +213,7 @@ def workload(args):
                "platen_speed_mps": 5.0, "floor_friction": 0.1, "dt_s": st.dt_max,
                "l2_policy": "inputs larger than L2 (~0.8 GB particle state)"}
         return [st], cfg
-    sts = scenes.honeycomb_batch(n=args.specimens, total=args.total)
+    sts = scenes.honeycomb_batch(n=args.specimens, total=args.total, device=device)
     counts = [st.n_particles for st in sts]
     cfg = {"workload": f"{len(sts)} square-honeycomb specimens crushed by rigid platens, one grid each, "
                        "contact path, batched in one engine",

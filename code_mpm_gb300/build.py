@@ -14,7 +14,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libmpm_gb300.so")
-SOURCES = ["engine.cu", "noalloc.cu", "surrogate.cu", "canvas.cu"]
+SOURCES = ["engine.cu", "noalloc.cu", "surrogate.cu", "canvas.cu", "scenegen.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

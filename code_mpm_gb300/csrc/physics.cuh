@@ -47,18 +47,17 @@ __device__ __forceinline__ void axis_bases_local(const Geom& g, int a, double x,
     }
 }
 
-// FP32 form, from the stored cell-local coordinate u (no FP64 at all).
+// FP32 form, from the stored cell-local coordinate u (no FP64 at all).  The
+// general form per node offset o is r = u - o, N = 1 - |r| (0 outside
+// [0, 1]), gradient sign(r) ih where 1e-12 < |r| < 1; every stored u lies in
+// [0, 1] (a fraction minus its floor, or the split form's (1e-4, 1 - 1e-4)),
+// where that reduces to the lines below, value for value.
 __device__ __forceinline__ void axis_bases_u(float u, float ih, float N[2], float gf[2]) {
-    const float r[2] = {u, u - 1.0f};
-#pragma unroll
-    for (int o = 0; o < 2; ++o) {
-        float ar = fabsf(r[o]);
-        float nv = 1.0f - ar;
-        if (nv < 0.0f || nv > 1.0f) nv = 0.0f;
-        N[o] = nv;
-        float s = (float)((r[o] > 0.0f) - (r[o] < 0.0f));
-        gf[o] = (ar > 1.0e-12f && ar < (float)(1.0 - 1.0e-12)) ? s * ih : 0.0f;
-    }
+    const float a1 = fabsf(u - 1.0f);
+    N[0] = 1.0f - u;
+    N[1] = 1.0f - a1;
+    gf[0] = (u > 1.0e-12f && u < 1.0f) ? ih : 0.0f;
+    gf[1] = (a1 > 1.0e-12f && a1 < 1.0f) ? -ih : 0.0f;
 }
 
 template <typename T>

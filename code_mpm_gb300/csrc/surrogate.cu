@@ -523,7 +523,9 @@ constexpr uint32_t SW1 = 0, SW2 = SW1 + HID * IN * 2, SW3 = SW2 + HID * HID * 2,
 // biases (FP32): b1, b2, b3 (128 each), b4 (16)
 constexpr uint32_t NBIAS = 3 * HID + 16;
 // kernel shared memory: weights, bias, A0 (128 x 16), A1 (128 x 128), mbarrier, TMEM address
-constexpr uint32_t S_BIAS = WBYTES, S_A0 = (S_BIAS + NBIAS * 4 + 1023) / 1024 * 1024, S_A1 = S_A0 + 128 * IN * 2,
+// hidden biases halved, as BF16 pairs (3 x HID / 2 words), for the packed SiLU of the epilogue
+constexpr uint32_t S_BIAS = WBYTES, S_HB = S_BIAS + NBIAS * 4,
+                   S_A0 = (S_HB + 3 * (HID / 2) * 4 + 1023) / 1024 * 1024, S_A1 = S_A0 + 128 * IN * 2,
                    S_BAR = S_A1 + 128 * HID * 2, S_TADDR = S_BAR + 8, SMEM_TC = S_TADDR + 8 + 1024;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -582,17 +584,23 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16]) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-__device__ __forceinline__ float tanh_approx(float x) {
-    float y;
-    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-// SiLU z * sigmoid(z) with sigmoid(z) = (1 + tanh(z/2)) / 2
-__device__ __forceinline__ float silu_tc(float z) { return z * fmaf(0.5f, tanh_approx(0.5f * z), 0.5f); }
-
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
     __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
     return *reinterpret_cast<uint32_t*>(&h);
+}
+
+constexpr uint32_t BF16X2_HALF = 0x3F003F00u;  // (0.5, 0.5) as BF16 pairs
+
+// SiLU of two accumulators in packed BF16: with h = z / 2 = v / 2 + b / 2,
+// z sigmoid(z) = h (1 + tanh h) = h + h tanh h; each step is one rounding to
+// BF16 (the next layer's A operand is BF16 anyway), two values per instruction
+__device__ __forceinline__ uint32_t silu_bf16x2(float v0, float v1, uint32_t hb2) {
+    const uint32_t x = pack_bf16(v0, v1);
+    uint32_t h, t, y;
+    asm("fma.rn.bf16x2 %0, %1, %2, %3;" : "=r"(h) : "r"(x), "r"(BF16X2_HALF), "r"(hb2));
+    asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t) : "r"(h));
+    asm("fma.rn.bf16x2 %0, %1, %2, %1;" : "=r"(y) : "r"(h), "r"(t));
+    return y;
 }
 
 // issue one layer: D = A (128 x K) . W^T (W: N x K), K in steps of 16
@@ -609,8 +617,9 @@ __device__ __forceinline__ void issue_layer(uint32_t tmem, uint32_t a_addr, int 
 // hidden-layer epilogue: warps w and w + 4 share TMEM lane quarter w % 4;
 // their thread t reads sample 32 (w % 4) + t's accumulators in columns
 // [64 (w / 4), 64 (w / 4) + 64), adds the bias, applies SiLU, and writes that
-// part of BF16 row r of the next A operand
-__device__ __forceinline__ void hidden_epilogue(uint32_t taddr_row, const float* bias, unsigned char* a1) {
+// part of BF16 row r of the next A operand; hb2 holds the layer's halved
+// biases as BF16 pairs
+__device__ __forceinline__ void hidden_epilogue(uint32_t taddr_row, const uint32_t* hb2, unsigned char* a1) {
     const int w = threadIdx.x >> 5, r = 32 * (w & 3) + (threadIdx.x & 31), half = w >> 2;
 #pragma unroll 1
     for (int c0 = 64 * half; c0 < 64 * half + 64; c0 += 32) {
@@ -620,10 +629,10 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t taddr_row, const float*
         for (int q = 0; q < 4; ++q) {
             uint4 pk;
             const int k = c0 + 8 * q;
-            pk.x = pack_bf16(silu_tc(v[8 * q + 0] + bias[k + 0]), silu_tc(v[8 * q + 1] + bias[k + 1]));
-            pk.y = pack_bf16(silu_tc(v[8 * q + 2] + bias[k + 2]), silu_tc(v[8 * q + 3] + bias[k + 3]));
-            pk.z = pack_bf16(silu_tc(v[8 * q + 4] + bias[k + 4]), silu_tc(v[8 * q + 5] + bias[k + 5]));
-            pk.w = pack_bf16(silu_tc(v[8 * q + 6] + bias[k + 6]), silu_tc(v[8 * q + 7] + bias[k + 7]));
+            pk.x = silu_bf16x2(v[8 * q + 0], v[8 * q + 1], hb2[(k >> 1) + 0]);
+            pk.y = silu_bf16x2(v[8 * q + 2], v[8 * q + 3], hb2[(k >> 1) + 1]);
+            pk.z = silu_bf16x2(v[8 * q + 4], v[8 * q + 5], hb2[(k >> 1) + 2]);
+            pk.w = silu_bf16x2(v[8 * q + 6], v[8 * q + 7], hb2[(k >> 1) + 3]);
             *reinterpret_cast<uint4*>(a1 + kmajor_off(r, k, 128)) = pk;
         }
     }
@@ -653,6 +662,11 @@ __global__ void __launch_bounds__(TC_THREADS, 2) k_mlp_tc(TcArgs a) {
     for (uint32_t i = t; i < WBYTES / 16; i += TC_THREADS) reinterpret_cast<uint4*>(s)[i] = a.wpack[i];
     float* bias = reinterpret_cast<float*>(s + S_BIAS);
     for (uint32_t i = t; i < NBIAS; i += TC_THREADS) bias[i] = a.bias[i];
+    uint32_t* hb2 = reinterpret_cast<uint32_t*>(s + S_HB);
+    for (uint32_t i = t; i < 3 * (HID / 2); i += TC_THREADS) {
+        const uint32_t l = i / (HID / 2), j = 2 * (i % (HID / 2));
+        hb2[i] = pack_bf16(0.5f * a.bias[l * HID + j], 0.5f * a.bias[l * HID + j + 1]);
+    }
     uint32_t* taddr_slot = reinterpret_cast<uint32_t*>(s + S_TADDR);
     const uint32_t bar = sbase + S_BAR;
     if (t == 0) {
@@ -720,7 +734,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) k_mlp_tc(TcArgs a) {
             phase ^= 1u;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             if (layer < 3) {
-                hidden_epilogue(trow, bias + layer * HID, s + S_A1);
+                hidden_epilogue(trow, hb2 + layer * (HID / 2), s + S_A1);
             } else {
                 float v[16];
                 if (w < 4) tmem_ld16(trow, v);

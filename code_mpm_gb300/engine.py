@@ -93,6 +93,18 @@ class SurrogateStats(C.Structure):
                 ("recheck_max", C.c_double), ("rejected", C.c_int64)]
 
 
+class HoneycombDesc(C.Structure):  # mpm_honeycomb_desc (include/mpm_scene.h)
+    _fields_ = [("wall", C.c_double), ("pitch", C.c_double), ("h", C.c_double), ("origin", C.c_double * 3),
+                ("ncell", C.c_int32), ("layers", C.c_int32)]
+
+
+class FoamDesc(C.Structure):  # mpm_foam_desc (include/mpm_scene.h)
+    _fields_ = [("pitch", C.c_double), ("t0", C.c_double), ("t1", C.c_double), ("h", C.c_double),
+                ("height", C.c_double), ("x0", C.c_double), ("y0", C.c_double), ("z0", C.c_double),
+                ("ncell", C.c_int32), ("width", C.c_int32), ("layers", C.c_int32), ("pad", C.c_int32),
+                ("fx", C.c_void_p), ("fy", C.c_void_p)]
+
+
 class KernelStat(C.Structure):
     _fields_ = [("name", C.c_char * 32), ("launches", C.c_int64), ("total_ms", C.c_double)]
 
@@ -184,6 +196,10 @@ def lib():
             "mpm_net_train_rows": ([vp, vp, i64, C.POINTER(NetReport)], C.c_int),
             "mpm_harvest_begin": ([vp, vp, i64, C.c_uint32, dbl], C.c_int),
             "mpm_harvest_end": ([vp, C.POINTER(i64)], C.c_int),
+            "mpm_scene_honeycomb": ([C.POINTER(HoneycombDesc), vp, vp, C.c_uint64, C.POINTER(C.c_uint64), vp],
+                                    C.c_int),
+            "mpm_scene_graded_foam": ([C.POINTER(FoamDesc), vp, vp, C.c_uint64, C.POINTER(C.c_uint64), vp],
+                                      C.c_int),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)

@@ -243,10 +243,65 @@ def mixed_small(seed: int = 1, h: float = 1.0e-3, ncell=(8, 10, 6), vscale: floa
     return st
 
 
+# ---------------------------------------------------------------------------
+# Body particles of the cellular scenes on the GPU (include/mpm_scene.h): the
+# same lattice, order and surface flags as the numpy code below, bit for bit.
+# ---------------------------------------------------------------------------
+def _scene_call(fn, desc):
+    import ctypes as C
+
+    from . import engine
+
+    n = C.c_uint64(0)
+    rc = fn(C.byref(desc), None, None, 0, C.byref(n), None)
+    if rc != 0:
+        raise engine.MPMError(rc, "scene generation failed")
+    pos = np.empty((n.value, 3), dtype=np.float64)
+    surf = np.empty(n.value, dtype=np.uint8)
+    rc = fn(C.byref(desc), pos.ctypes.data_as(C.c_void_p), surf.ctypes.data_as(C.c_void_p), n.value, C.byref(n),
+            None)
+    if rc != 0:
+        raise engine.MPMError(rc, "scene generation failed")
+    return pos, surf.astype(bool)
+
+
+def honeycomb_body_gpu(wall: float, pitch: float, ncell: int, h: float, layers: int,
+                       origin) -> Tuple[np.ndarray, np.ndarray]:
+    """Body particles and surface flags of honeycomb() generated on the GPU (mpm_scene_honeycomb)."""
+    from . import engine
+
+    L = engine.lib()
+    d = engine.HoneycombDesc()
+    d.wall, d.pitch, d.h = float(wall), float(pitch), float(h)
+    for a in range(3):
+        d.origin[a] = float(origin[a])
+    d.ncell, d.layers = int(ncell), int(layers)
+    return _scene_call(L.mpm_scene_honeycomb, d)
+
+
+def foam_body_gpu(pitch: float, t0: float, t1: float, h: float, height: float, x0: float, y0: float, z0: float,
+                  ncell: int, width: int, layers: int, fx: np.ndarray,
+                  fy: np.ndarray) -> Tuple[np.ndarray, np.ndarray]:
+    """Body particles and surface flags of graded_foam() generated on the GPU (mpm_scene_graded_foam)."""
+    import ctypes as C
+
+    from . import engine
+
+    L = engine.lib()
+    fx = np.ascontiguousarray(fx, dtype=np.float64)
+    fy = np.ascontiguousarray(fy, dtype=np.float64)
+    d = engine.FoamDesc()
+    d.pitch, d.t0, d.t1, d.h, d.height = float(pitch), float(t0), float(t1), float(h), float(height)
+    d.x0, d.y0, d.z0 = float(x0), float(y0), float(z0)
+    d.ncell, d.width, d.layers = int(ncell), int(width), int(layers)
+    d.fx, d.fy = fx.ctypes.data_as(C.c_void_p), fy.ctypes.data_as(C.c_void_p)
+    return _scene_call(L.mpm_scene_graded_foam, d)
+
+
 def honeycomb(wall: float, pitch: float, ncell: int, target: int, speed: float, h: float = 0.25e-3,
               E: float = 200.0e9, nu: float = 0.3, rho: float = 7850.0, yield_: float = 250.0e6,
               H: float = 2.0e9, C1: float = 1.0e12, friction: float = 0.1, pad: int = 2,
-              headroom: int = 3) -> State:
+              headroom: int = 3, device: bool = False) -> State:
     """A square honeycomb crushed in-plane by a rigid platen (contact path).
 
     Cross-section in the x-z plane: ncell x ncell square cells of pitch
@@ -257,28 +312,32 @@ def honeycomb(wall: float, pitch: float, ncell: int, target: int, speed: float, 
     particles.  A one-layer platen above the top moves down at `speed`
     (multiplier -speed on a unit timeline, so a batch can give each specimen
     its own speed); the floor nodes are fixed in z with Coulomb friction.
+    device: the body particles are generated on the GPU (honeycomb_body_gpu), bit for bit the same.
     """
     s = 0.5 * h
     W = ncell * pitch + wall
     n1 = int(np.ceil(W / s))
     c = (np.arange(n1) + 0.5) * s
-    inx = (np.mod(c, pitch) < wall) & (c < W)
-    X, Z = np.meshgrid(c, c, indexing="ij")
-    wall_xz = (inx[:, None] | inx[None, :]) & (X < W) & (Z < W)
-    per_layer = int(wall_xz.sum())
+    per_layer = honeycomb_layer_count(wall, pitch, ncell, h)
     ny = max(2, int(round(target / max(per_layer, 1))))
     nbx = n1 // 2 + 1
     cells = np.array([nbx + 2 * pad, ny // 2 + 1 + 2 * pad, nbx + pad + headroom], dtype=np.int32)
     length = cells * h
     org = np.array([pad * h, pad * h, pad * h])
-    ix, iz = np.nonzero(wall_xz)
-    # surface: a wall lattice site with an empty neighbour in x or z
-    padm = np.pad(wall_xz, 1)
-    surf2 = ~(padm[2:, 1:-1] & padm[:-2, 1:-1] & padm[1:-1, 2:] & padm[1:-1, :-2])[ix, iz]
-    yy = (np.arange(ny) + 0.5) * s
-    body = np.stack([np.repeat(org[0] + c[ix], ny), np.tile(org[1] + yy, len(ix)),
-                     np.repeat(org[2] + c[iz], ny)], axis=1)
-    bsurf = np.repeat(surf2, ny)
+    if device:
+        body, bsurf = honeycomb_body_gpu(wall, pitch, ncell, h, ny, org)
+    else:
+        inx = (np.mod(c, pitch) < wall) & (c < W)
+        X, Z = np.meshgrid(c, c, indexing="ij")
+        wall_xz = (inx[:, None] | inx[None, :]) & (X < W) & (Z < W)
+        ix, iz = np.nonzero(wall_xz)
+        # surface: a wall lattice site with an empty neighbour in x or z
+        padm = np.pad(wall_xz, 1)
+        surf2 = ~(padm[2:, 1:-1] & padm[:-2, 1:-1] & padm[1:-1, 2:] & padm[1:-1, :-2])[ix, iz]
+        yy = (np.arange(ny) + 0.5) * s
+        body = np.stack([np.repeat(org[0] + c[ix], ny), np.tile(org[1] + yy, len(ix)),
+                         np.repeat(org[2] + c[iz], ny)], axis=1)
+        bsurf = np.repeat(surf2, ny)
     ztop = org[2] + W + 0.5 * h
     px = org[0] + np.arange(-h + 0.5 * s, W + h, s)
     py = org[1] + np.arange(-h + 0.5 * s, ny * s + h, s)
@@ -308,7 +367,7 @@ def honeycomb(wall: float, pitch: float, ncell: int, target: int, speed: float, 
 
 
 def honeycomb_batch(n: int = 256, seed: int = 4, total: float = 40.0e6, nmin: int = 10_000, nmax: int = 500_000,
-                    h: float = 0.25e-3):
+                    h: float = 0.25e-3, device: bool = False):
     """The batched cellular workload: n honeycombs with walls U(0.4, 1.2) mm, pitch U(4, 8) mm,
     4-10 cells per side, particle counts log-uniform in [nmin, nmax] scaled so the batch holds
     about `total` particles, platen speed U(1, 10) m/s per specimen."""
@@ -326,7 +385,7 @@ def honeycomb_batch(n: int = 256, seed: int = 4, total: float = 40.0e6, nmin: in
                 break
         else:
             wall, pitch, ncell = 0.4e-3, 4.0e-3, 4
-        out.append(honeycomb(wall, pitch, ncell, int(counts[i]), speed[i], h=h))
+        out.append(honeycomb(wall, pitch, ncell, int(counts[i]), speed[i], h=h, device=device))
     return out
 
 
@@ -344,7 +403,7 @@ def graded_foam(ncell: int = 8, pitch: float = 5.0e-3, t0: float = 0.3e-3, t1: f
                 block=(0.2, 0.2, 0.1), h: float = 0.25e-3, perturb: float = 0.1, seed: int = 5,
                 E: float = 70.0e9, nu: float = 0.33, rho: float = 2700.0, yield_: float = 120.0e6, H: float = 700.0e6,
                 C1: float = 1.0e12, speed: float = 20.0, friction: float = 0.2, pad: int = 2, headroom: int = 4,
-                height: Optional[float] = None) -> State:
+                height: Optional[float] = None, device: bool = False) -> State:
     """Density-graded square-cell foam crushed out of plane by a rigid platen (contact path).
 
     The grid covers the whole block (block / h cells, 800 x 800 x 400 by default) while the foam occupies
@@ -354,6 +413,7 @@ def graded_foam(ncell: int = 8, pitch: float = 5.0e-3, t0: float = 0.3e-3, t1: f
     the walls (8 per cell); those with an empty lattice neighbour in x or y are surface particles.  A one-layer
     platen above the top moves down at `speed`; the floor node plane is fixed in z with Coulomb friction.  Grids
     above 50M nodes hold only the nodes' boundary conditions on the host (node_fields="bc").
+    device: the body particles are generated on the GPU (foam_body_gpu), bit for bit the same.
     """
     cells = np.array([int(round(block[a] / h)) for a in range(3)], dtype=np.int32)
     length = cells * h
@@ -370,22 +430,25 @@ def graded_foam(ncell: int = 8, pitch: float = 5.0e-3, t0: float = 0.3e-3, t1: f
     rng = np.random.Generator(np.random.PCG64(seed))
     fx = 1.0 + rng.uniform(-perturb, perturb, ncell + 1)
     fy = 1.0 + rng.uniform(-perturb, perturb, ncell + 1)
-    kx = np.minimum((c // pitch).astype(np.int64), ncell)
-    rel = c - kx * pitch
-    layers, surf_layers = [], []
-    for k in range(nz):
-        zc = (k + 0.5) * s
-        t = t0 + (t1 - t0) * zc / height
-        inx = rel < t * fx[kx]
-        iny = rel < t * fy[kx]
-        wall = inx[:, None] | iny[None, :]
-        ix, iy = np.nonzero(wall)
-        padm = np.pad(wall, 1)
-        surf = ~(padm[2:, 1:-1] & padm[:-2, 1:-1] & padm[1:-1, 2:] & padm[1:-1, :-2])[ix, iy]
-        layers.append(np.stack([x0 + c[ix], y0 + c[iy], np.full(ix.size, z0 + zc)], axis=1))
-        surf_layers.append(surf)
-    body = np.concatenate(layers)
-    bsurf = np.concatenate(surf_layers)
+    if device:
+        body, bsurf = foam_body_gpu(pitch, t0, t1, h, height, x0, y0, z0, ncell, m, nz, fx, fy)
+    else:
+        kx = np.minimum((c // pitch).astype(np.int64), ncell)
+        rel = c - kx * pitch
+        layers, surf_layers = [], []
+        for k in range(nz):
+            zc = (k + 0.5) * s
+            t = t0 + (t1 - t0) * zc / height
+            inx = rel < t * fx[kx]
+            iny = rel < t * fy[kx]
+            wall = inx[:, None] | iny[None, :]
+            ix, iy = np.nonzero(wall)
+            padm = np.pad(wall, 1)
+            surf = ~(padm[2:, 1:-1] & padm[:-2, 1:-1] & padm[1:-1, 2:] & padm[1:-1, :-2])[ix, iy]
+            layers.append(np.stack([x0 + c[ix], y0 + c[iy], np.full(ix.size, z0 + zc)], axis=1))
+            surf_layers.append(surf)
+        body = np.concatenate(layers)
+        bsurf = np.concatenate(surf_layers)
     ztop = z0 + height + 0.5 * h
     px = x0 + np.arange(-h + 0.5 * s, W + h, s)
     py = y0 + np.arange(-h + 0.5 * s, W + h, s)

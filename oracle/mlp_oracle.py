@@ -80,11 +80,14 @@ def bf16(a):
 
 
 def forward_bf16(theta, x):
-    """The inference kernel's arithmetic: bf16 weights and activations, exact products, float sums."""
+    """The inference kernel's arithmetic: bf16 weights and activations, exact products, float sums; the hidden
+    SiLU in bf16 steps, h = bf16(v/2 + bf16(b/2)) with v = bf16(sum), then bf16(h + h bf16(tanh h))."""
     W1, b1, W2, b2, W3, b3, W4, b4 = unpack(theta)
     h = bf16(x)
     for W, b in ((W1, b1), (W2, b2), (W3, b3)):
-        h = bf16(silu(h @ bf16(W).T + b))
+        v = bf16(h @ bf16(W).T)
+        hh = bf16(0.5 * v + bf16(0.5 * b))
+        h = bf16(hh + hh * bf16(np.tanh(hh)))
     return h @ bf16(W4).T + b4
 
 
