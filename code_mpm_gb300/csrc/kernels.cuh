@@ -420,19 +420,31 @@ struct P2GBlock {
     // CPT corners) sums the run's contributions in slot order and issues one
     // atomic per field; mark_active also marks the corners active.  MG: also the
     // node mass gradients.
+    //
+    // FP32: a warp holds consecutive runs, the TPR threads of a run in
+    // adjacent lanes.  When run r's cell follows run r - 1's in x (key + 1),
+    // the x = 1 corners of r - 1 are the x = 0 corners of r: one shuffle of
+    // the sums, TPR / 2 lanes up, adds them to r's, and only r's lanes issue
+    // the atomics (in the batch about three runs in four have such a
+    // neighbour, so a third of the corner atomics go).
     template <int CPT, bool MG>
     __device__ __forceinline__ void scatter(const NView<T>& nd, const Geom& g, int nslots, int mark_active) const {
         static_assert(CPT == 1 || CPT == 2 || CPT == 4, "corners per thread");
         constexpr int bs = BS;
-        const int t = threadIdx.x;
+        const int t = threadIdx.x, lane = t & 31;
         const long long nn = nd.nn;
         const unsigned* skey = cs.key;
         const int R = block_runs(skey, nslots, cs.run_start, cs.wsum);
         constexpr int TPR = 8 / CPT;  // threads per run
-        for (int item = t; item < R * TPR; item += bs) {
-            const int r = item / TPR, k0 = (item % TPR) * CPT;  // corners k0 .. k0 + CPT - 1
-            const int a = cs.run_start[r], e = cs.run_start[r + 1];
-            if (!(skey[a] < g.key_max)) continue;  // slots outside the grid
+        const int nitems = R * TPR;
+        // whole warps take the loop together (the merge shuffles)
+        for (int item = t; item - lane < nitems; item += bs) {
+            const bool live = item < nitems;
+            const int r = live ? item / TPR : 0, kq = item % TPR, k0 = kq * CPT;  // corners k0 .. k0 + CPT - 1
+            const int a = cs.run_start[r];
+            // slots outside the grid (and lanes past the items) sum nothing
+            const bool inb = live && skey[a] < g.key_max;
+            const int e = inb ? cs.run_start[r + 1] : a;
             T am[CPT], ap0[CPT], ap1[CPT], ap2[CPT], af0[CPT], af1[CPT], af2[CPT], g0[CPT], g1[CPT], g2[CPT];
     #pragma unroll
             for (int j = 0; j < CPT; ++j) am[j] = ap0[j] = ap1[j] = ap2[j] = af0[j] = af1[j] = af2[j] = g0[j] = g1[j] = g2[j] = 0;
@@ -525,6 +537,31 @@ struct P2GBlock {
                     }
                 }
             }
+            bool skip = !inb;
+            if constexpr (sizeof(T) == 4) {
+                constexpr int SH = TPR / 2;  // lanes from run r - 1's x = 1 corners to run r's x = 0 corners
+                const bool recv = inb && kq < SH && lane >= SH && r > 0 && skey[cs.run_start[r - 1]] + 1u == skey[a];
+#pragma unroll
+                for (int j = 0; j < CPT; ++j) {
+                    const float x0 = __shfl_up_sync(FULL_MASK, am[j], SH), x1 = __shfl_up_sync(FULL_MASK, ap0[j], SH);
+                    const float x2 = __shfl_up_sync(FULL_MASK, ap1[j], SH), x3 = __shfl_up_sync(FULL_MASK, ap2[j], SH);
+                    const float x4 = __shfl_up_sync(FULL_MASK, af0[j], SH), x5 = __shfl_up_sync(FULL_MASK, af1[j], SH);
+                    const float x6 = __shfl_up_sync(FULL_MASK, af2[j], SH);
+                    if (recv) {
+                        am[j] += x0, ap0[j] += x1, ap1[j] += x2, ap2[j] += x3;
+                        af0[j] += x4, af1[j] += x5, af2[j] += x6;
+                    }
+                    if constexpr (MG) {
+                        const float y0 = __shfl_up_sync(FULL_MASK, g0[j], SH);
+                        const float y1 = __shfl_up_sync(FULL_MASK, g1[j], SH);
+                        const float y2 = __shfl_up_sync(FULL_MASK, g2[j], SH);
+                        if (recv) g0[j] += y0, g1[j] += y1, g2[j] += y2;
+                    }
+                }
+                // a sender's sums went to the lane SH up (lanes near the warp's top read their own false)
+                if (__shfl_down_sync(FULL_MASK, recv ? 1 : 0, SH) && kq >= SH) skip = true;
+            }
+            if (skip) continue;
 #pragma unroll
             for (int j = 0; j < CPT; ++j) {
                 const long long nid = cs.node(a, k0 + j);
@@ -575,8 +612,16 @@ __device__ __forceinline__ void p2g_cells_run(const PView<T>& P, const NView<T>&
     blk.template scatter<CPT, MG>(nd, g, (int)min((long long)BS, n - blockIdx.x * (long long)BS), mark_active);
 }
 
+// FP32 with 1 or 2 corners per thread: registers capped for 1536 resident
+// threads per SM (40 registers, no spills at 2 corners), which hides more of
+// the staging loads' latency than 48 registers at 1280 threads.
+template <typename T, int CPT>
+__host__ __device__ constexpr int cells_min_blocks(int bs) {
+    return sizeof(T) == 4 && CPT < 4 ? 1536 / bs : 1;
+}
+
 template <typename T, int CPT, int BS>
-__global__ void __launch_bounds__(BS) k_p2g_cells(PView<T> P, NView<T> nd, Geom g, const unsigned* __restrict__ skeys,
+__global__ void __launch_bounds__(BS, cells_min_blocks<T, CPT>(BS)) k_p2g_cells(PView<T> P, NView<T> nd, Geom g, const unsigned* __restrict__ skeys,
                                                    const unsigned* __restrict__ perm, long long n, int mark_active) {
     p2g_cells_run<T, CPT, BS, false>(P, nd, g, skeys, perm, n, mark_active);
 }
@@ -811,8 +856,12 @@ __host__ __device__ constexpr size_t pass1_cells_smem(int bs) {
            (size_t)bs * CELL_SLOT_BYTES + (size_t)(bs + 1) * 4 + 64 * 4;
 }
 
+// FP32 with 1 or 2 corners per thread: registers capped for 1536 resident
+// threads per SM (40 registers, a few bytes spilled), about 10% faster than
+// 56 registers at 1152 threads: the kernel waits on its record gathers, and
+// more resident warps keep more of them in flight.
 template <typename T, int CPT, int BS>
-__global__ void __launch_bounds__(BS) k_pass1_cells(PView<T> P, NView<T> nd, Geom g,
+__global__ void __launch_bounds__(BS, cells_min_blocks<T, CPT>(BS)) k_pass1_cells(PView<T> P, NView<T> nd, Geom g,
                                                      const unsigned* __restrict__ skeys,
                                                      const unsigned* __restrict__ perm, long long n, T dt,
                                                      T mass_min, int contact) {
