@@ -554,7 +554,7 @@ def network_for_batch(args, contact, floor, steps):
     bsz = 8192
     epochs = int(max(20, math.ceil(5000 * bsz / max(n, 1))))  # about 5000 Adam steps
     net = engine.Net(E=200.0e9, nu=0.3, yield_=250.0e6, C0=2.0e-3, C1=1.0e12, n_samples=1000, epochs=epochs,
-                     batch=bsz, deps_sigma=dsig, lr=2.0e-3)
+                     batch=bsz, deps_sigma=dsig, lr=4.0e-3)
     rep = net.train_rows(rows.data_ptr(), n)
     del rows
     info = {"pilot": f"16 honeycomb specimens (seed 99, {ppk.state.n_particles} particles), plain FP64, {steps} steps "
@@ -582,7 +582,7 @@ def network_for_foam(args, contact, floor, steps):
     bsz = 8192
     epochs = int(max(20, math.ceil(5000 * bsz / max(n, 1))))
     net = engine.Net(E=70.0e9, nu=0.33, yield_=120.0e6, C0=700.0e6 / 1.0e12, C1=1.0e12, n_samples=1000,
-                     epochs=epochs, batch=bsz, deps_sigma=dsig, lr=2.0e-3)
+                     epochs=epochs, batch=bsz, deps_sigma=dsig, lr=4.0e-3)
     rep = net.train_rows(rows.data_ptr(), n)
     return net, {"pilot": f"reduced foam 2 x 2 cells (seed 9, {pilot.n_particles} particles), plain FP64, "
                           f"{steps} steps (inputs of one step in four)", "harvested_rows": n, "seconds_pilot": t1 - t0, "training": rep}
@@ -597,7 +597,7 @@ def network_isolated(contact_unused=None):
     from code_mpm_gb300 import engine
 
     net = engine.Net(E=200.0e9, nu=0.3, yield_=250.0e6, C0=2.0e-3, C1=1.0e12, n_samples=20_000_000, epochs=20,
-                     batch=65536, lr=2.0e-3)
+                     batch=65536, lr=4.0e-3)
     rep = net.train()
     n = 16 * 1024 * 1024
     g = torch.Generator(device="cuda")

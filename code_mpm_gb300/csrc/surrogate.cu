@@ -5,8 +5,11 @@
 // (ConstitutiveRelation_calculateIncrement_VonMisesHardening.cpp:4-92) for
 // clearly plastic trial states; it is this library's addition.
 //
-// Network: x (13 inputs, padded to 16) -> 128 -> 128 -> 128 (SiLU) -> 8 (7
-// used).  Inputs are scaled to O(1): stress and R by 1/yield, the strain
+// Network: x (13 inputs, padded to 16) -> 128 -> 128 -> 128 (ReLU) -> 8 (7
+// used).  ReLU rather than a smooth activation: its inference epilogue is a
+// bias add and one packed convert per two values, with nothing on the
+// special-function pipe, so the epilogue keeps pace with the tensor core.
+// Inputs are scaled to O(1): stress and R by 1/yield, the strain
 // increment by 1/deps_sigma; outputs are standardised by the training set's
 // mean and standard deviation.
 #include <cuda_bf16.h>
@@ -209,18 +212,12 @@ __global__ void k_normalise_targets(long long n, const float* __restrict__ t, co
 // FP32 GEMM for training: C[M x N] = op(A)[M x K] op(B)[K x N], 64 x 64 tiles,
 // 16-deep k slices, 4 x 4 outputs per thread.  op(A) = A (row-major, lda) or
 // A^T (A stored K x M); op(B) = B (row-major K x N) or B^T (B stored N x K,
-// the layer weights W[out][in]).  Epilogues: store (+bias), bias + SiLU
-// (keeps the pre-activation in aux), times SiLU'(aux) (backward), and atomic
+// the layer weights W[out][in]).  Epilogues: store (+bias), bias + ReLU
+// (keeps the pre-activation in aux), times ReLU'(aux) (backward), and atomic
 // accumulation of split-K partial sums (weight gradients; blockIdx.z picks
 // the k range).
 // ---------------------------------------------------------------------------
-enum { EPI_STORE = 0, EPI_SILU = 1, EPI_DSILU = 2, EPI_ATOMIC = 3 };
-
-__device__ __forceinline__ float silu_f(float z) { return z / (1.0f + __expf(-z)); }
-__device__ __forceinline__ float dsilu_f(float z) {
-    const float s = 1.0f / (1.0f + __expf(-z));
-    return s * (1.0f + z * (1.0f - s));
-}
+enum { EPI_STORE = 0, EPI_RELU = 1, EPI_DRELU = 2, EPI_ATOMIC = 3 };
 
 template <bool TA, bool TB, int EPI>
 __global__ void __launch_bounds__(256) k_sgemm(int M, int N, int K, const float* __restrict__ A, int lda,
@@ -294,12 +291,12 @@ __global__ void __launch_bounds__(256) k_sgemm(int M, int N, int K, const float*
             if constexpr (EPI == EPI_STORE) {
                 if (bias) v += bias[n];
                 C[o] = v;
-            } else if constexpr (EPI == EPI_SILU) {
+            } else if constexpr (EPI == EPI_RELU) {
                 v += bias[n];
                 aux[o] = v;
-                C[o] = silu_f(v);
-            } else if constexpr (EPI == EPI_DSILU) {
-                C[o] = v * dsilu_f(aux[o]);
+                C[o] = fmaxf(v, 0.0f);
+            } else if constexpr (EPI == EPI_DRELU) {
+                C[o] = aux[o] > 0.0f ? v : 0.0f;
             } else {
                 atomicAdd(&C[o], v);
             }
@@ -487,7 +484,7 @@ __global__ void k_exact_wide(long long n, const float* __restrict__ in, MatConst
 // without swizzle; the accumulator D (128 lanes x N columns FP32) sits in
 // tensor memory.  tcgen05.commit signals an mbarrier; each warp then reads
 // its 32 lanes (tcgen05.ld 32x32b: thread t of warp w <-> lane 32w + t =
-// sample), adds the bias, applies SiLU, rounds to BF16 and writes the next
+// sample), adds the bias, applies ReLU, rounds to BF16 and writes the next
 // layer's A operand.
 //
 // Shared-memory operand layout (K-major, no swizzle): 8-row x 16-byte core
@@ -522,11 +519,16 @@ constexpr uint32_t SW1 = 0, SW2 = SW1 + HID * IN * 2, SW3 = SW2 + HID * HID * 2,
                    WBYTES = SW4 + 16 * HID * 2;  // W4 padded to 16 rows
 // biases (FP32): b1, b2, b3 (128 each), b4 (16)
 constexpr uint32_t NBIAS = 3 * HID + 16;
-// kernel shared memory: weights, bias, A0 (128 x 16), A1 (128 x 128), mbarrier, TMEM address
-// hidden biases halved, as BF16 pairs (3 x HID / 2 words), for the packed SiLU of the epilogue
+// kernel shared memory: weights, the output bias (FP32), the hidden biases as
+// BF16 pairs (3 x HID / 2 words), then per tile slot (NSLOT) A0 (128 x 16) and
+// A1 (128 x 128), the mbarriers (MMA done and operand ready per slot, the
+// final drain), the TMEM address
+constexpr int NSLOT = 4;
+constexpr uint32_t TMEM_COLS = NSLOT <= 1 ? 128 : NSLOT <= 2 ? 256 : 512;  // a power of two >= 128 NSLOT
 constexpr uint32_t S_BIAS = WBYTES, S_HB = S_BIAS + NBIAS * 4,
-                   S_A0 = (S_HB + 3 * (HID / 2) * 4 + 1023) / 1024 * 1024, S_A1 = S_A0 + 128 * IN * 2,
-                   S_BAR = S_A1 + 128 * HID * 2, S_TADDR = S_BAR + 8, SMEM_TC = S_TADDR + 8 + 1024;
+                   S_A0 = (S_HB + 3 * (HID / 2) * 4 + 1023) / 1024 * 1024, A0_BYTES = 128 * IN * 2,
+                   S_A1 = S_A0 + NSLOT * A0_BYTES, A1_BYTES = 128 * HID * 2, S_BAR = S_A1 + NSLOT * A1_BYTES,
+                   S_TADDR = S_BAR + 8 * (2 * NSLOT + 1), SMEM_TC = S_TADDR + 8 + 1024;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -584,58 +586,130 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16]) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// the 64 columns at taddr of this warp's lanes into u: two loads in flight,
+// then the wait, in one statement so no use of u precedes the wait
+__device__ __forceinline__ void tmem_ld64(uint32_t taddr, uint32_t* u) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,"
+        "%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%64];\n"
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,"
+        "%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%65];\n"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]), "=r"(u[4]), "=r"(u[5]), "=r"(u[6]), "=r"(u[7]),
+          "=r"(u[8]), "=r"(u[9]), "=r"(u[10]), "=r"(u[11]), "=r"(u[12]), "=r"(u[13]), "=r"(u[14]), "=r"(u[15]),
+          "=r"(u[16]), "=r"(u[17]), "=r"(u[18]), "=r"(u[19]), "=r"(u[20]), "=r"(u[21]), "=r"(u[22]), "=r"(u[23]),
+          "=r"(u[24]), "=r"(u[25]), "=r"(u[26]), "=r"(u[27]), "=r"(u[28]), "=r"(u[29]), "=r"(u[30]), "=r"(u[31]),
+          "=r"(u[32]), "=r"(u[33]), "=r"(u[34]), "=r"(u[35]), "=r"(u[36]), "=r"(u[37]), "=r"(u[38]), "=r"(u[39]),
+          "=r"(u[40]), "=r"(u[41]), "=r"(u[42]), "=r"(u[43]), "=r"(u[44]), "=r"(u[45]), "=r"(u[46]), "=r"(u[47]),
+          "=r"(u[48]), "=r"(u[49]), "=r"(u[50]), "=r"(u[51]), "=r"(u[52]), "=r"(u[53]), "=r"(u[54]), "=r"(u[55]),
+          "=r"(u[56]), "=r"(u[57]), "=r"(u[58]), "=r"(u[59]), "=r"(u[60]), "=r"(u[61]), "=r"(u[62]), "=r"(u[63])
+        : "r"(taddr), "r"(taddr + 32u)
+        : "memory");
+}
+
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
     __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
     return *reinterpret_cast<uint32_t*>(&h);
 }
 
-constexpr uint32_t BF16X2_HALF = 0x3F003F00u;  // (0.5, 0.5) as BF16 pairs
+constexpr uint32_t BF16X2_ONE = 0x3F803F80u;  // (1, 1) as BF16 pairs
 
-// SiLU of two accumulators in packed BF16: with h = z / 2 = v / 2 + b / 2,
-// z sigmoid(z) = h (1 + tanh h) = h + h tanh h; each step is one rounding to
-// BF16 (the next layer's A operand is BF16 anyway), two values per instruction
-__device__ __forceinline__ uint32_t silu_bf16x2(float v0, float v1, uint32_t hb2) {
+// ReLU(v + b) of two accumulators in packed BF16: the accumulators are
+// rounded to BF16 (v0 to the low half, element k; v1 to the high half), then
+// one packed FMA adds the biases b2 (BF16 pair) and clamps at zero
+__device__ __forceinline__ uint32_t relu_bf16x2(float v0, float v1, uint32_t b2) {
     const uint32_t x = pack_bf16(v0, v1);
-    uint32_t h, t, y;
-    asm("fma.rn.bf16x2 %0, %1, %2, %3;" : "=r"(h) : "r"(x), "r"(BF16X2_HALF), "r"(hb2));
-    asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t) : "r"(h));
-    asm("fma.rn.bf16x2 %0, %1, %2, %1;" : "=r"(y) : "r"(h), "r"(t));
+    uint32_t y;
+    asm("fma.rn.relu.bf16x2 %0, %1, %2, %3;" : "=r"(y) : "r"(x), "r"(BF16X2_ONE), "r"(b2));
     return y;
 }
 
 // issue one layer: D = A (128 x K) . W^T (W: N x K), K in steps of 16
-__device__ __forceinline__ void issue_layer(uint32_t tmem, uint32_t a_addr, int K, uint32_t w_addr, int N) {
-    const uint32_t lbo_a = 128 / 8 * 128, lbo_b = (uint32_t)(N / 8) * 128;
-    const uint32_t id = idesc_bf16(128, N);
+// (the descriptors of successive K steps differ only in the start address
+// field, by two core matrices' leading offsets: one addition each)
+template <int K, int N>
+__device__ __forceinline__ void issue_layer(uint32_t tmem, uint32_t a_addr, uint32_t w_addr) {
+    constexpr uint32_t lbo_a = 128 / 8 * 128, lbo_b = (uint32_t)(N / 8) * 128;
+    constexpr uint32_t id = idesc_bf16(128, N);
+    uint64_t a = smem_desc(a_addr, lbo_a, 128), b = smem_desc(w_addr, lbo_b, 128);
+#pragma unroll
     for (int k = 0; k < K; k += 16) {
-        const uint64_t a = smem_desc(a_addr + (uint32_t)(k / 8) * lbo_a, lbo_a, 128);
-        const uint64_t b = smem_desc(w_addr + (uint32_t)(k / 8) * lbo_b, lbo_b, 128);
         mma_bf16(tmem, a, b, id, k > 0 ? 1u : 0u);
+        a += (2 * lbo_a) >> 4;
+        b += (2 * lbo_b) >> 4;
     }
 }
 
-// hidden-layer epilogue: warps w and w + 4 share TMEM lane quarter w % 4;
-// their thread t reads sample 32 (w % 4) + t's accumulators in columns
-// [64 (w / 4), 64 (w / 4) + 64), adds the bias, applies SiLU, and writes that
-// part of BF16 row r of the next A operand; hb2 holds the layer's halved
-// biases as BF16 pairs
-__device__ __forceinline__ void hidden_epilogue(uint32_t taddr_row, const uint32_t* hb2, unsigned char* a1) {
-    const int w = threadIdx.x >> 5, r = 32 * (w & 3) + (threadIdx.x & 31), half = w >> 2;
-#pragma unroll 1
-    for (int c0 = 64 * half; c0 < 64 * half + 64; c0 += 32) {
-        float v[32];
-        tmem_ld32(taddr_row + (uint32_t)c0, v);
+// hidden-layer epilogue of one tile by its group of WPS warps: thread t of
+// group warp j (TMEM lane quarter j % 4) owns sample r = 32 (j % 4) + t and
+// columns c0 .. c0 + SPAN - 1; it reads those accumulators (EPI_COLS per
+// wait), adds the bias, applies ReLU and writes that part of BF16 row r of
+// the next A operand; hb2 holds the layer's biases as BF16 pairs
+constexpr int EPI_COLS = 32;  // accumulator columns per TMEM read of the epilogue (32 or 64)
+constexpr int WPS = 4;        // epilogue warps per tile slot: 4 (all 128 columns each) or 8 (64 each)
+constexpr int SPAN = HID * 4 / WPS;  // columns per epilogue warp
+
+__device__ __forceinline__ void hidden_epilogue(uint32_t taddr_row, const uint32_t* hb2, unsigned char* a1, int r,
+                                                int c0) {
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
+    for (int h = c0; h < c0 + SPAN; h += EPI_COLS) {
+        uint32_t u[EPI_COLS];
+        if constexpr (EPI_COLS == 64) {
+            tmem_ld64(taddr_row + (uint32_t)h, u);
+        } else {
+            float v[32];
+            tmem_ld32(taddr_row + (uint32_t)h, v);
+#pragma unroll
+            for (int c = 0; c < 32; ++c) u[c] = __float_as_uint(v[c]);
+        }
+#pragma unroll
+        for (int k = 0; k < EPI_COLS; k += 8) {
+            const uint4 b = *reinterpret_cast<const uint4*>(hb2 + ((h + k) >> 1));
             uint4 pk;
-            const int k = c0 + 8 * q;
-            pk.x = silu_bf16x2(v[8 * q + 0], v[8 * q + 1], hb2[(k >> 1) + 0]);
-            pk.y = silu_bf16x2(v[8 * q + 2], v[8 * q + 3], hb2[(k >> 1) + 1]);
-            pk.z = silu_bf16x2(v[8 * q + 4], v[8 * q + 5], hb2[(k >> 1) + 2]);
-            pk.w = silu_bf16x2(v[8 * q + 6], v[8 * q + 7], hb2[(k >> 1) + 3]);
-            *reinterpret_cast<uint4*>(a1 + kmajor_off(r, k, 128)) = pk;
+            pk.x = relu_bf16x2(__uint_as_float(u[k + 0]), __uint_as_float(u[k + 1]), b.x);
+            pk.y = relu_bf16x2(__uint_as_float(u[k + 2]), __uint_as_float(u[k + 3]), b.y);
+            pk.z = relu_bf16x2(__uint_as_float(u[k + 4]), __uint_as_float(u[k + 5]), b.z);
+            pk.w = relu_bf16x2(__uint_as_float(u[k + 6]), __uint_as_float(u[k + 7]), b.w);
+            *reinterpret_cast<uint4*>(a1 + kmajor_off(r, h + k, 128)) = pk;
         }
     }
+}
+
+// a sample's 13 physical inputs (zero past n)
+__device__ __forceinline__ void load_inputs(const float* __restrict__ in, long long i, long long n, float x[NIN]) {
+#pragma unroll
+    for (int c = 0; c < NIN; ++c) x[c] = i < n ? in[i * NIN + c] : 0.0f;
+}
+
+// a warp's lanes have finished writing an operand: lane 0 arrives on the
+// slot's ready barrier (one arrival per warp) once the whole warp's shared
+// stores are visible to the tensor core's (async) proxy
+__device__ __forceinline__ void warp_arrive_ready(uint32_t bar) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// a warp waits for a barrier phase: lane 0 polls (bounded), the warp follows;
+// false on a timeout (same answer in every lane)
+__device__ __forceinline__ bool warp_wait(uint32_t bar, uint32_t parity, unsigned* err) {
+    int ok = 1;
+    if ((threadIdx.x & 31) == 0) ok = bar_wait(bar, parity, err) ? 1 : 0;
+    ok = __shfl_sync(FULL_MASK, ok, 0);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    return ok != 0;
+}
+
+// non-blocking test of an mbarrier phase
+__device__ __forceinline__ bool bar_test(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
 }
 
 struct TcArgs {
@@ -651,9 +725,22 @@ struct TcArgs {
     MatConst mat;              // for the elastic predictor D de
 };
 
-constexpr int TC_THREADS = 256;
+// NSLOT epilogue groups of WPS warps (one per tile slot; warp j of a group
+// reads TMEM lane quarter j % 4) and the MMA warp
+constexpr int TC_THREADS = 32 * (WPS * NSLOT + 1);
 
-__global__ void __launch_bounds__(TC_THREADS, 2) k_mlp_tc(TcArgs a) {
+// One CTA per SM takes groups of NSLOT 128-sample tiles, one per slot, and
+// runs the slots as independent pipelines that share the tensor core.  A
+// slot's epilogue group writes the operand (the inputs, or the previous
+// layer's activations) and arrives on the slot's `ready` mbarrier (128
+// arrivals); the MMA warp issues the layer of whichever slot is ready and
+// commits to that slot's `full` mbarrier; the group waits on `full`, turns
+// the accumulators (128 TMEM columns per slot) into the next operand, and so
+// on.  The group loads its next tile's inputs while the current tile runs.
+// Waits are bounded: on a timeout the error word is set and the roles stop;
+// the MMA thread then waits (bounded) for its last MMAs before the TMEM is
+// freed.
+__global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(TcArgs a) {
     extern __shared__ __align__(1024) unsigned char sm[];
     const int t = threadIdx.x, w = t >> 5;
     unsigned char* s = sm + ((1024 - (smem_u32(sm) & 1023u)) & 1023u);  // 1024-byte aligned base
@@ -663,18 +750,22 @@ __global__ void __launch_bounds__(TC_THREADS, 2) k_mlp_tc(TcArgs a) {
     float* bias = reinterpret_cast<float*>(s + S_BIAS);
     for (uint32_t i = t; i < NBIAS; i += TC_THREADS) bias[i] = a.bias[i];
     uint32_t* hb2 = reinterpret_cast<uint32_t*>(s + S_HB);
-    for (uint32_t i = t; i < 3 * (HID / 2); i += TC_THREADS) {
-        const uint32_t l = i / (HID / 2), j = 2 * (i % (HID / 2));
-        hb2[i] = pack_bf16(0.5f * a.bias[l * HID + j], 0.5f * a.bias[l * HID + j + 1]);
-    }
+    for (uint32_t i = t; i < 3 * (HID / 2); i += TC_THREADS)
+        hb2[i] = pack_bf16(a.bias[2 * i], a.bias[2 * i + 1]);
     uint32_t* taddr_slot = reinterpret_cast<uint32_t*>(s + S_TADDR);
-    const uint32_t bar = sbase + S_BAR;
+    // mbarriers: slot sl's MMA-done at full0 + 8 sl, its operand-ready at ready0 + 8 sl
+    const uint32_t full0 = sbase + S_BAR, ready0 = full0 + 8 * NSLOT, drain = ready0 + 8 * NSLOT;
     if (t == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        for (uint32_t sl = 0; sl < NSLOT; ++sl) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(full0 + 8 * sl) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(ready0 + 8 * sl), "n"(WPS) : "memory");
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(drain) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (w == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(smem_u32(taddr_slot))
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(taddr_slot)),
+                     "n"(TMEM_COLS)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -683,75 +774,115 @@ __global__ void __launch_bounds__(TC_THREADS, 2) k_mlp_tc(TcArgs a) {
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *taddr_slot;
-    const uint32_t trow = tmem + ((uint32_t)(32 * (w & 3)) << 16);  // this warp's lane quarter
     const long long n = a.count ? (long long)min((unsigned long long)*a.count, (unsigned long long)a.n) : a.n;
-    const long long ntiles = (n + 127) / 128;
-    uint32_t phase = 0;
-    bool ok = true;
-    for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        const long long i = tile * 128 + (t & 127);  // warps 0-3 own the samples' inputs and outputs
-        // inputs -> A0 (128 x 16 BF16)
-        float x[16];
+    const long long ngroups = (n + 128 * NSLOT - 1) / (128 * NSLOT);
+    // tile groups of this CTA: blockIdx.x, blockIdx.x + gridDim.x, ...
+    const long long mine = blockIdx.x < ngroups ? (ngroups - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    if (w == WPS * NSLOT) {
+        // the MMA warp: lane 0 issues the next layer of any slot whose operand is ready
+        if ((t & 31) == 0) {
+            const unsigned total = 4u * (unsigned)mine;  // layers per slot
+            unsigned issued[NSLOT];
 #pragma unroll
-        for (int c = 0; c < 16; ++c) x[c] = 0.0f;
-        if (t < 128 && i < n) {
+            for (int sl = 0; sl < NSLOT; ++sl) issued[sl] = 0u;
+            uint32_t ph = 0u;  // bit sl: slot sl's ready parity
+            bool ok = true;
+            unsigned idle = 0u;
+            for (unsigned left = NSLOT * total; left > 0 && ok;) {
+                bool progress = false;
 #pragma unroll
-            for (int c = 0; c < NIN; ++c) x[c] = a.in[i * NIN + c] * a.in_inv_scale[c];
-        }
-        uint4 p0, p1;
-        p0.x = pack_bf16(x[0], x[1]);
-        p0.y = pack_bf16(x[2], x[3]);
-        p0.z = pack_bf16(x[4], x[5]);
-        p0.w = pack_bf16(x[6], x[7]);
-        p1.x = pack_bf16(x[8], x[9]);
-        p1.y = pack_bf16(x[10], x[11]);
-        p1.z = pack_bf16(x[12], x[13]);
-        p1.w = pack_bf16(x[14], x[15]);
-        if (t < 128) {
-            *reinterpret_cast<uint4*>(s + S_A0 + kmajor_off(t, 0, 128)) = p0;
-            *reinterpret_cast<uint4*>(s + S_A0 + kmajor_off(t, 8, 128)) = p1;
-        }
-        for (int layer = 0; layer < 4 && ok; ++layer) {
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-            __syncthreads();
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            if (t == 0) {
-                if (layer == 0)
-                    issue_layer(tmem, sbase + S_A0, IN, sbase + SW1, HID);
-                else if (layer < 3)
-                    issue_layer(tmem, sbase + S_A1, HID, sbase + (layer == 1 ? SW2 : SW3), HID);
-                else
-                    issue_layer(tmem, sbase + S_A1, HID, sbase + SW4, 16);
-                mma_commit(bar);
+                for (int sl = 0; sl < NSLOT; ++sl) {
+                    if (issued[sl] < total && bar_test(ready0 + 8u * sl, (ph >> sl) & 1u)) {
+                        ph ^= 1u << sl;
+                        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                        const int layer = (int)(issued[sl] & 3u);
+                        const uint32_t d = tmem + 128u * sl;
+                        const uint32_t a1 = sbase + S_A1 + sl * A1_BYTES;
+                        if (layer == 0)
+                            issue_layer<IN, HID>(d, sbase + S_A0 + sl * A0_BYTES, sbase + SW1);
+                        else if (layer < 3)
+                            issue_layer<HID, HID>(d, a1, sbase + (layer == 1 ? SW2 : SW3));
+                        else
+                            issue_layer<HID, 16>(d, a1, sbase + SW4);
+                        mma_commit(full0 + 8u * sl);
+                        ++issued[sl];
+                        --left;
+                        progress = true;
+                    }
+                }
+                if (progress) {
+                    idle = 0u;
+                } else if (++idle > (1u << 26)) {
+                    atomicOr(a.err, ERR_WAIT_TIMEOUT);
+                    ok = false;
+                }
             }
-            // every thread decides alike, so no thread leaves a barrier the others reach
-            ok = __syncthreads_and(bar_wait(bar, phase, a.err) ? 1 : 0) != 0;
-            if (!ok) {
-                bar_wait(bar, phase, a.err);  // once more (bounded) for the MMAs in flight
-                break;
-            }
-            phase ^= 1u;
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            if (layer < 3) {
-                hidden_epilogue(trow, hb2 + layer * (HID / 2), s + S_A1);
-            } else {
-                float v[16];
-                if (w < 4) tmem_ld16(trow, v);
-                if (w < 4 && i < n) {
-                    float d[6];
-                    elastic_predictor(a.mat, a.in + i * NIN, d);
+            // every MMA issued has completed before the TMEM is freed
+            mma_commit(drain);
+            bar_wait(drain, 0u, a.err);
+        }
+    } else {
+        // epilogue group = slot sl; its warp j reads lanes 32 (j % 4) .. + 31, columns c0 .. c0 + SPAN - 1;
+        // the warps of columns from 0 own the samples' inputs and outputs
+        const int sl = w / WPS, j = w % WPS, r = 32 * (j & 3) + (t & 31), c0 = (j >> 2) * SPAN;
+        const bool owner = c0 == 0;
+        const uint32_t trow = tmem + 128u * (uint32_t)sl + ((uint32_t)(32 * (j & 3)) << 16);
+        unsigned char* a0 = s + S_A0 + sl * A0_BYTES;
+        unsigned char* a1 = s + S_A1 + sl * A1_BYTES;
+        uint32_t ph = 0u;
+        bool ok = true;
+        float x[NIN];  // the next tile's physical inputs, loaded one tile ahead
+        load_inputs(a.in, ((long long)blockIdx.x * NSLOT + sl) * 128 + r, owner ? n : 0, x);
+        for (long long k = 0; k < mine && ok; ++k) {
+            const long long i = (((long long)blockIdx.x + k * gridDim.x) * NSLOT + sl) * 128 + r;
+            // inputs -> A0 (128 x 16 BF16), then the next tile's inputs are requested
+            float xn[16];
 #pragma unroll
-                    for (int c = 0; c < NOUT; ++c)
-                        a.out[i * NOUT + c] =
-                            (v[c] + bias[3 * HID + c]) * a.out_scale[c] + a.out_shift[c] + (c < 6 ? d[c] : 0.0f);
+            for (int c = 0; c < 16; ++c) xn[c] = c < NIN ? x[c] * a.in_inv_scale[c] : 0.0f;
+            float de[6];  // this tile's strain increment, for the elastic predictor
+#pragma unroll
+            for (int c = 0; c < 6; ++c) de[c] = x[7 + c];
+            uint4 p0, p1;
+            p0.x = pack_bf16(xn[0], xn[1]);
+            p0.y = pack_bf16(xn[2], xn[3]);
+            p0.z = pack_bf16(xn[4], xn[5]);
+            p0.w = pack_bf16(xn[6], xn[7]);
+            p1.x = pack_bf16(xn[8], xn[9]);
+            p1.y = pack_bf16(xn[10], xn[11]);
+            p1.z = pack_bf16(xn[12], xn[13]);
+            p1.w = pack_bf16(xn[14], xn[15]);
+            if (owner) {
+                *reinterpret_cast<uint4*>(a0 + kmajor_off(r, 0, 128)) = p0;
+                *reinterpret_cast<uint4*>(a0 + kmajor_off(r, 8, 128)) = p1;
+                load_inputs(a.in, i + (long long)gridDim.x * NSLOT * 128, n, x);
+            }
+            for (int layer = 0; layer < 4 && ok; ++layer) {
+                // the operand (inputs, or the previous layer's activations) is ready
+                warp_arrive_ready(ready0 + 8 * sl);
+                ok = warp_wait(full0 + 8 * sl, ph, a.err);
+                if (!ok) break;
+                ph ^= 1u;
+                if (layer < 3) {
+                    hidden_epilogue(trow, hb2 + layer * (HID / 2), a1, r, c0);
+                } else if (owner) {
+                    float v[16];
+                    tmem_ld16(trow, v);
+                    if (i < n) {
+                        float d[6];
+                        trial_increment<float>(a.mat, de, d);  // the elastic predictor D de
+#pragma unroll
+                        for (int c = 0; c < NOUT; ++c)
+                            a.out[i * NOUT + c] =
+                                (v[c] + bias[3 * HID + c]) * a.out_scale[c] + a.out_shift[c] + (c < 6 ? d[c] : 0.0f);
+                    }
                 }
             }
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (w == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem) : "memory");
+    if (w == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(TMEM_COLS) : "memory");
 }
 
 }  // namespace net
@@ -860,9 +991,9 @@ static int pack_weights(mpm_net* net) {
 static void forward_fp32(mpm_net* net, cudaStream_t s, long long n, const float* x, float* z1, float* h1, float* z2,
                          float* h2, float* z3, float* h3, float* y) {
     const float* p = net->p;
-    sgemm<false, true, EPI_SILU>(s, (int)n, HID, IN, x, IN, p + OW1, IN, h1, HID, p + OB1, z1);
-    sgemm<false, true, EPI_SILU>(s, (int)n, HID, HID, h1, HID, p + OW2, HID, h2, HID, p + OB2, z2);
-    sgemm<false, true, EPI_SILU>(s, (int)n, HID, HID, h2, HID, p + OW3, HID, h3, HID, p + OB3, z3);
+    sgemm<false, true, EPI_RELU>(s, (int)n, HID, IN, x, IN, p + OW1, IN, h1, HID, p + OB1, z1);
+    sgemm<false, true, EPI_RELU>(s, (int)n, HID, HID, h1, HID, p + OW2, HID, h2, HID, p + OB2, z2);
+    sgemm<false, true, EPI_RELU>(s, (int)n, HID, HID, h2, HID, p + OW3, HID, h3, HID, p + OB3, z3);
     sgemm<false, true, EPI_STORE>(s, (int)n, OUT, HID, h3, HID, p + OW4, HID, y, OUT, p + OB4);
 }
 
@@ -877,15 +1008,15 @@ static void backward_fp32(mpm_net* net, cudaStream_t s, long long n, const float
     // layer 4
     sgemm<true, false, EPI_ATOMIC>(s, OUT, HID, (int)n, dy, OUT, h3, HID, g + OW4, HID, nullptr, nullptr, splits);
     k_colsum<OUT><<<cb, 256, 0, s>>>(n, dy, g + OB4);
-    sgemm<false, false, EPI_DSILU>(s, (int)n, HID, OUT, dy, OUT, p + OW4, HID, d1, HID, nullptr, (float*)z3);
+    sgemm<false, false, EPI_DRELU>(s, (int)n, HID, OUT, dy, OUT, p + OW4, HID, d1, HID, nullptr, (float*)z3);
     // layer 3
     sgemm<true, false, EPI_ATOMIC>(s, HID, HID, (int)n, d1, HID, h2, HID, g + OW3, HID, nullptr, nullptr, splits);
     k_colsum<HID><<<cb, 256, 0, s>>>(n, d1, g + OB3);
-    sgemm<false, false, EPI_DSILU>(s, (int)n, HID, HID, d1, HID, p + OW3, HID, d2, HID, nullptr, (float*)z2);
+    sgemm<false, false, EPI_DRELU>(s, (int)n, HID, HID, d1, HID, p + OW3, HID, d2, HID, nullptr, (float*)z2);
     // layer 2
     sgemm<true, false, EPI_ATOMIC>(s, HID, HID, (int)n, d2, HID, h1, HID, g + OW2, HID, nullptr, nullptr, splits);
     k_colsum<HID><<<cb, 256, 0, s>>>(n, d2, g + OB2);
-    sgemm<false, false, EPI_DSILU>(s, (int)n, HID, HID, d2, HID, p + OW2, HID, d1, HID, nullptr, (float*)z1);
+    sgemm<false, false, EPI_DRELU>(s, (int)n, HID, HID, d2, HID, p + OW2, HID, d1, HID, nullptr, (float*)z1);
     // layer 1
     sgemm<true, false, EPI_ATOMIC>(s, HID, IN, (int)n, d1, HID, x, IN, g + OW1, IN, nullptr, nullptr, splits);
     k_colsum<HID><<<cb, 256, 0, s>>>(n, d1, g + OB1);
@@ -1253,8 +1384,8 @@ int mpm_net_infer(mpm_net* net, const float* d_in, float* d_out, int64_t n, int 
         a.n = n;
         a.err = net->err;
         a.mat = net->mat;
-        const long long tiles = (n + 127) / 128;
-        const unsigned grid = (unsigned)std::min<long long>(tiles, 2LL * net->sm_count);
+        const long long groups = (n + 128 * NSLOT - 1) / (128 * NSLOT);
+        const unsigned grid = (unsigned)std::min<long long>(std::max<long long>(groups, 1), net->sm_count);
         k_mlp_tc<<<grid, TC_THREADS, SMEM_TC, s>>>(a);
         NCK(cudaGetLastError());
         return MPM_OK;
@@ -1313,7 +1444,7 @@ int net_run_queue(mpm_net* net, const SurrogateQueue& q, cudaStream_t s, unsigne
     a.n = q.cap;
     a.err = err;
     a.mat = net->mat;
-    k_mlp_tc<<<(unsigned)(2 * net->sm_count), TC_THREADS, SMEM_TC, s>>>(a);
+    k_mlp_tc<<<(unsigned)net->sm_count, TC_THREADS, SMEM_TC, s>>>(a);
     return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_ERR_CUDA;
 }
 

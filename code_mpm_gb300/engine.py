@@ -519,7 +519,7 @@ class Net:
     """The learned von Mises hardening return map (include/mpm_surrogate.h)."""
 
     def __init__(self, E=200.0e9, nu=0.3, yield_=250.0e6, C0=2.0e-3, C1=1.0e12, n_samples=20_000_000,
-                 batch=65536, epochs=20, lr=2.0e-3, stress_range=1.5, epbar_max=0.2, deps_sigma=2.0e-4, seed=7,
+                 batch=65536, epochs=20, lr=4.0e-3, stress_range=1.5, epbar_max=0.2, deps_sigma=2.0e-4, seed=7,
                  sampling=0):
         self._L = lib()
         self.cfg = NetConfig(float(E), float(nu), float(yield_), float(C0), float(C1), int(n_samples), int(batch),

@@ -1,7 +1,7 @@
 /* Learned return map for the von Mises hardening material: C ABI.
  *
  * A small network (13 inputs: stress[6], isotropic back stress R, strain
- * increment[6]; 3 hidden layers of 128 with SiLU; 7 outputs: stress
+ * increment[6]; 3 hidden layers of 128 with ReLU; 7 outputs: stress
  * increment[6], dR) that stands in for
  * ConstitutiveRelation::calculateIncrement_VonMisesHardening
  * (ConstitutiveRelation_calculateIncrement_VonMisesHardening.cpp:4-92)

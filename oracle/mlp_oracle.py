@@ -2,7 +2,7 @@
 
 Only tests and the bench's checks use this file.  It restates the network
 that code_mpm_gb300/csrc/surrogate.cu trains and runs, in float64 numpy:
-13 inputs padded to 16, three hidden layers of 128 with SiLU, 8 outputs
+13 inputs padded to 16, three hidden layers of 128 with ReLU, 8 outputs
 (7 used).  The weight layout is the kernels' own: W[out][in] row-major,
 packed as W1, b1, W2, b2, W3, b3, W4, b4.  Inputs and targets are in the
 network's normalised units (the caller applies the scalings).
@@ -29,24 +29,23 @@ def unpack(theta):
     return out
 
 
-def silu(z):
-    return z / (1.0 + np.exp(-z))
+def relu(z):
+    return np.maximum(z, 0.0)
 
 
-def dsilu(z):
-    s = 1.0 / (1.0 + np.exp(-z))
-    return s * (1.0 + z * (1.0 - s))
+def drelu(z):
+    return (z > 0.0).astype(np.float64)
 
 
 def forward(theta, x):
     """x: n x 16 -> (y n x 8, cache)."""
     W1, b1, W2, b2, W3, b3, W4, b4 = unpack(theta)
     z1 = x @ W1.T + b1
-    h1 = silu(z1)
+    h1 = relu(z1)
     z2 = h1 @ W2.T + b2
-    h2 = silu(z2)
+    h2 = relu(z2)
     z3 = h2 @ W3.T + b3
-    h3 = silu(z3)
+    h3 = relu(z3)
     y = h3 @ W4.T + b4
     return y, (x, z1, h1, z2, h2, z3, h3)
 
@@ -61,11 +60,11 @@ def loss_and_grad(theta, x, t, used=7):
     loss = float(np.sum(d * d) / (n * used))
     dy = 2.0 * d / (n * used)
     gW4, gb4 = dy.T @ h3, dy.sum(0)
-    dz3 = (dy @ W4) * dsilu(z3)
+    dz3 = (dy @ W4) * drelu(z3)
     gW3, gb3 = dz3.T @ h2, dz3.sum(0)
-    dz2 = (dz3 @ W3) * dsilu(z2)
+    dz2 = (dz3 @ W3) * drelu(z2)
     gW2, gb2 = dz2.T @ h1, dz2.sum(0)
-    dz1 = (dz2 @ W2) * dsilu(z1)
+    dz1 = (dz2 @ W2) * drelu(z1)
     gW1, gb1 = dz1.T @ x, dz1.sum(0)
     g = np.concatenate([a.ravel() for a in (gW1, gb1, gW2, gb2, gW3, gb3, gW4, gb4)])
     return loss, g
@@ -80,14 +79,12 @@ def bf16(a):
 
 
 def forward_bf16(theta, x):
-    """The inference kernel's arithmetic: bf16 weights and activations, exact products, float sums; the hidden
-    SiLU in bf16 steps, h = bf16(v/2 + bf16(b/2)) with v = bf16(sum), then bf16(h + h bf16(tanh h))."""
+    """The inference kernel's arithmetic: bf16 weights and activations, exact products, float sums; each hidden
+    layer's sum plus bias through ReLU, rounded to bf16 once."""
     W1, b1, W2, b2, W3, b3, W4, b4 = unpack(theta)
     h = bf16(x)
     for W, b in ((W1, b1), (W2, b2), (W3, b3)):
-        v = bf16(h @ bf16(W).T)
-        hh = bf16(0.5 * v + bf16(0.5 * b))
-        h = bf16(hh + hh * bf16(np.tanh(hh)))
+        h = bf16(relu(h @ bf16(W).T + b))
     return h @ bf16(W4).T + b4
 
 
