@@ -520,15 +520,18 @@ constexpr uint32_t SW1 = 0, SW2 = SW1 + HID * IN * 2, SW3 = SW2 + HID * HID * 2,
 // biases (FP32): b1, b2, b3 (128 each), b4 (16)
 constexpr uint32_t NBIAS = 3 * HID + 16;
 // kernel shared memory: weights, the output bias (FP32), the hidden biases as
-// BF16 pairs (3 x HID / 2 words), then per tile slot (NSLOT) A0 (128 x 16) and
-// A1 (128 x 128), the mbarriers (MMA done and operand ready per slot, the
-// final drain), the TMEM address
-constexpr int NSLOT = 4;
-constexpr uint32_t TMEM_COLS = NSLOT <= 1 ? 128 : NSLOT <= 2 ? 256 : 512;  // a power of two >= 128 NSLOT
+// BF16 pairs (3 x HID / 2 words), then per tile slot (NSLOT) the inputs A0
+// (128 x 16), the mbarriers (MMA done and operand ready per slot, the final
+// drain), the TMEM address.  Tensor memory per slot (256 columns): the
+// accumulator D (128 columns) and the hidden activations, the A operand of
+// layers 2-4 (128 x 128 BF16 = 64 columns), so the MMAs read only the
+// weights from shared memory.
+constexpr int NSLOT = 2;
+constexpr uint32_t SLOT_COLS = 256, TMEM_COLS = SLOT_COLS * NSLOT, ACT_COL = 128;
 constexpr uint32_t S_BIAS = WBYTES, S_HB = S_BIAS + NBIAS * 4,
                    S_A0 = (S_HB + 3 * (HID / 2) * 4 + 1023) / 1024 * 1024, A0_BYTES = 128 * IN * 2,
-                   S_A1 = S_A0 + NSLOT * A0_BYTES, A1_BYTES = 128 * HID * 2, S_BAR = S_A1 + NSLOT * A1_BYTES,
-                   S_TADDR = S_BAR + 8 * (2 * NSLOT + 1), SMEM_TC = S_TADDR + 8 + 1024;
+                   S_BAR = S_A0 + NSLOT * A0_BYTES, S_TADDR = S_BAR + 8 * (2 * NSLOT + 1),
+                   SMEM_TC = S_TADDR + 8 + 1024;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -614,6 +617,30 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
 
 constexpr uint32_t BF16X2_ONE = 0x3F803F80u;  // (1, 1) as BF16 pairs
 
+// 32 words of this warp's lanes to TMEM columns taddr .. taddr + 31 (the
+// caller waits with tcgen05.wait::st before the columns are read)
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t* w) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
+        "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
+        "r"(w[0]), "r"(w[1]), "r"(w[2]), "r"(w[3]), "r"(w[4]), "r"(w[5]), "r"(w[6]), "r"(w[7]), "r"(w[8]), "r"(w[9]),
+        "r"(w[10]), "r"(w[11]), "r"(w[12]), "r"(w[13]), "r"(w[14]), "r"(w[15]), "r"(w[16]), "r"(w[17]), "r"(w[18]),
+        "r"(w[19]), "r"(w[20]), "r"(w[21]), "r"(w[22]), "r"(w[23]), "r"(w[24]), "r"(w[25]), "r"(w[26]), "r"(w[27]),
+        "r"(w[28]), "r"(w[29]), "r"(w[30]), "r"(w[31])
+        : "memory");
+}
+
+// D (TMEM) = A (TMEM: 128 lanes = rows, two BF16 of K per 32-bit column) x
+// B (shared-memory descriptor), accumulate when acc != 0
+__device__ __forceinline__ void mma_bf16_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t b, uint32_t idesc,
+                                            uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "r"(a_tmem), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
 // ReLU(v + b) of two accumulators in packed BF16: the accumulators are
 // rounded to BF16 (v0 to the low half, element k; v1 to the high half), then
 // one packed FMA adds the biases b2 (BF16 pair) and clamps at zero
@@ -627,6 +654,19 @@ __device__ __forceinline__ uint32_t relu_bf16x2(float v0, float v1, uint32_t b2)
 // issue one layer: D = A (128 x K) . W^T (W: N x K), K in steps of 16
 // (the descriptors of successive K steps differ only in the start address
 // field, by two core matrices' leading offsets: one addition each)
+// with the activations in tensor memory: K / 16 steps of 8 columns
+template <int K, int N>
+__device__ __forceinline__ void issue_layer_ts(uint32_t tmem, uint32_t a_tmem, uint32_t w_addr) {
+    constexpr uint32_t lbo_b = (uint32_t)(N / 8) * 128;
+    constexpr uint32_t id = idesc_bf16(128, N);
+    uint64_t b = smem_desc(w_addr, lbo_b, 128);
+#pragma unroll
+    for (int k = 0; k < K; k += 16) {
+        mma_bf16_ts(tmem, a_tmem + (uint32_t)(k / 2), b, id, k > 0 ? 1u : 0u);
+        b += (2 * lbo_b) >> 4;
+    }
+}
+
 template <int K, int N>
 __device__ __forceinline__ void issue_layer(uint32_t tmem, uint32_t a_addr, uint32_t w_addr) {
     constexpr uint32_t lbo_a = 128 / 8 * 128, lbo_b = (uint32_t)(N / 8) * 128;
@@ -642,37 +682,29 @@ __device__ __forceinline__ void issue_layer(uint32_t tmem, uint32_t a_addr, uint
 
 // hidden-layer epilogue of one tile by its group of WPS warps: thread t of
 // group warp j (TMEM lane quarter j % 4) owns sample r = 32 (j % 4) + t and
-// columns c0 .. c0 + SPAN - 1; it reads those accumulators (EPI_COLS per
-// wait), adds the bias, applies ReLU and writes that part of BF16 row r of
-// the next A operand; hb2 holds the layer's biases as BF16 pairs
-constexpr int EPI_COLS = 32;  // accumulator columns per TMEM read of the epilogue (32 or 64)
-constexpr int WPS = 4;        // epilogue warps per tile slot: 4 (all 128 columns each) or 8 (64 each)
+// columns c0 .. c0 + SPAN - 1; 64 accumulator columns at a time it reads
+// them (one wait), adds the bias, applies ReLU and stores the 32 BF16 pairs
+// to the activation columns (c0 / 2 ...) of its lane; hb2 holds the layer's
+// biases as BF16 pairs
+constexpr int WPS = 4;               // epilogue warps per tile slot: 4 (all 128 columns each) or 8 (64 each)
 constexpr int SPAN = HID * 4 / WPS;  // columns per epilogue warp
 
-__device__ __forceinline__ void hidden_epilogue(uint32_t taddr_row, const uint32_t* hb2, unsigned char* a1, int r,
-                                                int c0) {
+__device__ __forceinline__ void hidden_epilogue(uint32_t d_row, uint32_t act_row, const uint32_t* hb2, int c0) {
 #pragma unroll
-    for (int h = c0; h < c0 + SPAN; h += EPI_COLS) {
-        uint32_t u[EPI_COLS];
-        if constexpr (EPI_COLS == 64) {
-            tmem_ld64(taddr_row + (uint32_t)h, u);
-        } else {
-            float v[32];
-            tmem_ld32(taddr_row + (uint32_t)h, v);
+    for (int h = c0; h < c0 + SPAN; h += 64) {
+        uint32_t u[64], y[32];
+        tmem_ld64(d_row + (uint32_t)h, u);
 #pragma unroll
-            for (int c = 0; c < 32; ++c) u[c] = __float_as_uint(v[c]);
-        }
-#pragma unroll
-        for (int k = 0; k < EPI_COLS; k += 8) {
+        for (int k = 0; k < 64; k += 8) {
             const uint4 b = *reinterpret_cast<const uint4*>(hb2 + ((h + k) >> 1));
-            uint4 pk;
-            pk.x = relu_bf16x2(__uint_as_float(u[k + 0]), __uint_as_float(u[k + 1]), b.x);
-            pk.y = relu_bf16x2(__uint_as_float(u[k + 2]), __uint_as_float(u[k + 3]), b.y);
-            pk.z = relu_bf16x2(__uint_as_float(u[k + 4]), __uint_as_float(u[k + 5]), b.z);
-            pk.w = relu_bf16x2(__uint_as_float(u[k + 6]), __uint_as_float(u[k + 7]), b.w);
-            *reinterpret_cast<uint4*>(a1 + kmajor_off(r, h + k, 128)) = pk;
+            y[k / 2 + 0] = relu_bf16x2(__uint_as_float(u[k + 0]), __uint_as_float(u[k + 1]), b.x);
+            y[k / 2 + 1] = relu_bf16x2(__uint_as_float(u[k + 2]), __uint_as_float(u[k + 3]), b.y);
+            y[k / 2 + 2] = relu_bf16x2(__uint_as_float(u[k + 4]), __uint_as_float(u[k + 5]), b.z);
+            y[k / 2 + 3] = relu_bf16x2(__uint_as_float(u[k + 6]), __uint_as_float(u[k + 7]), b.w);
         }
+        tmem_st32(act_row + (uint32_t)(h / 2), y);
     }
+    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
 
 // a sample's 13 physical inputs (zero past n)
@@ -796,14 +828,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(TcArgs a) {
                         ph ^= 1u << sl;
                         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                         const int layer = (int)(issued[sl] & 3u);
-                        const uint32_t d = tmem + 128u * sl;
-                        const uint32_t a1 = sbase + S_A1 + sl * A1_BYTES;
+                        const uint32_t d = tmem + SLOT_COLS * sl, act = d + ACT_COL;
                         if (layer == 0)
                             issue_layer<IN, HID>(d, sbase + S_A0 + sl * A0_BYTES, sbase + SW1);
                         else if (layer < 3)
-                            issue_layer<HID, HID>(d, a1, sbase + (layer == 1 ? SW2 : SW3));
+                            issue_layer_ts<HID, HID>(d, act, sbase + (layer == 1 ? SW2 : SW3));
                         else
-                            issue_layer<HID, 16>(d, a1, sbase + SW4);
+                            issue_layer_ts<HID, 16>(d, act, sbase + SW4);
                         mma_commit(full0 + 8u * sl);
                         ++issued[sl];
                         --left;
@@ -826,9 +857,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(TcArgs a) {
         // the warps of columns from 0 own the samples' inputs and outputs
         const int sl = w / WPS, j = w % WPS, r = 32 * (j & 3) + (t & 31), c0 = (j >> 2) * SPAN;
         const bool owner = c0 == 0;
-        const uint32_t trow = tmem + 128u * (uint32_t)sl + ((uint32_t)(32 * (j & 3)) << 16);
+        const uint32_t trow = tmem + SLOT_COLS * (uint32_t)sl + ((uint32_t)(32 * (j & 3)) << 16);
         unsigned char* a0 = s + S_A0 + sl * A0_BYTES;
-        unsigned char* a1 = s + S_A1 + sl * A1_BYTES;
         uint32_t ph = 0u;
         bool ok = true;
         float x[NIN];  // the next tile's physical inputs, loaded one tile ahead
@@ -863,7 +893,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(TcArgs a) {
                 if (!ok) break;
                 ph ^= 1u;
                 if (layer < 3) {
-                    hidden_epilogue(trow, hb2 + layer * (HID / 2), a1, r, c0);
+                    hidden_epilogue(trow, trow + ACT_COL, hb2 + layer * (HID / 2), c0);
                 } else if (owner) {
                     float v[16];
                     tmem_ld16(trow, v);
