@@ -514,22 +514,25 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-// shared-memory image of the packed weights (bytes)
-constexpr uint32_t SW1 = 0, SW2 = SW1 + HID * IN * 2, SW3 = SW2 + HID * HID * 2, SW4 = SW3 + HID * HID * 2,
+// shared-memory image of the packed weights (bytes).  The hidden layers'
+// biases ride in the MMAs: W1's input column 13 holds b1 (the inputs carry a
+// 1 there), and W2, W3 have K = 144 with b2, b3 in column 128 (the
+// activations carry a 1 in K column 128, zeros up to 143)
+constexpr int KH = HID + 16;
+constexpr uint32_t SW1 = 0, SW2 = SW1 + HID * IN * 2, SW3 = SW2 + HID * KH * 2, SW4 = SW3 + HID * KH * 2,
                    WBYTES = SW4 + 16 * HID * 2;  // W4 padded to 16 rows
 // biases (FP32): b1, b2, b3 (128 each), b4 (16)
 constexpr uint32_t NBIAS = 3 * HID + 16;
-// kernel shared memory: weights, the output bias (FP32), the hidden biases as
-// BF16 pairs (3 x HID / 2 words), then per tile slot (NSLOT) the inputs A0
-// (128 x 16), the mbarriers (MMA done and operand ready per slot, the final
-// drain), the TMEM address.  Tensor memory per slot (256 columns): the
-// accumulator D (128 columns) and the hidden activations, the A operand of
-// layers 2-4 (128 x 128 BF16 = 64 columns), so the MMAs read only the
-// weights from shared memory.
+// kernel shared memory: weights, biases (FP32; the output bias is used), then
+// per tile slot (NSLOT) the inputs A0 (128 x 16), the mbarriers (MMA done and
+// operand ready per slot, the final drain), the TMEM address.  Tensor memory
+// per slot (256 columns): the accumulator D (128 columns) and the hidden
+// activations, the A operand of layers 2-4 (128 x 144 BF16 = 72 columns, the
+// last 8 the constant bias column), so the MMAs read only the weights from
+// shared memory.
 constexpr int NSLOT = 2;
 constexpr uint32_t SLOT_COLS = 256, TMEM_COLS = SLOT_COLS * NSLOT, ACT_COL = 128;
-constexpr uint32_t S_BIAS = WBYTES, S_HB = S_BIAS + NBIAS * 4,
-                   S_A0 = (S_HB + 3 * (HID / 2) * 4 + 1023) / 1024 * 1024, A0_BYTES = 128 * IN * 2,
+constexpr uint32_t S_BIAS = WBYTES, S_A0 = (S_BIAS + NBIAS * 4 + 1023) / 1024 * 1024, A0_BYTES = 128 * IN * 2,
                    S_BAR = S_A0 + NSLOT * A0_BYTES, S_TADDR = S_BAR + 8 * (2 * NSLOT + 1),
                    SMEM_TC = S_TADDR + 8 + 1024;
 
@@ -615,8 +618,6 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
     return *reinterpret_cast<uint32_t*>(&h);
 }
 
-constexpr uint32_t BF16X2_ONE = 0x3F803F80u;  // (1, 1) as BF16 pairs
-
 // 32 words of this warp's lanes to TMEM columns taddr .. taddr + 31 (the
 // caller waits with tcgen05.wait::st before the columns are read)
 __device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t* w) {
@@ -630,6 +631,12 @@ __device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t* w) {
         : "memory");
 }
 
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t* w) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr), "r"(w[0]),
+                 "r"(w[1]), "r"(w[2]), "r"(w[3]), "r"(w[4]), "r"(w[5]), "r"(w[6]), "r"(w[7])
+                 : "memory");
+}
+
 // D (TMEM) = A (TMEM: 128 lanes = rows, two BF16 of K per 32-bit column) x
 // B (shared-memory descriptor), accumulate when acc != 0
 __device__ __forceinline__ void mma_bf16_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t b, uint32_t idesc,
@@ -641,13 +648,11 @@ __device__ __forceinline__ void mma_bf16_ts(uint32_t d_tmem, uint32_t a_tmem, ui
         : "memory");
 }
 
-// ReLU(v + b) of two accumulators in packed BF16: the accumulators are
-// rounded to BF16 (v0 to the low half, element k; v1 to the high half), then
-// one packed FMA adds the biases b2 (BF16 pair) and clamps at zero
-__device__ __forceinline__ uint32_t relu_bf16x2(float v0, float v1, uint32_t b2) {
-    const uint32_t x = pack_bf16(v0, v1);
+// ReLU of two accumulators (their biases already summed in), rounded to BF16
+// once: v0 to the low half (element k), v1 to the high half
+__device__ __forceinline__ uint32_t relu_bf16x2(float v0, float v1) {
     uint32_t y;
-    asm("fma.rn.relu.bf16x2 %0, %1, %2, %3;" : "=r"(y) : "r"(x), "r"(BF16X2_ONE), "r"(b2));
+    asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(y) : "f"(v1), "f"(v0));
     return y;
 }
 
@@ -683,25 +688,18 @@ __device__ __forceinline__ void issue_layer(uint32_t tmem, uint32_t a_addr, uint
 // hidden-layer epilogue of one tile by its group of WPS warps: thread t of
 // group warp j (TMEM lane quarter j % 4) owns sample r = 32 (j % 4) + t and
 // columns c0 .. c0 + SPAN - 1; 64 accumulator columns at a time it reads
-// them (one wait), adds the bias, applies ReLU and stores the 32 BF16 pairs
-// to the activation columns (c0 / 2 ...) of its lane; hb2 holds the layer's
-// biases as BF16 pairs
+// them (one wait; the bias is in the sums), applies ReLU and stores the 32
+// BF16 pairs to the activation columns (c0 / 2 ...) of its lane
 constexpr int WPS = 4;               // epilogue warps per tile slot: 4 (all 128 columns each) or 8 (64 each)
 constexpr int SPAN = HID * 4 / WPS;  // columns per epilogue warp
 
-__device__ __forceinline__ void hidden_epilogue(uint32_t d_row, uint32_t act_row, const uint32_t* hb2, int c0) {
+__device__ __forceinline__ void hidden_epilogue(uint32_t d_row, uint32_t act_row, int c0) {
 #pragma unroll
     for (int h = c0; h < c0 + SPAN; h += 64) {
         uint32_t u[64], y[32];
         tmem_ld64(d_row + (uint32_t)h, u);
 #pragma unroll
-        for (int k = 0; k < 64; k += 8) {
-            const uint4 b = *reinterpret_cast<const uint4*>(hb2 + ((h + k) >> 1));
-            y[k / 2 + 0] = relu_bf16x2(__uint_as_float(u[k + 0]), __uint_as_float(u[k + 1]), b.x);
-            y[k / 2 + 1] = relu_bf16x2(__uint_as_float(u[k + 2]), __uint_as_float(u[k + 3]), b.y);
-            y[k / 2 + 2] = relu_bf16x2(__uint_as_float(u[k + 4]), __uint_as_float(u[k + 5]), b.z);
-            y[k / 2 + 3] = relu_bf16x2(__uint_as_float(u[k + 6]), __uint_as_float(u[k + 7]), b.w);
-        }
+        for (int k = 0; k < 32; ++k) y[k] = relu_bf16x2(__uint_as_float(u[2 * k]), __uint_as_float(u[2 * k + 1]));
         tmem_st32(act_row + (uint32_t)(h / 2), y);
     }
     asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
@@ -781,9 +779,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(TcArgs a) {
     for (uint32_t i = t; i < WBYTES / 16; i += TC_THREADS) reinterpret_cast<uint4*>(s)[i] = a.wpack[i];
     float* bias = reinterpret_cast<float*>(s + S_BIAS);
     for (uint32_t i = t; i < NBIAS; i += TC_THREADS) bias[i] = a.bias[i];
-    uint32_t* hb2 = reinterpret_cast<uint32_t*>(s + S_HB);
-    for (uint32_t i = t; i < 3 * (HID / 2); i += TC_THREADS)
-        hb2[i] = pack_bf16(a.bias[2 * i], a.bias[2 * i + 1]);
     uint32_t* taddr_slot = reinterpret_cast<uint32_t*>(s + S_TADDR);
     // mbarriers: slot sl's MMA-done at full0 + 8 sl, its operand-ready at ready0 + 8 sl
     const uint32_t full0 = sbase + S_BAR, ready0 = full0 + 8 * NSLOT, drain = ready0 + 8 * NSLOT;
@@ -832,7 +827,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(TcArgs a) {
                         if (layer == 0)
                             issue_layer<IN, HID>(d, sbase + S_A0 + sl * A0_BYTES, sbase + SW1);
                         else if (layer < 3)
-                            issue_layer_ts<HID, HID>(d, act, sbase + (layer == 1 ? SW2 : SW3));
+                            issue_layer_ts<KH, HID>(d, act, sbase + (layer == 1 ? SW2 : SW3));
                         else
                             issue_layer_ts<HID, 16>(d, act, sbase + SW4);
                         mma_commit(full0 + 8u * sl);
@@ -859,6 +854,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(TcArgs a) {
         const bool owner = c0 == 0;
         const uint32_t trow = tmem + SLOT_COLS * (uint32_t)sl + ((uint32_t)(32 * (j & 3)) << 16);
         unsigned char* a0 = s + S_A0 + sl * A0_BYTES;
+        if (owner) {
+            // the activations' constant K columns 128 .. 143: 1, 0, ..., 0 (the bias column)
+            uint32_t one[8] = {0x3F80u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+            tmem_st8(trow + ACT_COL + HID / 2, one);
+            asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+        }
         uint32_t ph = 0u;
         bool ok = true;
         float x[NIN];  // the next tile's physical inputs, loaded one tile ahead
@@ -868,7 +869,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(TcArgs a) {
             // inputs -> A0 (128 x 16 BF16), then the next tile's inputs are requested
             float xn[16];
 #pragma unroll
-            for (int c = 0; c < 16; ++c) xn[c] = c < NIN ? x[c] * a.in_inv_scale[c] : 0.0f;
+            for (int c = 0; c < 16; ++c) xn[c] = c < NIN ? x[c] * a.in_inv_scale[c] : (c == NIN ? 1.0f : 0.0f);
             float de[6];  // this tile's strain increment, for the elastic predictor
 #pragma unroll
             for (int c = 0; c < 6; ++c) de[c] = x[7 + c];
@@ -893,7 +894,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(TcArgs a) {
                 if (!ok) break;
                 ph ^= 1u;
                 if (layer < 3) {
-                    hidden_epilogue(trow, trow + ACT_COL, hb2 + layer * (HID / 2), c0);
+                    hidden_epilogue(trow, trow + ACT_COL, c0);
                 } else if (owner) {
                     float v[16];
                     tmem_ld16(trow, v);
@@ -988,17 +989,20 @@ static int pack_weights(mpm_net* net) {
         u += 0x7fffu + ((u >> 16) & 1u);
         return (uint16_t)(u >> 16);
     };
-    auto put = [&](uint32_t base, int R, int K, long long off, int rows_valid) {
+    // R x Kimg image of the R x K weights at off, the bias at boff in column kb (kb < 0: none)
+    auto put = [&](uint32_t base, int R, int K, int Kimg, long long off, int rows_valid, int kb, long long boff) {
         for (int r = 0; r < R; ++r)
-            for (int k = 0; k < K; ++k) {
-                const float v = r < rows_valid ? p[off + (long long)r * K + k] : 0.0f;
+            for (int k = 0; k < Kimg; ++k) {
+                float v = 0.0f;
+                if (r < rows_valid && k == kb) v = p[boff + r];
+                else if (r < rows_valid && k < K) v = p[off + (long long)r * K + k];
                 img[(base + kmajor_off(r, k, R)) / 2] = bf(v);
             }
     };
-    put(SW1, HID, IN, OW1, HID);
-    put(SW2, HID, HID, OW2, HID);
-    put(SW3, HID, HID, OW3, HID);
-    put(SW4, 16, HID, OW4, OUT);
+    put(SW1, HID, IN, IN, OW1, HID, NIN, OB1);
+    put(SW2, HID, HID, KH, OW2, HID, HID, OB2);
+    put(SW3, HID, HID, KH, OW3, HID, HID, OB3);
+    put(SW4, 16, HID, HID, OW4, OUT, -1, 0);
     std::vector<float> bias(NBIAS, 0.0f);
     for (int i = 0; i < HID; ++i) {
         bias[i] = p[OB1 + i];

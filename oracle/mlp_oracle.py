@@ -79,12 +79,12 @@ def bf16(a):
 
 
 def forward_bf16(theta, x):
-    """The inference kernel's arithmetic: bf16 weights and activations, exact products, float sums; each hidden
-    layer's sum plus bias through ReLU, rounded to bf16 once."""
+    """The inference kernel's arithmetic: bf16 weights, biases and activations, exact products, float sums (the
+    hidden biases are summed with the products); each hidden layer's sum through ReLU, rounded to bf16 once."""
     W1, b1, W2, b2, W3, b3, W4, b4 = unpack(theta)
     h = bf16(x)
     for W, b in ((W1, b1), (W2, b2), (W3, b3)):
-        h = bf16(relu(h @ bf16(W).T + b))
+        h = bf16(relu(h @ bf16(W).T + bf16(b)))
     return h @ bf16(W4).T + b4
 
 
