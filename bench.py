@@ -81,6 +81,9 @@ def parse():
     ap.add_argument("--cell-sort", type=int, default=-1, choices=(-1, 0, 1),
                     help="FP32 form: 1 sorts the particles by cell every step, 0 takes the storage order "
                          "(the engine's default when -1)")
+    ap.add_argument("--host-scenes", action="store_true",
+                    help="build the cellular scene bodies with numpy on the host (as the reference arm does) instead "
+                         "of on the GPU; the particles are the same bit for bit")
     ap.add_argument("--no-network", action="store_true",
                     help="run the chosen form without the learned return map (and skip its isolated benchmark)")
     return ap.parse_args()
@@ -184,7 +187,7 @@ def workload(args):
     from code_mpm_gb300 import scenes
 
     # the GPU arm builds the cellular bodies on the device (same bits); the reference arm stays on the host
-    device = getattr(args, "impl", "gb300") != "reference"
+    device = getattr(args, "impl", "gb300") != "reference" and not getattr(args, "host_scenes", False)
     if args.workload == "foam":
         st = scenes.graded_foam(device=device)  # 800 x 800 x 400 cells, 8 x 8 graded cells of 5 mm, platen -20 m/s
         cfg = {"workload": "density-graded square-cell foam crushed by a rigid platen, contact path, single instance",
