@@ -255,6 +255,21 @@ __device__ __forceinline__ Quad<T> ld_quad(const T* __restrict__ p) {
     return *reinterpret_cast<const Quad<T>*>(p);
 }
 
+// Both halves of a node record, a = p[0..3], b = p[4..7]: one 32-byte load in
+// FP32 (records are 32-byte aligned and not written while they are read),
+// two 32-byte loads in FP64.
+template <typename T>
+__device__ __forceinline__ void ld_record(const T* __restrict__ p, Quad<T>& a, Quad<T>& b) {
+    if constexpr (sizeof(T) == 4) {
+        asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+            : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+            : "l"(p));
+    } else {
+        a = ld_quad(p);
+        b = ld_quad(p + 4);
+    }
+}
+
 // The nodes a node kernel works on, grid-stride: the active-node list when
 // one is given, else every node.  The body may `continue`, not `return`.
 // Node state bits beside the caller's (1 active, 2 contact, 4 / 8 contact

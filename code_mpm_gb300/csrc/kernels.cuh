@@ -1641,8 +1641,9 @@ __device__ __forceinline__ unsigned pass2_particle(const PView<T>& P, const NVie
                     const long long nid = cell_node(cn, W * h + j);
                     in[j] = (cn.mask >> (W * h + j)) & 1u;
                     const Quad<T> z{(T)0, (T)0, (T)0, (T)0};
-                    rq[j] = in[j] ? ld_quad(nd.rec + 8 * nid) : z;
-                    vq[j] = in[j] ? ld_quad(nd.rec + 8 * nid + 4) : z;
+                    rq[j] = z;
+                    vq[j] = z;
+                    if (in[j]) ld_record(nd.rec + 8 * nid, rq[j], vq[j]);
                 }
 #pragma unroll
                 for (int j = 0; j < W; ++j) {
