@@ -111,7 +111,6 @@ struct mpm_ctx {
     unsigned sg_mats = 0;
     std::vector<MatConst> mats_host;
     DevBuf q_in, q_out, q_vol, q_pidx, q_count, sg_acc;
-    DevBuf fb_in, fb_vol, fb_pidx, fb_count;  // the FP64 fallback's queue (FP32 form)
     // CUDA graph of two steps, replayed while nothing it captured changes
     int use_graph = 1;
     // One graph per key-buffer parity: a captured step reads the cell keys from
@@ -147,7 +146,6 @@ struct mpm_ctx {
                           &g_state, &g_fixed, &g_friction, &g_ratio, &g_q, &g_owner, &g_nowner, &g_need, &g_list, &g_count, &rs_chunk, &cstart,
                           &cend, &keys0, &vals0, &keys1, &vals1, &keys_copy, &counts, &dclist, &mats, &staging, &tune_backup, &surf, &mon_mask, &mon_acc, &loc, &geom_tab, &sid, &alist, &acount,
                           &q_in, &q_out, &q_vol, &q_pidx, &q_count, &sg_acc, &hv_count,
-                          &fb_in, &fb_vol, &fb_pidx, &fb_count,
                           &dsim, &tl_dev, &orig, &ptmp, &Fe, &work_acc};
         all.assign(std::begin(list), std::end(list));
     }
@@ -932,16 +930,6 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph, bool output) {
         a.sg_acc = nullptr;
         a.fb_wide = (sizeof(T) == 4 && c->fp64_fallback) ? 1 : 0;
         a.fb_band = c->sg_band;
-        a.fq = FallbackQueue{};
-        if (a.fb_wide) {
-            int rq;
-            if ((rq = ensure(c, c->fb_in, (size_t)n * 14 * 4)) || (rq = ensure(c, c->fb_vol, (size_t)n * 4)) ||
-                (rq = ensure(c, c->fb_pidx, (size_t)n * 4)) || (rq = ensure(c, c->fb_count, 64)))
-                return rq;
-            CK(cudaMemsetAsync(c->fb_count.p, 0, 4, c->stream));
-            a.fq = FallbackQueue{(float*)c->fb_in.p, (float*)c->fb_vol.p, (unsigned*)c->fb_pidx.p,
-                                 (unsigned*)c->fb_count.p, n};
-        }
         a.hv_on = c->hv_on;
         a.hv_mats = c->hv_mats;
         a.hv_band = c->hv_band;
@@ -1012,9 +1000,6 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph, bool output) {
                        graph ? &dsim->step : (const unsigned long long*)nullptr, a.sg_acc,
                        net_guard(c->net, c->sg_guard));
             }
-            if (a.fb_wide)
-                LAUNCH("fb_finish", k_fb_finish, (unsigned)c->sm_count * 8, 256, P, a.fq, (const MatConst*)c->mats.p,
-                       contact, dt);
         }
         c->keys_valid = true;
     }

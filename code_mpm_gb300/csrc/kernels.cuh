@@ -1204,17 +1204,6 @@ __global__ void __launch_bounds__(256, 4) k_node_phase_b(NView<T> nd, int contac
     }
 }
 
-// The FP64 fallback's queue: per entry the stress (6), R, the strain
-// increment (6) and the material index (as the bits of a float), the volume
-// and the particle.  Capacity n: a particle is appended at most once a step.
-struct FallbackQueue {
-    float* in;  // cap x 14
-    float* vol;
-    unsigned* pidx;
-    unsigned* count;
-    long long cap;
-};
-
 // TimeLine::getVelocity (TimeLine.h:33-46) is evaluated on the host each step
 // and passed in as tv.
 struct StepArgs {
@@ -1235,11 +1224,9 @@ struct StepArgs {
     SurrogateAcc* sg_acc;
     // FP32 form: von Mises hardening particles whose trial yield function is
     // above -fb_band x k0 (the fallback band and the plastic states the network
-    // does not take) run the exact map in FP64 (cr_increment_wide): pass 2
-    // appends them to fq and k_fb_finish applies the map after it
+    // does not take) run the exact map in FP64 (cr_increment_wide)
     int fb_wide;
     float fb_band;
-    FallbackQueue fq;
     // harvesting of return-map inputs (either form)
     int hv_on;
     unsigned hv_mats;
@@ -1758,10 +1745,19 @@ __device__ __forceinline__ unsigned pass2_particle(const PView<T>& P, const NVie
                     hr[6] = (float)R;
                 }
             }
-            // wide: the FP64 map runs after pass 2 over the queued particles
-            // (k_fb_finish), so its double-precision working set stays out of
-            // this kernel's registers
-            if (!queued && !wide) cr_return<T>(M, R, sig, e, tr, o);
+            if (!queued) {
+                if constexpr (sizeof(T) == 4) {
+                    if (wide) {
+                        CrOut<double> w;
+                        cr_increment_wide(M, R, sig, e, w);
+                        cr_narrow(w, o);
+                    } else {
+                        cr_return<T>(M, R, sig, e, tr, o);
+                    }
+                } else {
+                    cr_return<T>(M, R, sig, e, tr, o);
+                }
+            }
             T V;
             if (!a.contact) {
 #pragma unroll
@@ -1790,22 +1786,6 @@ __device__ __forceinline__ unsigned pass2_particle(const PView<T>& P, const NVie
                         qi[6] = R;
                         a.q.vol[slot] = V;
                         a.q.pidx[slot] = (unsigned)p;
-                    }
-                }
-            } else if (wide) {
-                if constexpr (sizeof(T) == 4) {
-                    const unsigned slot = warp_slot(a.fq.count);
-                    if (slot < (unsigned long long)a.fq.cap) {
-                        float* qi = a.fq.in + (long long)slot * 14;
-#pragma unroll
-                        for (int k = 0; k < 6; ++k) {
-                            qi[k] = sig[k];
-                            qi[7 + k] = e[k];
-                        }
-                        qi[6] = R;
-                        qi[13] = __int_as_float(mi);
-                        a.fq.vol[slot] = V;
-                        a.fq.pidx[slot] = (unsigned)p;
                     }
                 }
             } else {
@@ -2392,32 +2372,6 @@ __global__ void __launch_bounds__(256) k_monitor_force(NView<T> nd, double* acc)
 // guard replaces implausible results by that exact map, see below;
 // the network's result is kept).
 // ---------------------------------------------------------------------------
-// The FP64 fallback of the FP32 form over the particles pass 2 queued (the
-// band near the yield surface and the plastic states the network does not
-// take): the exact von Mises hardening map in FP64 (cr_increment_wide,
-// …_VonMisesHardening.cpp:4-92), narrowed to float and applied as pass 2
-// applies its own increments.  Grid-stride over the device count.
-static __global__ void k_fb_finish(PView<float> P, FallbackQueue fq, const MatConst* __restrict__ mats, int contact,
-                                   double dt) {
-    const unsigned cnt = (unsigned)min((unsigned long long)*fq.count, (unsigned long long)fq.cap);
-    for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < cnt; s += gridDim.x * blockDim.x) {
-        const float* qi = fq.in + (long long)s * 14;
-        float sig[6], e[6];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) {
-            sig[k] = qi[k];
-            e[k] = qi[7 + k];
-        }
-        const float R = qi[6];
-        const MatConst& M = mats[__float_as_int(qi[13])];
-        CrOut<double> w;
-        cr_increment_wide(M, R, sig, e, w);
-        CrOut<float> o;
-        cr_narrow(w, o);
-        apply_increment<float>(P, (long long)fq.pidx[s], sig, e, o, fq.vol[s], R, contact, dt);
-    }
-}
-
 static __global__ void k_sg_finish(PView<float> P, SurrogateQueue q, MatConst M, int contact, double dt, double inv_yield,
                             float recheck, unsigned long long step, const unsigned long long* step_dev,
                             SurrogateAcc* acc, SurrogateGuard gd) {
