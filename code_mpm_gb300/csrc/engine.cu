@@ -106,7 +106,7 @@ struct mpm_ctx {
     // return-map network (FP32 form)
     mpm_net* net = nullptr;
     float sg_band = 0.02f, sg_recheck = 0.01f;  // the fallback band also bounds the FP64 fallback without a network
-    float sg_guard = 0.002f;  // tolerance of the guard on the network's results, a fraction of k0 (0: off)
+    float sg_guard = 0.001f;  // tolerance of the guard on the network's results, a fraction of k0 (0: off)
     int fp64_fallback = 1;  // FP32 form: the exact map in FP64 for von Mises hardening particles near or past the surface
     unsigned sg_mats = 0;
     std::vector<MatConst> mats_host;

@@ -87,7 +87,7 @@ extern "C" {
                                     0.02 by default) and that the network does not take: the fallback band and
                                     every plastic state without a network; 0: FP32 throughout */
 #define MPM_OPT_SURROGATE_GUARD 14 /* FP32 form with the learned return map: tolerance of the guard on the network's
-                                      results as a fraction of k0 (default 0.002; 0 turns the guard off), see
+                                      results as a fraction of k0 (default 0.001; 0 turns the guard off), see
                                       mpm_attach_surrogate */
 #define MPM_OPT_CELL_SORT 9      /* FP32 form, P2G modes 2-4: 1 sorts the particles by cell every step; 0 (default) takes the storage order as it is (a cell whose particles are not adjacent is summed in several runs) and, with MPM_OPT_REORDER 0, restores the cell order every 256 steps */
 
