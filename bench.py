@@ -295,7 +295,10 @@ def apply_tune(e, tune):
     from code_mpm_gb300 import engine
 
     if tune:
-        e.set_option(engine.OPT_P2G_REDUCE, tune["p2g_reduce"])
+        # the pair-reduced P2G (modes 5, 6) exists in the FP32 form only; an FP64 engine given such a tuning takes
+        # the shared-memory cell runs
+        red = tune["p2g_reduce"]
+        e.set_option(engine.OPT_P2G_REDUCE, 3 if red >= 5 and e.form == engine.FORM_FP64 else red)
         e.set_option(engine.OPT_P2G_BLOCK, tune["p2g_block"])
         e.set_option(engine.OPT_PASS_BLOCK, tune["pass_block"])
         # the staged pass 2 (mode 2) exists in the FP32 form only; an FP64 engine given an FP32 tuning gathers
