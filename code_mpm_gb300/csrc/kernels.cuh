@@ -2419,9 +2419,10 @@ static __global__ void k_sg_finish(PView<float> P, SurrogateQueue q, MatConst M,
             atomicAdd(&acc->sq_err, sq / 6.0);
             atomicMax(reinterpret_cast<unsigned long long*>(&acc->max_err), (unsigned long long)__double_as_longlong(mx));
         }
-        // the guard: an input outside the training box, or a result that is not a radial return (the new stress
-        // off the yield surface k0 + R/sqrt 2, or a correction dsigma - D de with a hydrostatic part; both by more
-        // than tol k0), takes the exact map in FP64 instead
+        // the guard: an input outside the training box, or a result that is not the radial return of its trial
+        // state (the new stress off the yield surface k0 + R/sqrt 2, a correction dsigma - D de with a
+        // hydrostatic part, or a stress or R increment that differs from the radial return evaluated here in
+        // FP32; each by more than tol k0), takes the exact map in FP64 instead
         if (gd.tol > 0.0f) {
             bool ok = true;
 #pragma unroll
@@ -2440,6 +2441,16 @@ static __global__ void k_sg_finish(PView<float> P, SurrogateQueue q, MatConst M,
             const float hyd = ((o.dsig[0] - d[0]) + (o.dsig[1] - d[1]) + (o.dsig[2] - d[2])) * (1.0f / 3.0f);
             const float lim = gd.tol * M.fk0;
             ok = ok && fabsf(sqrtf(J2) - rad) <= lim && fabsf(hyd) <= lim;
+            if (ok) {
+                // the direction and the hardening: against the FP32 radial return of the same trial state
+                CrTrial<float> tr;
+                cr_trial<float>(M, R, sig, e, tr);
+                CrOut<float> x;
+                cr_return<float>(M, R, sig, e, tr, x);
+#pragma unroll
+                for (int k = 0; k < 6; ++k) ok = ok && fabsf(o.dsig[k] - x.dsig[k]) <= lim;
+                ok = ok && fabsf(o.dR - x.dR) <= lim;
+            }
             if (!ok) {
                 CrOut<double> w;
                 cr_increment_wide(M, R, sig, e, w);
