@@ -86,6 +86,11 @@ struct mpm_ctx {
     // sort
     DevBuf keys0, vals0, keys1, vals1, keys_copy, counts;
     DevBuf dclist, mats, staging, tune_backup, surf, mon_mask, mon_acc;
+    // particle-field transfers: a second staging buffer and a copy stream, so
+    // one field's copy runs while the next is packed or the previous unpacked
+    DevBuf staging2;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t xfer_ev[4] = {nullptr, nullptr, nullptr, nullptr};  // per buffer: copy done, kernel done
     DevBuf work_acc;  // boundary work since the last particle upload (FP64): displacement control, friction
     int nsurf = 0;
     bool have_mon = false;
@@ -144,7 +149,7 @@ struct mpm_ctx {
                           &e_strain, &e_strain_max, &e_strain_ti, &e_plastic, &backstress, &mp_mg, &strain_rate,
                           &material, &pflags, &dc_mult, &g_acc, &g_vel, &g_ftemp, &g_mg,
                           &g_state, &g_fixed, &g_friction, &g_ratio, &g_q, &g_owner, &g_nowner, &g_need, &g_list, &g_count, &rs_chunk, &cstart,
-                          &cend, &keys0, &vals0, &keys1, &vals1, &keys_copy, &counts, &dclist, &mats, &staging, &tune_backup, &surf, &mon_mask, &mon_acc, &loc, &geom_tab, &sid, &alist, &acount,
+                          &cend, &keys0, &vals0, &keys1, &vals1, &keys_copy, &counts, &dclist, &mats, &staging, &staging2, &tune_backup, &surf, &mon_mask, &mon_acc, &loc, &geom_tab, &sid, &alist, &acount,
                           &q_in, &q_out, &q_vol, &q_pidx, &q_count, &sg_acc, &hv_count,
                           &dsim, &tl_dev, &orig, &ptmp, &Fe, &work_acc};
         all.assign(std::begin(list), std::end(list));
@@ -559,6 +564,79 @@ int download_field(mpm_ctx* c, const DevBuf& src, double* host, long long n, int
         LAUNCH("pack", k_pack<float>, blocks_for(n * k), NTHREADS, (const float*)src.p + off, (double*)c->staging.p,
                n, k, shift_identity, orig, cs, ps);
     CK(cudaMemcpyAsync(host, c->staging.p, (size_t)n * k * 8, cudaMemcpyDeviceToHost, c->stream));
+    return MPM_OK;
+}
+
+// The copy stream and events of the particle-field transfers (created once).
+int xfer_ready(mpm_ctx* c) {
+    if (!c->copy_stream && cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        c->copy_stream = nullptr;
+        return fail(c, MPM_ERR_CUDA, "cannot create the copy stream");
+    }
+    for (auto& e : c->xfer_ev)
+        if (!e && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            e = nullptr;
+            return fail(c, MPM_ERR_CUDA, "cannot create transfer events");
+        }
+    return MPM_OK;
+}
+
+// Particle field i of an upload, double-buffered: the H2D copy into staging
+// buffer i % 2 runs on the copy stream once that buffer's previous unpack has
+// finished; the unpack on the engine stream waits for the copy.  So field
+// i + 1 crosses the link while field i is unpacked.
+int upload_field_pipelined(mpm_ctx* c, int i, DevBuf& dst, const double* host, long long n, int k, bool fp64,
+                           double def, int shift_identity = 0) {
+    if (!host || n == 0) return upload_field(c, dst, host, n, k, fp64, def, shift_identity);
+    const size_t esz = fp64 ? 8 : 4, bytes = (size_t)n * k * 8;
+    int rc = ensure(c, dst, (size_t)n * k * esz);
+    if (rc) return rc;
+    DevBuf& buf = (i & 1) ? c->staging2 : c->staging;
+    if ((rc = ensure(c, buf, bytes))) return rc;
+    cudaEvent_t copied = c->xfer_ev[2 * (i & 1)], unpacked = c->xfer_ev[2 * (i & 1) + 1];
+    // the buffer is free once its previous unpack is done (the first two fields: once the engine stream's
+    // earlier work, which may read the staging buffers, is done)
+    if (i < 2) CK(cudaEventRecord(unpacked, c->stream));
+    CK(cudaStreamWaitEvent(c->copy_stream, unpacked, 0));
+    CK(cudaMemcpyAsync(buf.p, host, bytes, cudaMemcpyHostToDevice, c->copy_stream));
+    CK(cudaEventRecord(copied, c->copy_stream));
+    CK(cudaStreamWaitEvent(c->stream, copied, 0));
+    if (fp64)
+        LAUNCH("unpack", k_unpack<double>, blocks_for(n * k), NTHREADS, (const double*)buf.p, (double*)dst.p, n, k,
+               shift_identity, n, 1);
+    else
+        LAUNCH("unpack", k_unpack<float>, blocks_for(n * k), NTHREADS, (const double*)buf.p, (float*)dst.p, n, k,
+               shift_identity, n, 1);
+    CK(cudaEventRecord(unpacked, c->stream));
+    return MPM_OK;
+}
+
+// Particle field i of a download, double-buffered the other way: the pack
+// into staging buffer i % 2 waits for that buffer's previous D2H copy, the
+// copy on the copy stream waits for the pack.  The caller synchronises the
+// copy stream once at the end.
+int download_field_pipelined(mpm_ctx* c, int i, const DevBuf& src, double* host, long long n, int k, bool fp64,
+                             int shift_identity) {
+    if (!host || n == 0) return MPM_OK;
+    DevBuf& buf = (i & 1) ? c->staging2 : c->staging;
+    const size_t bytes = (size_t)n * k * 8;
+    int rc = ensure(c, buf, bytes);
+    if (rc) return rc;
+    cudaEvent_t copied = c->xfer_ev[2 * (i & 1)], packed = c->xfer_ev[2 * (i & 1) + 1];
+    if (i >= 2) CK(cudaStreamWaitEvent(c->stream, copied, 0));
+    const unsigned* orig = c->have_orig ? (const unsigned*)c->orig.p : nullptr;
+    if (fp64)
+        LAUNCH("pack", k_pack<double>, blocks_for(n * k), NTHREADS, (const double*)src.p, (double*)buf.p, n, k,
+               shift_identity, orig, n, 1);
+    else
+        LAUNCH("pack", k_pack<float>, blocks_for(n * k), NTHREADS, (const float*)src.p, (double*)buf.p, n, k,
+               shift_identity, orig, n, 1);
+    CK(cudaEventRecord(packed, c->stream));
+    CK(cudaStreamWaitEvent(c->copy_stream, packed, 0));
+    CK(cudaMemcpyAsync(host, buf.p, bytes, cudaMemcpyDeviceToHost, c->copy_stream));
+    CK(cudaEventRecord(copied, c->copy_stream));
     return MPM_OK;
 }
 
@@ -1350,6 +1428,9 @@ void mpm_destroy(mpm_ctx* c) {
     if (c->h_sim) cudaFreeHost(c->h_sim);
     graph_reset(c);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    for (auto e : c->xfer_ev)
+        if (e) cudaEventDestroy(e);
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     delete c;
 }
 
@@ -1527,10 +1608,12 @@ int mpm_upload_particles(mpm_ctx* c, const mpm_particles* p, int64_t n) {
                   {&c->backstress, p->backstress, 1, f64, 0.0},
                   {&c->mp_mg, p->mp_mass_gradient, 3, f64, 0.0},
                   {&c->strain_rate, p->strain_rate, 6, f64, 0.0}};
+    if ((rc = xfer_ready(c))) return rc;
+    int fi = 0;
     for (auto& f : fields)
-        if ((rc = upload_field(c, *f.b, f.h, n, f.k, f.fp64, f.def))) return rc;
+        if ((rc = upload_field_pipelined(c, f.h ? fi++ : 0, *f.b, f.h, n, f.k, f.fp64, f.def))) return rc;
     if (p->F) {
-        if ((rc = upload_field(c, c->F, p->F, n, 9, f64, 0.0, f64 ? 0 : 1))) return rc;
+        if ((rc = upload_field_pipelined(c, fi++, c->F, p->F, n, 9, f64, 0.0, f64 ? 0 : 1))) return rc;
     } else if (n > 0) {
         if (f64)
             LAUNCH("fill", k_identity9, blocks_for(9 * n), NTHREADS, c->F.p, (long long)n, 1);
@@ -1710,12 +1793,15 @@ int mpm_download_particles(mpm_ctx* c, mpm_particles* p) {
                   {&c->mp_mg, p->mp_mass_gradient, 3, f64},
                   {&c->strain_rate, p->strain_rate, 6, f64},
                   {&c->Fe, f64 ? p->F_elastic : nullptr, 9, true}};
+    if ((rc = xfer_ready(c))) return rc;
+    int fi = 0;
     for (auto& f : fields) {
         if (!f.h) continue;
         const int shift = (f.b == &c->F && !f64) ? 1 : 0;
-        if ((rc = download_field(c, *f.b, f.h, n, f.k, f.fp64, shift, true))) return rc;
-        CK(cudaStreamSynchronize(c->stream));  // staging is reused by the next field
+        if ((rc = download_field_pipelined(c, fi++, *f.b, f.h, n, f.k, f.fp64, shift))) return rc;
     }
+    CK(cudaStreamSynchronize(c->copy_stream));
+    CK(cudaStreamSynchronize(c->stream));
     if (!f64 && p->F_elastic)  // the FP32 form has no large-strain pass: the identity
         for (long long i = 0; i < n; ++i)
             for (int k = 0; k < 9; ++k) p->F_elastic[9 * i + k] = (k == 0 || k == 4 || k == 8) ? 1.0 : 0.0;
