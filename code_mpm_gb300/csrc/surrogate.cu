@@ -477,15 +477,13 @@ __global__ void k_exact_wide(long long n, const float* __restrict__ in, MatConst
 }
 
 // ---------------------------------------------------------------------------
-// BF16 tcgen05 inference.  One CTA of 128 threads (4 warps) per SM-slot loops
-// over tiles of 128 samples.  Per layer, thread 0 issues tcgen05.mma
-// (kind::f16, BF16 x BF16 -> FP32, M = 128) with the activations (A, M x K)
-// and the weights (B = W[out][in], N x K) in shared memory, both K-major
-// without swizzle; the accumulator D (128 lanes x N columns FP32) sits in
-// tensor memory.  tcgen05.commit signals an mbarrier; each warp then reads
-// its 32 lanes (tcgen05.ld 32x32b: thread t of warp w <-> lane 32w + t =
-// sample), adds the bias, applies ReLU, rounds to BF16 and writes the next
-// layer's A operand.
+// BF16 tcgen05 inference (k_mlp_tc, below): tiles of 128 samples; per layer
+// one tcgen05.mma (kind::f16, BF16 x BF16 -> FP32, M = 128) per 16 of K with
+// the weights (B = W[out][in], N x K) in shared memory, K-major without
+// swizzle, and the accumulator D (128 lanes = samples x N columns FP32) in
+// tensor memory.  The first layer's A operand (the inputs) is in shared
+// memory; the hidden activations are written back to tensor memory
+// (tcgen05.st, one lane per sample) and are the A operand of the next layer.
 //
 // Shared-memory operand layout (K-major, no swizzle): 8-row x 16-byte core
 // matrices; element (r, k) of an R-row operand at byte
@@ -746,12 +744,13 @@ constexpr int TC_THREADS = 32 * (WPS * NSLOT + 1);
 
 // One CTA per SM takes groups of NSLOT 128-sample tiles, one per slot, and
 // runs the slots as independent pipelines that share the tensor core.  A
-// slot's epilogue group writes the operand (the inputs, or the previous
-// layer's activations) and arrives on the slot's `ready` mbarrier (128
-// arrivals); the MMA warp issues the layer of whichever slot is ready and
-// commits to that slot's `full` mbarrier; the group waits on `full`, turns
-// the accumulators (128 TMEM columns per slot) into the next operand, and so
-// on.  The group loads its next tile's inputs while the current tile runs.
+// slot's epilogue group writes the operand (the inputs into shared memory,
+// or the previous layer's activations into tensor memory) and arrives on the
+// slot's `ready` mbarrier (one arrival per warp); the MMA warp issues the
+// layer of whichever slot is ready and commits to that slot's `full`
+// mbarrier; the group waits on `full`, turns the accumulators into the next
+// operand, and so on.  The group loads its next tile's inputs while the
+// current tile runs.
 // Waits are bounded: on a timeout the error word is set and the roles stop;
 // the MMA thread then waits (bounded) for its last MMAs before the TMEM is
 // freed.
