@@ -110,7 +110,7 @@ struct mpm_ctx {
     DevBuf loc;
     // return-map network (FP32 form)
     mpm_net* net = nullptr;
-    float sg_band = 0.02f, sg_recheck = 0.01f;  // the fallback band also bounds the FP64 fallback without a network
+    float sg_band = 0.02f, sg_recheck = 0.01f;  // the network takes trial states at least sg_band k0 past the surface
     float sg_guard = 0.001f;  // tolerance of the guard on the network's results, a fraction of k0 (0: off)
     int fp64_fallback = 1;  // FP32 form: the exact map in FP64 for von Mises hardening particles near or past the surface
     unsigned sg_mats = 0;
@@ -1007,7 +1007,7 @@ int step_impl(mpm_ctx* c, double dt, int contact, bool graph, bool output) {
         a.q = SurrogateQueue{};
         a.sg_acc = nullptr;
         a.fb_wide = (sizeof(T) == 4 && c->fp64_fallback) ? 1 : 0;
-        a.fb_band = c->sg_band;
+        a.fb_below = 1.0e-3f;  // FP32 rounding of the trial yield function is below 1e-5 k0
         a.hv_on = c->hv_on;
         a.hv_mats = c->hv_mats;
         a.hv_band = c->hv_band;

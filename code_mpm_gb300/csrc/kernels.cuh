@@ -1223,10 +1223,13 @@ struct StepArgs {
     SurrogateQueue q;
     SurrogateAcc* sg_acc;
     // FP32 form: von Mises hardening particles whose trial yield function is
-    // above -fb_band x k0 (the fallback band and the plastic states the network
-    // does not take) run the exact map in FP64 (cr_increment_wide)
+    // above -fb_below x k0 and that the network does not take (the states at
+    // and past the yield surface, and elastic ones just below it, whose
+    // elastic/plastic decision FP32 rounding could flip) run the exact map in
+    // FP64 (cr_increment_wide).  Further below the surface the map is
+    // D de, which FP32 gives to within an ulp of the FP64 value rounded.
     int fb_wide;
-    float fb_band;
+    float fb_below;
     // harvesting of return-map inputs (either form)
     int hv_on;
     unsigned hv_mats;
@@ -1729,7 +1732,7 @@ __device__ __forceinline__ unsigned pass2_particle(const PView<T>& P, const NVie
                             if ((threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(&a.sg_acc->band, (unsigned long long)__popc(m));
                         }
                     }
-                    wide = a.fb_wide && !queued && f > -a.fb_band * M.fk0;
+                    wide = a.fb_wide && !queued && f > -a.fb_below * M.fk0;
                 }
             }
             if (a.hv_on && mi < 32 && ((a.hv_mats >> mi) & 1u) && M.type == 4 &&
