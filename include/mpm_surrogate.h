@@ -20,10 +20,12 @@
  * the queued particles against the exact map (in FP64) every step: the judge
  * of the network's error, recorded in mpm_surrogate_stats.  A guard then
  * checks every network result: its inputs must lie in the box of inputs the
- * network was trained on, and the result must be a radial return (the new
- * stress on the yield surface k0 + R/sqrt 2 and the correction dsigma - D de
- * deviatoric, both to MPM_OPT_SURROGATE_GUARD x k0, default 0.01); a result
- * that fails takes the exact map in FP64 instead (counted as rejected).
+ * network was trained on, and the result must be the radial return of its
+ * trial state (the new stress on the yield surface k0 + R/sqrt 2, the
+ * correction dsigma - D de deviatoric, and each stress component and dR
+ * equal to the FP32 radial return, all to MPM_OPT_SURROGATE_GUARD x k0,
+ * default 0.001); a result that fails takes the exact map in FP64 instead
+ * (counted as rejected).
  *
  * All functions return MPM_OK (0) or a negative MPM_ERR_* code.  Samples
  * are rows of floats in physical units: inputs n x 13, outputs n x 7.
