@@ -83,9 +83,10 @@ extern "C" {
 #define MPM_OPT_LARGE_STRAIN 12  /* FP64 form, non-contact loop: 1 runs the large-strain pass 2 (G2P_P2_LargeStrain, PhysicsEngine_runSimulation_Classic_DoublePass_MPLocks.cpp:281-437), which the reference ships disabled (:605); 0 (default) the small-strain pass */
 #define MPM_OPT_FP64_FALLBACK 13 /* FP32 form: 1 (default) computes the von Mises hardening return map
                                     (…_VonMisesHardening.cpp:4-92) in FP64 for particles whose FP32 trial yield
-                                    function is above -band x k0 (band: the fallback band of mpm_attach_surrogate,
-                                    0.02 by default) and that the network does not take: the fallback band and
-                                    every plastic state without a network; 0: FP32 throughout */
+                                    function is above -0.001 x k0 and that the network does not take: with a
+                                    network the states up to its band (mpm_attach_surrogate, 0.02 by default) past
+                                    the surface, every plastic state without one, and the elastic states just
+                                    below the surface; 0: FP32 throughout */
 #define MPM_OPT_SURROGATE_GUARD 14 /* FP32 form with the learned return map: tolerance of the guard on the network's
                                       results as a fraction of k0 (default 0.001; 0 turns the guard off), see
                                       mpm_attach_surrogate */
